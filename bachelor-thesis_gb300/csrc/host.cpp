@@ -1,0 +1,844 @@
+// Host side of gbmm: handle, errors, text / GMP-limb conversion, transfers and
+// the matrix-recursion drivers (Winograd, Strassen, block recursion, squarify)
+// that enqueue the device kernels.  Every entry point returns a status; no
+// host synchronisation happens inside the recursion, so a whole product can
+// be captured into a CUDA graph.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gbmm_internal.h"
+
+namespace gbmm {
+
+static thread_local std::string g_last_error;
+
+gbmm_status set_error(gbmm_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+gbmm_status cuda_error(cudaError_t e, const char *what) {
+    return set_error(e == cudaErrorMemoryAllocation ? GBMM_ERR_NOMEM : GBMM_ERR_CUDA, "%s: %s (%s)", what,
+                     cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+// ---- launch accounting ---------------------------------------------------------------
+static std::atomic<uint64_t> g_launches{0};
+void count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+struct ProfRecord {
+    std::string name;
+    cudaEvent_t start, stop;
+};
+static std::mutex g_prof_mu;
+static bool g_prof_on = false;
+static std::vector<ProfRecord> g_prof;
+
+LaunchScope::LaunchScope(const char *name, cudaStream_t s) : name_(name), s_(s), slot_(-1) {
+    count_launch();
+    if (!g_prof_on) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    ProfRecord r;
+    r.name = name;
+    if (cudaEventCreate(&r.start) != cudaSuccess) return;
+    if (cudaEventCreate(&r.stop) != cudaSuccess) { cudaEventDestroy(r.start); return; }
+    cudaEventRecord(r.start, s);
+    slot_ = (int)g_prof.size();
+    g_prof.push_back(r);
+}
+LaunchScope::~LaunchScope() {
+    if (slot_ < 0) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    cudaEventRecord(g_prof[slot_].stop, s_);
+}
+
+// ---- per-device error word ----------------------------------------------------------
+static std::mutex g_err_mu;
+static uint32_t *g_err_words[64];
+
+uint32_t *device_error_word() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    if (!g_err_words[dev]) {
+        uint32_t *p = nullptr;
+        if (cudaMalloc(&p, sizeof(uint32_t)) != cudaSuccess) return nullptr;
+        cudaMemset(p, 0, sizeof(uint32_t));
+        cudaDeviceSynchronize();
+        g_err_words[dev] = p;
+    }
+    return g_err_words[dev];
+}
+
+gbmm_status check_device_error(cudaStream_t s) {
+    uint32_t *w = device_error_word();
+    if (!w) return set_error(GBMM_ERR_CUDA, "device error word unavailable");
+    uint32_t v = 0;
+    GBMM_CUDA_TRY(cudaMemcpyAsync(&v, w, sizeof v, cudaMemcpyDeviceToHost, s));
+    GBMM_CUDA_TRY(cudaStreamSynchronize(s));
+    if (v) {
+        GBMM_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(uint32_t), s));
+        GBMM_CUDA_TRY(cudaStreamSynchronize(s));
+        if (v & DEVERR_CAPACITY) return set_error(GBMM_ERR_CAPACITY, "a result needed more limb planes than its output has");
+        if (v & DEVERR_TIMEOUT) return set_error(GBMM_ERR_TIMEOUT, "a bounded device-side wait expired");
+        return set_error(GBMM_ERR_INVALID, "device kernel rejected its arguments (flags 0x%x)", v);
+    }
+    return GBMM_OK;
+}
+
+gbmm_status validate_mat(const gbmm_mat &m, const char *name) {
+    if (m.rows < 0 || m.cols < 0) return set_error(GBMM_ERR_INVALID, "%s: negative shape", name);
+    if ((int64_t)m.rows * m.cols == 0) return GBMM_OK;
+    if (!m.limbs || !m.sizes) return set_error(GBMM_ERR_INVALID, "%s: null pointer", name);
+    if (m.nlimbs < 0) return set_error(GBMM_ERR_INVALID, "%s: negative nlimbs", name);
+    if (m.rs < m.cols) return set_error(GBMM_ERR_INVALID, "%s: row stride %lld < cols %d", name, (long long)m.rs, m.cols);
+    if (m.nlimbs > 1 && m.ld < (int64_t)(m.rows - 1) * m.rs + m.cols)
+        return set_error(GBMM_ERR_INVALID, "%s: plane stride %lld too small", name, (long long)m.ld);
+    return GBMM_OK;
+}
+
+// ---- arena ------------------------------------------------------------------------------
+gbmm_status arena_reserve(gbmm_handle h, size_t bytes) {
+    if (h->ws.top + bytes <= h->ws.cap) return GBMM_OK;
+    if (h->ws.top != 0) return set_error(GBMM_ERR_INVALID, "workspace grow while in use");
+    size_t want = std::max(bytes, h->ws.cap * 2);
+    want = (want + 0xFFFFF) & ~(size_t)0xFFFFF;
+    GBMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (h->ws.base) GBMM_CUDA_TRY(cudaFree(h->ws.base));
+    h->ws.base = nullptr;
+    h->ws.cap = 0;
+    void *p = nullptr;
+    GBMM_CUDA_TRY(cudaMalloc(&p, want));
+    h->ws.base = (char *)p;
+    h->ws.cap = want;
+    return GBMM_OK;
+}
+
+void *arena_alloc(gbmm_handle h, size_t bytes) {
+    size_t top = (h->ws.top + 255) & ~(size_t)255;
+    if (top + bytes > h->ws.cap) return nullptr;
+    h->ws.top = top + bytes;
+    return h->ws.base + top;
+}
+
+// A temporary matrix carved from the arena.
+static bool arena_mat(gbmm_handle h, int rows, int cols, int nlimbs, gbmm_mat &m) {
+    int64_t n = (int64_t)rows * cols;
+    m.rows = rows; m.cols = cols; m.nlimbs = nlimbs; m.pad_ = 0;
+    m.rs = cols; m.ld = n;
+    m.limbs = (uint32_t *)arena_alloc(h, (size_t)n * nlimbs * 4 + 16);
+    m.sizes = (int32_t *)arena_alloc(h, (size_t)n * 4 + 16);
+    return m.limbs && m.sizes;
+}
+static size_t mat_bytes(int64_t n, int nlimbs) { return (size_t)n * nlimbs * 4 + (size_t)n * 4 + 2 * 256 + 32; }
+
+}  // namespace gbmm
+
+using namespace gbmm;
+
+// ======================================================================================
+// handle / errors
+// ======================================================================================
+extern "C" const char *gbmm_last_error_string(void) { return g_last_error.c_str(); }
+extern "C" const char *gbmm_version(void) { return "gbmm 0.1"; }
+extern "C" uint64_t gbmm_kernel_launches(void) { return g_launches.load(); }
+
+extern "C" gbmm_status gbmm_profile(int32_t enable) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (auto &r : g_prof) { cudaEventDestroy(r.start); cudaEventDestroy(r.stop); }
+    g_prof.clear();
+    g_prof_on = enable != 0;
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_profile_read(char *out, size_t cap, size_t *written) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    std::vector<std::pair<std::string, std::pair<int, double>>> agg;
+    for (auto &r : g_prof) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(r.stop) != cudaSuccess) return set_error(GBMM_ERR_CUDA, "profile event sync");
+        cudaEventElapsedTime(&ms, r.start, r.stop);
+        bool found = false;
+        for (auto &a : agg)
+            if (a.first == r.name) { a.second.first++; a.second.second += ms; found = true; break; }
+        if (!found) agg.push_back({r.name, {1, (double)ms}});
+    }
+    std::string js = "{";
+    for (size_t i = 0; i < agg.size(); i++) {
+        char buf[256];
+        snprintf(buf, sizeof buf, "%s\"%s\": [%d, %.6f]", i ? ", " : "", agg[i].first.c_str(), agg[i].second.first,
+                 agg[i].second.second);
+        js += buf;
+    }
+    js += "}";
+    if (written) *written = js.size();
+    if (out && cap) {
+        size_t n = std::min(cap - 1, js.size());
+        memcpy(out, js.data(), n);
+        out[n] = 0;
+    }
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_create(gbmm_handle *out) {
+    if (!out) return set_error(GBMM_ERR_INVALID, "null handle pointer");
+    gbmm_handle h = new (std::nothrow) gbmm_handle_s();
+    if (!h) return set_error(GBMM_ERR_NOMEM, "handle allocation");
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) { delete h; return cuda_error(e, "cudaGetDevice"); }
+    if (!device_error_word()) { delete h; return set_error(GBMM_ERR_CUDA, "cannot allocate the device error word"); }
+    h->crt = crt_cache_create();
+    *out = h;
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_destroy(gbmm_handle h) {
+    if (!h) return GBMM_OK;
+    cudaStreamSynchronize(h->stream);
+    if (h->ws.base) cudaFree(h->ws.base);
+    crt_cache_destroy(h->crt);
+    delete h;
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_set_stream(gbmm_handle h, void *stream) {
+    if (!h) return set_error(GBMM_ERR_INVALID, "null handle");
+    h->stream = as_stream(stream);
+    return GBMM_OK;
+}
+
+// ======================================================================================
+// text <-> limb planes
+// ======================================================================================
+static inline int hexval(unsigned char c) {
+    if (c >= '0' && c <= '9') return c - '0';
+    if (c >= 'a' && c <= 'f') return c - 'a' + 10;
+    if (c >= 'A' && c <= 'F') return c - 'A' + 10;
+    return -1;
+}
+static inline bool is_ws(unsigned char c) { return c == ' ' || c == '\n' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
+
+extern "C" gbmm_status gbmm_parse_hex(const char *text, size_t len, int64_t count, uint32_t *limbs, int32_t *sizes,
+                                      int32_t nlimbs, int64_t ld, size_t *consumed) {
+    if ((!text && len) || (count > 0 && (!limbs || !sizes))) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (count > 0 && nlimbs > 0 && ld < count) return set_error(GBMM_ERR_INVALID, "plane stride %lld < count", (long long)ld);
+    size_t p = 0;
+    for (int64_t e = 0; e < count; e++) {
+        while (p < len && is_ws((unsigned char)text[p])) p++;
+        bool neg = false;
+        if (p < len && text[p] == '-') { neg = true; p++; }
+        size_t s = p;
+        while (p < len && hexval((unsigned char)text[p]) >= 0) p++;
+        size_t nd = p - s;
+        if (nd == 0) {
+            if (consumed) *consumed = p;
+            return set_error(GBMM_ERR_PARSE, "entry %lld: expected a hexadecimal digit at byte %zu", (long long)e, p);
+        }
+        if (p < len && !is_ws((unsigned char)text[p])) {
+            if (consumed) *consumed = p;
+            return set_error(GBMM_ERR_PARSE, "entry %lld: invalid character '%c' at byte %zu", (long long)e, text[p], p);
+        }
+        // skip leading zeros
+        while (nd > 1 && text[s] == '0') { s++; nd--; }
+        int need = (int)((nd + 7) / 8);
+        if (nd == 1 && text[s] == '0') need = 0;
+        if (need > nlimbs) {
+            if (consumed) *consumed = p;
+            return set_error(GBMM_ERR_CAPACITY, "entry %lld needs %d limbs, capacity %d", (long long)e, need, nlimbs);
+        }
+        for (int i = 0; i < nlimbs; i++) limbs[(int64_t)i * ld + e] = 0u;
+        for (size_t i = 0; i < nd; i++) {
+            size_t pos = nd - 1 - i;  // digit index from the least significant end
+            if (pos / 8 < (size_t)nlimbs)
+                limbs[(int64_t)(pos / 8) * ld + e] |= (uint32_t)hexval((unsigned char)text[s + i]) << (4 * (pos % 8));
+        }
+        int n = need;
+        while (n > 0 && limbs[(int64_t)(n - 1) * ld + e] == 0) n--;
+        sizes[e] = neg ? -n : n;
+    }
+    if (consumed) *consumed = p;
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_format_hex(const uint32_t *limbs, const int32_t *sizes, int32_t nlimbs, int64_t ld,
+                                       int32_t rows, int32_t cols, int64_t rs, char *out, size_t cap, size_t *written) {
+    if (!sizes || (nlimbs > 0 && !limbs)) return set_error(GBMM_ERR_INVALID, "null pointer");
+    size_t w = 0;
+    auto put = [&](char c) {
+        if (out && w < cap) out[w] = c;
+        w++;
+    };
+    static const char *hx = "0123456789abcdef";
+    for (int32_t r = 0; r < rows; r++) {
+        for (int32_t c = 0; c < cols; c++) {
+            if (c) put(' ');
+            int64_t e = (int64_t)r * rs + c;
+            int s = sizes[e], n = s < 0 ? -s : s;
+            if (n > nlimbs) return set_error(GBMM_ERR_INVALID, "entry (%d,%d): size %d exceeds %d planes", r, c, s, nlimbs);
+            while (n > 0 && limbs[(int64_t)(n - 1) * ld + e] == 0) n--;
+            if (n == 0) { put('0'); continue; }
+            if (s < 0) put('-');
+            bool started = false;
+            for (int i = n - 1; i >= 0; i--) {
+                uint32_t v = limbs[(int64_t)i * ld + e];
+                for (int k = 7; k >= 0; k--) {
+                    int d = (v >> (4 * k)) & 15;
+                    if (d || started) { put(hx[d]); started = true; }
+                }
+            }
+        }
+        put('\n');
+    }
+    put('\n');
+    if (out && w < cap) out[w] = 0;
+    if (written) *written = w;
+    if (out && w > cap) return set_error(GBMM_ERR_INVALID, "output buffer too small (%zu < %zu)", cap, w);
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_import_gmp(int64_t count, const uint64_t *limbs64, const int64_t *offsets,
+                                       const int32_t *sizes64, uint32_t *limbs, int32_t *sizes, int32_t nlimbs,
+                                       int64_t ld) {
+    if (count > 0 && (!limbs64 || !offsets || !sizes64 || !limbs || !sizes))
+        return set_error(GBMM_ERR_INVALID, "null pointer");
+    for (int64_t e = 0; e < count; e++) {
+        int s = sizes64[e], n64 = s < 0 ? -s : s;
+        const uint64_t *d = limbs64 + offsets[e];
+        int n = 2 * n64;
+        while (n > 0 && (uint32_t)(d[(n - 1) / 2] >> (32 * ((n - 1) % 2))) == 0) n--;
+        if (n > nlimbs) return set_error(GBMM_ERR_CAPACITY, "entry %lld needs %d limbs, capacity %d", (long long)e, n, nlimbs);
+        for (int i = 0; i < nlimbs; i++) limbs[(int64_t)i * ld + e] = i < n ? (uint32_t)(d[i / 2] >> (32 * (i % 2))) : 0u;
+        sizes[e] = s < 0 ? -n : n;
+    }
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_export_gmp(int64_t count, const uint32_t *limbs, const int32_t *sizes, int32_t nlimbs,
+                                       int64_t ld, uint64_t *limbs64, const int64_t *offsets, int32_t *sizes64) {
+    if (count > 0 && (!limbs64 || !offsets || !sizes64 || !limbs || !sizes))
+        return set_error(GBMM_ERR_INVALID, "null pointer");
+    for (int64_t e = 0; e < count; e++) {
+        int s = sizes[e], n = s < 0 ? -s : s;
+        if (n > nlimbs) return set_error(GBMM_ERR_INVALID, "entry %lld: size exceeds planes", (long long)e);
+        int n64 = (n + 1) / 2;
+        uint64_t *d = limbs64 + offsets[e];
+        for (int i = 0; i < n64; i++) {
+            uint64_t lo = limbs[(int64_t)(2 * i) * ld + e];
+            uint64_t hi = 2 * i + 1 < n ? limbs[(int64_t)(2 * i + 1) * ld + e] : 0u;
+            d[i] = lo | (hi << 32);
+        }
+        sizes64[e] = s < 0 ? -n64 : n64;
+    }
+    return GBMM_OK;
+}
+
+// ======================================================================================
+// transfers
+// ======================================================================================
+static gbmm_status copy_planes(gbmm_mat m, uint32_t *hl, int32_t *hs, int32_t hn, int64_t hld, bool up, cudaStream_t s) {
+    GBMM_TRY(validate_mat(m, "matrix"));
+    if ((int64_t)m.rows * m.cols == 0) return GBMM_OK;
+    if (!hl || !hs) return set_error(GBMM_ERR_INVALID, "null host pointer");
+    if (hld < (int64_t)m.rows * m.cols) return set_error(GBMM_ERR_INVALID, "host plane stride too small");
+    const cudaMemcpyKind kind = up ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    // sizes: rows with stride rs on the device, contiguous on the host
+    GBMM_CUDA_TRY(cudaMemcpy2DAsync(up ? (void *)m.sizes : (void *)hs, (up ? m.rs : m.cols) * 4,
+                                    up ? (const void *)hs : (const void *)m.sizes, (up ? m.cols : m.rs) * 4,
+                                    (size_t)m.cols * 4, m.rows, kind, s));
+    for (int i = 0; i < m.nlimbs; i++) {
+        uint32_t *dp = m.limbs + (int64_t)i * m.ld;
+        if (i < hn) {
+            uint32_t *hp = hl + (int64_t)i * hld;
+            GBMM_CUDA_TRY(cudaMemcpy2DAsync(up ? (void *)dp : (void *)hp, (up ? m.rs : m.cols) * 4,
+                                            up ? (const void *)hp : (const void *)dp, (up ? m.cols : m.rs) * 4,
+                                            (size_t)m.cols * 4, m.rows, kind, s));
+        } else if (up) {
+            GBMM_CUDA_TRY(cudaMemset2DAsync(dp, m.rs * 4, 0, (size_t)m.cols * 4, m.rows, s));
+        }
+    }
+    if (!up) {
+        // host planes beyond the device capacity are zero
+        for (int i = m.nlimbs; i < hn; i++) memset(hl + (int64_t)i * hld, 0, (size_t)m.rows * m.cols * 4);
+    }
+    GBMM_CUDA_TRY(cudaStreamSynchronize(s));
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_upload(gbmm_mat dst, const uint32_t *host_limbs, const int32_t *host_sizes,
+                                   int32_t host_nlimbs, int64_t host_ld, void *stream) {
+    if (host_nlimbs > dst.nlimbs) {
+        // higher host planes must be empty: check sizes
+        for (int64_t e = 0; e < (int64_t)dst.rows * dst.cols; e++) {
+            int s = host_sizes[e];
+            if ((s < 0 ? -s : s) > dst.nlimbs)
+                return set_error(GBMM_ERR_CAPACITY, "entry %lld needs %d limbs, device capacity %d", (long long)e, s < 0 ? -s : s,
+                                 dst.nlimbs);
+        }
+    }
+    return copy_planes(dst, const_cast<uint32_t *>(host_limbs), const_cast<int32_t *>(host_sizes), host_nlimbs, host_ld,
+                       true, as_stream(stream));
+}
+
+extern "C" gbmm_status gbmm_download(gbmm_mat src, uint32_t *host_limbs, int32_t *host_sizes, int32_t host_nlimbs,
+                                     int64_t host_ld, void *stream) {
+    GBMM_TRY(copy_planes(src, host_limbs, host_sizes, host_nlimbs, host_ld, false, as_stream(stream)));
+    for (int64_t e = 0; e < (int64_t)src.rows * src.cols; e++) {
+        int s = host_sizes[e];
+        if ((s < 0 ? -s : s) > host_nlimbs)
+            return set_error(GBMM_ERR_CAPACITY, "entry %lld has %d limbs, host capacity %d", (long long)e, s, host_nlimbs);
+    }
+    return check_device_error(as_stream(stream));
+}
+
+extern "C" gbmm_status gbmm_import_hex(gbmm_mat dst, const char *text, size_t len, size_t *consumed, void *stream) {
+    GBMM_TRY(validate_mat(dst, "dst"));
+    int64_t n = (int64_t)dst.rows * dst.cols;
+    std::vector<uint32_t> hl((size_t)n * std::max(dst.nlimbs, 1));
+    std::vector<int32_t> hs((size_t)n);
+    GBMM_TRY(gbmm_parse_hex(text, len, n, hl.data(), hs.data(), dst.nlimbs, n, consumed));
+    return gbmm_upload(dst, hl.data(), hs.data(), dst.nlimbs, n, stream);
+}
+
+extern "C" gbmm_status gbmm_export_hex(gbmm_mat src, char *out, size_t cap, size_t *written, void *stream) {
+    GBMM_TRY(validate_mat(src, "src"));
+    int64_t n = (int64_t)src.rows * src.cols;
+    std::vector<uint32_t> hl((size_t)n * std::max(src.nlimbs, 1));
+    std::vector<int32_t> hs((size_t)n);
+    GBMM_TRY(gbmm_download(src, hl.data(), hs.data(), src.nlimbs, n, stream));
+    return gbmm_format_hex(hl.data(), hs.data(), src.nlimbs, n, src.rows, src.cols, src.cols, out, cap, written);
+}
+
+extern "C" gbmm_status gbmm_max_bits(gbmm_mat a, int64_t *bits, void *stream) {
+    GBMM_TRY(validate_mat(a, "a"));
+    if (!bits) return set_error(GBMM_ERR_INVALID, "null pointer");
+    cudaStream_t s = as_stream(stream);
+    int64_t n = (int64_t)a.rows * a.cols;
+    if (n == 0 || a.nlimbs == 0) { *bits = 0; return GBMM_OK; }
+    int32_t *d = nullptr;
+    GBMM_CUDA_TRY(cudaMallocAsync(&d, sizeof(int32_t), s));
+    gbmm_status st = launch_max_size(a, d, s);
+    int32_t mx = 0;
+    if (st == GBMM_OK) {
+        cudaError_t e = cudaMemcpyAsync(&mx, d, sizeof mx, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = cuda_error(e, "max_bits readback");
+    }
+    cudaFreeAsync(d, s);
+    *bits = (int64_t)mx * 32;
+    return st;
+}
+
+// ======================================================================================
+// matrix add / sub
+// ======================================================================================
+static gbmm_status check_same_shape(const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b) {
+    GBMM_TRY(validate_mat(c, "C"));
+    GBMM_TRY(validate_mat(a, "A"));
+    GBMM_TRY(validate_mat(b, "B"));
+    if (a.rows != c.rows || b.rows != c.rows || a.cols != c.cols || b.cols != c.cols)
+        return set_error(GBMM_ERR_INVALID, "shapes differ");
+    return GBMM_OK;
+}
+extern "C" gbmm_status gbmm_mat_add(gbmm_mat c, gbmm_mat a, gbmm_mat b, void *stream) {
+    GBMM_TRY(check_same_shape(c, a, b));
+    return launch_mat_addsub(c, a, b, 0, as_stream(stream));
+}
+extern "C" gbmm_status gbmm_mat_sub(gbmm_mat c, gbmm_mat a, gbmm_mat b, void *stream) {
+    GBMM_TRY(check_same_shape(c, a, b));
+    return launch_mat_addsub(c, a, b, 1, as_stream(stream));
+}
+
+extern "C" gbmm_status gbmm_mat_mul_naive(gbmm_mat c, gbmm_mat a, gbmm_mat b, int32_t accumulate, void *stream) {
+    GBMM_TRY(validate_mat(c, "C"));
+    GBMM_TRY(validate_mat(a, "A"));
+    GBMM_TRY(validate_mat(b, "B"));
+    if (a.rows != c.rows || b.cols != c.cols || a.cols != b.rows) return set_error(GBMM_ERR_INVALID, "shape mismatch");
+    if (c.limbs == a.limbs || c.limbs == b.limbs) return set_error(GBMM_ERR_INVALID, "C must not alias A or B");
+    return launch_limb_matmul(c, a, b, accumulate, as_stream(stream));
+}
+
+// ======================================================================================
+// recursion drivers (limb path)
+// ======================================================================================
+namespace {
+
+struct RecCtx {
+    gbmm_handle h;
+    cudaStream_t s;
+    int cutoff;
+    int capSA, capSB;  // capacities of A-side and B-side sums
+    int capP;          // capacity of products / C quadrants
+};
+
+static unsigned ilog2u(unsigned n) { unsigned r = 0; while (n >>= 1) r++; return r; }
+static unsigned remove_factors(unsigned n, unsigned b) { while (n && n % b == 0) n /= b; return n; }
+
+static gbmm_mat with_limbs(gbmm_mat m, int nl) { m.nlimbs = nl; return m; }
+
+gbmm_status rec_square(RecCtx &c, int method, gbmm_mat C, gbmm_mat A, gbmm_mat B, int N, int levels, int addmul);
+
+// Winograd's 7-product scheme with 3 temporaries; the operation order is that
+// of the reference (WINOGRAD_SEQUENCE / WINOGRAD_ADDMUL_SEQUENCE,
+// mat-gpu/mat-defines.h:144-187; mat-cpu/mat.c:193-334).  p1 holds A-side
+// sums, p2 B-side sums, p3 products; operand views are narrowed to the
+// capacity of what they hold so the leaf kernel does no padded work.
+gbmm_status rec_winograd(RecCtx &c, gbmm_mat C, gbmm_mat A, gbmm_mat B, int N, int levels, int addmul) {
+    const int h = N / 2;
+    size_t mark = arena_mark(c.h);
+    const int capT = std::max(std::max(c.capSA, c.capSB), c.capP);
+    gbmm_mat T1, T2, T3;
+    if (!arena_mat(c.h, h, h, capT, T1) || !arena_mat(c.h, h, h, capT, T2) || !arena_mat(c.h, h, h, capT, T3))
+        return set_error(GBMM_ERR_NOMEM, "winograd temporaries exceed the reserved workspace");
+    gbmm_mat a11 = sub_view(A, 0, 0, h, h), a12 = sub_view(A, 0, h, h, h), a21 = sub_view(A, h, 0, h, h),
+             a22 = sub_view(A, h, h, h, h);
+    gbmm_mat b11 = sub_view(B, 0, 0, h, h), b12 = sub_view(B, 0, h, h, h), b21 = sub_view(B, h, 0, h, h),
+             b22 = sub_view(B, h, h, h, h);
+    gbmm_mat c11 = sub_view(C, 0, 0, h, h), c12 = sub_view(C, 0, h, h, h), c21 = sub_view(C, h, 0, h, h),
+             c22 = sub_view(C, h, h, h, h);
+    gbmm_mat p1 = with_limbs(T1, c.capSA), p2 = with_limbs(T2, c.capSB), p3 = with_limbs(T3, c.capP);
+#define ADD(x, y, z) GBMM_TRY(launch_mat_addsub(x, y, z, 0, c.s))
+#define SUB(x, y, z) GBMM_TRY(launch_mat_addsub(x, y, z, 1, c.s))
+#define MUL(x, y, z) GBMM_TRY(rec_square(c, GBMM_METHOD_WINOGRAD, x, y, z, h, levels - 1, 0))
+#define AML(x, y, z) GBMM_TRY(rec_square(c, GBMM_METHOD_WINOGRAD, x, y, z, h, levels - 1, 1))
+    if (!addmul) {
+        ADD(p1, a21, a22);
+        SUB(p2, b12, b11);
+        MUL(c22, p1, p2);
+        SUB(p1, p1, a11);
+        SUB(p2, b22, p2);
+        MUL(p3, a11, b11);
+        MUL(c11, a12, b21);
+        ADD(c11, c11, p3);
+        AML(p3, p1, p2);
+        SUB(p1, a12, p1);
+        SUB(p2, b21, p2);
+        MUL(c12, p1, b22);
+        ADD(c12, c12, c22);
+        ADD(c12, c12, p3);
+        MUL(c21, a22, p2);
+        SUB(p1, a11, a21);
+        SUB(p2, b22, b12);
+        AML(p3, p1, p2);
+        ADD(c21, c21, p3);
+        ADD(c22, c22, p3);
+    } else {
+        ADD(p1, a21, a22);
+        SUB(p2, b12, b11);
+        MUL(p3, p1, p2);
+        ADD(c12, c12, p3);
+        ADD(c22, c22, p3);
+        SUB(p1, p1, a11);
+        SUB(p2, b22, p2);
+        MUL(p3, a11, b11);
+        ADD(c11, c11, p3);
+        AML(p3, p1, p2);
+        AML(c11, a12, b21);
+        SUB(p1, a12, p1);
+        SUB(p2, b21, p2);
+        AML(c12, p1, b22);
+        ADD(c12, c12, p3);
+        AML(c21, a22, p2);
+        SUB(p1, a11, a21);
+        SUB(p2, b22, b12);
+        AML(p3, p1, p2);
+        ADD(c21, c21, p3);
+        ADD(c22, c22, p3);
+    }
+#undef MUL
+#undef AML
+    arena_release(c.h, mark);
+    return GBMM_OK;
+}
+
+// Strassen's scheme with 3 temporaries (mat-gpu/mat-defines.h:78-117,
+// mat-cpu/mat.c:103-191).  Here p1 holds A sums, B sums and products in turn,
+// so each use gets a view with the matching capacity.
+gbmm_status rec_strassen(RecCtx &c, gbmm_mat C, gbmm_mat A, gbmm_mat B, int N, int levels) {
+    const int h = N / 2;
+    size_t mark = arena_mark(c.h);
+    const int capT = std::max(std::max(c.capSA, c.capSB), c.capP);
+    gbmm_mat T1, T2, T3;
+    if (!arena_mat(c.h, h, h, capT, T1) || !arena_mat(c.h, h, h, capT, T2) || !arena_mat(c.h, h, h, capT, T3))
+        return set_error(GBMM_ERR_NOMEM, "strassen temporaries exceed the reserved workspace");
+    gbmm_mat a11 = sub_view(A, 0, 0, h, h), a12 = sub_view(A, 0, h, h, h), a21 = sub_view(A, h, 0, h, h),
+             a22 = sub_view(A, h, h, h, h);
+    gbmm_mat b11 = sub_view(B, 0, 0, h, h), b12 = sub_view(B, 0, h, h, h), b21 = sub_view(B, h, 0, h, h),
+             b22 = sub_view(B, h, h, h, h);
+    gbmm_mat c11 = sub_view(C, 0, 0, h, h), c12 = sub_view(C, 0, h, h, h), c21 = sub_view(C, h, 0, h, h),
+             c22 = sub_view(C, h, h, h, h);
+    gbmm_mat p1A = with_limbs(T1, c.capSA), p1B = with_limbs(T1, c.capSB), p1P = with_limbs(T1, c.capP);
+    gbmm_mat p2A = with_limbs(T2, c.capSA), p2B = with_limbs(T2, c.capSB);
+    gbmm_mat p3B = with_limbs(T3, c.capSB);
+#define MUL(x, y, z) GBMM_TRY(rec_square(c, GBMM_METHOD_STRASSEN, x, y, z, h, levels - 1, 0))
+    ADD(p1A, a11, a22);
+    ADD(p2B, b11, b22);
+    MUL(c11, p1A, p2B);
+    SUB(p1B, b12, b22);
+    MUL(c12, a11, p1B);
+    ADD(c22, c11, c12);
+    ADD(p1A, a21, a22);
+    MUL(c21, p1A, b11);
+    SUB(c22, c22, c21);
+    SUB(p2A, a12, a22);
+    ADD(p3B, b21, b22);
+    MUL(p1P, p2A, p3B);
+    ADD(c11, c11, p1P);
+    SUB(p2A, a21, a11);
+    ADD(p3B, b11, b12);
+    MUL(p1P, p2A, p3B);
+    ADD(c22, c22, p1P);
+    SUB(p2B, b21, b11);
+    MUL(p1P, a22, p2B);
+    ADD(c11, c11, p1P);
+    ADD(c21, c21, p1P);
+    ADD(p2A, a11, a12);
+    MUL(p1P, p2A, b22);
+    SUB(c11, c11, p1P);
+    ADD(c12, c12, p1P);
+#undef MUL
+    arena_release(c.h, mark);
+    return GBMM_OK;
+}
+
+// Plain 8-product block recursion with one temporary (NAIVE_RECURSIVE_SEQUENCE,
+// mat-gpu/mat-defines.h:21-36).
+gbmm_status rec_naive(RecCtx &c, gbmm_mat C, gbmm_mat A, gbmm_mat B, int N, int levels) {
+    const int h = N / 2;
+    size_t mark = arena_mark(c.h);
+    gbmm_mat T;
+    if (!arena_mat(c.h, h, h, c.capP, T)) return set_error(GBMM_ERR_NOMEM, "workspace");
+    gbmm_mat a11 = sub_view(A, 0, 0, h, h), a12 = sub_view(A, 0, h, h, h), a21 = sub_view(A, h, 0, h, h),
+             a22 = sub_view(A, h, h, h, h);
+    gbmm_mat b11 = sub_view(B, 0, 0, h, h), b12 = sub_view(B, 0, h, h, h), b21 = sub_view(B, h, 0, h, h),
+             b22 = sub_view(B, h, h, h, h);
+    gbmm_mat c11 = sub_view(C, 0, 0, h, h), c12 = sub_view(C, 0, h, h, h), c21 = sub_view(C, h, 0, h, h),
+             c22 = sub_view(C, h, h, h, h);
+#define MUL(x, y, z) GBMM_TRY(rec_square(c, GBMM_METHOD_NAIVE_REC, x, y, z, h, levels - 1, 0))
+    MUL(c11, a11, b11); MUL(T, a12, b21); ADD(c11, c11, T);
+    MUL(c12, a11, b12); MUL(T, a12, b22); ADD(c12, c12, T);
+    MUL(c21, a21, b11); MUL(T, a22, b21); ADD(c21, c21, T);
+    MUL(c22, a21, b12); MUL(T, a22, b22); ADD(c22, c22, T);
+#undef MUL
+    arena_release(c.h, mark);
+    return GBMM_OK;
+}
+
+gbmm_status rec_square(RecCtx &c, int method, gbmm_mat C, gbmm_mat A, gbmm_mat B, int N, int levels, int addmul) {
+    if (levels <= 0 || N % 2 != 0 || N / 2 < 1) return launch_limb_matmul(C, A, B, addmul, c.s);
+    if (method == GBMM_METHOD_WINOGRAD) return rec_winograd(c, C, A, B, N, levels, addmul);
+    if (addmul) return launch_limb_matmul(C, A, B, 1, c.s);
+    if (method == GBMM_METHOD_STRASSEN) return rec_strassen(c, C, A, B, N, levels);
+    if (method == GBMM_METHOD_NAIVE_REC) return rec_naive(c, C, A, B, N, levels);
+    return launch_limb_matmul(C, A, B, 0, c.s);
+}
+
+static int levels_for(int N, int cutoff) {
+    if (N <= cutoff) return 0;
+    int l = (int)ilog2u((unsigned)(N / cutoff));
+    while (l > 0 && (N % (1 << l)) != 0) l--;
+    return l;
+}
+
+// Workspace bytes for a square recursion of `levels` levels on N.
+static size_t rec_ws(int method, int N, int levels, int capT) {
+    size_t total = 0;
+    int n = N;
+    for (int l = 0; l < levels; l++) {
+        int h = n / 2;
+        int ntemps = method == GBMM_METHOD_NAIVE_REC ? 1 : 3;
+        total += (size_t)ntemps * mat_bytes((int64_t)h * h, capT);
+        n = h;
+    }
+    return total;
+}
+
+// squarify: power-of-two core plus remainders (mat-gpu/mat-pregpu.cu:548-576,
+// mat-cpu/matj.c:680-780).  Small or non-square shapes go to the per-entry
+// kernel, which handles any shape in one launch.
+gbmm_status squarify(RecCtx &c, int method, gbmm_mat C, gbmm_mat A, gbmm_mat B) {
+    const int K = A.rows, M = A.cols, N = B.cols;
+    if (K == 0 || N == 0) return GBMM_OK;
+    if (M == 0) return launch_mat_zero(C, c.s);
+    const int base = c.cutoff;
+    if (method == GBMM_METHOD_NAIVE || K <= base || M <= base || N <= base) return launch_limb_matmul(C, A, B, 0, c.s);
+    if (K == M && M == N && remove_factors((unsigned)K, 2) <= (unsigned)base)
+        return rec_square(c, method, C, A, B, K, levels_for(K, base), 0);
+    int mindim = std::min(std::min(K, M), N);
+    int pt = 1 << ilog2u((unsigned)mindim);
+    size_t mark = arena_mark(c.h);
+    gbmm_mat T;
+    if (!arena_mat(c.h, K, N, c.capP, T)) return set_error(GBMM_ERR_NOMEM, "squarify temporary");
+    auto A_ = [&](int r, int cc) { return sub_view(A, r ? pt : 0, cc ? pt : 0, r ? K - pt : pt, cc ? M - pt : pt); };
+    auto B_ = [&](int r, int cc) { return sub_view(B, r ? pt : 0, cc ? pt : 0, r ? M - pt : pt, cc ? N - pt : pt); };
+    auto C_ = [&](const gbmm_mat &X, int r, int cc) {
+        return sub_view(X, r ? pt : 0, cc ? pt : 0, r ? K - pt : pt, cc ? N - pt : pt);
+    };
+    for (int r = 0; r < 2; r++)
+        for (int cc = 0; cc < 2; cc++) {
+            gbmm_mat cq = C_(C, r, cc);
+            if (cq.rows == 0 || cq.cols == 0) continue;
+            GBMM_TRY(squarify(c, method, cq, A_(r, 0), B_(0, cc)));
+            if (M > pt) {
+                gbmm_mat tq = C_(T, r, cc);
+                GBMM_TRY(squarify(c, method, tq, A_(r, 1), B_(1, cc)));
+                GBMM_TRY(launch_mat_addsub(cq, cq, tq, 0, c.s));
+            }
+        }
+    arena_release(c.h, mark);
+    return GBMM_OK;
+}
+
+static size_t squarify_ws(int method, int K, int M, int N, int base, int capT, int capP) {
+    if (K == 0 || M == 0 || N == 0) return 0;
+    if (method == GBMM_METHOD_NAIVE || K <= base || M <= base || N <= base) return 0;
+    if (K == M && M == N && remove_factors((unsigned)K, 2) <= (unsigned)base)
+        return rec_ws(method, K, levels_for(K, base), capT);
+    int mindim = std::min(std::min(K, M), N);
+    int pt = 1 << ilog2u((unsigned)mindim);
+    size_t own = mat_bytes((int64_t)K * N, capP);
+    size_t sub = 0;
+    int ks[2] = {pt, K - pt}, ms[2] = {pt, M - pt}, ns[2] = {pt, N - pt};
+    for (int r = 0; r < 2; r++)
+        for (int cc = 0; cc < 2; cc++)
+            for (int kk = 0; kk < 2; kk++) sub = std::max(sub, squarify_ws(method, ks[r], ms[kk], ns[cc], base, capT, capP));
+    return own + sub;
+}
+
+}  // namespace
+
+// Limbs a C view needs: product bound plus recursion headroom (each recursion
+// level can grow intermediate magnitudes by a few bits; 32 bits of headroom per
+// 8 levels are provided).
+static int limbs_needed(int la, int lb, int inner, int levels) {
+    int logm = 0;
+    while ((1 << logm) < std::max(inner, 1)) logm++;
+    int bits = 32 * (la + lb) + logm + 4 * levels + 2;
+    return (bits + 31) / 32;
+}
+
+extern "C" gbmm_status gbmm_matmul_limbs_needed(int32_t a_nlimbs, int32_t b_nlimbs, int32_t inner, const gbmm_opts *opts,
+                                                int32_t *nlimbs) {
+    if (!nlimbs) return set_error(GBMM_ERR_INVALID, "null pointer");
+    int levels = 0;
+    if (opts && opts->path != GBMM_PATH_CRT && opts->method != GBMM_METHOD_NAIVE) {
+        int cutoff = opts->cutoff > 0 ? opts->cutoff : 32;
+        levels = levels_for(inner, cutoff);
+        if (levels < 0) levels = 0;
+        levels += 2;  // squarify splits
+    }
+    *nlimbs = limbs_needed(a_nlimbs, b_nlimbs, inner, levels);
+    return GBMM_OK;
+}
+
+namespace gbmm {
+gbmm_status matmul_limb(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, int method, int cutoff,
+                        int accumulate, cudaStream_t s) {
+    if (accumulate && (method == GBMM_METHOD_NAIVE || a.rows != a.cols || a.cols != b.cols ||
+                       remove_factors((unsigned)a.rows, 2) > (unsigned)cutoff || method != GBMM_METHOD_WINOGRAD))
+        return launch_limb_matmul(c, a, b, 1, s);
+    RecCtx ctx;
+    ctx.h = h;
+    ctx.s = s;
+    ctx.cutoff = cutoff;
+    ctx.capSA = a.nlimbs + 1;
+    ctx.capSB = b.nlimbs + 1;
+    ctx.capP = c.nlimbs;
+    const int capT = std::max(std::max(ctx.capSA, ctx.capSB), ctx.capP);
+    size_t ws = accumulate ? rec_ws(method, a.rows, levels_for(a.rows, cutoff), capT)
+                           : squarify_ws(method, a.rows, a.cols, b.cols, cutoff, capT, ctx.capP);
+    if (ws) GBMM_TRY(arena_reserve(h, ws + 4096));
+    if (accumulate) return rec_square(ctx, method, c, a, b, a.rows, levels_for(a.rows, cutoff), 1);
+    return squarify(ctx, method, c, a, b);
+}
+}  // namespace gbmm
+
+extern "C" gbmm_status gbmm_matmul(gbmm_handle h, gbmm_mat c, gbmm_mat a, gbmm_mat b, const gbmm_opts *opts) {
+    if (!h) return set_error(GBMM_ERR_INVALID, "null handle");
+    GBMM_TRY(validate_mat(c, "C"));
+    GBMM_TRY(validate_mat(a, "A"));
+    GBMM_TRY(validate_mat(b, "B"));
+    if (a.rows != c.rows || b.cols != c.cols || a.cols != b.rows)
+        return set_error(GBMM_ERR_INVALID, "shape mismatch: C %dx%d, A %dx%d, B %dx%d", c.rows, c.cols, a.rows, a.cols,
+                         b.rows, b.cols);
+    if (c.limbs == a.limbs || c.limbs == b.limbs) return set_error(GBMM_ERR_INVALID, "C must not alias A or B");
+    gbmm_opts o;
+    memset(&o, 0, sizeof o);
+    if (opts) o = *opts;
+    if (o.method == 0) o.method = GBMM_METHOD_WINOGRAD;
+    const int cutoff = o.cutoff > 0 ? o.cutoff : h->limb_cutoff;
+    int path = o.path;
+    if (path == GBMM_PATH_AUTO) {
+        // plain heuristic: the CRT form pays off once products are large enough
+        // to amortise residue / reconstruction passes
+        int64_t work = (int64_t)a.rows * a.cols * b.cols * a.nlimbs * b.nlimbs;
+        path = (a.nlimbs + b.nlimbs >= 16 && work >= ((int64_t)1 << 22)) ? GBMM_PATH_CRT : GBMM_PATH_LIMB;
+    }
+    if (path == GBMM_PATH_CRT)
+        return crt_matmul(h, c, a, b, 32LL * a.nlimbs, 32LL * b.nlimbs, o.nprimes, o.accumulate, h->stream);
+    int levels = o.method == GBMM_METHOD_NAIVE ? 0 : levels_for(std::max(std::max(a.rows, a.cols), b.cols), cutoff) + 2;
+    int need = limbs_needed(a.nlimbs, b.nlimbs, a.cols, levels);
+    if (c.nlimbs < need && o.method != GBMM_METHOD_NAIVE) {
+        // The recursion needs headroom for intermediate values: run it into a
+        // workspace matrix with enough planes, then copy into C (the copy
+        // flags a capacity error if the exact result does not fit C).
+        const int capT = std::max(std::max(a.nlimbs + 1, b.nlimbs + 1), need);
+        size_t rec = o.accumulate ? rec_ws(o.method, a.rows, levels_for(a.rows, cutoff), capT)
+                                  : squarify_ws(o.method, a.rows, a.cols, b.cols, cutoff, capT, need);
+        GBMM_TRY(arena_reserve(h, mat_bytes((int64_t)c.rows * c.cols, need) + rec + 8192));
+        size_t mark = arena_mark(h);
+        gbmm_mat T;
+        if (!arena_mat(h, c.rows, c.cols, need, T)) return set_error(GBMM_ERR_NOMEM, "workspace");
+        if (o.accumulate) GBMM_TRY(launch_mat_copy(T, c, h->stream));
+        gbmm_status st = matmul_limb(h, T, a, b, o.method, cutoff, o.accumulate, h->stream);
+        if (st == GBMM_OK) st = launch_mat_copy(c, T, h->stream);
+        arena_release(h, mark);
+        return st;
+    }
+    return matmul_limb(h, c, a, b, o.method, cutoff, o.accumulate, h->stream);
+}
+
+extern "C" gbmm_status gbmm_mpn_mul(gbmm_handle h, uint32_t *rp, const uint32_t *up, int32_t un, const uint32_t *vp,
+                                    int32_t vn, int64_t ld, int64_t nb) {
+    if (!h) return set_error(GBMM_ERR_INVALID, "null handle");
+    if (un < vn || vn < 1) return set_error(GBMM_ERR_INVALID, "mpn_mul needs un >= vn >= 1");
+    const int s = un >> 1, n = un - s, t = vn - n;
+    const bool toom = vn >= 32 && 4 * un < 5 * vn && 0 < t && t <= s;  // balanced and large enough
+    if (!toom) return gbmm_mpn_mul_basecase(rp, up, un, vp, vn, ld, nb, h->stream);
+    size_t need = (size_t)gbmm_mpn_toom22_mul_itch(un, vn) * (size_t)ld * 4;
+    GBMM_TRY(arena_reserve(h, need + 4096));
+    size_t mark = arena_mark(h);
+    uint32_t *scratch = (uint32_t *)arena_alloc(h, need);
+    gbmm_status st = gbmm_mpn_toom22_mul(rp, up, un, vp, vn, scratch, ld, nb, h->stream);
+    arena_release(h, mark);
+    return st;
+}
+
+extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_t njobs, const gbmm_opts *opts) {
+    if (!h || (njobs > 0 && !jobs)) return set_error(GBMM_ERR_INVALID, "null argument");
+    for (int32_t j = 0; j < njobs; j++) {
+        gbmm_opts o;
+        memset(&o, 0, sizeof o);
+        if (opts) o = *opts;
+        o.path = jobs[j].path;
+        if (jobs[j].cutoff) o.cutoff = jobs[j].cutoff;
+        if (jobs[j].nprimes) o.nprimes = jobs[j].nprimes;
+        GBMM_TRY(gbmm_matmul(h, jobs[j].c, jobs[j].a, jobs[j].b, &o));
+        jobs[j].chosen_path = o.path;
+    }
+    return GBMM_OK;
+}

@@ -1,0 +1,963 @@
+// Batched limb kernels: the plain (non-CRT) form of gbmm.
+//
+// Numbers are sign-magnitude with 32-bit limbs in limb planes (structure of
+// arrays): limb i of operand b lives at p[i*ld + b], so neighbouring threads
+// touch neighbouring words.  This is the layout of the reference's interleaved
+// mode (mat-gpu/gmp-es-mpz.h:38-42) without the fixed capacity.
+//
+// Contents
+//   - warp carry-lookahead add_n / sub_n        (GMP mpn_add_n / mpn_sub_n)
+//   - mul_1 / addmul_1 / submul_1                 (GMP mpn_mul_1 family)
+//   - mul_basecase (column / product scanning)   (GMP mpn_mul_basecase)
+//   - toom22 (one Karatsuba split)               (GMP mpn_toom22_mul)
+//   - mpz add / sub / mul / addmul / submul       (GMP mpz semantics)
+//   - elementwise matrix add / sub                (mat-gpu add/sub_matrices_gpu)
+//   - the per-entry matrix product kernel         (mat-gpu launcher_mul/addmul)
+// All arithmetic algorithms are the textbook ones (Knuth TAOCP vol. 2 §4.3.1,
+// §4.3.3); the code is written for GB300, not translated from the reference.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbmm_internal.h"
+
+namespace gbmm {
+
+// ---- small device helpers ---------------------------------------------------------
+__device__ __forceinline__ int iabs_d(int x) { return x < 0 ? -x : x; }
+
+// 96-bit column accumulator (c0, c1, c2) += a * b.  One 32x32->64 wide multiply
+// accumulating into c0, then the high word and the carry.
+#define MAC96(c0, c1, c2, a, b)                                                   \
+    do {                                                                          \
+        uint64_t t_ = (uint64_t)(a) * (uint64_t)(b) + (uint64_t)(c0);             \
+        (c0) = (uint32_t)t_;                                                      \
+        uint64_t u_ = (uint64_t)(c1) + (t_ >> 32);                                \
+        (c1) = (uint32_t)u_;                                                      \
+        (c2) += (uint32_t)(u_ >> 32);                                             \
+    } while (0)
+
+struct MatArgs {
+    uint32_t *limbs;
+    int32_t *sizes;
+    int64_t rs, ld;
+    int32_t rows, cols, nlimbs;
+};
+static inline MatArgs margs(const gbmm_mat &m) {
+    MatArgs a;
+    a.limbs = m.limbs; a.sizes = m.sizes; a.rs = m.rs; a.ld = m.ld;
+    a.rows = m.rows; a.cols = m.cols; a.nlimbs = m.nlimbs;
+    return a;
+}
+
+// ======================================================================================
+// mpn add_n / sub_n with warp-level carry-lookahead.
+//
+// A CTA takes 32 operands.  A chunk of up to 32*Q limbs of those operands is
+// staged in shared memory with coalesced loads (limb-major rows, operand
+// columns).  Each warp then processes one operand at a time: lane l owns limbs
+// [l*Q, l*Q+Q) of the chunk, adds them with carry-in 0, and publishes
+// generate (carry out) and propagate (result all ones) bits with __ballot_sync.
+// The lane carry-ins are the carries of the 32-bit addition (G|P) + G + cin,
+// the classic carry-lookahead identity, so the whole chunk resolves in O(1)
+// warp steps instead of a 32*Q-long ripple.
+// ======================================================================================
+namespace {
+constexpr int CLA_Q = 4;                 // limbs per lane per chunk
+constexpr int CLA_CHUNK = 32 * CLA_Q;    // limbs per chunk
+constexpr int CLA_OPS = 32;              // operands per CTA
+}
+
+template <bool SUB>
+__global__ void __launch_bounds__(256) k_mpn_addsub_n_cla(uint32_t *rp, const uint32_t *up, const uint32_t *vp,
+                                                          int n, int64_t ld, int64_t nb, uint32_t *cy) {
+    __shared__ uint32_t su[CLA_CHUNK][CLA_OPS + 1];
+    __shared__ uint32_t sv[CLA_CHUNK][CLA_OPS + 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t b0 = (int64_t)blockIdx.x * CLA_OPS;
+    // carry state per operand handled by this warp (operands warp, warp+8, ...)
+    uint32_t carry[CLA_OPS / 8];
+#pragma unroll
+    for (int j = 0; j < CLA_OPS / 8; j++) carry[j] = 0;
+
+    for (int c0 = 0; c0 < n; c0 += CLA_CHUNK) {
+        const int clen = min(CLA_CHUNK, n - c0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < clen * CLA_OPS; q += blockDim.x) {
+            int i = q / CLA_OPS, b = q % CLA_OPS;
+            int64_t ob = b0 + b;
+            uint32_t x = 0, y = 0;
+            if (ob < nb) {
+                x = up[(int64_t)(c0 + i) * ld + ob];
+                y = vp[(int64_t)(c0 + i) * ld + ob];
+            }
+            su[i][b] = x;
+            sv[i][b] = y;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < CLA_OPS / 8; j++) {
+            const int b = warp + 8 * j;
+            uint32_t r[CLA_Q];
+            uint32_t g = 0, allsat = 1;
+            // local add / sub with carry-in 0
+            uint32_t c = 0;
+#pragma unroll
+            for (int t = 0; t < CLA_Q; t++) {
+                int i = lane * CLA_Q + t;
+                uint32_t x = i < clen ? su[i][b] : 0u, y = i < clen ? sv[i][b] : 0u;
+                if (!SUB) {
+                    uint64_t s = (uint64_t)x + y + c;
+                    r[t] = (uint32_t)s; c = (uint32_t)(s >> 32);
+                    allsat &= (r[t] == 0xFFFFFFFFu) | (i >= clen);
+                } else {
+                    uint64_t d = (uint64_t)x - y - c;
+                    r[t] = (uint32_t)d; c = (uint32_t)(d >> 63);
+                    allsat &= (r[t] == 0u) | (i >= clen);
+                }
+            }
+            g = c;
+            // lanes entirely past the chunk end neither generate nor propagate
+            if (lane * CLA_Q >= clen) { g = 0; allsat = 0; }
+            const uint32_t G = __ballot_sync(0xFFFFFFFFu, g);
+            const uint32_t P = __ballot_sync(0xFFFFFFFFu, allsat && !g);
+            const uint64_t sum = (uint64_t)(G | P) + (uint64_t)G + (uint64_t)carry[j];
+            const uint32_t cin_mask = (uint32_t)sum ^ P;  // carry into each lane (bit l)
+            // carry out of the chunk: out of the last lane that holds limbs
+            const int last_lane = (clen - 1) / CLA_Q;
+            uint32_t cin = (cin_mask >> lane) & 1u;
+            const uint32_t lane_out = g | (((P >> lane) & 1u) & cin);
+            const uint32_t chunk_out = __shfl_sync(0xFFFFFFFFu, lane_out, last_lane);
+#pragma unroll
+            for (int t = 0; t < CLA_Q; t++) {
+                if (!SUB) {
+                    uint64_t s = (uint64_t)r[t] + cin;
+                    r[t] = (uint32_t)s; cin = (uint32_t)(s >> 32);
+                } else {
+                    uint64_t d = (uint64_t)r[t] - cin;
+                    r[t] = (uint32_t)d; cin = (uint32_t)(d >> 63);
+                }
+                int i = lane * CLA_Q + t;
+                if (i < clen) su[i][b] = r[t];
+            }
+            carry[j] = chunk_out;
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < clen * CLA_OPS; q += blockDim.x) {
+            int i = q / CLA_OPS, b = q % CLA_OPS;
+            int64_t ob = b0 + b;
+            if (ob < nb) rp[(int64_t)(c0 + i) * ld + ob] = su[i][b];
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < CLA_OPS / 8; j++) {
+            int64_t ob = b0 + warp + 8 * j;
+            if (ob < nb) cy[ob] = carry[j];
+        }
+    }
+}
+
+// ---- mul_1 family: one thread per operand, serial over limbs (coalesced) -----------
+template <int OP>  // 0 mul_1, 1 addmul_1, 2 submul_1
+__global__ void k_mpn_mul1ops(uint32_t *rp, const uint32_t *up, int n, const uint32_t *vl, int64_t ld, int64_t nb,
+                              uint32_t *cy) {
+    int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const uint64_t v = vl[b];
+    uint64_t c = 0;
+    for (int i = 0; i < n; i++) {
+        uint64_t p = (uint64_t)up[(int64_t)i * ld + b] * v + c;
+        uint32_t lo = (uint32_t)p;
+        c = p >> 32;
+        if (OP == 0) {
+            rp[(int64_t)i * ld + b] = lo;
+        } else if (OP == 1) {
+            uint64_t s = (uint64_t)rp[(int64_t)i * ld + b] + lo;
+            rp[(int64_t)i * ld + b] = (uint32_t)s;
+            c += s >> 32;
+        } else {
+            uint32_t r = rp[(int64_t)i * ld + b];
+            rp[(int64_t)i * ld + b] = r - lo;
+            c += (r < lo);
+        }
+    }
+    cy[b] = (uint32_t)c;
+}
+
+// ---- per-thread strided mpn helpers (operand stride `s`) ------------------------------
+// r[0..un+vn) = u * v by product scanning: column t is summed in a 96-bit
+// accumulator and written once.
+__device__ void dev_mul_basecase(uint32_t *r, int64_t rs, const uint32_t *u, int un, int64_t us, const uint32_t *v,
+                                 int vn, int64_t vs) {
+    uint32_t c0 = 0, c1 = 0, c2 = 0;
+    for (int t = 0; t < un + vn - 1; t++) {
+        int i0 = t - vn + 1 > 0 ? t - vn + 1 : 0;
+        int i1 = t < un - 1 ? t : un - 1;
+        for (int i = i0; i <= i1; i++) {
+            uint32_t a = u[(int64_t)i * us], b = v[(int64_t)(t - i) * vs];
+            MAC96(c0, c1, c2, a, b);
+        }
+        r[(int64_t)t * rs] = c0;
+        c0 = c1; c1 = c2; c2 = 0;
+    }
+    r[(int64_t)(un + vn - 1) * rs] = c0;
+}
+__device__ int dev_cmp(const uint32_t *a, int64_t as, const uint32_t *b, int64_t bs, int n) {
+    for (int i = n - 1; i >= 0; i--) {
+        uint32_t x = a[(int64_t)i * as], y = b[(int64_t)i * bs];
+        if (x != y) return x < y ? -1 : 1;
+    }
+    return 0;
+}
+// r = a - b over n limbs (a >= b assumed by callers that care); returns borrow
+__device__ uint32_t dev_sub_n(uint32_t *r, int64_t rs, const uint32_t *a, int64_t as, const uint32_t *b, int64_t bs,
+                              int n) {
+    uint32_t br = 0;
+    for (int i = 0; i < n; i++) {
+        uint64_t d = (uint64_t)a[(int64_t)i * as] - b[(int64_t)i * bs] - br;
+        r[(int64_t)i * rs] = (uint32_t)d;
+        br = (uint32_t)(d >> 63);
+    }
+    return br;
+}
+// r (rn limbs) += a (an <= rn limbs), carry propagated inside rn; returns carry out
+__device__ uint32_t dev_add_into(uint32_t *r, int64_t rs, int rn, const uint32_t *a, int64_t as, int an) {
+    uint32_t c = 0;
+    int i = 0;
+    for (; i < an; i++) {
+        uint64_t s = (uint64_t)r[(int64_t)i * rs] + a[(int64_t)i * as] + c;
+        r[(int64_t)i * rs] = (uint32_t)s;
+        c = (uint32_t)(s >> 32);
+    }
+    for (; c && i < rn; i++) {
+        uint32_t x = r[(int64_t)i * rs] + 1;
+        r[(int64_t)i * rs] = x;
+        c = x == 0;
+    }
+    return c;
+}
+__device__ uint32_t dev_sub_from(uint32_t *r, int64_t rs, int rn, const uint32_t *a, int64_t as, int an) {
+    uint32_t br = 0;
+    int i = 0;
+    for (; i < an; i++) {
+        uint64_t d = (uint64_t)r[(int64_t)i * rs] - a[(int64_t)i * as] - br;
+        r[(int64_t)i * rs] = (uint32_t)d;
+        br = (uint32_t)(d >> 63);
+    }
+    for (; br && i < rn; i++) {
+        uint32_t x = r[(int64_t)i * rs];
+        r[(int64_t)i * rs] = x - 1;
+        br = x == 0;
+    }
+    return br;
+}
+
+__global__ void k_mpn_mul_basecase(uint32_t *rp, const uint32_t *up, int un, const uint32_t *vp, int vn, int64_t ld,
+                                   int64_t nb) {
+    int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    dev_mul_basecase(rp + b, ld, up + b, un, ld, vp + b, vn, ld);
+}
+
+// One Karatsuba split (Toom-2.2, Knuth 4.3.3): with a = a1 B^n + a0 and
+// b = b1 B^n + b0,  a*b = v0 + (v0 + vinf - vm1) B^n + vinf B^2n  where
+// v0 = a0 b0, vinf = a1 b1, vm1 = (a0 - a1)(b0 - b1).  Sub-products use the
+// basecase.  Scratch per operand: 6n + 2 limbs (itch).
+__global__ void k_mpn_toom22(uint32_t *pp, const uint32_t *ap, int an, const uint32_t *bp, int bn, uint32_t *scratch,
+                             int64_t ld, int64_t nb) {
+    int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const int s = an >> 1, n = an - s, t = bn - n;
+    const uint32_t *a = ap + b, *bb = bp + b;
+    uint32_t *p = pp + b, *w = scratch + b;
+    uint32_t *asm1 = w, *bsm1 = w + (int64_t)n * ld, *vm1 = w + (int64_t)2 * n * ld,
+             *mid = w + (int64_t)4 * n * ld;
+    // asm1 = |a0 - a1| (a1 has s limbs, zero-extended to n)
+    int neg = 0;
+    {
+        int c = 0;
+        // compare a0 (n limbs) with a1 (s limbs, top limb 0 if s < n)
+        for (int i = n - 1; i >= 0 && c == 0; i--) {
+            uint32_t x = a[(int64_t)i * ld], y = i < s ? a[(int64_t)(n + i) * ld] : 0u;
+            if (x != y) c = x < y ? -1 : 1;
+        }
+        uint32_t br = 0;
+        for (int i = 0; i < n; i++) {
+            uint32_t x = a[(int64_t)i * ld], y = i < s ? a[(int64_t)(n + i) * ld] : 0u;
+            if (c < 0) { uint32_t tt = x; x = y; y = tt; }
+            uint64_t d = (uint64_t)x - y - br;
+            asm1[(int64_t)i * ld] = (uint32_t)d;
+            br = (uint32_t)(d >> 63);
+        }
+        neg ^= c < 0;
+    }
+    {
+        int c = 0;
+        for (int i = n - 1; i >= 0 && c == 0; i--) {
+            uint32_t x = bb[(int64_t)i * ld], y = i < t ? bb[(int64_t)(n + i) * ld] : 0u;
+            if (x != y) c = x < y ? -1 : 1;
+        }
+        uint32_t br = 0;
+        for (int i = 0; i < n; i++) {
+            uint32_t x = bb[(int64_t)i * ld], y = i < t ? bb[(int64_t)(n + i) * ld] : 0u;
+            if (c < 0) { uint32_t tt = x; x = y; y = tt; }
+            uint64_t d = (uint64_t)x - y - br;
+            bsm1[(int64_t)i * ld] = (uint32_t)d;
+            br = (uint32_t)(d >> 63);
+        }
+        neg ^= c < 0;
+    }
+    dev_mul_basecase(vm1, ld, asm1, n, ld, bsm1, n, ld);                 // 2n limbs
+    dev_mul_basecase(p, ld, a, n, ld, bb, n, ld);                         // v0 -> p[0..2n)
+    if (s >= t) dev_mul_basecase(p + (int64_t)2 * n * ld, ld, a + (int64_t)n * ld, s, ld, bb + (int64_t)n * ld, t, ld);
+    else dev_mul_basecase(p + (int64_t)2 * n * ld, ld, bb + (int64_t)n * ld, t, ld, a + (int64_t)n * ld, s, ld);
+    // mid = v0 + vinf -/+ vm1   (2n + 1 limbs, nonnegative: equals a0 b1 + a1 b0)
+    for (int i = 0; i < 2 * n + 1; i++) mid[(int64_t)i * ld] = i < 2 * n ? p[(int64_t)i * ld] : 0u;
+    dev_add_into(mid, ld, 2 * n + 1, p + (int64_t)2 * n * ld, ld, s + t);
+    if (neg) dev_add_into(mid, ld, 2 * n + 1, vm1, ld, 2 * n);
+    else dev_sub_from(mid, ld, 2 * n + 1, vm1, ld, 2 * n);
+    dev_add_into(p + (int64_t)n * ld, ld, an + bn - n, mid, ld, 2 * n + 1 < an + bn - n ? 2 * n + 1 : an + bn - n);
+}
+
+// ======================================================================================
+// mpz layer (sign-magnitude with GMP size convention) on matrix views.
+// ======================================================================================
+__device__ __forceinline__ int64_t ent(const MatArgs &m, int64_t e) {
+    // elementwise ops treat the view as rows x cols; e is the row-major index
+    int64_t r = e / m.cols, c = e - r * m.cols;
+    return r * m.rs + c;
+}
+
+// w = u + sgn * v, one thread per entry.  For opposite signs the magnitudes
+// are compared from the top before the subtraction (GMP mpz_add semantics).
+__global__ void k_mpz_addsub(MatArgs W, MatArgs U, MatArgs V, int sub, int64_t count, uint32_t *err) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    const int64_t iw = ent(W, e), iu = ent(U, e), iv = ent(V, e);
+    int su = U.sizes[iu], sv = V.sizes[iv];
+    if (sub) sv = -sv;
+    const int un = iabs_d(su), vn = iabs_d(sv);
+    const uint32_t *up = U.limbs + iu, *vp = V.limbs + iv;
+    uint32_t *wp = W.limbs + iw;
+    int len = 0, neg = 0;
+    if ((su < 0) == (sv < 0) || un == 0 || vn == 0) {
+        neg = un ? (su < 0) : (sv < 0);
+        const int mx = un > vn ? un : vn;
+        if (mx > W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
+        uint32_t c = 0;
+        for (int i = 0; i < mx; i++) {
+            uint64_t s = (uint64_t)(i < un ? up[(int64_t)i * U.ld] : 0u) + (i < vn ? vp[(int64_t)i * V.ld] : 0u) + c;
+            wp[(int64_t)i * W.ld] = (uint32_t)s;
+            c = (uint32_t)(s >> 32);
+        }
+        len = mx;
+        if (c) {
+            if (mx >= W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
+            wp[(int64_t)mx * W.ld] = c;
+            len = mx + 1;
+        }
+    } else {
+        int cmp = un != vn ? (un < vn ? -1 : 1) : dev_cmp(up, U.ld, vp, V.ld, un);
+        const uint32_t *xp = up, *yp = vp;
+        int xn = un, yn = vn;
+        int64_t xs = U.ld, ys = V.ld;
+        neg = su < 0;
+        if (cmp < 0) { xp = vp; yp = up; xn = vn; yn = un; xs = V.ld; ys = U.ld; neg = sv < 0; }
+        if (xn > W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
+        uint32_t br = 0;
+        for (int i = 0; i < xn; i++) {
+            uint64_t d = (uint64_t)xp[(int64_t)i * xs] - (i < yn ? yp[(int64_t)i * ys] : 0u) - br;
+            uint32_t r = (uint32_t)d;
+            wp[(int64_t)i * W.ld] = r;
+            br = (uint32_t)(d >> 63);
+            if (r) len = i + 1;
+        }
+    }
+    for (int i = len; i < W.nlimbs; i++) wp[(int64_t)i * W.ld] = 0u;
+    W.sizes[iw] = len == 0 ? 0 : (neg ? -len : len);
+}
+
+// w = u * v (op 0), w += u * v (op 1), w -= u * v (op 2); one thread per entry.
+// The product is formed column by column (product scanning) and merged with w
+// in the same pass.  When w and the product have opposite signs the merge is a
+// two's complement subtraction; a final borrow means |uv| > |w| and the
+// written limbs are negated in place.
+__global__ void k_mpz_mulops(MatArgs W, MatArgs U, MatArgs V, int op, int64_t count, uint32_t *err) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    const int64_t iw = ent(W, e), iu = ent(U, e), iv = ent(V, e);
+    const int su = U.sizes[iu], sv = V.sizes[iv];
+    const int un = iabs_d(su), vn = iabs_d(sv);
+    const uint32_t *up = U.limbs + iu, *vp = V.limbs + iv;
+    uint32_t *wp = W.limbs + iw;
+    const int64_t ws = W.ld;
+    int sw = op == 0 ? 0 : W.sizes[iw];
+    const int wn = iabs_d(sw);
+    int pneg = (su < 0) ^ (sv < 0);
+    if (op == 2) pneg ^= 1;
+    const int pn = (un && vn) ? un + vn : 0;
+    const int subtract = wn && pn && ((sw < 0) != pneg);
+    const int rn = (pn > wn ? pn : wn) + (subtract ? 0 : 1);
+    const int cap = W.nlimbs;
+    // Result limbs [0, rn).  Limbs of w beyond wn are zero by invariant.  Limbs
+    // at t >= cap are not stored; hi_nz / hi_ones remember whether any of them
+    // is nonzero / all of them are all-ones, which decides overflow below.
+    uint32_t c0 = 0, c1 = 0, c2 = 0;  // product column accumulator
+    uint32_t carry = 0;              // merge carry / borrow
+    int top = 0;
+    bool hi_nz = false, hi_ones = true;
+    for (int t = 0; t < rn; t++) {
+        uint32_t pl = 0;
+        if (t < pn - 1) {
+            int i0 = t - vn + 1 > 0 ? t - vn + 1 : 0;
+            int i1 = t < un - 1 ? t : un - 1;
+            for (int i = i0; i <= i1; i++) MAC96(c0, c1, c2, up[(int64_t)i * U.ld], vp[(int64_t)(t - i) * V.ld]);
+            pl = c0; c0 = c1; c1 = c2; c2 = 0;
+        } else if (t == pn - 1) {
+            pl = c0;
+        }
+        uint32_t wl = (op != 0 && t < wn) ? wp[(int64_t)t * ws] : 0u;
+        uint32_t r;
+        if (!subtract) {
+            uint64_t s = (uint64_t)wl + pl + carry;
+            r = (uint32_t)s; carry = (uint32_t)(s >> 32);
+        } else {
+            uint64_t d = (uint64_t)wl - pl - carry;
+            r = (uint32_t)d; carry = (uint32_t)(d >> 63);
+        }
+        if (t < cap) {
+            wp[(int64_t)t * ws] = r;
+            if (r) top = t + 1;
+        } else {
+            hi_nz |= r != 0u;
+            hi_ones &= r == 0xFFFFFFFFu;
+        }
+    }
+    int neg = op == 0 ? pneg : (wn ? (sw < 0) : pneg);
+    if (subtract && carry) {
+        // negative: |result| = 2^(32 rn) - r; it fits in cap limbs iff the
+        // dropped high limbs are all ones and the kept low part is nonzero
+        if (rn > cap && !(hi_ones && top != 0)) { atomicOr(err, DEVERR_CAPACITY); return; }
+        neg = pneg;
+        uint32_t c = 1;
+        top = 0;
+        const int kept = rn < cap ? rn : cap;
+        for (int t = 0; t < kept; t++) {
+            uint64_t s = (uint64_t)(~wp[(int64_t)t * ws]) + c;
+            uint32_t r = (uint32_t)s;
+            c = (uint32_t)(s >> 32);
+            wp[(int64_t)t * ws] = r;
+            if (r) top = t + 1;
+        }
+    } else if (hi_nz) {
+        atomicOr(err, DEVERR_CAPACITY);
+        return;
+    }
+    for (int t = rn < cap ? rn : cap; t < cap; t++) wp[(int64_t)t * ws] = 0u;
+    W.sizes[iw] = top == 0 ? 0 : (neg ? -top : top);
+}
+
+__global__ void k_mat_zero(MatArgs C, int64_t count) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    const int64_t ic = ent(C, e);
+    for (int i = 0; i < C.nlimbs; i++) C.limbs[(int64_t)i * C.ld + ic] = 0u;
+    C.sizes[ic] = 0;
+}
+
+// dst = src (entries copied with their sizes; planes beyond the value zeroed)
+__global__ void k_mat_copy(MatArgs D, MatArgs S, int64_t count, uint32_t *err) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    const int64_t id = ent(D, e), is = ent(S, e);
+    const int ss = S.sizes[is], n = iabs_d(ss);
+    if (n > D.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
+    for (int i = 0; i < D.nlimbs; i++) D.limbs[(int64_t)i * D.ld + id] = i < n ? S.limbs[(int64_t)i * S.ld + is] : 0u;
+    D.sizes[id] = ss;
+}
+
+__global__ void k_max_size(MatArgs A, int64_t count, int32_t *out) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int v = 0;
+    if (e < count) v = iabs_d(A.sizes[ent(A, e)]);
+    for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    if ((threadIdx.x & 31) == 0 && v) atomicMax(out, v);
+}
+
+// ======================================================================================
+// Per-entry matrix product  C (K x N) = A (K x M) * B (M x N)   [or C += A*B]
+//
+// The reference gives one thread a whole C[y][x] and runs mpz_mul followed by
+// M-1 serial mpz_addmul calls (mat-gpu/mat-core.h:31-53).  Here a group of G
+// threads shares one output entry: the La x Lb limb-product square of every
+// term A[y][k]*B[k][x] is tiled into R x R blocks, thread (I, J) of the group
+// owns block (I, J) for all k, and accumulates its 2R-1 partial columns in
+// 96-bit registers with no carry propagation inside the k loop.  Products
+// with a positive and a negative sign go to separate accumulator sets (the
+// sign is uniform across the group, so the branch is warp-uniform when a
+// group spans whole warps).  After the k loop the group reduces its partial
+// columns in shared memory (64-bit atomics on 32-bit words), one thread per
+// entry propagates carries, subtracts the negative sum from the positive sum,
+// and writes the sign-magnitude result.  A/B limbs for a chunk of KC terms
+// are staged in shared memory with loads that are coalesced along k (A) and
+// along x (B), and reused by every thread of the CTA's TY x TX entries.
+// ======================================================================================
+namespace {
+constexpr int MM_THREADS = 256;
+constexpr int MM_KC = 8;
+}
+
+struct MMCfg {
+    int R;        // block edge in limbs
+    int La, Lb;   // padded limb counts (multiples of R)
+    int G, Gp;    // threads per entry (active, padded)
+    int TY, TX;   // entries per CTA
+    int M;        // inner dimension
+    int accumulate;
+};
+
+// Final step of one output entry: pl / nl hold the magnitudes of the positive
+// and negative partial sums (L2 limbs each).  Optionally adds the old C, then
+// writes sign(P-N) * |P-N| as a normalized sign-magnitude entry.
+__device__ void finish_entry(uint32_t *pl, uint32_t *nl, int L2, const MatArgs &C, int64_t ic, int accumulate,
+                             uint32_t *err) {
+    if (accumulate) {
+        const int sc = C.sizes[ic];
+        const int cn = iabs_d(sc);
+        uint32_t *dst = sc < 0 ? nl : pl;
+        uint32_t c = 0;
+        for (int t = 0; t < L2; t++) {
+            uint64_t s = (uint64_t)dst[t] + (t < cn ? C.limbs[(int64_t)t * C.ld + ic] : 0u) + c;
+            dst[t] = (uint32_t)s;
+            c = (uint32_t)(s >> 32);
+        }
+        if (c || cn > L2) { atomicOr(err, DEVERR_CAPACITY); return; }
+    }
+    int cmp = 0;
+    for (int t = L2 - 1; t >= 0 && cmp == 0; t--)
+        if (pl[t] != nl[t]) cmp = pl[t] < nl[t] ? -1 : 1;
+    const uint32_t *xp = cmp >= 0 ? pl : nl, *yp = cmp >= 0 ? nl : pl;
+    int top = 0;
+    uint32_t br = 0;
+    uint32_t *cl = C.limbs + ic;
+    for (int t = 0; t < L2; t++) {
+        uint64_t d = (uint64_t)xp[t] - yp[t] - br;
+        uint32_t r = (uint32_t)d;
+        br = (uint32_t)(d >> 63);
+        if (r) top = t + 1;
+        if (t < C.nlimbs) cl[(int64_t)t * C.ld] = r;
+        else if (r) { atomicOr(err, DEVERR_CAPACITY); return; }
+    }
+    for (int t = L2; t < C.nlimbs; t++) cl[(int64_t)t * C.ld] = 0u;
+    C.sizes[ic] = top == 0 ? 0 : (cmp < 0 ? -top : top);
+}
+
+template <int R>
+__global__ void __launch_bounds__(MM_THREADS) k_limb_matmul(MatArgs C, MatArgs A, MatArgs B, MMCfg cfg,
+                                                            uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int La = cfg.La, Lb = cfg.Lb, TY = cfg.TY, TX = cfg.TX;
+    const int sa_stride = La + 4, sb_stride = Lb + 4;  // +4 words: fewer bank conflicts, 16B aligned rows
+    uint32_t *sA = reinterpret_cast<uint32_t *>(smem_raw);                 // [TY][KC][La+4]
+    uint32_t *sB = sA + TY * MM_KC * sa_stride;                            // [KC][TX][Lb+4]
+    int32_t *ssA = reinterpret_cast<int32_t *>(sB + MM_KC * TX * sb_stride);  // [TY][KC]
+    int32_t *ssB = ssA + TY * MM_KC;                                       // [KC][TX]
+
+    const int tid = threadIdx.x;
+    const int g = tid / cfg.Gp, lt = tid % cfg.Gp;
+    const int EPC = TY * TX;
+    const bool has_entry = g < EPC;
+    const int ty = has_entry ? g / TX : 0, tx = has_entry ? g % TX : 0;
+    const int y0 = blockIdx.y * TY, x0 = blockIdx.x * TX;
+    const int y = y0 + ty, x = x0 + tx;
+    const bool valid = has_entry && y < C.rows && x < C.cols;
+    const int nbB = Lb / R;
+    const bool active = valid && lt < cfg.G;
+    const int I0 = active ? lt / nbB : 0, J0 = active ? lt % nbB : 0;
+
+    uint32_t P[2 * R - 1][3], Nn[2 * R - 1][3];
+#pragma unroll
+    for (int c = 0; c < 2 * R - 1; c++) {
+        P[c][0] = P[c][1] = P[c][2] = 0;
+        Nn[c][0] = Nn[c][1] = Nn[c][2] = 0;
+    }
+
+    const int M = cfg.M;
+    for (int k0 = 0; k0 < M; k0 += MM_KC) {
+        const int kc = min(MM_KC, M - k0);
+        __syncthreads();
+        // stage A[y0..y0+TY)[k0..k0+kc) : consecutive threads walk k (contiguous in a plane row)
+        for (int q = tid; q < TY * La * MM_KC; q += MM_THREADS) {
+            int kk = q % MM_KC, rest = q / MM_KC, i = rest % La, tyy = rest / La;
+            int yy = y0 + tyy;
+            uint32_t v = 0;
+            if (kk < kc && yy < A.rows && i < A.nlimbs) v = A.limbs[(int64_t)i * A.ld + (int64_t)yy * A.rs + k0 + kk];
+            sA[(tyy * MM_KC + kk) * sa_stride + i] = v;
+        }
+        // stage B[k0..k0+kc)[x0..x0+TX) : consecutive threads walk x
+        for (int q = tid; q < MM_KC * Lb * TX; q += MM_THREADS) {
+            int txx = q % TX, rest = q / TX, i = rest % Lb, kk = rest / Lb;
+            int xx = x0 + txx;
+            uint32_t v = 0;
+            if (kk < kc && xx < B.cols && i < B.nlimbs) v = B.limbs[(int64_t)i * B.ld + (int64_t)(k0 + kk) * B.rs + xx];
+            sB[(kk * TX + txx) * sb_stride + i] = v;
+        }
+        for (int q = tid; q < TY * MM_KC; q += MM_THREADS) {
+            int kk = q % MM_KC, tyy = q / MM_KC, yy = y0 + tyy;
+            ssA[q] = (kk < kc && yy < A.rows) ? A.sizes[(int64_t)yy * A.rs + k0 + kk] : 0;
+        }
+        for (int q = tid; q < MM_KC * TX; q += MM_THREADS) {
+            int txx = q % TX, kk = q / TX, xx = x0 + txx;
+            ssB[q] = (kk < kc && xx < B.cols) ? B.sizes[(int64_t)(k0 + kk) * B.rs + xx] : 0;
+        }
+        __syncthreads();
+        if (active) {
+            for (int kk = 0; kk < kc; kk++) {
+                const int sa = ssA[ty * MM_KC + kk], sb = ssB[kk * TX + tx];
+                if (sa == 0 || sb == 0) continue;
+                if (I0 * R >= iabs_d(sa) || J0 * R >= iabs_d(sb)) continue;
+                const uint32_t *pa = sA + (ty * MM_KC + kk) * sa_stride + I0 * R;
+                const uint32_t *pb = sB + (kk * TX + tx) * sb_stride + J0 * R;
+                uint32_t a[R], b[R];
+                if (R >= 4) {
+#pragma unroll
+                    for (int v = 0; v < R; v += 4) {
+                        uint4 qa = *reinterpret_cast<const uint4 *>(pa + v);
+                        uint4 qb = *reinterpret_cast<const uint4 *>(pb + v);
+                        a[v] = qa.x; a[v + 1] = qa.y; a[v + 2] = qa.z; a[v + 3] = qa.w;
+                        b[v] = qb.x; b[v + 1] = qb.y; b[v + 2] = qb.z; b[v + 3] = qb.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int v = 0; v < R; v++) { a[v] = pa[v]; b[v] = pb[v]; }
+                }
+                if ((sa ^ sb) >= 0) {
+#pragma unroll
+                    for (int i = 0; i < R; i++)
+#pragma unroll
+                        for (int j = 0; j < R; j++) MAC96(P[i + j][0], P[i + j][1], P[i + j][2], a[i], b[j]);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < R; i++)
+#pragma unroll
+                        for (int j = 0; j < R; j++) MAC96(Nn[i + j][0], Nn[i + j][1], Nn[i + j][2], a[i], b[j]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- reduction of partial columns --------------------------------------------
+    const int Lc = La + Lb;  // product columns
+    if (cfg.G == 1) {
+        // one thread owns the whole entry: its registers already hold every column
+        if (!valid) return;
+        uint32_t pl[2 * R + 2], nl[2 * R + 2];
+        unsigned __int128 cp = 0, cn = 0;
+#pragma unroll
+        for (int t = 0; t < 2 * R - 1; t++) {
+            cp += (unsigned __int128)P[t][0] + ((unsigned __int128)P[t][1] << 32) + ((unsigned __int128)P[t][2] << 64);
+            cn += (unsigned __int128)Nn[t][0] + ((unsigned __int128)Nn[t][1] << 32) + ((unsigned __int128)Nn[t][2] << 64);
+            pl[t] = (uint32_t)cp; cp >>= 32;
+            nl[t] = (uint32_t)cn; cn >>= 32;
+        }
+        pl[2 * R - 1] = (uint32_t)cp; pl[2 * R] = (uint32_t)(cp >> 32); pl[2 * R + 1] = 0;
+        nl[2 * R - 1] = (uint32_t)cn; nl[2 * R] = (uint32_t)(cn >> 32); nl[2 * R + 1] = 0;
+        finish_entry(pl, nl, 2 * R + 2, C, (int64_t)y * C.rs + x, cfg.accumulate, err);
+        return;
+    }
+    unsigned long long *red = reinterpret_cast<unsigned long long *>(smem_raw);  // [EPC][2][Lc][3]
+    uint32_t *limbs_buf = reinterpret_cast<uint32_t *>(red + (size_t)EPC * 2 * Lc * 3);  // [EPC][2][Lc+2]
+    for (int q = tid; q < EPC * 2 * Lc * 3; q += MM_THREADS) red[q] = 0ull;
+    __syncthreads();
+    if (active) {
+        unsigned long long *rp = red + (size_t)g * 2 * Lc * 3;
+        const int cb = (I0 + J0) * R;
+#pragma unroll
+        for (int c = 0; c < 2 * R - 1; c++) {
+            const int col = cb + c;
+            if (P[c][0] | P[c][1] | P[c][2]) {
+                atomicAdd(&rp[(0 * Lc + col) * 3 + 0], (unsigned long long)P[c][0]);
+                atomicAdd(&rp[(0 * Lc + col) * 3 + 1], (unsigned long long)P[c][1]);
+                atomicAdd(&rp[(0 * Lc + col) * 3 + 2], (unsigned long long)P[c][2]);
+            }
+            if (Nn[c][0] | Nn[c][1] | Nn[c][2]) {
+                atomicAdd(&rp[(1 * Lc + col) * 3 + 0], (unsigned long long)Nn[c][0]);
+                atomicAdd(&rp[(1 * Lc + col) * 3 + 1], (unsigned long long)Nn[c][1]);
+                atomicAdd(&rp[(1 * Lc + col) * 3 + 2], (unsigned long long)Nn[c][2]);
+            }
+        }
+    }
+    __syncthreads();
+    if (!(valid && lt == 0)) return;
+
+    // ---- carry propagation, then P - N written back (one thread per entry) -----------
+    const unsigned long long *rp = red + (size_t)g * 2 * Lc * 3;
+    uint32_t *pl = limbs_buf + (size_t)g * 2 * (Lc + 2);
+    uint32_t *nl = pl + (Lc + 2);
+    for (int s = 0; s < 2; s++) {
+        uint32_t *dst = s ? nl : pl;
+        // value of column t = w0 + w1 2^32 + w2 2^64 ; the running carry fits in 128 bits
+        unsigned __int128 carry = 0;
+        for (int t = 0; t < Lc; t++) {
+            const unsigned long long *w = rp + (s * Lc + t) * 3;
+            unsigned __int128 v = carry + (unsigned __int128)w[0] + ((unsigned __int128)w[1] << 32) +
+                                  ((unsigned __int128)w[2] << 64);
+            dst[t] = (uint32_t)v;
+            carry = v >> 32;
+        }
+        dst[Lc] = (uint32_t)carry;
+        dst[Lc + 1] = (uint32_t)(carry >> 32);
+    }
+    finish_entry(pl, nl, Lc + 2, C, (int64_t)y * C.rs + x, cfg.accumulate, err);
+}
+
+// ---- host launchers ---------------------------------------------------------------------
+static inline int64_t nentries(const gbmm_mat &m) { return (int64_t)m.rows * m.cols; }
+static inline unsigned grid1(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+gbmm_status launch_mat_addsub(const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, int sub, cudaStream_t s) {
+    const int64_t n = nentries(c);
+    if (n == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpz_addsub", s);
+    k_mpz_addsub<<<grid1(n, 256), 256, 0, s>>>(margs(c), margs(a), margs(b), sub, n, device_error_word());
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+gbmm_status launch_mat_zero(const gbmm_mat &c, cudaStream_t s) {
+    const int64_t n = nentries(c);
+    if (n == 0) return GBMM_OK;
+    LaunchScope ls_("k_mat_zero", s);
+    k_mat_zero<<<grid1(n, 256), 256, 0, s>>>(margs(c), n);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+gbmm_status launch_mat_copy(const gbmm_mat &dst, const gbmm_mat &src, cudaStream_t s) {
+    const int64_t n = nentries(dst);
+    if (n == 0) return GBMM_OK;
+    LaunchScope ls_("k_mat_copy", s);
+    k_mat_copy<<<grid1(n, 256), 256, 0, s>>>(margs(dst), margs(src), n, device_error_word());
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+gbmm_status launch_max_size(const gbmm_mat &a, int32_t *d_out, cudaStream_t s) {
+    const int64_t n = nentries(a);
+    GBMM_CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(int32_t), s));
+    if (n == 0) return GBMM_OK;
+    LaunchScope ls_("k_max_size", s);
+    k_max_size<<<grid1(n, 256), 256, 0, s>>>(margs(a), n, d_out);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+gbmm_status launch_mpz_mulops(const gbmm_mat &w, const gbmm_mat &u, const gbmm_mat &v, int op, cudaStream_t s) {
+    const int64_t n = nentries(w);
+    if (n == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpz_mulops", s);
+    k_mpz_mulops<<<grid1(n, 128), 128, 0, s>>>(margs(w), margs(u), margs(v), op, n, device_error_word());
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+static int roundup(int x, int m) { return (x + m - 1) / m * m; }
+
+// Picks the block edge R and group size for limb counts la x lb.
+static bool choose_mm(int la, int lb, MMCfg &cfg) {
+    la = la < 1 ? 1 : la;
+    lb = lb < 1 ? 1 : lb;
+    const int cand[3] = {8, 4, 2};
+    for (int ci = 0; ci < 3; ci++) {
+        int R = cand[ci];
+        int pa = roundup(la, R), pb = roundup(lb, R);
+        int G = (pa / R) * (pb / R);
+        if (G >= 32 && G <= MM_THREADS) {
+            cfg.R = R; cfg.La = pa; cfg.Lb = pb; cfg.G = G; cfg.Gp = roundup(G, 32);
+            return true;
+        }
+    }
+    int mx = la > lb ? la : lb;
+    if (mx <= 8) {
+        int R = mx <= 1 ? 1 : mx <= 2 ? 2 : mx <= 4 ? 4 : 8;
+        cfg.R = R; cfg.La = R; cfg.Lb = R; cfg.G = 1; cfg.Gp = 1;
+        return true;
+    }
+    {
+        int R = 2, pa = roundup(la, R), pb = roundup(lb, R), G = (pa / R) * (pb / R);
+        if (G <= MM_THREADS) {
+            cfg.R = R; cfg.La = pa; cfg.Lb = pb; cfg.G = G; cfg.Gp = roundup(G, 32);
+            return true;
+        }
+    }
+    return false;
+}
+
+static size_t mm_smem(const MMCfg &c) {
+    size_t stage = (size_t)c.TY * MM_KC * (c.La + 4) * 4 + (size_t)MM_KC * c.TX * (c.Lb + 4) * 4 +
+                   (size_t)(c.TY + c.TX) * MM_KC * 4;
+    const int EPC = c.TY * c.TX, Lc = c.La + c.Lb;
+    size_t red = c.G == 1 ? 0 : (size_t)EPC * 2 * Lc * 3 * 8 + (size_t)EPC * 2 * (Lc + 2) * 4;
+    return stage > red ? stage : red;
+}
+
+gbmm_status launch_limb_matmul(const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, int accumulate,
+                               cudaStream_t s) {
+    if (c.rows == 0 || c.cols == 0) return GBMM_OK;
+    if (a.cols == 0) {
+        if (accumulate) return GBMM_OK;
+        return launch_mat_zero(c, s);
+    }
+    MMCfg cfg;
+    if (!choose_mm(a.nlimbs, b.nlimbs, cfg))
+        return set_error(GBMM_ERR_UNSUPPORTED, "limb matmul: %d x %d limb entries exceed the per-entry kernel", a.nlimbs,
+                         b.nlimbs);
+    const int EPC = cfg.Gp >= MM_THREADS ? 1 : MM_THREADS / cfg.Gp;
+    int TY = 1;
+    while (TY * TY * 4 <= EPC) TY *= 2;
+    cfg.TY = TY;
+    cfg.TX = EPC / TY;
+    cfg.M = a.cols;
+    cfg.accumulate = accumulate;
+    size_t smem = mm_smem(cfg);
+    if (smem > 200 * 1024) return set_error(GBMM_ERR_UNSUPPORTED, "limb matmul: shared memory %zu too large", smem);
+    dim3 grid((unsigned)((c.cols + cfg.TX - 1) / cfg.TX), (unsigned)((c.rows + cfg.TY - 1) / cfg.TY));
+    uint32_t *err = device_error_word();
+#define LAUNCH_R(RR)                                                                                   \
+    do {                                                                                               \
+        if (smem > 48 * 1024)                                                                          \
+            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_limb_matmul<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                               (int)smem));                                            \
+        LaunchScope ls_("k_limb_matmul", s);                                                            \
+        k_limb_matmul<RR><<<grid, MM_THREADS, smem, s>>>(margs(c), margs(a), margs(b), cfg, err);     \
+    } while (0)
+    switch (cfg.R) {
+        case 1: LAUNCH_R(1); break;
+        case 2: LAUNCH_R(2); break;
+        case 4: LAUNCH_R(4); break;
+        default: LAUNCH_R(8); break;
+    }
+#undef LAUNCH_R
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+}  // namespace gbmm
+
+// ======================================================================================
+// C ABI: batched mpn / mpz entry points
+// ======================================================================================
+using namespace gbmm;
+
+static gbmm_status check_batch(const void *a, const void *b, int64_t ld, int64_t nb, int n) {
+    if (!a || !b) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (nb < 0 || n < 0 || ld < nb) return set_error(GBMM_ERR_INVALID, "bad batch shape n=%d ld=%lld nb=%lld", n,
+                                                     (long long)ld, (long long)nb);
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_mpn_add_n(uint32_t *rp, const uint32_t *up, const uint32_t *vp, int32_t n, int64_t ld,
+                                      int64_t nb, uint32_t *cy, void *stream) {
+    GBMM_TRY(check_batch(rp, up, ld, nb, n));
+    if (!vp || !cy) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_addsub_n_cla", as_stream(stream));
+    k_mpn_addsub_n_cla<false><<<grid1(nb, CLA_OPS), 256, 0, as_stream(stream)>>>(rp, up, vp, n, ld, nb, cy);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+extern "C" gbmm_status gbmm_mpn_sub_n(uint32_t *rp, const uint32_t *up, const uint32_t *vp, int32_t n, int64_t ld,
+                                      int64_t nb, uint32_t *cy, void *stream) {
+    GBMM_TRY(check_batch(rp, up, ld, nb, n));
+    if (!vp || !cy) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_addsub_n_cla", as_stream(stream));
+    k_mpn_addsub_n_cla<true><<<grid1(nb, CLA_OPS), 256, 0, as_stream(stream)>>>(rp, up, vp, n, ld, nb, cy);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+template <int OP>
+static gbmm_status mul1_entry(uint32_t *rp, const uint32_t *up, int32_t n, const uint32_t *vl, int64_t ld, int64_t nb,
+                              uint32_t *cy, void *stream) {
+    GBMM_TRY(check_batch(rp, up, ld, nb, n));
+    if (!vl || !cy) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_mul1ops", as_stream(stream));
+    k_mpn_mul1ops<OP><<<grid1(nb, 256), 256, 0, as_stream(stream)>>>(rp, up, n, vl, ld, nb, cy);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+extern "C" gbmm_status gbmm_mpn_mul_1(uint32_t *rp, const uint32_t *up, int32_t n, const uint32_t *vl, int64_t ld,
+                                      int64_t nb, uint32_t *cy, void *stream) {
+    return mul1_entry<0>(rp, up, n, vl, ld, nb, cy, stream);
+}
+extern "C" gbmm_status gbmm_mpn_addmul_1(uint32_t *rp, const uint32_t *up, int32_t n, const uint32_t *vl, int64_t ld,
+                                         int64_t nb, uint32_t *cy, void *stream) {
+    return mul1_entry<1>(rp, up, n, vl, ld, nb, cy, stream);
+}
+extern "C" gbmm_status gbmm_mpn_submul_1(uint32_t *rp, const uint32_t *up, int32_t n, const uint32_t *vl, int64_t ld,
+                                         int64_t nb, uint32_t *cy, void *stream) {
+    return mul1_entry<2>(rp, up, n, vl, ld, nb, cy, stream);
+}
+extern "C" gbmm_status gbmm_mpn_mul_basecase(uint32_t *rp, const uint32_t *up, int32_t un, const uint32_t *vp,
+                                             int32_t vn, int64_t ld, int64_t nb, void *stream) {
+    GBMM_TRY(check_batch(rp, up, ld, nb, un));
+    if (!vp) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (un < vn || vn < 1) return set_error(GBMM_ERR_INVALID, "mul_basecase needs un >= vn >= 1 (un=%d vn=%d)", un, vn);
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_mul_basecase", as_stream(stream));
+    k_mpn_mul_basecase<<<grid1(nb, 128), 128, 0, as_stream(stream)>>>(rp, up, un, vp, vn, ld, nb);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+extern "C" int32_t gbmm_mpn_toom22_mul_itch(int32_t an, int32_t bn) {
+    (void)bn;
+    int32_t n = an - (an >> 1);
+    return 6 * n + 2;
+}
+extern "C" gbmm_status gbmm_mpn_toom22_mul(uint32_t *pp, const uint32_t *ap, int32_t an, const uint32_t *bp, int32_t bn,
+                                           uint32_t *scratch, int64_t ld, int64_t nb, void *stream) {
+    GBMM_TRY(check_batch(pp, ap, ld, nb, an));
+    if (!bp || !scratch) return set_error(GBMM_ERR_INVALID, "null pointer");
+    const int s = an >> 1, n = an - s, t = bn - n;
+    if (an < bn || !(0 < s && s <= n && s >= n - 1) || !(0 < t && t <= s))
+        return set_error(GBMM_ERR_INVALID, "toom22 preconditions violated (an=%d bn=%d)", an, bn);
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_toom22", as_stream(stream));
+    k_mpn_toom22<<<grid1(nb, 128), 128, 0, as_stream(stream)>>>(pp, ap, an, bp, bn, scratch, ld, nb);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+static gbmm_status check_elementwise(const gbmm_mat &w, const gbmm_mat &u, const gbmm_mat &v) {
+    GBMM_TRY(validate_mat(w, "w"));
+    GBMM_TRY(validate_mat(u, "u"));
+    GBMM_TRY(validate_mat(v, "v"));
+    if (u.rows != w.rows || v.rows != w.rows || u.cols != w.cols || v.cols != w.cols)
+        return set_error(GBMM_ERR_INVALID, "elementwise shapes differ");
+    return GBMM_OK;
+}
+extern "C" gbmm_status gbmm_mpz_add(gbmm_mat w, gbmm_mat u, gbmm_mat v, void *stream) {
+    GBMM_TRY(check_elementwise(w, u, v));
+    return launch_mat_addsub(w, u, v, 0, as_stream(stream));
+}
+extern "C" gbmm_status gbmm_mpz_sub(gbmm_mat w, gbmm_mat u, gbmm_mat v, void *stream) {
+    GBMM_TRY(check_elementwise(w, u, v));
+    return launch_mat_addsub(w, u, v, 1, as_stream(stream));
+}
+static gbmm_status mulops_entry(gbmm_mat w, gbmm_mat u, gbmm_mat v, int op, void *stream) {
+    GBMM_TRY(check_elementwise(w, u, v));
+    if (w.limbs == u.limbs || w.limbs == v.limbs)
+        return set_error(GBMM_ERR_INVALID, "mpz mul: w must not alias u or v (as gpu_mpz_mul, mpz-mul.cu:97-101)");
+    return launch_mpz_mulops(w, u, v, op, as_stream(stream));
+}
+extern "C" gbmm_status gbmm_mpz_mul(gbmm_mat w, gbmm_mat u, gbmm_mat v, void *stream) {
+    return mulops_entry(w, u, v, 0, stream);
+}
+extern "C" gbmm_status gbmm_mpz_addmul(gbmm_mat w, gbmm_mat u, gbmm_mat v, void *stream) {
+    return mulops_entry(w, u, v, 1, stream);
+}
+extern "C" gbmm_status gbmm_mpz_submul(gbmm_mat w, gbmm_mat u, gbmm_mat v, void *stream) {
+    return mulops_entry(w, u, v, 2, stream);
+}

@@ -1,0 +1,413 @@
+#!/usr/bin/env python
+"""Benchmark: exact signed big-integer matrix multiplication C = A*B.
+
+One step = one complete exact product through gbmm's public C ABI
+(gbmm_matmul) on synthetic seeded matrices already resident in HBM.  The
+metric is 64-bit limb-MACs per second:
+    limb-MACs = sum_k (sum_i L64(A_ik)) * (sum_j L64(B_kj)),
+L64 = 64-bit limb count of an entry's magnitude (schoolbook-equivalent work,
+so Winograd / Karatsuba / CRT savings count as speed).
+
+`--impl reference` times the reference's CPU implementation of the path
+instead (the mat-cpu algorithm; the reference binary when it was built on this
+machine, else the CPU restatement in oracle/) on a bounded row sample of the
+same workload with all host cores.
+
+Multi-GPU: the product does not shard across this run's GPUs; under torchrun
+every rank runs an independent replica (weak scaling) and value is the
+aggregate over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "bachelor-thesis_gb300")
+for _p in (PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WORKLOADS = {
+    # 256x256x256, 2048-bit signed entries, 5% exact zeros, 5% shortened to 64 bits
+    "cfg2": dict(K=256, M=256, N=256, bits=2048, zero=0.05, short=0.05, short_bits=64, cutoff=32,
+                 label="256x256x256 2048-bit signed, 5% zero, 5% 64-bit entries"),
+    # 512x512x512, 4096-bit uniform signed entries
+    "cfg3": dict(K=512, M=512, N=512, bits=4096, zero=0.0, short=0.0, short_bits=0, cutoff=32,
+                 label="512x512x512 4096-bit signed"),
+    # 64x64x64, 1024-bit uniform signed entries
+    "cfg1": dict(K=64, M=64, N=64, bits=1024, zero=0.0, short=0.0, short_bits=0, cutoff=32,
+                 label="64x64x64 1024-bit signed"),
+}
+DEFAULT_WORKLOAD = "cfg3"
+DEFAULT_PATH = "crt"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def gen_planes(rng, n, bits, zero, short, short_bits):
+    """Seeded synthetic entries: magnitudes uniform in [0, 2^bits), fair sign,
+    a fraction of exact zeros and of entries shortened to short_bits."""
+    L = (bits + 31) // 32
+    limbs = rng.integers(0, 2**32, size=(L, n), dtype=np.uint64).astype(np.uint32)
+    top = bits - 32 * (L - 1)
+    if top < 32:
+        limbs[L - 1] &= np.uint32((1 << top) - 1)
+    u = rng.random(n)
+    zmask = u < zero
+    smask = (u >= zero) & (u < zero + short)
+    limbs[:, zmask] = 0
+    if short_bits:
+        Ls = (short_bits + 31) // 32
+        limbs[Ls:, smask] = 0
+    nz = limbs != 0
+    rev = nz[::-1]
+    size = np.where(nz.any(axis=0), L - rev.argmax(axis=0), 0).astype(np.int32)
+    sign = rng.random(n) < 0.5
+    size[sign] = -size[sign]
+    return limbs, size
+
+
+def limb_macs(K, M, N, As, Bs):
+    """sum_k (sum_i L64(A_ik)) (sum_j L64(B_kj)) with 64-bit limb counts."""
+    a64 = ((np.abs(As.astype(np.int64)) + 1) // 2).reshape(K, M)
+    b64 = ((np.abs(Bs.astype(np.int64)) + 1) // 2).reshape(M, N)
+    return int((a64.sum(axis=0) * b64.sum(axis=1)).sum())
+
+
+def entry_int(limbs, sizes, e):
+    s = int(sizes[e])
+    m = int.from_bytes(np.ascontiguousarray(limbs[:, e]).tobytes(), "little")
+    return -m if s < 0 else m
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons every 200 ms."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        import torch
+        if not torch.cuda.is_available():
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------------------------
+# CPU leg (reference algorithm on the host cores)
+# ------------------------------------------------------------------------------------
+def cpu_rows_sample(W, Al, As, Bl, Bs, target_s, nthreads):
+    """Times the CPU implementation on the first r rows of C = A*B, r chosen so
+    the sample takes about target_s seconds.  Returns (limb-MACs/s, seconds, rows, kind)."""
+    import oracle as orc
+    K, M, N = W["K"], W["M"], W["N"]
+    kind = "port"
+    use_gmp = orc.gmp_available()
+    if use_gmp:
+        orc.set_backend(1)
+    cn = 2 * ((W["bits"] + 31) // 32) + 4
+
+    def run(rows):
+        Ar = (Al[:, :rows * M], As[:rows * M])
+        t0 = time.perf_counter()
+        orc.matmul_planes(rows, M, N, Ar, (Bl, Bs), cn, method=1, nthreads=nthreads)
+        return time.perf_counter() - t0
+
+    probe = max(1, min(K, nthreads))
+    t = run(probe)
+    rows = int(min(K, max(probe, probe * target_s / max(t, 1e-6))))
+    t = run(rows)
+    macs = limb_macs(rows, M, N, As[:rows * M], Bs)
+    orc.set_backend(0)
+    sample = (f"first {rows} of {K} rows of C ({rows}x{M}x{N}), naive mat_mul order (mat-cpu -m 1), "
+              f"{'libgmp.so.10' if use_gmp else 'restated GMP'} arithmetic, {nthreads} threads")
+    return macs / t, t, rows, kind, sample
+
+
+def run_reference(args, W, world, rank):
+    if rank != 0:
+        return 0
+    rng = np.random.default_rng(args.seed)
+    Al, As = gen_planes(rng, W["K"] * W["M"], W["bits"], W["zero"], W["short"], W["short_bits"])
+    Bl, Bs = gen_planes(rng, W["M"] * W["N"], W["bits"], W["zero"], W["short"], W["short_bits"])
+    nthreads = os.cpu_count() or 1
+    vals, secs = [], []
+    for i in range(args.warmup + args.steps):
+        v, t, rows, kind, sample = cpu_rows_sample(W, Al, As, Bl, Bs, args.cpu_seconds, nthreads)
+        if i >= args.warmup:
+            vals.append(v)
+            secs.append(t)
+    value = statistics.median(vals)
+    full_s = limb_macs(W["K"], W["M"], W["N"], As, Bs) / value
+    line = {
+        "impl": "reference", "metric": "limb-MAC/s", "value": value, "unit": "limb-MAC/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * full_s, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": W["label"], "seed": args.seed, "extrapolated_full_product_s": full_s},
+        "cpu_baseline": {"value": value, "unit": "limb-MAC/s", "cores": nthreads, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": "limb-MAC/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------
+# GPU leg
+# ------------------------------------------------------------------------------------
+def run_gpu(args, W, world, rank, local):
+    import torch
+    import gbmm
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    rng = np.random.default_rng(args.seed + 0 * rank)
+    K, M, N, bits = W["K"], W["M"], W["N"], W["bits"]
+    Al, As = gen_planes(rng, K * M, bits, W["zero"], W["short"], W["short_bits"])
+    Bl, Bs = gen_planes(rng, M * N, bits, W["zero"], W["short"], W["short_bits"])
+    macs = limb_macs(K, M, N, As, Bs)
+    path = {"limb": gbmm.PATH_LIMB, "crt": gbmm.PATH_CRT, "auto": gbmm.PATH_AUTO}[args.path]
+    method = {"winograd": gbmm.METHOD_WINOGRAD, "naive": gbmm.METHOD_NAIVE, "strassen": gbmm.METHOD_STRASSEN}[
+        args.method]
+    cutoff = args.cutoff or W["cutoff"]
+    nl = Al.shape[0]
+    h = gbmm.Handle()
+    dA = gbmm.DeviceMatrix(K, M, nl)
+    dB = gbmm.DeviceMatrix(M, N, nl)
+    dA.upload(Al, As)
+    dB.upload(Bl, Bs)
+    cn = gbmm.limbs_needed(nl, nl, M, path=path, method=method, cutoff=cutoff)
+    dC = gbmm.DeviceMatrix(K, N, cn)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device="cuda")
+
+    def step():
+        h.matmul(dC, dA, dB, path=path, method=method, cutoff=cutoff)
+
+    # correctness on a sample of entries (bit-exact against Python integers)
+    step()
+    torch.cuda.synchronize()
+    Cl, Cs = dC.download()
+    srng = np.random.default_rng(7)
+    for _ in range(args.check):
+        y, x = int(srng.integers(K)), int(srng.integers(N))
+        exp = sum(entry_int(Al, As, y * M + k) * entry_int(Bl, Bs, k * N + x) for k in range(M))
+        got = entry_int(Cl, Cs, y * N + x)
+        if got != exp:
+            raise SystemExit(f"bench: C[{y}][{x}] differs from the exact product")
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = gbmm.kernel_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.fill_(i)  # evict L2 between timed steps (outside the events)
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = gbmm.kernel_launches() - launches0
+    barrier(world)
+    per = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(per) / len(per)
+    ms = max_over_ranks(world, ms)
+
+    # per-kernel CUDA-event timing over extra profiled steps (roofline of the dominant kernel)
+    gbmm.profile(True)
+    for i in range(max(1, args.profile_steps)):
+        flush.fill_(i)
+        step()
+    torch.cuda.synchronize()
+    prof = gbmm.profile_read()
+    gbmm.profile(False)
+    clocks = sampler.stop()
+
+    # end to end through the C ABI with host buffers: H2D of A and B, product, D2H of C
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).pin_memory()
+    hA, hAs, hB, hBs = pin(Al), pin(As), pin(Bl), pin(Bs)
+    hC = torch.empty(cn * K * N, dtype=torch.int32).pin_memory()
+    hCs = torch.empty(K * N, dtype=torch.int32).pin_memory()
+    L = gbmm.lib()
+
+    def e2e_step():
+        gbmm.check(L.gbmm_upload(dA.mat, hA.data_ptr(), hAs.data_ptr(), nl, K * M, stream.cuda_stream))
+        gbmm.check(L.gbmm_upload(dB.mat, hB.data_ptr(), hBs.data_ptr(), nl, M * N, stream.cuda_stream))
+        step()
+        gbmm.check(L.gbmm_download(dC.mat, hC.data_ptr(), hCs.data_ptr(), cn, K * N, stream.cuda_stream))
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ne = max(2, args.steps)
+    for _ in range(ne):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(world, (time.perf_counter() - t0) / ne)
+    h2d = (Al.nbytes + As.nbytes + Bl.nbytes + Bs.nbytes)
+    d2h = 4 * cn * K * N + 4 * K * N
+
+    # roofline of the dominant kernel
+    top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("", (1, 0.0))
+    kname, (klaunch, kms) = top
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    roof = kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof)
+
+    if rank != 0:
+        return 0
+    value = world * macs / (ms * 1e-3)
+    line = {
+        "metric": "limb-MAC/s", "value": value, "unit": "limb-MAC/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16" if path == gbmm.PATH_CRT else "u32", "data": "synthetic",
+        "config": {"workload": W["label"], "path": args.path, "method": args.method, "cutoff": cutoff,
+                   "seed": args.seed, "limb_macs_per_step": macs, "l2": "flushed between timed steps (512 MiB write)",
+                   "check": f"{args.check} entries bit-exact vs Python integers",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roof,
+        "kernels": {k: {"launches": v[0], "ms_total": round(v[1], 4)} for k, v in sorted(prof.items())},
+        "e2e": {"value": world * macs / e2e_s, "unit": "limb-MAC/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "s_per_step": e2e_s},
+        "gpu_launches": int(launches // max(1, args.steps)) * args.steps,
+        "clocks": clocks,
+    }
+    if not args.no_cpu and world == 1:
+        v, t, rows, kind, sample = cpu_rows_sample(W, Al, As, Bl, Bs, args.cpu_seconds, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": v, "unit": "limb-MAC/s", "cores": os.cpu_count() or 1, "kind": kind,
+                                "sample": sample}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof):
+    """Algorithmic work of the dominant kernel per launch / its mean CUDA-event time."""
+    per_ms = kms / max(1, klaunch)
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    src = "measured" if peaks else "fallback"
+    try:
+        import gbmm_roofline
+        r = gbmm_roofline.describe(kname, K, M, N, nl, cn, args)
+    except Exception:
+        r = None
+    if r is None:
+        # limb traffic: A and B read once, C written once (planes + sizes), per launch
+        bytes_ = (4 * nl * (K * M + M * N) + 4 * (K * M + M * N) + 4 * cn * K * N + 4 * K * N) / max(1, klaunch)
+        ach = bytes_ / (per_ms * 1e-3) / 1e9
+        return {"kernel": kname, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "traffic": None, "peak_source": src, "ms_per_launch": per_ms,
+                "note": "integer-MAC bound kernel; algorithmic bytes = A+B read once, C written once"}
+    unit_peak = bf16 if r["bound"] == "tensor" else hbm
+    ach = r["work"] / (per_ms * 1e-3) / (1e12 if r["bound"] == "tensor" else 1e9)
+    return {"kernel": kname, "bound": r["bound"], "achieved": ach, "peak": unit_peak,
+            "unit": "TFLOP/s" if r["bound"] == "tensor" else "GB/s", "frac": ach / unit_peak,
+            "traffic": r.get("traffic"), "peak_source": src, "ms_per_launch": per_ms, "note": r.get("note", "")}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbmm", choices=["gbmm", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--path", default=DEFAULT_PATH, choices=["limb", "crt", "auto"])
+    ap.add_argument("--method", default="winograd", choices=["winograd", "naive", "strassen"])
+    ap.add_argument("--cutoff", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--check", type=int, default=16)
+    ap.add_argument("--profile-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    W = WORKLOADS[args.workload]
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        return run_reference(args, W, world, rank)
+    return run_gpu(args, W, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,231 @@
+"""Parity of the plain limb path (batched mpn / mpz kernels, matrix add/sub, the
+per-entry product kernel and the Winograd / Strassen / squarify recursions)
+against the CPU oracle and the golden fixtures.  Integer work: bit-exact."""
+import random
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def g(built_lib):
+    import gbmm
+    gbmm.default_handle()
+    return gbmm
+
+
+def _rand_planes(rng, n, nb, special=None):
+    u = rng.integers(0, 2**32, size=(n, nb), dtype=np.uint64).astype(np.uint32)
+    if special == "ones":
+        u[:, : nb // 2] = 0xFFFFFFFF
+    return u
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).cuda()
+
+
+def _host(t):
+    return t.cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.parametrize("n", [1, 3, 31, 32, 128, 129, 300])
+@pytest.mark.parametrize("sub", [False, True])
+def test_mpn_add_sub_n_cla(g, oracle, n, sub):
+    import torch
+    rng = np.random.default_rng(n + 7 * sub)
+    nb = 70
+    u = _rand_planes(rng, n, nb, "ones")
+    v = _rand_planes(rng, n, nb)
+    v[:, :8] = 0 if sub else 1          # long carry / borrow chains
+    v[0, :8] = 1
+    if sub:
+        u[:, 8:16] = 0                   # borrow through all-zero limbs
+    exp_r, exp_c = oracle.mpn_add_n(u, v, sub=sub)
+    du, dv, dr = _dev(torch, u), _dev(torch, v), torch.zeros(n * nb, dtype=torch.int32, device="cuda")
+    cy = torch.zeros(nb, dtype=torch.int32, device="cuda")
+    (g.mpn_sub_n if sub else g.mpn_add_n)(dr, du, dv, n, nb, nb, cy)
+    torch.cuda.synchronize()
+    assert (_host(dr).reshape(n, nb) == exp_r).all()
+    assert (_host(cy) == exp_c).all()
+
+
+@pytest.mark.parametrize("op", [0, 1, 2])
+def test_mpn_mul1ops(g, oracle, op):
+    import torch
+    rng = np.random.default_rng(op)
+    n, nb = 17, 300
+    u = _rand_planes(rng, n, nb, "ones")
+    r0 = _rand_planes(rng, n, nb)
+    vl = rng.integers(0, 2**32, size=nb, dtype=np.uint64).astype(np.uint32)
+    vl[:5] = 0xFFFFFFFF
+    exp_r, exp_c = oracle.mpn_mul1ops(op, r0, u, vl)
+    dr, du, dvl = _dev(torch, r0), _dev(torch, u), _dev(torch, vl)
+    cy = torch.zeros(nb, dtype=torch.int32, device="cuda")
+    [g.mpn_mul_1, g.mpn_addmul_1, g.mpn_submul_1][op](dr, du, n, dvl, nb, nb, cy)
+    torch.cuda.synchronize()
+    assert (_host(dr).reshape(n, nb) == exp_r).all()
+    assert (_host(cy) == exp_c).all()
+
+
+@pytest.mark.parametrize("un,vn", [(1, 1), (5, 3), (32, 32), (64, 17), (100, 100)])
+def test_mpn_mul_basecase(g, oracle, un, vn):
+    import torch
+    rng = np.random.default_rng(un * 1000 + vn)
+    nb = 64
+    u = _rand_planes(rng, un, nb, "ones")
+    v = _rand_planes(rng, vn, nb, "ones")
+    exp = oracle.mpn_mul_basecase(u, v)
+    dr = torch.zeros((un + vn) * nb, dtype=torch.int32, device="cuda")
+    g.mpn_mul_basecase(dr, _dev(torch, u), un, _dev(torch, v), vn, nb, nb)
+    torch.cuda.synchronize()
+    assert (_host(dr).reshape(un + vn, nb) == exp).all()
+
+
+@pytest.mark.parametrize("an,bn", [(2, 2), (3, 2), (8, 5), (40, 40), (41, 40), (128, 128), (127, 100)])
+def test_mpn_toom22_and_mul(g, oracle, an, bn):
+    import torch
+    rng = np.random.default_rng(an * 7 + bn)
+    nb = 40
+    a = _rand_planes(rng, an, nb, "ones")
+    b = _rand_planes(rng, bn, nb, "ones")
+    a[:, 3] = 0
+    a[an - 1, 3] = 1
+    exp = oracle.mpn_mul_basecase(a, b)
+    dp = torch.zeros((an + bn) * nb, dtype=torch.int32, device="cuda")
+    scratch = torch.zeros(g.mpn_toom22_mul_itch(an, bn) * nb, dtype=torch.int32, device="cuda")
+    g.mpn_toom22_mul(dp, _dev(torch, a), an, _dev(torch, b), bn, scratch, nb, nb)
+    torch.cuda.synchronize()
+    assert (_host(dp).reshape(an + bn, nb) == exp).all()
+    dp.zero_()
+    g.mpn_mul(dp, _dev(torch, a), an, _dev(torch, b), bn, nb, nb)
+    torch.cuda.synchronize()
+    assert (_host(dp).reshape(an + bn, nb) == exp).all()
+
+
+def _signed(rng, n, bits, zero=0.1):
+    out = []
+    for i in range(n):
+        b = rng.choice([0, 1, 31, 32, 33, 64, bits])
+        m = 0 if rng.random() < zero else rng.getrandbits(b) if b else 0
+        if rng.random() < 0.1:
+            m = (1 << bits) - 1
+        out.append(-m if rng.random() < 0.5 else m)
+    return out
+
+
+@pytest.mark.parametrize("sub", [False, True])
+def test_mpz_add_sub(g, sub):
+    rng = random.Random(3 + sub)
+    n = 999
+    U = _signed(rng, n, 200)
+    V = _signed(rng, n, 200)
+    V[:50] = [(-u if not sub else u) for u in U[:50]]   # exact cancellation
+    V[50:100] = [(-u - 1 if not sub else u + 1) for u in U[50:100]]
+    du = g.DeviceMatrix.from_ints(1, n, U, 7)
+    dv = g.DeviceMatrix.from_ints(1, n, V, 7)
+    dw = g.DeviceMatrix(1, n, 8)
+    (g.mpz_sub if sub else g.mpz_add)(dw, du, dv)
+    assert dw.to_ints() == [(u - v if sub else u + v) for u, v in zip(U, V)]
+
+
+@pytest.mark.parametrize("op", ["mul", "addmul", "submul"])
+def test_mpz_mulops(g, op):
+    rng = random.Random(len(op))
+    n = 777
+    U = _signed(rng, n, 150)
+    V = _signed(rng, n, 120)
+    W = _signed(rng, n, 270)
+    # force the |uv| > |w| / |uv| < |w| / equal cases of the signed merge
+    W[:20] = [u * v * (1 if op == "submul" else -1) for u, v in zip(U[:20], V[:20])]
+    du = g.DeviceMatrix.from_ints(1, n, U, 5)
+    dv = g.DeviceMatrix.from_ints(1, n, V, 4)
+    dw = g.DeviceMatrix.from_ints(1, n, W, 10)
+    getattr(g, "mpz_" + op)(dw, du, dv)
+    if op == "mul":
+        exp = [u * v for u, v in zip(U, V)]
+    elif op == "addmul":
+        exp = [w + u * v for u, v, w in zip(U, V, W)]
+    else:
+        exp = [w - u * v for u, v, w in zip(U, V, W)]
+    assert dw.to_ints() == exp
+
+
+def _golden_device(g, name):
+    text, expect = load_golden(name)
+    K, M, N, A, B = g.parse_matrix_text(text)
+    dA = g.DeviceMatrix.from_ints(K, M, A)
+    dB = g.DeviceMatrix.from_ints(M, N, B)
+    return K, M, N, dA, dB, expect
+
+
+@pytest.mark.parametrize("name", golden_cases())
+@pytest.mark.parametrize("method,cutoff", [(1, 0), (35, 4), (3, 4), (4, 4), (35, 32)])
+def test_limb_matmul_golden(g, name, method, cutoff):
+    K, M, N, dA, dB, expect = _golden_device(g, name)
+    nl = g.limbs_needed(dA.nlimbs, dB.nlimbs, M, method=method, cutoff=cutoff)
+    dC = g.DeviceMatrix(K, N, nl)
+    g.squarify_mul(K, M, N, dC, dA, dB, method=method, cutoff=cutoff, path=g.PATH_LIMB)
+    limbs, sizes = dC.download()
+    assert g.format_hex(limbs, sizes, K, N) == expect
+
+
+@pytest.mark.parametrize("K,M,N,bits", [(33, 17, 9, 4096), (96, 96, 96, 130), (128, 128, 128, 64),
+                                        (5, 300, 3, 800), (64, 64, 64, 2048)])
+def test_limb_matmul_random_vs_oracle(g, oracle, K, M, N, bits):
+    rng = random.Random(K * 131 + M + N + bits)
+    A = _signed(rng, K * M, bits, 0.05)
+    B = _signed(rng, M * N, bits, 0.05)
+    nla = nlb = (bits + 31) // 32
+    dA = g.DeviceMatrix.from_ints(K, M, A, nla)
+    dB = g.DeviceMatrix.from_ints(M, N, B, nlb)
+    nl = g.limbs_needed(nla, nlb, M, cutoff=16)
+    dC = g.DeviceMatrix(K, N, nl)
+    g.squarify_mul(K, M, N, dC, dA, dB, method=g.METHOD_WINOGRAD, cutoff=16)
+    Cl, Cs = oracle.matmul_planes(K, M, N, g.ints_to_planes(A, nla), g.ints_to_planes(B, nlb), nl, method=1,
+                                  nthreads=4)
+    limbs, sizes = dC.download()
+    assert (sizes == Cs).all()
+    assert (limbs == Cl).all()
+
+
+def test_limb_addmul_accumulates(g):
+    rng = random.Random(9)
+    K = M = N = 32
+    A = _signed(rng, K * M, 300)
+    B = _signed(rng, M * N, 300)
+    C0 = _signed(rng, K * N, 600)
+    dA = g.DeviceMatrix.from_ints(K, M, A, 10)
+    dB = g.DeviceMatrix.from_ints(M, N, B, 10)
+    for method, cutoff in ((1, 0), (35, 8)):
+        nl = g.limbs_needed(10, 10, M, method=method, cutoff=cutoff) + 1
+        dC = g.DeviceMatrix.from_ints(K, N, C0, nl)
+        g.mat_addmul(K, M, N, dC, dA, dB, method=method, cutoff=cutoff)
+        exp = [C0[y * N + x] + sum(A[y * M + k] * B[k * N + x] for k in range(M)) for y in range(K) for x in range(N)]
+        assert dC.to_ints() == exp
+
+
+def test_limb_matmul_capacity_error(g):
+    dA = g.DeviceMatrix.from_ints(2, 2, [2**200] * 4, 7)
+    dB = g.DeviceMatrix.from_ints(2, 2, [2**200] * 4, 7)
+    dC = g.DeviceMatrix(2, 2, 3)
+    g.mat_mul(2, 2, 2, dC, dA, dB, method=g.METHOD_NAIVE)
+    with pytest.raises(g.GbmmError) as e:
+        dC.download()
+    assert e.value.status == g.ERR_CAPACITY
+
+
+def test_empty_shapes(g):
+    dA = g.DeviceMatrix(0, 5, 2)
+    dB = g.DeviceMatrix(5, 3, 2)
+    dC = g.DeviceMatrix(0, 3, 5)
+    g.mat_mul(0, 5, 3, dC, dA, dB)
+    dA = g.DeviceMatrix.from_ints(2, 0, [], 1)
+    dB = g.DeviceMatrix.from_ints(0, 2, [], 1)
+    dC = g.DeviceMatrix.from_ints(2, 2, [5, 6, 7, 8], 3)
+    g.mat_mul(2, 0, 2, dC, dA, dB, method=g.METHOD_NAIVE)
+    assert dC.to_ints() == [0, 0, 0, 0]
