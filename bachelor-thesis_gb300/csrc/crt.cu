@@ -1,11 +1,1137 @@
-// CRT (multi-modular) path -- filled in below.
+// Multi-modular (CRT) form of the exact product C = A * B on the tcgen05
+// tensor cores.
+//
+// Moduli: the P largest primes below 2^16 with prod p_i = Mod > 2^(bitsA +
+// bitsB + log2 k + 18).  Every GEMM below multiplies signed 8-bit digits held
+// exactly in bf16 and accumulates in FP32; each accumulation is bounded so that
+// every partial sum is an integer of magnitude < 2^24, hence exact.
+//
+//  1. digits    : limb planes -> rows of unsigned byte digits (bf16), one row
+//                 per entry (A in row-major order, B in column-major order).
+//  2. residue   : [entries x digits] x [digits x 2P] GEMM with the table
+//                 256^j mod p_i (balanced, split in two signed bytes); the
+//                 epilogue folds the two halves, reduces mod p_i, applies the
+//                 entry's sign and stores the residue as two balanced digits in
+//                 per-modulus planes.
+//  3. product   : for each modulus, [A1;A0] x [B1|B0]^T (two MMAs of
+//                 128x256xK into 512 TMEM columns); the epilogue combines the
+//                 four digit products mod p_i, multiplies by (Mod/p_i)^-1 mod
+//                 p_i (Garner / CRT weight) and stores the balanced result y_i as
+//                 two digits in per-modulus planes.
+//  4. reconstruct: [entries x 2P] x [2P x (8 + Dout)] GEMM against the digits
+//                 of Mod/p_i (and 256*Mod/p_i) plus fixed-point digits of
+//                 2^48/p_i; the epilogue gets q = round(sum y_i / p_i), folds
+//                 out q*Mod, propagates carries across the digit columns and
+//                 writes sign-magnitude limbs.  C = sum y_i Mod/p_i - q*Mod.
+// The CRT itself is the textbook one (HAC 14.5, Knuth 4.3.2); the reference's
+// crt.cpp (split / merge of one integer through a tree of coprime pairs) is
+// unused by the reference and only the idea carries over.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <vector>
+
 #include "gbmm_internal.h"
+#include "tc.cuh"
+
 namespace gbmm {
-struct crt_cache {};
+
+namespace {
+constexpr int BM = 128;  // tile rows (TMEM lanes)
+constexpr int BK = 64;   // bf16 elements per K step (one 128-byte swizzle row)
+constexpr int UK = 16;   // K of one kind::f16 MMA
+constexpr int GROUP_STEPS = 8;  // K steps per exact accumulation group (512 digits)
+constexpr int SROWS = 8;        // fixed-point rows at the top of the reconstruction table
+constexpr int FIXB = 48;        // fixed-point bits of the 1/p_i weights
+constexpr int EPI_THREADS = 128;
+constexpr int CTA_THREADS = 192;  // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+}  // namespace
+
+struct ModConst {
+    int32_t p;
+    float inv_p;
+    uint32_t mu;   // floor(2^32 / p)
+    uint32_t h16;  // 2^16 mod p
+    uint32_t w;    // (Mod / p)^-1 mod p
+    uint32_t pad[3];
+};
+
+// ---- modular helpers (device) ---------------------------------------------------------
+// s mod p for |s| < 2^25 using an FP32 quotient estimate (error <= 1) and two fixes.
+__device__ __forceinline__ int32_t mod_s32(int32_t s, int32_t p, float inv_p) {
+    int32_t q = __float2int_rd(__int2float_rn(s) * inv_p);
+    int32_t r = s - q * p;
+    r += r < 0 ? p : 0;
+    r += r < 0 ? p : 0;
+    r -= r >= p ? p : 0;
+    r -= r >= p ? p : 0;
+    return r;
+}
+// v mod p for any 32-bit unsigned v (Barrett with mu = floor(2^32/p)).
+__device__ __forceinline__ uint32_t mod_u32(uint32_t v, uint32_t p, uint32_t mu) {
+    uint32_t q = __umulhi(v, mu);
+    uint32_t r = v - q * p;
+    return r >= p ? r - p : r;
+}
+// residue r in [0,p) -> balanced value in (-p/2, p/2] split as hi*256 + lo with
+// lo in [-128, 127] and hi in [-128, 128]
+__device__ __forceinline__ void balanced_digits(int32_t r, int32_t p, float &hi, float &lo) {
+    int32_t b = r > (p >> 1) ? r - p : r;
+    int32_t d0 = ((b + 128) & 255) - 128;
+    int32_t d1 = (b - d0) >> 8;
+    hi = (float)d1;
+    lo = (float)d0;
+}
+
+struct Barriers {
+    uint64_t full[8];
+    uint64_t empty[8];
+    uint64_t tfull[2];
+    uint64_t tempty[2];
+    uint32_t tmem_base;
+    int abort_flag;
+};
+
+__device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
+    uintptr_t v = reinterpret_cast<uintptr_t>(p);
+    return reinterpret_cast<uint8_t *>((v + 1023) & ~(uintptr_t)1023);
+}
+
+// Common prologue: barrier init by thread 0, TMEM allocation by warp 1.
+__device__ __forceinline__ void cta_setup(Barriers *bars, int stages, uint32_t tmem_cols, uint32_t full_count,
+                                          uint32_t tempty_count) {
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < stages; s++) {
+            tc::mbar_init(&bars->full[s], full_count);
+            tc::mbar_init(&bars->empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(&bars->tfull[b], 1);
+            tc::mbar_init(&bars->tempty[b], tempty_count);
+        }
+        bars->abort_flag = 0;
+        tc::fence_mbar_init();
+    }
+    if (warp == 1) {
+        tc::tmem_alloc(&bars->tmem_base, tmem_cols);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+}
+
+__device__ __forceinline__ void cta_teardown(Barriers *bars, uint32_t tmem_cols) {
+    tc::fence_before_sync();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 1) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(bars->tmem_base, tmem_cols);
+    }
+}
+
+__device__ __forceinline__ void set_abort(Barriers *bars, uint32_t *err) {
+    atomicOr(err, DEVERR_TIMEOUT);
+    *(volatile int *)&bars->abort_flag = 1;
+}
+__device__ __forceinline__ bool aborted(Barriers *bars) { return *(volatile int *)&bars->abort_flag != 0; }
+
+// epilogue warps 2..5 cover TMEM lane quadrants (warp % 4)
+__device__ __forceinline__ int epi_row() { return ((threadIdx.x >> 5) & 3) * 32 + (threadIdx.x & 31); }
+__device__ __forceinline__ uint32_t lane_base(uint32_t tmem) { return tmem + (((threadIdx.x >> 5) & 3) * 32u << 16); }
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+// ======================================================================================
+// 1. digits
+// ======================================================================================
+struct DigitArgs {
+    const uint32_t *limbs;
+    int64_t ld, rs;
+    int32_t rows, cols, nlimbs;
+    int32_t transpose;  // 0: out row r*cols + c ; 1: out row c*rows + r
+    int32_t dxp;        // digits per out row (multiple of 64)
+    __nv_bfloat16 *out;
+};
+
+__global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
+    __shared__ uint32_t s[128][65];
+    const int tr = 4, tcn = 32;
+    const int r0 = blockIdx.y * tr, c0 = blockIdx.x * tcn;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nchunk = (a.dxp / 4 + 63) / 64;
+    for (int ch = 0; ch < nchunk; ch++) {
+        const int l0 = ch * 64;
+        __syncthreads();
+        // load limbs [l0, l0+64) of the 4 x 32 entries, coalesced along c
+        for (int q = threadIdx.x; q < 64 * 128; q += 256) {
+            int cc = q & 31, rr = (q >> 5) & 3, li = q >> 7;
+            int r = r0 + rr, c = c0 + cc, l = l0 + li;
+            uint32_t v = 0;
+            if (r < a.rows && c < a.cols && l < a.nlimbs) v = a.limbs[(int64_t)l * a.ld + (int64_t)r * a.rs + c];
+            s[rr * 32 + cc][li] = v;
+        }
+        __syncthreads();
+        // each warp writes whole digit rows: lane j -> limbs l0+2j, l0+2j+1 (8 digits, 16 bytes)
+        for (int ent = warp; ent < 128; ent += 8) {
+            int rr = ent >> 5, cc = ent & 31;
+            int r = r0 + rr, c = c0 + cc;
+            if (r >= a.rows || c >= a.cols) continue;
+            int64_t row = a.transpose ? (int64_t)c * a.rows + r : (int64_t)r * a.cols + c;
+            int dg = 4 * (l0 + 2 * lane);
+            if (dg >= a.dxp) continue;
+            uint32_t v0 = s[ent][2 * lane], v1 = s[ent][2 * lane + 1];
+            __nv_bfloat162 p0 = __floats2bfloat162_rn((float)(v0 & 255u), (float)((v0 >> 8) & 255u));
+            __nv_bfloat162 p1 = __floats2bfloat162_rn((float)((v0 >> 16) & 255u), (float)(v0 >> 24));
+            __nv_bfloat162 p2 = __floats2bfloat162_rn((float)(v1 & 255u), (float)((v1 >> 8) & 255u));
+            __nv_bfloat162 p3 = __floats2bfloat162_rn((float)((v1 >> 16) & 255u), (float)(v1 >> 24));
+            uint4 pk;
+            pk.x = *reinterpret_cast<uint32_t *>(&p0);
+            pk.y = *reinterpret_cast<uint32_t *>(&p1);
+            pk.z = *reinterpret_cast<uint32_t *>(&p2);
+            pk.w = *reinterpret_cast<uint32_t *>(&p3);
+            *reinterpret_cast<uint4 *>(a.out + row * a.dxp + dg) = pk;
+        }
+    }
+}
+
+// ======================================================================================
+// 2. residue GEMM
+// ======================================================================================
+struct ResidueArgs {
+    const int32_t *sizes;  // sizes of the source matrix (for the entry signs)
+    int64_t rs;
+    int32_t transpose, kdim;  // entry e -> (e / kdim, e % kdim) in digit-row order
+    int64_t E;                // entries (digit rows)
+    int32_t nk;               // K steps of 64 digits
+    int32_t BN, G;            // table columns per tile, accumulation groups
+    int32_t P;
+    const ModConst *mods;
+    __nv_bfloat16 *R;  // planes [2P][rowsR][kp]
+    int64_t plane;     // rowsR * kp
+    int32_t kp;
+};
+
+template <int STAGES>
+__global__ void __launch_bounds__(CTA_THREADS, 1)
+    k_crt_residue(const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmT, ResidueArgs a,
+                  uint32_t *err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *base = align1024(smem_raw);
+    const uint32_t A_BYTES = BM * 128, B_BYTES = (uint32_t)a.BN * 128, STAGE = A_BYTES + B_BYTES;
+    Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n0 = blockIdx.x * a.BN;
+    const int64_t e0 = (int64_t)blockIdx.y * BM;
+    cta_setup(bars, STAGES, 512, 1, 1);
+    const uint32_t tmem = bars->tmem_base;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            tc::prefetch_tmap(&tmD);
+            tc::prefetch_tmap(&tmT);
+            for (int s = 0; s < a.nk; s++) {
+                const int st = s % STAGES;
+                if (s >= STAGES && !tc::mbar_wait(&bars->empty[st], ((s / STAGES) & 1) ^ 1)) {
+                    set_abort(bars, err);
+                    break;
+                }
+                if (aborted(bars)) break;
+                uint8_t *sa = base + st * STAGE;
+                tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                tc::tma_load_2d(sa, &tmD, &bars->full[st], s * BK, (int)e0);
+                tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, n0);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16_f32(BM, a.BN, 0, 0);
+            bool ok = true;
+            for (int s = 0; s < a.nk; s++) {
+                const int st = s % STAGES;
+                if (!tc::mbar_wait(&bars->full[st], (s / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+                tc::fence_after_sync();
+                const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
+                const int g = s / GROUP_STEPS;
+                const uint32_t d = tmem + (uint32_t)(g * a.BN);
+#pragma unroll
+                for (int kk = 0; kk < BK / UK; kk++) {
+                    tc::mma_bf16(d, tc::sdesc_kmajor(sa + kk * 32), tc::sdesc_kmajor(sb + kk * 32), idesc,
+                                 (s % GROUP_STEPS) != 0 || kk != 0);
+                }
+                tc::mma_commit(&bars->empty[st]);
+            }
+            if (ok) tc::mma_commit(&bars->tfull[0]);
+        }
+    } else {
+        // epilogue: one thread per digit row (entry)
+        const int row = epi_row();
+        const int64_t e = e0 + row;
+        bool ok = tc::mbar_wait(&bars->tfull[0], 0);
+        if (!ok) set_abort(bars, err);
+        tc::fence_after_sync();
+        int neg = 0;
+        if (ok && e < a.E) {
+            int64_t r = e / a.kdim, c = e % a.kdim;
+            int64_t src = a.transpose ? c * a.rs + r : r * a.rs + c;
+            neg = a.sizes[src] < 0;
+        }
+        const uint32_t lb = lane_base(tmem);
+        for (int c0 = 0; c0 < a.BN && ok; c0 += 32) {
+            int32_t res[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) res[j] = 0;
+            for (int g = 0; g < a.G; g++) {
+                uint32_t v[32];
+                tc::tmem_ld32(lb + (uint32_t)(g * a.BN + c0), v);
+                tc::tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int mi = (n0 + c0) / 2 + j;
+                    const ModConst mc = a.mods[mi < a.P ? mi : 0];
+                    int32_t r0 = mod_s32(tc::acc_int(v[2 * j]), mc.p, mc.inv_p);
+                    int32_t r1 = mod_s32(tc::acc_int(v[2 * j + 1]), mc.p, mc.inv_p);
+                    uint32_t t = mod_u32((uint32_t)r1 * 256u + (uint32_t)r0 + (uint32_t)res[j], (uint32_t)mc.p, mc.mu);
+                    res[j] = (int32_t)t;
+                }
+            }
+            if (e < a.E) {
+                const int64_t off = (e / a.kdim) * a.kp + (e % a.kdim);
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int mi = (n0 + c0) / 2 + j;
+                    if (mi >= a.P) continue;
+                    const int32_t p = a.mods[mi].p;
+                    int32_t r = res[j];
+                    if (neg && r) r = p - r;
+                    float hi, lo;
+                    balanced_digits(r, p, hi, lo);
+                    a.R[(int64_t)(2 * mi) * a.plane + off] = __float2bfloat16_rn(hi);
+                    a.R[(int64_t)(2 * mi + 1) * a.plane + off] = __float2bfloat16_rn(lo);
+                }
+            }
+        }
+    }
+    cta_teardown(bars, 512);
+}
+
+// ======================================================================================
+// 3. per-modulus product GEMM
+// ======================================================================================
+struct ProductArgs {
+    int32_t m, n, nk, P;
+    const ModConst *mods;
+    __nv_bfloat16 *Y;  // planes [2Pp][Ep]
+    int64_t Ep;
+};
+
+template <int STAGES>
+__global__ void __launch_bounds__(CTA_THREADS, 1)
+    k_crt_product(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, ProductArgs a,
+                  uint32_t *err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *base = align1024(smem_raw);
+    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = 2 * BM * 128, STAGE = 2 * A_BYTES + B_BYTES;
+    Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int x0 = blockIdx.x * BM, y0 = blockIdx.y * BM, mi = blockIdx.z;
+    cta_setup(bars, STAGES, 512, 1, 1);
+    const uint32_t tmem = bars->tmem_base;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            tc::prefetch_tmap(&tmA);
+            tc::prefetch_tmap(&tmB);
+            for (int s = 0; s < a.nk; s++) {
+                const int st = s % STAGES;
+                if (s >= STAGES && !tc::mbar_wait(&bars->empty[st], ((s / STAGES) & 1) ^ 1)) {
+                    set_abort(bars, err);
+                    break;
+                }
+                if (aborted(bars)) break;
+                uint8_t *sa = base + st * STAGE;
+                tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                tc::tma_load_2d(sa, &tmA, &bars->full[st], s * BK, (2 * mi) * a.m + y0);
+                tc::tma_load_2d(sa + A_BYTES, &tmA, &bars->full[st], s * BK, (2 * mi + 1) * a.m + y0);
+                tc::tma_load_2d(sa + 2 * A_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi) * a.n + x0);
+                tc::tma_load_2d(sa + 2 * A_BYTES + BM * 128, &tmB, &bars->full[st], s * BK, (2 * mi + 1) * a.n + x0);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16_f32(BM, 2 * BM, 0, 0);
+            bool ok = true;
+            for (int s = 0; s < a.nk; s++) {
+                const int st = s % STAGES;
+                if (!tc::mbar_wait(&bars->full[st], (s / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+                tc::fence_after_sync();
+                const uint32_t sa1 = tc::smem_u32(base + st * STAGE), sa0 = sa1 + A_BYTES, sb = sa1 + 2 * A_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < BK / UK; kk++) {
+                    const uint64_t bd = tc::sdesc_kmajor(sb + kk * 32);
+                    tc::mma_bf16(tmem, tc::sdesc_kmajor(sa1 + kk * 32), bd, idesc, s != 0 || kk != 0);
+                    tc::mma_bf16(tmem + 256, tc::sdesc_kmajor(sa0 + kk * 32), bd, idesc, s != 0 || kk != 0);
+                }
+                tc::mma_commit(&bars->empty[st]);
+            }
+            if (ok) tc::mma_commit(&bars->tfull[0]);
+        }
+    } else {
+        const int row = epi_row();
+        bool ok = tc::mbar_wait(&bars->tfull[0], 0);
+        if (!ok) set_abort(bars, err);
+        tc::fence_after_sync();
+        const ModConst mc = a.mods[mi];
+        // staging for coalesced stores: [2 planes][128 rows][128 x] bf16, in the idle pipeline buffers
+        __nv_bfloat16 *stg = reinterpret_cast<__nv_bfloat16 *>(base);
+        const uint32_t lb = lane_base(tmem);
+        for (int xb = 0; xb < BM && ok; xb += 32) {
+            uint32_t d11[32], d10[32], d01[32], d00[32];
+            tc::tmem_ld32(lb + (uint32_t)xb, d11);
+            tc::tmem_ld32(lb + (uint32_t)(BM + xb), d10);
+            tc::tmem_ld32(lb + (uint32_t)(2 * BM + xb), d01);
+            tc::tmem_ld32(lb + (uint32_t)(3 * BM + xb), d00);
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                int32_t r11 = mod_s32(tc::acc_int(d11[j]), mc.p, mc.inv_p);
+                int32_t r1 = mod_s32(tc::acc_int(d10[j]) + tc::acc_int(d01[j]), mc.p, mc.inv_p);
+                int32_t r0 = mod_s32(tc::acc_int(d00[j]), mc.p, mc.inv_p);
+                uint32_t t = mod_u32((uint32_t)r11 * mc.h16, (uint32_t)mc.p, mc.mu);
+                uint32_t c = mod_u32(t + (uint32_t)r1 * 256u + (uint32_t)r0, (uint32_t)mc.p, mc.mu);
+                uint32_t y = mod_u32(c * mc.w, (uint32_t)mc.p, mc.mu);
+                float hi, lo;
+                balanced_digits((int32_t)y, mc.p, hi, lo);
+                stg[(0 * BM + row) * BM + xb + j] = __float2bfloat16_rn(hi);
+                stg[(1 * BM + row) * BM + xb + j] = __float2bfloat16_rn(lo);
+            }
+        }
+        epi_bar();
+        if (ok) {
+            // 4 warps write rows: each warp-row store is 128 x 2 bytes contiguous
+            const int ew = (threadIdx.x >> 5) - 2;
+            for (int q = ew; q < 2 * BM; q += 4) {
+                const int d = q / BM, r = q % BM, y = y0 + r;
+                if (y >= a.m) continue;
+                __nv_bfloat16 *dst = a.Y + (int64_t)(2 * mi + d) * a.Ep + (int64_t)y * a.n + x0;
+                const __nv_bfloat16 *src = stg + (d * BM + r) * BM;
+                if ((reinterpret_cast<uintptr_t>(dst) & 7) == 0 && x0 + BM <= a.n) {
+                    // 8-byte vector stores only when the row segment is 8-byte aligned and complete
+                    *reinterpret_cast<uint2 *>(dst + lane * 4) = *reinterpret_cast<const uint2 *>(src + lane * 4);
+                } else {
+                    for (int x = lane; x < BM; x += 32)
+                        if (x0 + x < a.n) dst[x] = src[x];
+                }
+            }
+        }
+    }
+    cta_teardown(bars, 512);
+}
+
+// ======================================================================================
+// 4. reconstruction GEMM
+// ======================================================================================
+struct ReconArgs {
+    int64_t E;       // entries of C
+    int32_t ncols;   // columns of C (entry e -> row e / ncols, col e % ncols)
+    int32_t nk;      // K steps over 2Pp
+    int32_t gsplit;  // first K step of accumulation group 1
+    int32_t NT;      // N tiles of 128 table rows
+    int32_t Dout;    // output digit positions
+    const int8_t *mdig;  // balanced base-256 digits of Mod, Dout entries
+    uint32_t *climbs;
+    int32_t *csizes;
+    int64_t cld, crs;
+    int32_t cnlimbs;
+};
+
+template <int STAGES>
+__global__ void __launch_bounds__(CTA_THREADS, 1)
+    k_crt_recon(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmT, ReconArgs a,
+                uint32_t *err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *base = align1024(smem_raw);
+    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = BM * 128, STAGE = A_BYTES + B_BYTES;
+    Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t e0 = (int64_t)blockIdx.x * BM;
+    cta_setup(bars, STAGES, 512, 1, 4);
+    const uint32_t tmem = bars->tmem_base;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            tc::prefetch_tmap(&tmY);
+            tc::prefetch_tmap(&tmT);
+            int it = 0;
+            for (int j = 0; j < a.NT && !aborted(bars); j++) {
+                for (int s = 0; s < a.nk; s++, it++) {
+                    const int st = it % STAGES;
+                    if (it >= STAGES && !tc::mbar_wait(&bars->empty[st], ((it / STAGES) & 1) ^ 1)) {
+                        set_abort(bars, err);
+                        break;
+                    }
+                    if (aborted(bars)) break;
+                    uint8_t *sa = base + st * STAGE;
+                    tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                    // A (MN-major): two boxes of 64 entries x 64 K-rows
+                    tc::tma_load_2d(sa, &tmY, &bars->full[st], (int)e0, s * BK);
+                    tc::tma_load_2d(sa + A_BYTES / 2, &tmY, &bars->full[st], (int)e0 + 64, s * BK);
+                    tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, j * BM);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16_f32(BM, BM, 1, 0);
+            int it = 0;
+            bool ok = true;
+            for (int j = 0; j < a.NT && ok; j++) {
+                const int b = j & 1;
+                if (j >= 2 && !tc::mbar_wait(&bars->tempty[b], ((j >> 1) & 1) ^ 1)) {
+                    set_abort(bars, err);
+                    ok = false;
+                    break;
+                }
+                tc::fence_after_sync();
+                for (int s = 0; s < a.nk; s++, it++) {
+                    const int st = it % STAGES;
+                    if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+                    tc::fence_after_sync();
+                    const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
+                    const int g = s >= a.gsplit;
+                    const uint32_t d = tmem + (uint32_t)(256 * b + 128 * g);
+                    const int first = g ? (s == a.gsplit) : (s == 0);
+#pragma unroll
+                    for (int kk = 0; kk < BK / UK; kk++) {
+                        tc::mma_bf16(d, tc::sdesc_mnmajor(sa + kk * 2048, A_BYTES / 2), tc::sdesc_kmajor(sb + kk * 32),
+                                     idesc, !(first && kk == 0));
+                    }
+                    tc::mma_commit(&bars->empty[st]);
+                }
+                if (ok) tc::mma_commit(&bars->tfull[b]);
+            }
+        }
+    } else {
+        const int row = epi_row();
+        const int64_t e = e0 + row;
+        const bool live = e < a.E;
+        const bool two = a.gsplit < a.nk;  // accumulation group 1 is empty when K has a single step
+        const int64_t coff = live ? (e / a.ncols) * a.crs + (e % a.ncols) : 0;
+        const uint32_t lb = lane_base(tmem);
+        int64_t carry = 0;
+        int32_t q = 0, sigma = 1;
+        bool ambiguous = false, ok = true;
+        uint32_t limb = 0;
+        int pos = 0, top = 0;
+        bool drop_nz = false, drop_ones = true;
+        for (int j = 0; j < a.NT; j++) {
+            const int b = j & 1;
+            if (!tc::mbar_wait(&bars->tfull[b], (j >> 1) & 1)) { set_abort(bars, err); ok = false; break; }
+            tc::fence_after_sync();
+            for (int c0 = 0; c0 < BM; c0 += 32) {
+                uint32_t g0[32], g1[32];
+                tc::tmem_ld32(lb + (uint32_t)(256 * b + c0), g0);
+                tc::tmem_ld32(lb + (uint32_t)(256 * b + 128 + c0), g1);
+                tc::tmem_ld_wait();
+                if (c0 + 32 >= BM) {
+                    // this tile's TMEM is fully read: release it to the MMA warp
+                    tc::fence_before_sync();
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
+                }
+                int jbeg = 0;
+                if (j == 0 && c0 == 0) {
+                    // fixed-point sum S = sum y_i 2^48 / p_i in the first SROWS columns
+                    __int128 S = 0;
+#pragma unroll
+                    for (int t = SROWS - 1; t >= 0; t--) S = S * 256 + (tc::acc_int(g0[t]) + (two ? tc::acc_int(g1[t]) : 0));
+                    const __int128 half = (__int128)1 << (FIXB - 1);
+                    __int128 qq = (S + half) >> FIXB;
+                    __int128 frac = S - (qq << FIXB);
+                    q = (int32_t)qq;
+                    const __int128 tol = (__int128)1 << 20;
+                    if (frac > tol) sigma = 1;
+                    else if (frac < -tol) sigma = -1;
+                    else { sigma = 1; ambiguous = true; }
+                    jbeg = SROWS;
+                }
+                if (!live) continue;
+#pragma unroll
+                for (int t = 0; t < 32; t++) {
+                    if (t < jbeg || pos >= a.Dout) continue;
+                    int64_t v = (int64_t)(tc::acc_int(g0[t]) + (two ? tc::acc_int(g1[t]) : 0)) - (int64_t)q * a.mdig[pos];
+                    v = sigma * v + carry;
+                    const uint32_t dg = (uint32_t)(v & 255);
+                    carry = v >> 8;
+                    limb |= dg << (8 * (pos & 3));
+                    if ((pos & 3) == 3) {
+                        const int li = pos >> 2;
+                        if (li < a.cnlimbs) {
+                            a.climbs[(int64_t)li * a.cld + coff] = limb;
+                            if (limb) top = li + 1;
+                        } else {
+                            drop_nz |= limb != 0u;
+                            drop_ones &= limb == 0xFFFFFFFFu;
+                        }
+                        limb = 0;
+                    }
+                    pos++;
+                }
+            }
+        }
+        if (ok && live) {
+            // flush a partial limb
+            if (pos & 3) {
+                const int li = pos >> 2;
+                if (carry < 0) limb |= 0xFFFFFFFFu << (8 * (pos & 3));
+                if (li < a.cnlimbs) {
+                    a.climbs[(int64_t)li * a.cld + coff] = limb;
+                    if (limb) top = li + 1;
+                } else {
+                    drop_nz |= limb != 0u;
+                    drop_ones &= limb == 0xFFFFFFFFu;
+                }
+                pos = (li + 1) * 4;
+            }
+            const int written = pos >> 2 < a.cnlimbs ? pos >> 2 : a.cnlimbs;
+            int neg = sigma < 0;
+            if (carry < 0) {
+                // only reachable on the ambiguous path: two's complement -> magnitude
+                if (!ambiguous || (pos >> 2 > a.cnlimbs && !(drop_ones && top != 0))) atomicOr(err, DEVERR_CAPACITY);
+                uint32_t cc = 1;
+                top = 0;
+                for (int li = 0; li < written; li++) {
+                    uint64_t s = (uint64_t)(~a.climbs[(int64_t)li * a.cld + coff]) + cc;
+                    const uint32_t r = (uint32_t)s;
+                    cc = (uint32_t)(s >> 32);
+                    a.climbs[(int64_t)li * a.cld + coff] = r;
+                    if (r) top = li + 1;
+                }
+                neg = 1;
+            } else if (carry != 0 || drop_nz) {
+                atomicOr(err, DEVERR_CAPACITY);
+            }
+            for (int li = written; li < a.cnlimbs; li++) a.climbs[(int64_t)li * a.cld + coff] = 0u;
+            a.csizes[coff] = top == 0 ? 0 : (neg ? -top : top);
+        }
+    }
+    cta_teardown(bars, 512);
+}
+
+// ======================================================================================
+// tcgen05 GEMM self-test: D[M x N] (int32) = A * B^T with A K-major [M x K] or
+// MN-major [K x M], B K-major [N x K]; used by tests to pin the descriptor
+// layouts independently of the CRT arithmetic.
+// ======================================================================================
+struct TestArgs {
+    int32_t M, N, nk, a_mn;
+    int32_t *D;
+};
+
+template <int STAGES>
+__global__ void __launch_bounds__(CTA_THREADS, 1)
+    k_gemm_test(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TestArgs a,
+                uint32_t *err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *base = align1024(smem_raw);
+    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = BM * 128, STAGE = A_BYTES + B_BYTES;
+    Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BM;
+    cta_setup(bars, STAGES, 128, 1, 1);
+    const uint32_t tmem = bars->tmem_base;
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int s = 0; s < a.nk; s++) {
+                const int st = s % STAGES;
+                if (s >= STAGES && !tc::mbar_wait(&bars->empty[st], ((s / STAGES) & 1) ^ 1)) {
+                    set_abort(bars, err);
+                    break;
+                }
+                uint8_t *sa = base + st * STAGE;
+                tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                if (a.a_mn) {
+                    tc::tma_load_2d(sa, &tmA, &bars->full[st], m0, s * BK);
+                    tc::tma_load_2d(sa + A_BYTES / 2, &tmA, &bars->full[st], m0 + 64, s * BK);
+                } else {
+                    tc::tma_load_2d(sa, &tmA, &bars->full[st], s * BK, m0);
+                }
+                tc::tma_load_2d(sa + A_BYTES, &tmB, &bars->full[st], s * BK, n0);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16_f32(BM, BM, a.a_mn, 0);
+            bool ok = true;
+            for (int s = 0; s < a.nk; s++) {
+                const int st = s % STAGES;
+                if (!tc::mbar_wait(&bars->full[st], (s / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+                tc::fence_after_sync();
+                const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < BK / UK; kk++) {
+                    const uint64_t ad =
+                        a.a_mn ? tc::sdesc_mnmajor(sa + kk * 2048, A_BYTES / 2) : tc::sdesc_kmajor(sa + kk * 32);
+                    tc::mma_bf16(tmem, ad, tc::sdesc_kmajor(sb + kk * 32), idesc, s != 0 || kk != 0);
+                }
+                tc::mma_commit(&bars->empty[st]);
+            }
+            if (ok) tc::mma_commit(&bars->tfull[0]);
+        }
+    } else {
+        const int row = epi_row();
+        bool ok = tc::mbar_wait(&bars->tfull[0], 0);
+        if (!ok) set_abort(bars, err);
+        tc::fence_after_sync();
+        const uint32_t lb = lane_base(tmem);
+        for (int c0 = 0; c0 < BM && ok; c0 += 32) {
+            uint32_t v[32];
+            tc::tmem_ld32(lb + (uint32_t)c0, v);
+            tc::tmem_ld_wait();
+            const int m = m0 + row;
+            if (m < a.M)
+                for (int j = 0; j < 32; j++)
+                    if (n0 + c0 + j < a.N) a.D[(int64_t)m * a.N + n0 + c0 + j] = tc::acc_int(v[j]);
+        }
+    }
+    cta_teardown(bars, 128);
+}
+
+// ======================================================================================
+// host side
+// ======================================================================================
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                     const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static PFN_encodeTiled get_encode() {
+    static PFN_encodeTiled fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_encodeTiled>(p);
+    });
+    return fn;
+}
+
+// 2-D bf16 tensor map: inner dimension `inner` (contiguous), `outer` rows with
+// a pitch of `pitch_elems`; box = box_inner x box_outer, 128-byte swizzle.
+static gbmm_status make_map(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer, uint64_t pitch_elems,
+                            uint32_t box_inner, uint32_t box_outer) {
+    PFN_encodeTiled enc = get_encode();
+    if (!enc) return set_error(GBMM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    if ((reinterpret_cast<uintptr_t>(ptr) & 15) || (pitch_elems * 2) % 16)
+        return set_error(GBMM_ERR_INVALID, "tensor map base or pitch not 16-byte aligned");
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {pitch_elems * 2};
+    cuuint32_t box[2] = {box_inner, box_outer};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(GBMM_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return GBMM_OK;
+}
+
+// ---- host big integers (tables only) ---------------------------------------------------------
+typedef std::vector<uint32_t> big;  // little-endian 32-bit limbs
+static void big_mul_small(big &x, uint32_t m) {
+    uint64_t c = 0;
+    for (auto &l : x) {
+        uint64_t t = (uint64_t)l * m + c;
+        l = (uint32_t)t;
+        c = t >> 32;
+    }
+    if (c) x.push_back((uint32_t)c);
+}
+static big big_div_small(const big &x, uint32_t d, uint32_t *rem) {
+    big q(x.size());
+    uint64_t r = 0;
+    for (size_t i = x.size(); i-- > 0;) {
+        uint64_t cur = (r << 32) | x[i];
+        q[i] = (uint32_t)(cur / d);
+        r = cur % d;
+    }
+    while (!q.empty() && q.back() == 0) q.pop_back();
+    if (rem) *rem = (uint32_t)r;
+    return q;
+}
+static uint32_t big_mod_small(const big &x, uint32_t d) {
+    uint64_t r = 0;
+    for (size_t i = x.size(); i-- > 0;) r = ((r << 32) | x[i]) % d;
+    return (uint32_t)r;
+}
+// balanced base-256 digits (each in [-128, 127]) of a nonnegative integer
+static std::vector<int> balanced256(const big &x, int ndig) {
+    std::vector<int> out(ndig, 0);
+    std::vector<int> bytes;
+    for (uint32_t l : x)
+        for (int b = 0; b < 4; b++) bytes.push_back((l >> (8 * b)) & 255);
+    int carry = 0;
+    for (int t = 0; t < ndig; t++) {
+        int v = (t < (int)bytes.size() ? bytes[t] : 0) + carry;
+        int d = v >= 128 ? v - 256 : v;
+        carry = (v - d) / 256;
+        out[t] = d;
+    }
+    return out;
+}
+static uint32_t inv_mod(uint32_t a, uint32_t p) {
+    int64_t t = 0, nt = 1, r = p, nr = a % p;
+    while (nr) {
+        int64_t q = r / nr;
+        int64_t tmp = t - q * nt; t = nt; nt = tmp;
+        tmp = r - q * nr; r = nr; nr = tmp;
+    }
+    if (t < 0) t += p;
+    return (uint32_t)t;
+}
+static const std::vector<uint32_t> &primes_desc() {
+    static std::vector<uint32_t> pr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        std::vector<char> sieve(65536, 1);
+        sieve[0] = sieve[1] = 0;
+        for (int i = 2; i * i < 65536; i++)
+            if (sieve[i])
+                for (int j = i * i; j < 65536; j += i) sieve[j] = 0;
+        for (int i = 65535; i >= 3; i--)
+            if (sieve[i]) pr.push_back((uint32_t)i);
+    });
+    return pr;
+}
+
+static uint16_t bf16_bits(float f) {
+    __nv_bfloat16 h = __float2bfloat16_rn(f);
+    uint16_t b;
+    memcpy(&b, &h, 2);
+    return b;
+}
+
+struct crt_tables {
+    int P = 0, Pp = 0;   // moduli, padded 2P/2 (2Pp multiple of 64)
+    int Dout = 0, NT = 0;
+    ModConst *d_mods = nullptr;
+    __nv_bfloat16 *d_recon = nullptr;  // [NT*128][2Pp]
+    int8_t *d_mdig = nullptr;          // [Dout]
+    std::map<int, __nv_bfloat16 *> residue;  // dxp -> [2P rows][dxp]
+    std::vector<ModConst> h_mods;
+};
+
+struct crt_cache {
+    std::mutex mu;
+    std::map<int, crt_tables *> by_p;
+    ~crt_cache() {
+        for (auto &kv : by_p) {
+            crt_tables *t = kv.second;
+            cudaFree(t->d_mods);
+            cudaFree(t->d_recon);
+            cudaFree(t->d_mdig);
+            for (auto &r : t->residue) cudaFree(r.second);
+            delete t;
+        }
+    }
+};
+
 crt_cache *crt_cache_create() { return new crt_cache(); }
 void crt_cache_destroy(crt_cache *c) { delete c; }
-gbmm_status crt_matmul(gbmm_handle, const gbmm_mat &, const gbmm_mat &, const gbmm_mat &, int64_t, int64_t, int, int,
-                       cudaStream_t) {
-    return set_error(GBMM_ERR_UNSUPPORTED, "CRT path not built");
+
+// number of moduli for a product bound of `bits` bits (plus margin)
+static int moduli_for_bits(int64_t bits) {
+    const auto &pr = primes_desc();
+    double acc = 0;
+    int n = 0;
+    while (acc < (double)bits && n < (int)pr.size()) acc += std::log2((double)pr[n++]);
+    return acc >= (double)bits ? n : -1;
 }
+
+static gbmm_status build_tables(crt_tables *t, int P) {
+    const auto &pr = primes_desc();
+    t->P = P;
+    t->Pp = (2 * P + 63) / 64 * 32;
+    big Mod{1};
+    for (int i = 0; i < P; i++) big_mul_small(Mod, pr[i]);
+    int modbits = (int)(32 * Mod.size());
+    t->Dout = (modbits + 7) / 8 + 2;
+    t->NT = (SROWS + t->Dout + BM - 1) / BM;
+    const int rows = t->NT * BM, cols = 2 * t->Pp;
+    std::vector<uint16_t> tab((size_t)rows * cols, bf16_bits(0.f));
+    t->h_mods.resize(P);
+    for (int i = 0; i < P; i++) {
+        const uint32_t p = pr[i];
+        uint32_t rem = 0;
+        big Mi = big_div_small(Mod, p, &rem);
+        big Mi256 = Mi;
+        big_mul_small(Mi256, 256);
+        const uint32_t w = inv_mod(big_mod_small(Mi, p), p);
+        ModConst mc;
+        memset(&mc, 0, sizeof mc);
+        mc.p = (int32_t)p;
+        mc.inv_p = 1.0f / (float)p;
+        mc.mu = (uint32_t)(((uint64_t)1 << 32) / p);
+        mc.h16 = (uint32_t)((1u << 16) % p);
+        mc.w = w;
+        t->h_mods[i] = mc;
+        // column 2i multiplies the high digit (x256), column 2i+1 the low digit
+        std::vector<int> dh = balanced256(Mi256, t->Dout), dl = balanced256(Mi, t->Dout);
+        for (int r = 0; r < t->Dout; r++) {
+            tab[(size_t)(SROWS + r) * cols + 2 * i] = bf16_bits((float)dh[r]);
+            tab[(size_t)(SROWS + r) * cols + 2 * i + 1] = bf16_bits((float)dl[r]);
+        }
+        // fixed-point weights: round(2^56 / p) for the high digit, round(2^48 / p) for the low digit
+        const unsigned __int128 one = 1;
+        uint64_t gh = (uint64_t)(((one << (FIXB + 8)) + p / 2) / p);
+        uint64_t gl = (uint64_t)(((one << FIXB) + p / 2) / p);
+        big bh{(uint32_t)gh, (uint32_t)(gh >> 32)}, bl{(uint32_t)gl, (uint32_t)(gl >> 32)};
+        std::vector<int> sh = balanced256(bh, SROWS), sl = balanced256(bl, SROWS);
+        for (int r = 0; r < SROWS; r++) {
+            tab[(size_t)r * cols + 2 * i] = bf16_bits((float)sh[r]);
+            tab[(size_t)r * cols + 2 * i + 1] = bf16_bits((float)sl[r]);
+        }
+    }
+    std::vector<int> md = balanced256(Mod, t->Dout);
+    std::vector<int8_t> md8(t->Dout);
+    for (int r = 0; r < t->Dout; r++) md8[r] = (int8_t)md[r];
+    GBMM_CUDA_TRY(cudaMalloc(&t->d_mods, sizeof(ModConst) * P));
+    GBMM_CUDA_TRY(cudaMemcpy(t->d_mods, t->h_mods.data(), sizeof(ModConst) * P, cudaMemcpyHostToDevice));
+    GBMM_CUDA_TRY(cudaMalloc(&t->d_recon, tab.size() * 2));
+    GBMM_CUDA_TRY(cudaMemcpy(t->d_recon, tab.data(), tab.size() * 2, cudaMemcpyHostToDevice));
+    GBMM_CUDA_TRY(cudaMalloc(&t->d_mdig, t->Dout));
+    GBMM_CUDA_TRY(cudaMemcpy(t->d_mdig, md8.data(), t->Dout, cudaMemcpyHostToDevice));
+    return GBMM_OK;
+}
+
+static gbmm_status residue_table(crt_tables *t, int dxp, __nv_bfloat16 **out) {
+    auto it = t->residue.find(dxp);
+    if (it != t->residue.end()) { *out = it->second; return GBMM_OK; }
+    const auto &pr = primes_desc();
+    const int rows = 2 * t->P;
+    std::vector<uint16_t> tab((size_t)rows * dxp);
+    for (int i = 0; i < t->P; i++) {
+        const uint32_t p = pr[i];
+        uint32_t v = 1;  // 256^j mod p
+        for (int j = 0; j < dxp; j++) {
+            int32_t b = v > p / 2 ? (int32_t)v - (int32_t)p : (int32_t)v;
+            int32_t d0 = ((b + 128) & 255) - 128;
+            int32_t d1 = (b - d0) / 256;
+            tab[(size_t)(2 * i) * dxp + j] = bf16_bits((float)d0);      // x1
+            tab[(size_t)(2 * i + 1) * dxp + j] = bf16_bits((float)d1);  // x256
+            v = (uint32_t)(((uint64_t)v * 256) % p);
+        }
+    }
+    __nv_bfloat16 *d = nullptr;
+    GBMM_CUDA_TRY(cudaMalloc(&d, tab.size() * 2));
+    GBMM_CUDA_TRY(cudaMemcpy(d, tab.data(), tab.size() * 2, cudaMemcpyHostToDevice));
+    t->residue[dxp] = d;
+    *out = d;
+    return GBMM_OK;
+}
+
+static gbmm_status get_tables(crt_cache *c, int P, crt_tables **out) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto it = c->by_p.find(P);
+    if (it != c->by_p.end()) { *out = it->second; return GBMM_OK; }
+    crt_tables *t = new crt_tables();
+    gbmm_status st = build_tables(t, P);
+    if (st != GBMM_OK) { delete t; return st; }
+    c->by_p[P] = t;
+    *out = t;
+    return GBMM_OK;
+}
+
+static constexpr int RES_STAGES = 4, PROD_STAGES = 3, REC_STAGES = 6, TEST_STAGES = 4;
+static size_t smem_bytes(int stages, size_t stage_bytes) { return stages * stage_bytes + sizeof(Barriers) + 1024 + 64; }
+
+static gbmm_status set_smem(const void *fn, size_t bytes) {
+    GBMM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return GBMM_OK;
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// digits + residues of one operand into planes [2P][rowsR][kp]
+static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat &X, int transpose, int rowsR, int kdim,
+                                    int kp, __nv_bfloat16 *R, cudaStream_t s) {
+    const int L = std::max(X.nlimbs, 1);
+    const int dxp = (4 * L + 63) / 64 * 64;
+    const int64_t E = (int64_t)X.rows * X.cols;
+    __nv_bfloat16 *D = (__nv_bfloat16 *)arena_alloc(h, (size_t)E * dxp * 2 + 1024);
+    if (!D) return set_error(GBMM_ERR_NOMEM, "crt: workspace for digits");
+    {
+        DigitArgs a;
+        a.limbs = X.limbs; a.ld = X.ld; a.rs = X.rs; a.rows = X.rows; a.cols = X.cols;
+        a.nlimbs = X.nlimbs; a.transpose = transpose; a.dxp = dxp; a.out = D;
+        dim3 grid((unsigned)((X.cols + 31) / 32), (unsigned)((X.rows + 3) / 4));
+        LaunchScope ls_("k_crt_digits", s);
+        k_crt_digits<<<grid, 256, 0, s>>>(a);
+        GBMM_CUDA_TRY(cudaGetLastError());
+    }
+    __nv_bfloat16 *T = nullptr;
+    GBMM_TRY(residue_table(t, dxp, &T));
+    const int nk = dxp / BK;
+    const int G = (nk + GROUP_STEPS - 1) / GROUP_STEPS;
+    int BN = 256;
+    while (BN * G > 512) BN /= 2;
+    if (BN < 32) return set_error(GBMM_ERR_UNSUPPORTED, "crt: entries too long for the residue kernel");
+    CUtensorMap tmD, tmT;
+    GBMM_TRY(make_map(&tmD, D, dxp, E, dxp, BK, BM));
+    GBMM_TRY(make_map(&tmT, T, dxp, 2 * t->P, dxp, BK, BN));
+    ResidueArgs a;
+    a.sizes = X.sizes; a.rs = X.rs; a.transpose = transpose; a.kdim = kdim; a.E = E; a.nk = nk;
+    a.BN = BN; a.G = G; a.P = t->P; a.mods = t->d_mods; a.R = R; a.plane = (int64_t)rowsR * kp; a.kp = kp;
+    const size_t sm = smem_bytes(RES_STAGES, BM * 128 + (size_t)BN * 128);
+    GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES>, sm));
+    dim3 grid((unsigned)((2 * t->P + BN - 1) / BN), (unsigned)((E + BM - 1) / BM));
+    LaunchScope ls_("k_crt_residue", s);
+    k_crt_residue<RES_STAGES><<<grid, CTA_THREADS, sm, s>>>(tmD, tmT, a, device_error_word());
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+int crt_moduli(int64_t bits_a, int64_t bits_b, int k) {
+    int lg = 0;
+    while ((1LL << lg) < std::max(k, 1)) lg++;
+    return moduli_for_bits(bits_a + bits_b + lg + 2 + 16);
+}
+
+// device workspace (bytes) one crt_matmul call carves from the arena
+static size_t crt_workspace(const gbmm_mat &a, const gbmm_mat &b, const gbmm_mat &, int64_t bits_a, int64_t bits_b,
+                            int nprimes) {
+    const int m = a.rows, k = a.cols, n = b.cols;
+    int P = nprimes > 0 ? nprimes : crt_moduli(bits_a, bits_b, k);
+    if (P <= 0) return 0;
+    const int Pp = (2 * P + 63) / 64 * 32;
+    const int kp = (k + 63) / 64 * 64;
+    const int64_t Ep = ((int64_t)m * n + 63) / 64 * 64;
+    const int dxa = (4 * std::max(a.nlimbs, 1) + 63) / 64 * 64, dxb = (4 * std::max(b.nlimbs, 1) + 63) / 64 * 64;
+    return align256((size_t)2 * P * m * kp * 2) + align256((size_t)2 * P * n * kp * 2) + align256((size_t)2 * Pp * Ep * 2) +
+           std::max(align256((size_t)m * k * dxa * 2 + 1024), align256((size_t)k * n * dxb * 2 + 1024)) + 8192;
+}
+
+gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, int64_t bits_a,
+                       int64_t bits_b, int nprimes, int accumulate, cudaStream_t s) {
+    const int m = a.rows, k = a.cols, n = b.cols;
+    if (m == 0 || n == 0) return GBMM_OK;
+    if (k == 0) return accumulate ? GBMM_OK : launch_mat_zero(c, s);
+    if (accumulate) {
+        // C += A*B: product into a workspace matrix, then one elementwise add
+        size_t mark = arena_mark(h);
+        const int cn = std::max(c.nlimbs, (int)((bits_a + bits_b + 64) / 32) + 2);
+        size_t need = align256((size_t)m * n * cn * 4) + align256((size_t)m * n * 4) + 4096;
+        GBMM_TRY(arena_reserve(h, need + crt_workspace(a, b, c, bits_a, bits_b, nprimes)));
+        gbmm_mat T;
+        T.rows = m; T.cols = n; T.nlimbs = cn; T.pad_ = 0; T.rs = n; T.ld = (int64_t)m * n;
+        T.limbs = (uint32_t *)arena_alloc(h, (size_t)m * n * cn * 4);
+        T.sizes = (int32_t *)arena_alloc(h, (size_t)m * n * 4);
+        if (!T.limbs || !T.sizes) return set_error(GBMM_ERR_NOMEM, "crt: accumulate workspace");
+        gbmm_status st = crt_matmul(h, T, a, b, bits_a, bits_b, nprimes, 0, s);
+        if (st == GBMM_OK) st = launch_mat_addsub(c, c, T, 0, s);
+        arena_release(h, mark);
+        return st;
+    }
+    if (k > GROUP_STEPS * BK) return set_error(GBMM_ERR_UNSUPPORTED, "crt: inner dimension %d > 512 per call", k);
+    int P = nprimes > 0 ? nprimes : crt_moduli(bits_a, bits_b, k);
+    if (P <= 0 || P > (int)primes_desc().size())
+        return set_error(GBMM_ERR_UNSUPPORTED, "crt: product bound needs more moduli than available");
+    crt_tables *t = nullptr;
+    GBMM_TRY(get_tables(h->crt, P, &t));
+    if (!get_encode()) return set_error(GBMM_ERR_CUDA, "crt: no tensor-map encoder");
+
+    const int kp = (k + 63) / 64 * 64;  // residue-plane row pitch (TMA needs 16-byte pitches)
+    const int64_t E = (int64_t)m * n;
+    const int64_t Ep = (E + 63) / 64 * 64;
+    const int dxa = (4 * std::max(a.nlimbs, 1) + 63) / 64 * 64, dxb = (4 * std::max(b.nlimbs, 1) + 63) / 64 * 64;
+    (void)dxa; (void)dxb;
+    GBMM_TRY(arena_reserve(h, crt_workspace(a, b, c, bits_a, bits_b, P)));
+    size_t mark = arena_mark(h);
+    __nv_bfloat16 *RA = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * P * m * kp * 2);
+    __nv_bfloat16 *RB = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * P * n * kp * 2);
+    __nv_bfloat16 *Y = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * t->Pp * Ep * 2);
+    if (!RA || !RB || !Y) return set_error(GBMM_ERR_NOMEM, "crt: workspace");
+    if (kp != k) {
+        GBMM_CUDA_TRY(cudaMemsetAsync(RA, 0, (size_t)2 * P * m * kp * 2, s));
+        GBMM_CUDA_TRY(cudaMemsetAsync(RB, 0, (size_t)2 * P * n * kp * 2, s));
+    }
+    if (Ep != E || t->Pp != P) GBMM_CUDA_TRY(cudaMemsetAsync(Y, 0, (size_t)2 * t->Pp * Ep * 2, s));
+    {
+        size_t mk = arena_mark(h);
+        GBMM_TRY(operand_residues(h, t, a, 0, m, k, kp, RA, s));
+        arena_release(h, mk);
+        GBMM_TRY(operand_residues(h, t, b, 1, n, k, kp, RB, s));
+        arena_release(h, mk);
+    }
+    uint32_t *err = device_error_word();
+    {
+        CUtensorMap tmA, tmB;
+        GBMM_TRY(make_map(&tmA, RA, kp, (uint64_t)2 * P * m, kp, BK, BM));
+        GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)2 * P * n, kp, BK, BM));
+        ProductArgs pa;
+        pa.m = m; pa.n = n; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.Ep = Ep;
+        const size_t sm = smem_bytes(PROD_STAGES, 4 * BM * 128);
+        GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES>, sm));
+        dim3 grid((unsigned)((n + BM - 1) / BM), (unsigned)((m + BM - 1) / BM), (unsigned)P);
+        LaunchScope ls_("k_crt_product", s);
+        k_crt_product<PROD_STAGES><<<grid, CTA_THREADS, sm, s>>>(tmA, tmB, pa, err);
+        GBMM_CUDA_TRY(cudaGetLastError());
+    }
+    {
+        CUtensorMap tmY, tmT;
+        GBMM_TRY(make_map(&tmY, Y, Ep, (uint64_t)2 * t->Pp, Ep, 64, BK));
+        GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * BM, 2 * t->Pp, BK, BM));
+        ReconArgs ra;
+        ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.gsplit = (ra.nk + 1) / 2; ra.NT = t->NT; ra.Dout = t->Dout;
+        ra.mdig = t->d_mdig; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
+        ra.cnlimbs = c.nlimbs;
+        const size_t sm = smem_bytes(REC_STAGES, 2 * BM * 128);
+        GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES>, sm));
+        dim3 grid((unsigned)((E + BM - 1) / BM));
+        LaunchScope ls_("k_crt_recon", s);
+        k_crt_recon<REC_STAGES><<<grid, CTA_THREADS, sm, s>>>(tmY, tmT, ra, err);
+        GBMM_CUDA_TRY(cudaGetLastError());
+    }
+    arena_release(h, mark);
+    return GBMM_OK;
+}
+
 }  // namespace gbmm
+
+using namespace gbmm;
+
+// Internal test hook (not part of the public ABI): D = A * B^T through the
+// tcgen05 pipeline.  A: bf16 [M x K] (a_mn = 0) or [K x M] (a_mn = 1), B: bf16
+// [N x K]; K a multiple of 64, M and N multiples of 128 ... any (padded by TMA).
+extern "C" gbmm_status gbmmx_test_gemm(const void *A, const void *B, int32_t *D, int32_t M, int32_t N, int32_t K,
+                                       int32_t a_mn, void *stream) {
+    cudaStream_t s = as_stream(stream);
+    if (K % 64 || M % 8 || N % 8) return set_error(GBMM_ERR_INVALID, "test gemm: K % 64, M % 8, N % 8 required");
+    CUtensorMap tmA, tmB;
+    if (a_mn) GBMM_TRY(make_map(&tmA, A, M, K, M, 64, BK));
+    else GBMM_TRY(make_map(&tmA, A, K, M, K, BK, BM));
+    GBMM_TRY(make_map(&tmB, B, K, N, K, BK, BM));
+    TestArgs ta;
+    ta.M = M; ta.N = N; ta.nk = K / BK; ta.a_mn = a_mn; ta.D = D;
+    const size_t sm = smem_bytes(TEST_STAGES, 2 * BM * 128);
+    GBMM_TRY(set_smem((const void *)k_gemm_test<TEST_STAGES>, sm));
+    dim3 grid((unsigned)((N + BM - 1) / BM), (unsigned)((M + BM - 1) / BM));
+    LaunchScope ls_("k_gemm_test", s);
+    k_gemm_test<TEST_STAGES><<<grid, CTA_THREADS, sm, s>>>(tmA, tmB, ta, device_error_word());
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return check_device_error(s);
+}
+
+extern "C" gbmm_status gbmmx_crt_params(int64_t bits_a, int64_t bits_b, int32_t k, int32_t *nmoduli) {
+    if (!nmoduli) return set_error(GBMM_ERR_INVALID, "null pointer");
+    *nmoduli = crt_moduli(bits_a, bits_b, k);
+    return GBMM_OK;
+}

@@ -104,15 +104,18 @@ __global__ void __launch_bounds__(256) k_mpn_addsub_n_cla(uint32_t *rp, const ui
 #pragma unroll
             for (int t = 0; t < CLA_Q; t++) {
                 int i = lane * CLA_Q + t;
-                uint32_t x = i < clen ? su[i][b] : 0u, y = i < clen ? sv[i][b] : 0u;
-                if (!SUB) {
-                    uint64_t s = (uint64_t)x + y + c;
-                    r[t] = (uint32_t)s; c = (uint32_t)(s >> 32);
-                    allsat &= (r[t] == 0xFFFFFFFFu) | (i >= clen);
-                } else {
-                    uint64_t d = (uint64_t)x - y - c;
-                    r[t] = (uint32_t)d; c = (uint32_t)(d >> 63);
-                    allsat &= (r[t] == 0u) | (i >= clen);
+                r[t] = 0u;
+                if (i < clen) {  // the chain stops at the chunk end
+                    uint32_t x = su[i][b], y = sv[i][b];
+                    if (!SUB) {
+                        uint64_t s = (uint64_t)x + y + c;
+                        r[t] = (uint32_t)s; c = (uint32_t)(s >> 32);
+                        allsat &= r[t] == 0xFFFFFFFFu;
+                    } else {
+                        uint64_t d = (uint64_t)x - y - c;
+                        r[t] = (uint32_t)d; c = (uint32_t)(d >> 63);
+                        allsat &= r[t] == 0u;
+                    }
                 }
             }
             g = c;
@@ -491,16 +494,17 @@ __global__ void k_max_size(MatArgs A, int64_t count, int32_t *out) {
 // M-1 serial mpz_addmul calls (mat-gpu/mat-core.h:31-53).  Here a group of G
 // threads shares one output entry: the La x Lb limb-product square of every
 // term A[y][k]*B[k][x] is tiled into R x R blocks, thread (I, J) of the group
-// owns block (I, J) for all k, and accumulates its 2R-1 partial columns in
-// 96-bit registers with no carry propagation inside the k loop.  Products
-// with a positive and a negative sign go to separate accumulator sets (the
-// sign is uniform across the group, so the branch is warp-uniform when a
-// group spans whole warps).  After the k loop the group reduces its partial
-// columns in shared memory (64-bit atomics on 32-bit words), one thread per
-// entry propagates carries, subtracts the negative sum from the positive sum,
-// and writes the sign-magnitude result.  A/B limbs for a chunk of KC terms
-// are staged in shared memory with loads that are coalesced along k (A) and
-// along x (B), and reused by every thread of the CTA's TY x TX entries.
+// owns block (I, J) for all k and keeps its 2R-1 partial columns in 96-bit
+// two's-complement registers: a term with positive sign is added, a negative
+// one subtracted (the sign is the same for the whole group, so the branch is
+// warp-uniform when groups span whole warps).  No carry leaves a column inside
+// the k loop.  After the loop each thread parks its columns in shared memory,
+// the CTA sums the partial columns of every entry (a column gathers the
+// blocks on two neighbouring anti-diagonals), one thread per entry propagates
+// the signed carries, adds the old C for C += A*B, and writes the
+// sign-magnitude result.  A/B limbs for a chunk of KC terms are staged in
+// shared memory with loads coalesced along k (A) and along x (B), read back
+// as 128-bit vectors and reused by every thread of the CTA's TY x TX entries.
 // ======================================================================================
 namespace {
 constexpr int MM_THREADS = 256;
@@ -516,40 +520,35 @@ struct MMCfg {
     int accumulate;
 };
 
-// Final step of one output entry: pl / nl hold the magnitudes of the positive
-// and negative partial sums (L2 limbs each).  Optionally adds the old C, then
-// writes sign(P-N) * |P-N| as a normalized sign-magnitude entry.
-__device__ void finish_entry(uint32_t *pl, uint32_t *nl, int L2, const MatArgs &C, int64_t ic, int accumulate,
-                             uint32_t *err) {
-    if (accumulate) {
-        const int sc = C.sizes[ic];
-        const int cn = iabs_d(sc);
-        uint32_t *dst = sc < 0 ? nl : pl;
-        uint32_t c = 0;
-        for (int t = 0; t < L2; t++) {
-            uint64_t s = (uint64_t)dst[t] + (t < cn ? C.limbs[(int64_t)t * C.ld + ic] : 0u) + c;
-            dst[t] = (uint32_t)s;
-            c = (uint32_t)(s >> 32);
+// (c0, c1, c2) -= a * b on a 96-bit two's-complement accumulator
+#define MSC96(c0, c1, c2, a, b)                                                   \
+    do {                                                                          \
+        uint64_t t_ = (uint64_t)(a) * (uint64_t)(b);                              \
+        uint64_t l_ = ((uint64_t)(c1) << 32) | (c0);                              \
+        (c2) -= (uint32_t)(l_ < t_);                                              \
+        l_ -= t_;                                                                 \
+        (c0) = (uint32_t)l_;                                                      \
+        (c1) = (uint32_t)(l_ >> 32);                                              \
+    } while (0)
+
+// Writes the signed multi-limb value held in buf[0..L) (two's complement,
+// `neg` = its sign) into entry ic of C as sign-magnitude.
+__device__ void store_signed(uint32_t *buf, int L, bool neg, const MatArgs &C, int64_t ic, uint32_t *err) {
+    if (neg) {
+        uint32_t c = 1;
+        for (int t = 0; t < L; t++) {
+            uint64_t v = (uint64_t)(~buf[t]) + c;
+            buf[t] = (uint32_t)v;
+            c = (uint32_t)(v >> 32);
         }
-        if (c || cn > L2) { atomicOr(err, DEVERR_CAPACITY); return; }
     }
-    int cmp = 0;
-    for (int t = L2 - 1; t >= 0 && cmp == 0; t--)
-        if (pl[t] != nl[t]) cmp = pl[t] < nl[t] ? -1 : 1;
-    const uint32_t *xp = cmp >= 0 ? pl : nl, *yp = cmp >= 0 ? nl : pl;
     int top = 0;
-    uint32_t br = 0;
+    for (int t = 0; t < L; t++)
+        if (buf[t]) top = t + 1;
+    if (top > C.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
     uint32_t *cl = C.limbs + ic;
-    for (int t = 0; t < L2; t++) {
-        uint64_t d = (uint64_t)xp[t] - yp[t] - br;
-        uint32_t r = (uint32_t)d;
-        br = (uint32_t)(d >> 63);
-        if (r) top = t + 1;
-        if (t < C.nlimbs) cl[(int64_t)t * C.ld] = r;
-        else if (r) { atomicOr(err, DEVERR_CAPACITY); return; }
-    }
-    for (int t = L2; t < C.nlimbs; t++) cl[(int64_t)t * C.ld] = 0u;
-    C.sizes[ic] = top == 0 ? 0 : (cmp < 0 ? -top : top);
+    for (int t = 0; t < C.nlimbs; t++) cl[(int64_t)t * C.ld] = t < top ? buf[t] : 0u;
+    C.sizes[ic] = neg ? -top : top;
 }
 
 template <int R>
@@ -571,16 +570,13 @@ __global__ void __launch_bounds__(MM_THREADS) k_limb_matmul(MatArgs C, MatArgs A
     const int y0 = blockIdx.y * TY, x0 = blockIdx.x * TX;
     const int y = y0 + ty, x = x0 + tx;
     const bool valid = has_entry && y < C.rows && x < C.cols;
-    const int nbB = Lb / R;
+    const int nbA = La / R, nbB = Lb / R;
     const bool active = valid && lt < cfg.G;
     const int I0 = active ? lt / nbB : 0, J0 = active ? lt % nbB : 0;
 
-    uint32_t P[2 * R - 1][3], Nn[2 * R - 1][3];
+    uint32_t P[2 * R - 1][3];
 #pragma unroll
-    for (int c = 0; c < 2 * R - 1; c++) {
-        P[c][0] = P[c][1] = P[c][2] = 0;
-        Nn[c][0] = Nn[c][1] = Nn[c][2] = 0;
-    }
+    for (int c = 0; c < 2 * R - 1; c++) P[c][0] = P[c][1] = P[c][2] = 0;
 
     const int M = cfg.M;
     for (int k0 = 0; k0 < M; k0 += MM_KC) {
@@ -640,76 +636,84 @@ __global__ void __launch_bounds__(MM_THREADS) k_limb_matmul(MatArgs C, MatArgs A
 #pragma unroll
                     for (int i = 0; i < R; i++)
 #pragma unroll
-                        for (int j = 0; j < R; j++) MAC96(Nn[i + j][0], Nn[i + j][1], Nn[i + j][2], a[i], b[j]);
+                        for (int j = 0; j < R; j++) MSC96(P[i + j][0], P[i + j][1], P[i + j][2], a[i], b[j]);
                 }
             }
         }
     }
     __syncthreads();
 
-    // ---- reduction of partial columns --------------------------------------------
-    const int Lc = La + Lb;  // product columns
-    if (cfg.G == 1) {
-        // one thread owns the whole entry: its registers already hold every column
-        if (!valid) return;
-        uint32_t pl[2 * R + 2], nl[2 * R + 2];
-        unsigned __int128 cp = 0, cn = 0;
-#pragma unroll
-        for (int t = 0; t < 2 * R - 1; t++) {
-            cp += (unsigned __int128)P[t][0] + ((unsigned __int128)P[t][1] << 32) + ((unsigned __int128)P[t][2] << 64);
-            cn += (unsigned __int128)Nn[t][0] + ((unsigned __int128)Nn[t][1] << 32) + ((unsigned __int128)Nn[t][2] << 64);
-            pl[t] = (uint32_t)cp; cp >>= 32;
-            nl[t] = (uint32_t)cn; cn >>= 32;
-        }
-        pl[2 * R - 1] = (uint32_t)cp; pl[2 * R] = (uint32_t)(cp >> 32); pl[2 * R + 1] = 0;
-        nl[2 * R - 1] = (uint32_t)cn; nl[2 * R] = (uint32_t)(cn >> 32); nl[2 * R + 1] = 0;
-        finish_entry(pl, nl, 2 * R + 2, C, (int64_t)y * C.rs + x, cfg.accumulate, err);
-        return;
-    }
-    unsigned long long *red = reinterpret_cast<unsigned long long *>(smem_raw);  // [EPC][2][Lc][3]
-    uint32_t *limbs_buf = reinterpret_cast<uint32_t *>(red + (size_t)EPC * 2 * Lc * 3);  // [EPC][2][Lc+2]
-    for (int q = tid; q < EPC * 2 * Lc * 3; q += MM_THREADS) red[q] = 0ull;
-    __syncthreads();
+    // ---- reduction of partial columns ---------------------------------------------------
+    const int Lc = La + Lb;       // product columns
+    const int LB = Lc + 2;        // result limbs (two extra for the carry out of the sum over k)
+    const int NC = 2 * R - 1;
+    uint32_t *part = reinterpret_cast<uint32_t *>(smem_raw);  // [EPC][G][NC][3]
+    const size_t part_words = (size_t)EPC * cfg.G * NC * 3;
+    unsigned long long *cs = reinterpret_cast<unsigned long long *>(part + ((part_words + 1) & ~(size_t)1));  // [EPC][Lc][3]
+    uint32_t *res = reinterpret_cast<uint32_t *>(cs + (size_t)EPC * Lc * 3);                                  // [EPC][LB]
     if (active) {
-        unsigned long long *rp = red + (size_t)g * 2 * Lc * 3;
-        const int cb = (I0 + J0) * R;
+        uint32_t *dst = part + ((size_t)g * cfg.G + lt) * NC * 3;
 #pragma unroll
-        for (int c = 0; c < 2 * R - 1; c++) {
-            const int col = cb + c;
-            if (P[c][0] | P[c][1] | P[c][2]) {
-                atomicAdd(&rp[(0 * Lc + col) * 3 + 0], (unsigned long long)P[c][0]);
-                atomicAdd(&rp[(0 * Lc + col) * 3 + 1], (unsigned long long)P[c][1]);
-                atomicAdd(&rp[(0 * Lc + col) * 3 + 2], (unsigned long long)P[c][2]);
-            }
-            if (Nn[c][0] | Nn[c][1] | Nn[c][2]) {
-                atomicAdd(&rp[(1 * Lc + col) * 3 + 0], (unsigned long long)Nn[c][0]);
-                atomicAdd(&rp[(1 * Lc + col) * 3 + 1], (unsigned long long)Nn[c][1]);
-                atomicAdd(&rp[(1 * Lc + col) * 3 + 2], (unsigned long long)Nn[c][2]);
+        for (int c = 0; c < NC; c++) {
+            dst[c * 3 + 0] = P[c][0];
+            dst[c * 3 + 1] = P[c][1];
+            dst[c * 3 + 2] = P[c][2];
+        }
+    }
+    __syncthreads();
+    // column t of entry gg gathers block diagonal d = t / R at offset t % R and
+    // diagonal d - 1 at offset t % R + R
+    for (int item = tid; item < EPC * Lc; item += MM_THREADS) {
+        const int gg = item / Lc, t = item % Lc;
+        unsigned long long s0 = 0, s1 = 0;
+        long long s2 = 0;
+        for (int h = 0; h < 2; h++) {
+            const int d = t / R - h, off = t % R + h * R;
+            if (d < 0 || off >= NC) continue;
+            const int i_lo = d - nbB + 1 > 0 ? d - nbB + 1 : 0, i_hi = d < nbA - 1 ? d : nbA - 1;
+            for (int i = i_lo; i <= i_hi; i++) {
+                const uint32_t *w = part + ((size_t)gg * cfg.G + i * nbB + (d - i)) * NC * 3 + off * 3;
+                s0 += w[0];
+                s1 += w[1];
+                s2 += (int32_t)w[2];
             }
         }
+        unsigned long long *o = cs + ((size_t)gg * Lc + t) * 3;
+        o[0] = s0;
+        o[1] = s1;
+        o[2] = (unsigned long long)s2;
     }
     __syncthreads();
     if (!(valid && lt == 0)) return;
 
-    // ---- carry propagation, then P - N written back (one thread per entry) -----------
-    const unsigned long long *rp = red + (size_t)g * 2 * Lc * 3;
-    uint32_t *pl = limbs_buf + (size_t)g * 2 * (Lc + 2);
-    uint32_t *nl = pl + (Lc + 2);
-    for (int s = 0; s < 2; s++) {
-        uint32_t *dst = s ? nl : pl;
-        // value of column t = w0 + w1 2^32 + w2 2^64 ; the running carry fits in 128 bits
-        unsigned __int128 carry = 0;
-        for (int t = 0; t < Lc; t++) {
-            const unsigned long long *w = rp + (s * Lc + t) * 3;
-            unsigned __int128 v = carry + (unsigned __int128)w[0] + ((unsigned __int128)w[1] << 32) +
-                                  ((unsigned __int128)w[2] << 64);
-            dst[t] = (uint32_t)v;
-            carry = v >> 32;
-        }
-        dst[Lc] = (uint32_t)carry;
-        dst[Lc + 1] = (uint32_t)(carry >> 32);
+    // ---- signed carry propagation, optional C += , write back (one thread per entry) --------
+    const int64_t ic = (int64_t)y * C.rs + x;
+    const unsigned long long *col = cs + (size_t)g * Lc * 3;
+    uint32_t *buf = res + (size_t)g * LB;
+    int sc = 0, cn = 0;
+    if (cfg.accumulate) {
+        sc = C.sizes[ic];
+        cn = iabs_d(sc);
+        if (cn > LB) { atomicOr(err, DEVERR_CAPACITY); return; }
     }
-    finish_entry(pl, nl, Lc + 2, C, (int64_t)y * C.rs + x, cfg.accumulate, err);
+    long long carry = 0;  // |carry| < 2^52
+    for (int t = 0; t < LB; t++) {
+        unsigned long long w0 = 0, w1 = 0;
+        long long w2 = 0;
+        if (t < Lc) {
+            w0 = col[t * 3];
+            w1 = col[t * 3 + 1];
+            w2 = (long long)col[t * 3 + 2];
+        }
+        long long extra = 0;
+        if (t < cn) extra = sc < 0 ? -(long long)C.limbs[(int64_t)t * C.ld + ic] : (long long)C.limbs[(int64_t)t * C.ld + ic];
+        const long long lo = (long long)(w0 & 0xFFFFFFFFull) + (carry & 0xFFFFFFFFll) + extra;
+        buf[t] = (uint32_t)lo;
+        carry = (lo >> 32) + (carry >> 32) + (long long)(w0 >> 32) + (long long)w1 + (w2 << 32);
+    }
+    // the exact sum fits LB limbs, so what is left is the sign extension (0 or -1)
+    if (carry != 0 && carry != -1) { atomicOr(err, DEVERR_CAPACITY); return; }
+    store_signed(buf, LB, carry < 0, C, ic, err);
 }
 
 // ---- host launchers ---------------------------------------------------------------------
@@ -797,8 +801,8 @@ static bool choose_mm(int la, int lb, MMCfg &cfg) {
 static size_t mm_smem(const MMCfg &c) {
     size_t stage = (size_t)c.TY * MM_KC * (c.La + 4) * 4 + (size_t)MM_KC * c.TX * (c.Lb + 4) * 4 +
                    (size_t)(c.TY + c.TX) * MM_KC * 4;
-    const int EPC = c.TY * c.TX, Lc = c.La + c.Lb;
-    size_t red = c.G == 1 ? 0 : (size_t)EPC * 2 * Lc * 3 * 8 + (size_t)EPC * 2 * (Lc + 2) * 4;
+    const int EPC = c.TY * c.TX, Lc = c.La + c.Lb, NC = 2 * c.R - 1;
+    size_t red = (size_t)EPC * c.G * NC * 3 * 4 + 8 + (size_t)EPC * Lc * 3 * 8 + (size_t)EPC * (Lc + 2) * 4;
     return stage > red ? stage : red;
 }
 

@@ -361,29 +361,65 @@ def run_gpu(args, W, world, rank, local):
     return 0
 
 
+def primes_desc_16():
+    sieve = bytearray([1]) * 65536
+    sieve[0] = sieve[1] = 0
+    for i in range(2, 256):
+        if sieve[i]:
+            sieve[i * i::i] = bytearray(len(sieve[i * i::i]))
+    return [i for i in range(65535, 2, -1) if sieve[i]]
+
+
+def crt_params(bits_a, bits_b, k):
+    """Moduli count P and output digit count Dout chosen by the CRT path."""
+    import math
+    lg = max(0, math.ceil(math.log2(max(k, 1))))
+    bound = bits_a + bits_b + lg + 2 + 16
+    pr = primes_desc_16()
+    acc, P, mod = 0.0, 0, 1
+    while acc < bound:
+        acc += math.log2(pr[P])
+        mod *= pr[P]
+        P += 1
+    modbits = 32 * ((mod.bit_length() + 31) // 32)
+    return P, (modbits + 7) // 8 + 2
+
+
 def kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof):
-    """Algorithmic work of the dominant kernel per launch / its mean CUDA-event time."""
+    """Algorithmic work of the dominant kernel per launch / its mean CUDA-event time.
+    Tensor kernels: useful bf16 FLOPs (2 per digit MAC, no tile padding counted).
+    Memory kernels: bytes that must move (inputs read once, outputs written once)."""
     per_ms = kms / max(1, klaunch)
     hbm = peaks.get("hbm_gbs", 6800.0)
     bf16 = peaks.get("bf16_tflops", 1900.0)
     src = "measured" if peaks else "fallback"
-    try:
-        import gbmm_roofline
-        r = gbmm_roofline.describe(kname, K, M, N, nl, cn, args)
-    except Exception:
-        r = None
-    if r is None:
-        # limb traffic: A and B read once, C written once (planes + sizes), per launch
+    P, Dout = crt_params(32 * nl, 32 * nl, M)
+    dx = 4 * nl
+    flops = None
+    note = ""
+    if kname == "k_crt_product":
+        flops = 2.0 * K * M * N * 4 * P
+        note = f"4 digit-pair GEMMs per modulus, P={P} moduli, {K}x{M}x{N}"
+    elif kname == "k_crt_residue":
+        flops = 2.0 * (K * M + M * N) / 2 * dx * 2 * P  # one launch per operand (square: equal halves)
+        note = f"entries x {dx} digits x {2 * P} table columns per operand"
+    elif kname == "k_crt_recon":
+        flops = 2.0 * K * N * 2 * P * (8 + Dout)
+        note = f"entries x {2 * P} moduli digits x {8 + Dout} output columns"
+    if flops is not None:
+        ach = flops / (per_ms * 1e-3) / 1e12
+        return {"kernel": kname, "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+                "frac": ach / bf16, "traffic": None, "peak_source": src + " (bf16 dense, burst)",
+                "ms_per_launch": per_ms, "note": note}
+    # memory-bound kernels: algorithmic bytes per launch
+    if kname == "k_crt_digits":
+        bytes_ = ((K * M + M * N) / 2) * (4 * nl + 2 * ((4 * nl + 63) // 64 * 64))
+    else:
         bytes_ = (4 * nl * (K * M + M * N) + 4 * (K * M + M * N) + 4 * cn * K * N + 4 * K * N) / max(1, klaunch)
-        ach = bytes_ / (per_ms * 1e-3) / 1e9
-        return {"kernel": kname, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                "traffic": None, "peak_source": src, "ms_per_launch": per_ms,
-                "note": "integer-MAC bound kernel; algorithmic bytes = A+B read once, C written once"}
-    unit_peak = bf16 if r["bound"] == "tensor" else hbm
-    ach = r["work"] / (per_ms * 1e-3) / (1e12 if r["bound"] == "tensor" else 1e9)
-    return {"kernel": kname, "bound": r["bound"], "achieved": ach, "peak": unit_peak,
-            "unit": "TFLOP/s" if r["bound"] == "tensor" else "GB/s", "frac": ach / unit_peak,
-            "traffic": r.get("traffic"), "peak_source": src, "ms_per_launch": per_ms, "note": r.get("note", "")}
+        note = "integer-MAC bound kernel; algorithmic bytes = A+B read once, C written once"
+    ach = bytes_ / (per_ms * 1e-3) / 1e9
+    return {"kernel": kname, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+            "traffic": None, "peak_source": src, "ms_per_launch": per_ms, "note": note}
 
 
 def main():

@@ -704,11 +704,24 @@ int oracle_matmul_planes(int K, int M, int N,
                          uint32_t *Cl, int32_t *Cs, int32_t cn, int64_t ldc,
                          int method, int basesz, int jobsz, int nthreads, int accumulate) {
     const num_ops *saved = g_ops;
+    const int use_gmp = g_ops == &g_gmp_ops;
     g_ops = &g_own_ops;
     mat_t A = mat_init((unsigned)M, (unsigned)K), B = mat_init((unsigned)N, (unsigned)M), C = mat_init((unsigned)N, (unsigned)K);
     for (int64_t e = 0; e < (int64_t)K * M; e++) planes_to_own(&A[e], Al, As, lda, e);
     for (int64_t e = 0; e < (int64_t)M * N; e++) planes_to_own(&B[e], Bl, Bs, ldb, e);
     if (accumulate) for (int64_t e = 0; e < (int64_t)K * N; e++) planes_to_own(&C[e], Cl, Cs, ldc, e);
+    if (use_gmp) {
+        /* move the operands into GMP-managed numbers (same struct shape) */
+        g_ops = &g_gmp_ops;
+        mat_t A2 = mat_init((unsigned)M, (unsigned)K), B2 = mat_init((unsigned)N, (unsigned)M), C2 = mat_init((unsigned)N, (unsigned)K);
+        for (int64_t e = 0; e < (int64_t)K * M; e++) g_gmp_ops.set(&A2[e], &A[e]);
+        for (int64_t e = 0; e < (int64_t)M * N; e++) g_gmp_ops.set(&B2[e], &B[e]);
+        for (int64_t e = 0; e < (int64_t)K * N; e++) g_gmp_ops.set(&C2[e], &C[e]);
+        g_ops = &g_own_ops;
+        mat_free((unsigned)M, (unsigned)K, A); mat_free((unsigned)N, (unsigned)M, B); mat_free((unsigned)N, (unsigned)K, C);
+        A = A2; B = B2; C = C2;
+        g_ops = &g_gmp_ops;
+    }
     if (basesz <= 0) basesz = 32;
     if (jobsz <= 0) jobsz = 128;
     if (accumulate) naive_threaded((unsigned)K, (unsigned)M, (unsigned)N, C, N, A, M, B, N, nthreads, 1);

@@ -1,0 +1,167 @@
+"""The CRT tensor-core path: the tcgen05 GEMM core against exact integer
+products, and whole products C = A*B against the golden fixtures and the CPU
+oracle (bit-exact).  Also size-independent checks at the 512^3 / 4096-bit
+scale: sampled entries against Python integers and the linearity
+A*(B1 + B2) = A*B1 + A*B2."""
+import ctypes
+import random
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def g(built_lib):
+    import gbmm
+    gbmm.default_handle()
+    return gbmm
+
+
+def _bf16(torch, ints):
+    return torch.tensor(ints, dtype=torch.float32).to(torch.bfloat16).cuda()
+
+
+@pytest.mark.parametrize("M,N,K,a_mn", [(128, 128, 64, 0), (256, 384, 512, 0), (200, 136, 192, 0),
+                                        (128, 128, 64, 1), (256, 128, 1024, 1), (192, 256, 128, 1)])
+def test_tcgen05_gemm_core(g, M, N, K, a_mn):
+    import torch
+    rng = np.random.default_rng(M + N + K + a_mn)
+    A = rng.integers(-128, 128, size=(M, K))
+    B = rng.integers(-128, 128, size=(N, K))
+    A[0, :] = -128
+    B[0, :] = -128                       # the largest |partial sum| the CRT GEMMs rely on
+    exp = A @ B.T
+    dA = _bf16(torch, A.T.copy() if a_mn else A)
+    dB = _bf16(torch, B)
+    D = torch.zeros(M * N, dtype=torch.int32, device="cuda")
+    L = g.lib()
+    L.gbmmx_test_gemm.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int32] * 4 + [ctypes.c_void_p]
+    g.check(L.gbmmx_test_gemm(dA.data_ptr(), dB.data_ptr(), D.data_ptr(), M, N, K, a_mn, g.stream_ptr()))
+    torch.cuda.synchronize()
+    got = D.cpu().numpy().reshape(M, N)
+    assert (got == exp).all(), f"{(got != exp).sum()} mismatches"
+
+
+def _crt(g, K, M, N, dA, dB, nl=None, nprimes=0):
+    nl = nl or g.limbs_needed(dA.nlimbs, dB.nlimbs, M, path=g.PATH_CRT)
+    dC = g.DeviceMatrix(K, N, nl)
+    g.default_handle().matmul(dC, dA, dB, path=g.PATH_CRT, nprimes=nprimes)
+    return dC
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_crt_matmul_golden(g, name):
+    text, expect = load_golden(name)
+    K, M, N, A, B = g.parse_matrix_text(text)
+    dA = g.DeviceMatrix.from_ints(K, M, A)
+    dB = g.DeviceMatrix.from_ints(M, N, B)
+    dC = _crt(g, K, M, N, dA, dB)
+    limbs, sizes = dC.download()
+    assert g.format_hex(limbs, sizes, K, N) == expect
+
+
+def _signed(rng, n, bits, zero=0.05):
+    out = []
+    for _ in range(n):
+        r = rng.random()
+        if r < zero:
+            m = 0
+        elif r < zero + 0.05:
+            m = rng.getrandbits(64)
+        elif r < zero + 0.1:
+            m = (1 << bits) - 1
+        else:
+            m = rng.getrandbits(bits)
+        out.append(-m if rng.random() < 0.5 else m)
+    return out
+
+
+@pytest.mark.parametrize("K,M,N,bits", [(129, 65, 130, 2048), (64, 512, 64, 1024), (3, 7, 5, 16384),
+                                        (256, 256, 256, 512), (1, 1, 300, 4096), (40, 200, 33, 33)])
+def test_crt_matmul_vs_oracle(g, oracle, K, M, N, bits):
+    rng = random.Random(K * 7 + M * 11 + N + bits)
+    A = _signed(rng, K * M, bits)
+    B = _signed(rng, M * N, bits)
+    nl = (bits + 31) // 32
+    dA = g.DeviceMatrix.from_ints(K, M, A, nl)
+    dB = g.DeviceMatrix.from_ints(M, N, B, nl)
+    dC = _crt(g, K, M, N, dA, dB)
+    Cl, Cs = oracle.matmul_planes(K, M, N, g.ints_to_planes(A, nl), g.ints_to_planes(B, nl), dC.nlimbs, method=1,
+                                  nthreads=8)
+    limbs, sizes = dC.download()
+    assert (sizes == Cs).all()
+    assert (limbs == Cl).all()
+
+
+def test_crt_cancellation_and_tiny_results(g):
+    # rows of A whose products cancel exactly (C entries 0 or tiny): the sign is
+    # then decided on the two's-complement path of the reconstruction
+    rng = random.Random(4)
+    K, M, N, bits = 130, 64, 20, 3000
+    A = _signed(rng, K * M, bits)
+    B = _signed(rng, M * N, bits)
+    for y in range(0, K, 2):
+        for k in range(0, M, 2):
+            A[y * M + k + 1] = -A[y * M + k]
+    for k in range(0, M, 2):
+        for x in range(N):
+            B[(k + 1) * N + x] = B[k * N + x] + (1 if (k + x) % 3 == 0 else 0)
+    nl = (bits + 31) // 32
+    dA = g.DeviceMatrix.from_ints(K, M, A, nl)
+    dB = g.DeviceMatrix.from_ints(M, N, B, nl)
+    dC = _crt(g, K, M, N, dA, dB)
+    exp = [sum(A[y * M + k] * B[k * N + x] for k in range(M)) for y in range(K) for x in range(N)]
+    assert dC.to_ints() == exp
+
+
+def test_crt_accumulate(g):
+    rng = random.Random(8)
+    K, M, N, bits = 70, 30, 50, 700
+    A, B = _signed(rng, K * M, bits), _signed(rng, M * N, bits)
+    C0 = _signed(rng, K * N, 1500)
+    nl = (bits + 31) // 32
+    dA = g.DeviceMatrix.from_ints(K, M, A, nl)
+    dB = g.DeviceMatrix.from_ints(M, N, B, nl)
+    dC = g.DeviceMatrix.from_ints(K, N, C0, 2 * nl + 3)
+    g.default_handle().matmul(dC, dA, dB, path=g.PATH_CRT, accumulate=True)
+    exp = [C0[y * N + x] + sum(A[y * M + k] * B[k * N + x] for k in range(M)) for y in range(K) for x in range(N)]
+    assert dC.to_ints() == exp
+
+
+def _entry(limbs, sizes, e):
+    m = int.from_bytes(np.ascontiguousarray(limbs[:, e]).tobytes(), "little")
+    return -m if sizes[e] < 0 else m
+
+
+def test_crt_full_size_512_4096_sampled_and_linear(g):
+    """512x512x512 at 4096 bits: 64 sampled entries exact against Python
+    integers, and A*(B1+B2) == A*B1 + A*B2 over the whole matrix."""
+    import bench
+    rng = np.random.default_rng(99)
+    K = M = N = 512
+    Al, As = bench.gen_planes(rng, K * M, 4096, 0, 0, 0)
+    B1l, B1s = bench.gen_planes(rng, M * N, 4095, 0, 0, 0)
+    B2l, B2s = bench.gen_planes(rng, M * N, 4095, 0, 0, 0)
+    dA = g.DeviceMatrix(K, M, 128)
+    dA.upload(Al, As)
+    dB1, dB2, dBs = g.DeviceMatrix(M, N, 128), g.DeviceMatrix(M, N, 128), g.DeviceMatrix(M, N, 128)
+    dB1.upload(B1l, B1s)
+    dB2.upload(B2l, B2s)
+    g.mat_add(dBs, dB1, dB2)
+    nl = g.limbs_needed(128, 128, M, path=g.PATH_CRT)
+    C1, C2, Cs = (_crt(g, K, M, N, dA, d, nl) for d in (dB1, dB2, dBs))
+    Csum = g.DeviceMatrix(K, N, nl)
+    g.mat_add(Csum, C1, C2)
+    l1, s1 = Cs.download()
+    l2, s2 = Csum.download()
+    assert (s1 == s2).all() and (l1 == l2).all()
+    lc, sc = C1.download()
+    srng = np.random.default_rng(5)
+    for _ in range(64):
+        y, x = int(srng.integers(K)), int(srng.integers(N))
+        exp = sum(_entry(Al, As, y * M + k) * _entry(B1l, B1s, k * N + x) for k in range(M))
+        assert _entry(lc, sc, y * N + x) == exp

@@ -100,3 +100,16 @@ def test_null_arguments_rejected(built_lib):
     assert L.gbmm_create(None) == gbmm.ERR_INVALID
     assert L.gbmm_mpn_add_n(None, None, None, 4, 4, 1, None, None) == gbmm.ERR_INVALID
     assert b"null" in L.gbmm_last_error_string()
+
+
+def test_cli_generate_matches_oracle_generator(built_lib, oracle):
+    import subprocess
+    import build as gbuild
+    cli = gbuild.CLI
+    ref = oracle.CLI_PATH
+    if not os.path.exists(ref):
+        oracle.build(with_ref=False)
+    for args in (["-n", "3,4,5", "-b", "200", "-s", "9"], ["-n", "1,7,2", "-b", "64", "-s", "1"]):
+        a = subprocess.run([cli, "-g"] + args, stdout=subprocess.PIPE, check=True).stdout
+        b = subprocess.run([ref, "-g"] + args, stdout=subprocess.PIPE, check=True).stdout
+        assert a == b

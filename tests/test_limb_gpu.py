@@ -86,7 +86,7 @@ def test_mpn_mul_basecase(g, oracle, un, vn):
     assert (_host(dr).reshape(un + vn, nb) == exp).all()
 
 
-@pytest.mark.parametrize("an,bn", [(2, 2), (3, 2), (8, 5), (40, 40), (41, 40), (128, 128), (127, 100)])
+@pytest.mark.parametrize("an,bn", [(2, 2), (3, 2), (3, 3), (8, 5), (40, 40), (41, 40), (128, 128), (127, 100), (9, 6)])
 def test_mpn_toom22_and_mul(g, oracle, an, bn):
     import torch
     rng = np.random.default_rng(an * 7 + bn)
@@ -97,10 +97,15 @@ def test_mpn_toom22_and_mul(g, oracle, an, bn):
     a[an - 1, 3] = 1
     exp = oracle.mpn_mul_basecase(a, b)
     dp = torch.zeros((an + bn) * nb, dtype=torch.int32, device="cuda")
-    scratch = torch.zeros(g.mpn_toom22_mul_itch(an, bn) * nb, dtype=torch.int32, device="cuda")
-    g.mpn_toom22_mul(dp, _dev(torch, a), an, _dev(torch, b), bn, scratch, nb, nb)
-    torch.cuda.synchronize()
-    assert (_host(dp).reshape(an + bn, nb) == exp).all()
+    s, n = an >> 1, an - (an >> 1)
+    if 0 < bn - n <= s:  # GMP's toom22 preconditions (toom22_mul.cu:134-135)
+        scratch = torch.zeros(g.mpn_toom22_mul_itch(an, bn) * nb, dtype=torch.int32, device="cuda")
+        g.mpn_toom22_mul(dp, _dev(torch, a), an, _dev(torch, b), bn, scratch, nb, nb)
+        torch.cuda.synchronize()
+        assert (_host(dp).reshape(an + bn, nb) == exp).all()
+    else:
+        with pytest.raises(g.GbmmError):
+            g.mpn_toom22_mul(dp, _dev(torch, a), an, _dev(torch, b), bn, dp, nb, nb)
     dp.zero_()
     g.mpn_mul(dp, _dev(torch, a), an, _dev(torch, b), bn, nb, nb)
     torch.cuda.synchronize()
