@@ -48,10 +48,12 @@ constexpr int BM = 128;  // tile rows (TMEM lanes)
 constexpr int BK = 64;   // bf16 elements per K step (one 128-byte swizzle row)
 constexpr int UK = 16;   // K of one kind::f16 MMA
 constexpr int GROUP_STEPS = 8;  // K steps per exact accumulation group (512 digits)
-constexpr int SROWS = 8;        // fixed-point rows at the top of the reconstruction table
+constexpr int SROWS = 32;       // columns before the first output digit in the reconstruction table
+constexpr int SUSED = 8;        // of which the fixed-point sum uses the first 8
 constexpr int FIXB = 48;        // fixed-point bits of the 1/p_i weights
-constexpr int EPI_THREADS = 128;
-constexpr int CTA_THREADS = 192;  // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+constexpr int CTA_THREADS = 192;   // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+constexpr int CTA_THREADS8 = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue (two per lane quadrant)
+constexpr int RBN = 256;           // reconstruction N tile (output digit columns)
 }  // namespace
 
 struct ModConst {
@@ -203,7 +205,8 @@ __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
 }
 
 // ======================================================================================
-// 2. residue GEMM
+// 2. residue GEMM (persistent; TMEM double-buffered so a tile's epilogue overlaps
+//    the next tile's MMAs; 8 epilogue warps, two per TMEM lane quadrant)
 // ======================================================================================
 struct ResidueArgs {
     const int32_t *sizes;  // sizes of the source matrix (for the entry signs)
@@ -211,8 +214,10 @@ struct ResidueArgs {
     int32_t transpose, kdim;  // entry e -> (e / kdim, e % kdim) in digit-row order
     int64_t E;                // entries (digit rows)
     int32_t nk;               // K steps of 64 digits
-    int32_t BN, G;            // table columns per tile, accumulation groups
+    int32_t BN, G;            // table columns per tile, accumulation groups (G * BN <= 256)
     int32_t P;
+    int32_t n_ntiles;
+    int64_t ntiles;
     const ModConst *mods;
     __nv_bfloat16 *R;  // planes [2P][rowsR][kp]
     int64_t plane;     // rowsR * kp
@@ -220,7 +225,7 @@ struct ResidueArgs {
 };
 
 template <int STAGES>
-__global__ void __launch_bounds__(CTA_THREADS, 1)
+__global__ void __launch_bounds__(CTA_THREADS8, 1)
     k_crt_residue(const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmT, ResidueArgs a,
                   uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
@@ -228,93 +233,109 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
     const uint32_t A_BYTES = BM * 128, B_BYTES = (uint32_t)a.BN * 128, STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n0 = blockIdx.x * a.BN;
-    const int64_t e0 = (int64_t)blockIdx.y * BM;
-    cta_setup(bars, STAGES, 512, 1, 1);
+    cta_setup(bars, STAGES, 512, 1, 8);
     const uint32_t tmem = bars->tmem_base;
 
     if (warp == 0) {
         if (lane == 0) {
             tc::prefetch_tmap(&tmD);
             tc::prefetch_tmap(&tmT);
-            for (int s = 0; s < a.nk; s++) {
-                const int st = s % STAGES;
-                if (s >= STAGES && !tc::mbar_wait(&bars->empty[st], ((s / STAGES) & 1) ^ 1)) {
-                    set_abort(bars, err);
-                    break;
+            int it = 0;
+            for (int64_t t = blockIdx.x; t < a.ntiles && !aborted(bars); t += gridDim.x) {
+                const int64_t e0 = (t / a.n_ntiles) * BM;
+                const int n0 = (int)(t % a.n_ntiles) * a.BN;
+                for (int s = 0; s < a.nk; s++, it++) {
+                    const int st = it % STAGES;
+                    if (it >= STAGES && !tc::mbar_wait(&bars->empty[st], ((it / STAGES) & 1) ^ 1)) {
+                        set_abort(bars, err);
+                        break;
+                    }
+                    uint8_t *sa = base + st * STAGE;
+                    tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                    tc::tma_load_2d(sa, &tmD, &bars->full[st], s * BK, (int)e0);
+                    tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, n0);
                 }
-                if (aborted(bars)) break;
-                uint8_t *sa = base + st * STAGE;
-                tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                tc::tma_load_2d(sa, &tmD, &bars->full[st], s * BK, (int)e0);
-                tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, n0);
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
             const uint32_t idesc = tc::idesc_bf16_f32(BM, a.BN, 0, 0);
+            int it = 0, lt = 0;
             bool ok = true;
-            for (int s = 0; s < a.nk; s++) {
-                const int st = s % STAGES;
-                if (!tc::mbar_wait(&bars->full[st], (s / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+            for (int64_t t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x, lt++) {
+                const int b = lt & 1;
+                if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
                 tc::fence_after_sync();
-                const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
-                const int g = s / GROUP_STEPS;
-                const uint32_t d = tmem + (uint32_t)(g * a.BN);
+                for (int s = 0; s < a.nk; s++, it++) {
+                    const int st = it % STAGES;
+                    if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+                    tc::fence_after_sync();
+                    const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
+                    const uint32_t d = tmem + (uint32_t)(256 * b + (s / GROUP_STEPS) * a.BN);
 #pragma unroll
-                for (int kk = 0; kk < BK / UK; kk++) {
-                    tc::mma_bf16(d, tc::sdesc_kmajor(sa + kk * 32), tc::sdesc_kmajor(sb + kk * 32), idesc,
-                                 (s % GROUP_STEPS) != 0 || kk != 0);
+                    for (int kk = 0; kk < BK / UK; kk++)
+                        tc::mma_bf16(d, tc::sdesc_kmajor(sa + kk * 32), tc::sdesc_kmajor(sb + kk * 32), idesc,
+                                     (s % GROUP_STEPS) != 0 || kk != 0);
+                    tc::mma_commit(&bars->empty[st]);
                 }
-                tc::mma_commit(&bars->empty[st]);
+                if (ok) tc::mma_commit(&bars->tfull[b]);
             }
-            if (ok) tc::mma_commit(&bars->tfull[0]);
         }
     } else {
-        // epilogue: one thread per digit row (entry)
-        const int row = epi_row();
-        const int64_t e = e0 + row;
-        bool ok = tc::mbar_wait(&bars->tfull[0], 0);
-        if (!ok) set_abort(bars, err);
-        tc::fence_after_sync();
-        int neg = 0;
-        if (ok && e < a.E) {
-            int64_t r = e / a.kdim, c = e % a.kdim;
-            int64_t src = a.transpose ? c * a.rs + r : r * a.rs + c;
-            neg = a.sizes[src] < 0;
-        }
-        const uint32_t lb = lane_base(tmem);
-        for (int c0 = 0; c0 < a.BN && ok; c0 += 32) {
-            int32_t res[16];
-#pragma unroll
-            for (int j = 0; j < 16; j++) res[j] = 0;
-            for (int g = 0; g < a.G; g++) {
-                uint32_t v[32];
-                tc::tmem_ld32(lb + (uint32_t)(g * a.BN + c0), v);
-                tc::tmem_ld_wait();
-#pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    const int mi = (n0 + c0) / 2 + j;
-                    const ModConst mc = a.mods[mi < a.P ? mi : 0];
-                    int32_t r0 = mod_s32(tc::acc_int(v[2 * j]), mc.p, mc.inv_p);
-                    int32_t r1 = mod_s32(tc::acc_int(v[2 * j + 1]), mc.p, mc.inv_p);
-                    uint32_t t = mod_u32((uint32_t)r1 * 256u + (uint32_t)r0 + (uint32_t)res[j], (uint32_t)mc.p, mc.mu);
-                    res[j] = (int32_t)t;
-                }
-            }
+        // epilogue: warp (2..9) -> lane quadrant warp % 4, column half (warp - 2) / 4
+        const int quad = warp & 3, half = (warp - 2) >> 2;
+        const int hcols = a.BN / 2;
+        const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
+        int lt = 0;
+        for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, lt++) {
+            const int b = lt & 1;
+            const int64_t e = (t / a.n_ntiles) * BM + quad * 32 + lane;
+            const int n0 = (int)(t % a.n_ntiles) * a.BN;
+            if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); break; }
+            tc::fence_after_sync();
+            int neg = 0;
+            int64_t off = 0;
             if (e < a.E) {
-                const int64_t off = (e / a.kdim) * a.kp + (e % a.kdim);
+                const int64_t r = e / a.kdim, c = e % a.kdim;
+                neg = a.sizes[a.transpose ? c * a.rs + r : r * a.rs + c] < 0;
+                off = r * a.kp + c;
+            }
+            for (int c0 = half * hcols; c0 < (half + 1) * hcols; c0 += 32) {
+                int32_t res[16];
 #pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    const int mi = (n0 + c0) / 2 + j;
-                    if (mi >= a.P) continue;
-                    const int32_t p = a.mods[mi].p;
-                    int32_t r = res[j];
-                    if (neg && r) r = p - r;
-                    float hi, lo;
-                    balanced_digits(r, p, hi, lo);
-                    a.R[(int64_t)(2 * mi) * a.plane + off] = __float2bfloat16_rn(hi);
-                    a.R[(int64_t)(2 * mi + 1) * a.plane + off] = __float2bfloat16_rn(lo);
+                for (int j = 0; j < 16; j++) res[j] = 0;
+                const int mi0 = (n0 + c0) / 2;
+                for (int g = 0; g < a.G; g++) {
+                    uint32_t v[32];
+                    tc::tmem_ld32(lb + (uint32_t)(256 * b + g * a.BN + c0), v);
+                    tc::tmem_ld_wait();
+                    if (g == a.G - 1 && c0 + 32 >= (half + 1) * hcols) {
+                        // last TMEM read of this tile by this warp: hand the buffer back
+                        tc::fence_before_sync();
+                        __syncwarp();
+                        if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
+                    }
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const ModConst mc = a.mods[mi0 + j < a.P ? mi0 + j : 0];
+                        // s0 + 256 * s1 (+ residue of earlier groups), each |s| < 2^24
+                        const int32_t r1 = mod_s32(tc::acc_int(v[2 * j + 1]), mc.p, mc.inv_p);
+                        res[j] = mod_s32(tc::acc_int(v[2 * j]) + 256 * r1 + res[j], mc.p, mc.inv_p);
+                    }
+                }
+                if (e < a.E) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const int mi = mi0 + j;
+                        if (mi >= a.P) continue;
+                        const int32_t p = a.mods[mi].p;
+                        int32_t r = res[j];
+                        if (neg && r) r = p - r;
+                        float hi, lo;
+                        balanced_digits(r, p, hi, lo);
+                        a.R[(int64_t)(2 * mi) * a.plane + off] = __float2bfloat16_rn(hi);
+                        a.R[(int64_t)(2 * mi + 1) * a.plane + off] = __float2bfloat16_rn(lo);
+                    }
                 }
             }
         }
@@ -323,111 +344,145 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
 }
 
 // ======================================================================================
-// 3. per-modulus product GEMM
+// 3. per-modulus product GEMM (persistent over (modulus, 128 x 64 output tiles);
+//    TMEM double-buffered; 8 epilogue warps)
 // ======================================================================================
 struct ProductArgs {
     int32_t m, n, nk, P;
+    int32_t nyt, nxt;
+    int64_t ntiles;
     const ModConst *mods;
     __nv_bfloat16 *Y;  // planes [2Pp][Ep]
     int64_t Ep;
 };
+constexpr int PBX = 64;  // output columns per product tile
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
 
 template <int STAGES>
-__global__ void __launch_bounds__(CTA_THREADS, 1)
+__global__ void __launch_bounds__(CTA_THREADS8, 1)
     k_crt_product(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, ProductArgs a,
                   uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
-    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = 2 * BM * 128, STAGE = 2 * A_BYTES + B_BYTES;
+    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = PBX * 128, STAGE = 2 * A_BYTES + 2 * B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int x0 = blockIdx.x * BM, y0 = blockIdx.y * BM, mi = blockIdx.z;
-    cta_setup(bars, STAGES, 512, 1, 1);
+    cta_setup(bars, STAGES, 512, 1, 8);
     const uint32_t tmem = bars->tmem_base;
+    const int64_t per_mod = (int64_t)a.nyt * a.nxt;
 
     if (warp == 0) {
         if (lane == 0) {
             tc::prefetch_tmap(&tmA);
             tc::prefetch_tmap(&tmB);
-            for (int s = 0; s < a.nk; s++) {
-                const int st = s % STAGES;
-                if (s >= STAGES && !tc::mbar_wait(&bars->empty[st], ((s / STAGES) & 1) ^ 1)) {
-                    set_abort(bars, err);
-                    break;
+            int it = 0;
+            for (int64_t t = blockIdx.x; t < a.ntiles && !aborted(bars); t += gridDim.x) {
+                const int mi = (int)(t / per_mod), r = (int)(t % per_mod);
+                const int y0 = (r / a.nxt) * BM, x0 = (r % a.nxt) * PBX;
+                for (int s = 0; s < a.nk; s++, it++) {
+                    const int st = it % STAGES;
+                    if (it >= STAGES && !tc::mbar_wait(&bars->empty[st], ((it / STAGES) & 1) ^ 1)) {
+                        set_abort(bars, err);
+                        break;
+                    }
+                    uint8_t *sa = base + st * STAGE;
+                    tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                    tc::tma_load_2d(sa, &tmA, &bars->full[st], s * BK, (2 * mi) * a.m + y0);
+                    tc::tma_load_2d(sa + A_BYTES, &tmA, &bars->full[st], s * BK, (2 * mi + 1) * a.m + y0);
+                    tc::tma_load_2d(sa + 2 * A_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi) * a.n + x0);
+                    tc::tma_load_2d(sa + 2 * A_BYTES + B_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi + 1) * a.n + x0);
                 }
-                if (aborted(bars)) break;
-                uint8_t *sa = base + st * STAGE;
-                tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                tc::tma_load_2d(sa, &tmA, &bars->full[st], s * BK, (2 * mi) * a.m + y0);
-                tc::tma_load_2d(sa + A_BYTES, &tmA, &bars->full[st], s * BK, (2 * mi + 1) * a.m + y0);
-                tc::tma_load_2d(sa + 2 * A_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi) * a.n + x0);
-                tc::tma_load_2d(sa + 2 * A_BYTES + BM * 128, &tmB, &bars->full[st], s * BK, (2 * mi + 1) * a.n + x0);
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = tc::idesc_bf16_f32(BM, 2 * BM, 0, 0);
+            // [B1|B0] is one 128-row operand; A1 -> columns [0,128), A0 -> [128,256) of the buffer
+            const uint32_t idesc = tc::idesc_bf16_f32(BM, 2 * PBX, 0, 0);
+            int it = 0, lt = 0;
             bool ok = true;
-            for (int s = 0; s < a.nk; s++) {
-                const int st = s % STAGES;
-                if (!tc::mbar_wait(&bars->full[st], (s / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+            for (int64_t t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x, lt++) {
+                const int b = lt & 1;
+                if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
                 tc::fence_after_sync();
-                const uint32_t sa1 = tc::smem_u32(base + st * STAGE), sa0 = sa1 + A_BYTES, sb = sa1 + 2 * A_BYTES;
+                const uint32_t d = tmem + 256u * b;
+                for (int s = 0; s < a.nk; s++, it++) {
+                    const int st = it % STAGES;
+                    if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+                    tc::fence_after_sync();
+                    const uint32_t sa1 = tc::smem_u32(base + st * STAGE), sa0 = sa1 + A_BYTES, sb = sa1 + 2 * A_BYTES;
 #pragma unroll
-                for (int kk = 0; kk < BK / UK; kk++) {
-                    const uint64_t bd = tc::sdesc_kmajor(sb + kk * 32);
-                    tc::mma_bf16(tmem, tc::sdesc_kmajor(sa1 + kk * 32), bd, idesc, s != 0 || kk != 0);
-                    tc::mma_bf16(tmem + 256, tc::sdesc_kmajor(sa0 + kk * 32), bd, idesc, s != 0 || kk != 0);
+                    for (int kk = 0; kk < BK / UK; kk++) {
+                        const uint64_t bd = tc::sdesc_kmajor(sb + kk * 32);
+                        tc::mma_bf16(d, tc::sdesc_kmajor(sa1 + kk * 32), bd, idesc, s != 0 || kk != 0);
+                        tc::mma_bf16(d + 2 * PBX, tc::sdesc_kmajor(sa0 + kk * 32), bd, idesc, s != 0 || kk != 0);
+                    }
+                    tc::mma_commit(&bars->empty[st]);
                 }
-                tc::mma_commit(&bars->empty[st]);
+                if (ok) tc::mma_commit(&bars->tfull[b]);
             }
-            if (ok) tc::mma_commit(&bars->tfull[0]);
         }
     } else {
-        const int row = epi_row();
-        bool ok = tc::mbar_wait(&bars->tfull[0], 0);
-        if (!ok) set_abort(bars, err);
-        tc::fence_after_sync();
-        const ModConst mc = a.mods[mi];
-        // staging for coalesced stores: [2 planes][128 rows][128 x] bf16, in the idle pipeline buffers
-        __nv_bfloat16 *stg = reinterpret_cast<__nv_bfloat16 *>(base);
-        const uint32_t lb = lane_base(tmem);
-        for (int xb = 0; xb < BM && ok; xb += 32) {
-            uint32_t d11[32], d10[32], d01[32], d00[32];
-            tc::tmem_ld32(lb + (uint32_t)xb, d11);
-            tc::tmem_ld32(lb + (uint32_t)(BM + xb), d10);
-            tc::tmem_ld32(lb + (uint32_t)(2 * BM + xb), d01);
-            tc::tmem_ld32(lb + (uint32_t)(3 * BM + xb), d00);
-            tc::tmem_ld_wait();
+        const int quad = warp & 3, half = (warp - 2) >> 2;
+        const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
+        int lt = 0;
+        for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, lt++) {
+            const int b = lt & 1;
+            const int mi = (int)(t / per_mod), r = (int)(t % per_mod);
+            const int y = (r / a.nxt) * BM + quad * 32 + lane;
+            const int xh = (r % a.nxt) * PBX + half * 32;  // this warp's 32 output columns
+            if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); break; }
+            tc::fence_after_sync();
+            const ModConst mc = a.mods[mi];
+            __nv_bfloat16 *yhi = a.Y + (int64_t)(2 * mi) * a.Ep + (int64_t)y * a.n + xh;
+            __nv_bfloat16 *ylo = a.Y + (int64_t)(2 * mi + 1) * a.Ep + (int64_t)y * a.n + xh;
+            const bool full_row = y < a.m && xh + 32 <= a.n && ((reinterpret_cast<uintptr_t>(yhi) | reinterpret_cast<uintptr_t>(ylo)) & 15) == 0;
+            for (int c = 0; c < 32; c += 16) {
+                uint32_t d11[16], d10[16], d01[16], d00[16];
+                const uint32_t col = 256u * b + half * 32 + c;
+                tc::tmem_ld16(lb + col, d11);
+                tc::tmem_ld16(lb + col + PBX, d10);
+                tc::tmem_ld16(lb + col + 2 * PBX, d01);
+                tc::tmem_ld16(lb + col + 3 * PBX, d00);
+                tc::tmem_ld_wait();
+                if (c == 16) {
+                    tc::fence_before_sync();
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
+                }
+                uint32_t phi[8], plo[8];
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-                int32_t r11 = mod_s32(tc::acc_int(d11[j]), mc.p, mc.inv_p);
-                int32_t r1 = mod_s32(tc::acc_int(d10[j]) + tc::acc_int(d01[j]), mc.p, mc.inv_p);
-                int32_t r0 = mod_s32(tc::acc_int(d00[j]), mc.p, mc.inv_p);
-                uint32_t t = mod_u32((uint32_t)r11 * mc.h16, (uint32_t)mc.p, mc.mu);
-                uint32_t c = mod_u32(t + (uint32_t)r1 * 256u + (uint32_t)r0, (uint32_t)mc.p, mc.mu);
-                uint32_t y = mod_u32(c * mc.w, (uint32_t)mc.p, mc.mu);
-                float hi, lo;
-                balanced_digits((int32_t)y, mc.p, hi, lo);
-                stg[(0 * BM + row) * BM + xb + j] = __float2bfloat16_rn(hi);
-                stg[(1 * BM + row) * BM + xb + j] = __float2bfloat16_rn(lo);
-            }
-        }
-        epi_bar();
-        if (ok) {
-            // 4 warps write rows: each warp-row store is 128 x 2 bytes contiguous
-            const int ew = (threadIdx.x >> 5) - 2;
-            for (int q = ew; q < 2 * BM; q += 4) {
-                const int d = q / BM, r = q % BM, y = y0 + r;
-                if (y >= a.m) continue;
-                __nv_bfloat16 *dst = a.Y + (int64_t)(2 * mi + d) * a.Ep + (int64_t)y * a.n + x0;
-                const __nv_bfloat16 *src = stg + (d * BM + r) * BM;
-                if ((reinterpret_cast<uintptr_t>(dst) & 7) == 0 && x0 + BM <= a.n) {
-                    // 8-byte vector stores only when the row segment is 8-byte aligned and complete
-                    *reinterpret_cast<uint2 *>(dst + lane * 4) = *reinterpret_cast<const uint2 *>(src + lane * 4);
-                } else {
-                    for (int x = lane; x < BM; x += 32)
-                        if (x0 + x < a.n) dst[x] = src[x];
+                for (int j = 0; j < 16; j += 2) {
+                    float h2[2], l2[2];
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        const int32_t r11 = mod_s32(tc::acc_int(d11[j + u]), mc.p, mc.inv_p);
+                        const int32_t r1 = mod_s32(tc::acc_int(d10[j + u]) + tc::acc_int(d01[j + u]), mc.p, mc.inv_p);
+                        const uint32_t t16 = mod_u32((uint32_t)r11 * mc.h16, (uint32_t)mc.p, mc.mu);
+                        const int32_t cc = mod_s32((int32_t)t16 + 256 * r1 + tc::acc_int(d00[j + u]), mc.p, mc.inv_p);
+                        const uint32_t yv = mod_u32((uint32_t)cc * mc.w, (uint32_t)mc.p, mc.mu);
+                        balanced_digits((int32_t)yv, mc.p, h2[u], l2[u]);
+                    }
+                    phi[j / 2] = pack_bf16x2(h2[0], h2[1]);
+                    plo[j / 2] = pack_bf16x2(l2[0], l2[1]);
+                }
+                if (full_row) {
+                    uint4 *dh = reinterpret_cast<uint4 *>(yhi + c), *dl = reinterpret_cast<uint4 *>(ylo + c);
+                    dh[0] = make_uint4(phi[0], phi[1], phi[2], phi[3]);
+                    dh[1] = make_uint4(phi[4], phi[5], phi[6], phi[7]);
+                    dl[0] = make_uint4(plo[0], plo[1], plo[2], plo[3]);
+                    dl[1] = make_uint4(plo[4], plo[5], plo[6], plo[7]);
+                } else if (y < a.m) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        if (xh + c + j >= a.n) break;
+                        const uint32_t wh = phi[j / 2] >> (16 * (j & 1)), wl = plo[j / 2] >> (16 * (j & 1));
+                        reinterpret_cast<uint16_t *>(yhi)[c + j] = (uint16_t)wh;
+                        reinterpret_cast<uint16_t *>(ylo)[c + j] = (uint16_t)wl;
+                    }
                 }
             }
         }
@@ -436,16 +491,17 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
 }
 
 // ======================================================================================
-// 4. reconstruction GEMM
+// 4. reconstruction GEMM (one CTA per 128 entries, N tiles of 256 digit columns,
+//    TMEM double-buffered across tiles; base-128 table digits so one FP32
+//    accumulation over all 2P rows stays exact: 2P * 128 * 64 < 2^24)
 // ======================================================================================
 struct ReconArgs {
     int64_t E;       // entries of C
     int32_t ncols;   // columns of C (entry e -> row e / ncols, col e % ncols)
     int32_t nk;      // K steps over 2Pp
-    int32_t gsplit;  // first K step of accumulation group 1
-    int32_t NT;      // N tiles of 128 table rows
-    int32_t Dout;    // output digit positions
-    const int8_t *mdig;  // balanced base-256 digits of Mod, Dout entries
+    int32_t NT;      // N tiles of RBN table rows
+    int32_t Dout;    // output base-128 digit positions
+    const int8_t *mdig;  // balanced base-128 digits of Mod, Dout entries
     uint32_t *climbs;
     int32_t *csizes;
     int64_t cld, crs;
@@ -458,10 +514,12 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
                 uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
-    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = BM * 128, STAGE = A_BYTES + B_BYTES;
+    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = RBN * 128, STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
+    int8_t *smdig = reinterpret_cast<int8_t *>(bars + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t e0 = (int64_t)blockIdx.x * BM;
+    for (int i = threadIdx.x; i < a.Dout + 32; i += blockDim.x) smdig[i] = i < a.Dout ? a.mdig[i] : 0;
     cta_setup(bars, STAGES, 512, 1, 4);
     const uint32_t tmem = bars->tmem_base;
 
@@ -477,42 +535,34 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
                         set_abort(bars, err);
                         break;
                     }
-                    if (aborted(bars)) break;
                     uint8_t *sa = base + st * STAGE;
                     tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
                     // A (MN-major): two boxes of 64 entries x 64 K-rows
                     tc::tma_load_2d(sa, &tmY, &bars->full[st], (int)e0, s * BK);
                     tc::tma_load_2d(sa + A_BYTES / 2, &tmY, &bars->full[st], (int)e0 + 64, s * BK);
-                    tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, j * BM);
+                    tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, j * RBN);
                 }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = tc::idesc_bf16_f32(BM, BM, 1, 0);
+            const uint32_t idesc = tc::idesc_bf16_f32(BM, RBN, 1, 0);
             int it = 0;
             bool ok = true;
             for (int j = 0; j < a.NT && ok; j++) {
                 const int b = j & 1;
-                if (j >= 2 && !tc::mbar_wait(&bars->tempty[b], ((j >> 1) & 1) ^ 1)) {
-                    set_abort(bars, err);
-                    ok = false;
-                    break;
-                }
+                if (j >= 2 && !tc::mbar_wait(&bars->tempty[b], ((j >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
                 tc::fence_after_sync();
+                const uint32_t d = tmem + 256u * b;
                 for (int s = 0; s < a.nk; s++, it++) {
                     const int st = it % STAGES;
                     if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
                     tc::fence_after_sync();
                     const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
-                    const int g = s >= a.gsplit;
-                    const uint32_t d = tmem + (uint32_t)(256 * b + 128 * g);
-                    const int first = g ? (s == a.gsplit) : (s == 0);
 #pragma unroll
-                    for (int kk = 0; kk < BK / UK; kk++) {
+                    for (int kk = 0; kk < BK / UK; kk++)
                         tc::mma_bf16(d, tc::sdesc_mnmajor(sa + kk * 2048, A_BYTES / 2), tc::sdesc_kmajor(sb + kk * 32),
-                                     idesc, !(first && kk == 0));
-                    }
+                                     idesc, s != 0 || kk != 0);
                     tc::mma_commit(&bars->empty[st]);
                 }
                 if (ok) tc::mma_commit(&bars->tfull[b]);
@@ -522,57 +572,54 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
         const int row = epi_row();
         const int64_t e = e0 + row;
         const bool live = e < a.E;
-        const bool two = a.gsplit < a.nk;  // accumulation group 1 is empty when K has a single step
         const int64_t coff = live ? (e / a.ncols) * a.crs + (e % a.ncols) : 0;
         const uint32_t lb = lane_base(tmem);
-        int64_t carry = 0;
-        int32_t q = 0, sigma = 1;
+        int32_t carry = 0, q = 0, smask = 0;  // smask = -1 flips every digit column (C < 0)
         bool ambiguous = false, ok = true;
-        uint32_t limb = 0;
         int pos = 0, top = 0;
         bool drop_nz = false, drop_ones = true;
         for (int j = 0; j < a.NT; j++) {
             const int b = j & 1;
             if (!tc::mbar_wait(&bars->tfull[b], (j >> 1) & 1)) { set_abort(bars, err); ok = false; break; }
             tc::fence_after_sync();
-            for (int c0 = 0; c0 < BM; c0 += 32) {
-                uint32_t g0[32], g1[32];
-                tc::tmem_ld32(lb + (uint32_t)(256 * b + c0), g0);
-                tc::tmem_ld32(lb + (uint32_t)(256 * b + 128 + c0), g1);
+            for (int c0 = 0; c0 < RBN; c0 += 32) {
+                uint32_t g[32];
+                tc::tmem_ld32(lb + (uint32_t)(256 * b + c0), g);
                 tc::tmem_ld_wait();
-                if (c0 + 32 >= BM) {
-                    // this tile's TMEM is fully read: release it to the MMA warp
+                if (c0 + 32 >= RBN) {
                     tc::fence_before_sync();
                     __syncwarp();
                     if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
                 }
-                int jbeg = 0;
                 if (j == 0 && c0 == 0) {
-                    // fixed-point sum S = sum y_i 2^48 / p_i in the first SROWS columns
+                    // fixed-point sum S = sum y_i 2^48 / p_i from the first SUSED columns (base 128)
                     __int128 S = 0;
 #pragma unroll
-                    for (int t = SROWS - 1; t >= 0; t--) S = S * 256 + (tc::acc_int(g0[t]) + (two ? tc::acc_int(g1[t]) : 0));
-                    const __int128 half = (__int128)1 << (FIXB - 1);
-                    __int128 qq = (S + half) >> FIXB;
-                    __int128 frac = S - (qq << FIXB);
+                    for (int t = SUSED - 1; t >= 0; t--) S = S * 128 + tc::acc_int(g[t]);
+                    const __int128 halfw = (__int128)1 << (FIXB - 1);
+                    const __int128 qq = (S + halfw) >> FIXB;
+                    const __int128 frac = S - (qq << FIXB);
                     q = (int32_t)qq;
                     const __int128 tol = (__int128)1 << 20;
-                    if (frac > tol) sigma = 1;
-                    else if (frac < -tol) sigma = -1;
-                    else { sigma = 1; ambiguous = true; }
-                    jbeg = SROWS;
+                    smask = frac < -tol ? -1 : 0;
+                    ambiguous = frac <= tol && frac >= -tol;
+                    continue;
                 }
-                if (!live) continue;
+                if (!live || pos >= a.Dout) continue;
+                // 32 base-128 digits = 224 bits = 7 limbs; chunks start on limb boundaries
+                uint64_t bits = 0;
+                int nb = 0, li = pos / 32 * 7;
 #pragma unroll
                 for (int t = 0; t < 32; t++) {
-                    if (t < jbeg || pos >= a.Dout) continue;
-                    int64_t v = (int64_t)(tc::acc_int(g0[t]) + (two ? tc::acc_int(g1[t]) : 0)) - (int64_t)q * a.mdig[pos];
-                    v = sigma * v + carry;
-                    const uint32_t dg = (uint32_t)(v & 255);
-                    carry = v >> 8;
-                    limb |= dg << (8 * (pos & 3));
-                    if ((pos & 3) == 3) {
-                        const int li = pos >> 2;
+                    int32_t v = tc::acc_int(g[t]) - q * (int32_t)smdig[pos + t];
+                    v = ((v ^ smask) - smask) + carry;
+                    carry = v >> 7;
+                    bits |= (uint64_t)(uint32_t)(v & 127) << nb;
+                    nb += 7;
+                    if (nb >= 32) {
+                        const uint32_t limb = (uint32_t)bits;
+                        bits >>= 32;
+                        nb -= 32;
                         if (li < a.cnlimbs) {
                             a.climbs[(int64_t)li * a.cld + coff] = limb;
                             if (limb) top = li + 1;
@@ -580,31 +627,20 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
                             drop_nz |= limb != 0u;
                             drop_ones &= limb == 0xFFFFFFFFu;
                         }
-                        limb = 0;
+                        li++;
                     }
-                    pos++;
                 }
+                pos += 32;
             }
         }
         if (ok && live) {
-            // flush a partial limb
-            if (pos & 3) {
-                const int li = pos >> 2;
-                if (carry < 0) limb |= 0xFFFFFFFFu << (8 * (pos & 3));
-                if (li < a.cnlimbs) {
-                    a.climbs[(int64_t)li * a.cld + coff] = limb;
-                    if (limb) top = li + 1;
-                } else {
-                    drop_nz |= limb != 0u;
-                    drop_ones &= limb == 0xFFFFFFFFu;
-                }
-                pos = (li + 1) * 4;
-            }
-            const int written = pos >> 2 < a.cnlimbs ? pos >> 2 : a.cnlimbs;
-            int neg = sigma < 0;
+            const int nl = pos / 32 * 7;  // limbs produced
+            const int written = nl < a.cnlimbs ? nl : a.cnlimbs;
+            int neg = smask != 0;
             if (carry < 0) {
                 // only reachable on the ambiguous path: two's complement -> magnitude
-                if (!ambiguous || (pos >> 2 > a.cnlimbs && !(drop_ones && top != 0))) atomicOr(err, DEVERR_CAPACITY);
+                if (!ambiguous || carry != -1 || (nl > a.cnlimbs && !(drop_ones && top != 0)))
+                    atomicOr(err, DEVERR_CAPACITY);
                 uint32_t cc = 1;
                 top = 0;
                 for (int li = 0; li < written; li++) {
@@ -772,17 +808,19 @@ static uint32_t big_mod_small(const big &x, uint32_t d) {
     for (size_t i = x.size(); i-- > 0;) r = ((r << 32) | x[i]) % d;
     return (uint32_t)r;
 }
-// balanced base-256 digits (each in [-128, 127]) of a nonnegative integer
-static std::vector<int> balanced256(const big &x, int ndig) {
+// balanced base-128 digits (each in [-64, 63]) of a nonnegative integer
+static std::vector<int> balanced128(const big &x, int ndig) {
     std::vector<int> out(ndig, 0);
-    std::vector<int> bytes;
-    for (uint32_t l : x)
-        for (int b = 0; b < 4; b++) bytes.push_back((l >> (8 * b)) & 255);
+    const int nbits = (int)(32 * x.size());
     int carry = 0;
     for (int t = 0; t < ndig; t++) {
-        int v = (t < (int)bytes.size() ? bytes[t] : 0) + carry;
-        int d = v >= 128 ? v - 256 : v;
-        carry = (v - d) / 256;
+        int v = carry;
+        for (int b = 0; b < 7; b++) {
+            const int bit = 7 * t + b;
+            if (bit < nbits && ((x[bit / 32] >> (bit % 32)) & 1u)) v += 1 << b;
+        }
+        const int d = v >= 64 ? v - 128 : v;
+        carry = (v - d) / 128;
         out[t] = d;
     }
     return out;
@@ -863,9 +901,9 @@ static gbmm_status build_tables(crt_tables *t, int P) {
     big Mod{1};
     for (int i = 0; i < P; i++) big_mul_small(Mod, pr[i]);
     int modbits = (int)(32 * Mod.size());
-    t->Dout = (modbits + 7) / 8 + 2;
-    t->NT = (SROWS + t->Dout + BM - 1) / BM;
-    const int rows = t->NT * BM, cols = 2 * t->Pp;
+    t->Dout = (modbits + 6) / 7 + 2;  // base-128 output digits
+    t->NT = (SROWS + t->Dout + RBN - 1) / RBN;
+    const int rows = t->NT * RBN, cols = 2 * t->Pp;
     std::vector<uint16_t> tab((size_t)rows * cols, bf16_bits(0.f));
     t->h_mods.resize(P);
     for (int i = 0; i < P; i++) {
@@ -884,7 +922,7 @@ static gbmm_status build_tables(crt_tables *t, int P) {
         mc.w = w;
         t->h_mods[i] = mc;
         // column 2i multiplies the high digit (x256), column 2i+1 the low digit
-        std::vector<int> dh = balanced256(Mi256, t->Dout), dl = balanced256(Mi, t->Dout);
+        std::vector<int> dh = balanced128(Mi256, t->Dout), dl = balanced128(Mi, t->Dout);
         for (int r = 0; r < t->Dout; r++) {
             tab[(size_t)(SROWS + r) * cols + 2 * i] = bf16_bits((float)dh[r]);
             tab[(size_t)(SROWS + r) * cols + 2 * i + 1] = bf16_bits((float)dl[r]);
@@ -894,13 +932,13 @@ static gbmm_status build_tables(crt_tables *t, int P) {
         uint64_t gh = (uint64_t)(((one << (FIXB + 8)) + p / 2) / p);
         uint64_t gl = (uint64_t)(((one << FIXB) + p / 2) / p);
         big bh{(uint32_t)gh, (uint32_t)(gh >> 32)}, bl{(uint32_t)gl, (uint32_t)(gl >> 32)};
-        std::vector<int> sh = balanced256(bh, SROWS), sl = balanced256(bl, SROWS);
-        for (int r = 0; r < SROWS; r++) {
+        std::vector<int> sh = balanced128(bh, SUSED), sl = balanced128(bl, SUSED);
+        for (int r = 0; r < SUSED; r++) {
             tab[(size_t)r * cols + 2 * i] = bf16_bits((float)sh[r]);
             tab[(size_t)r * cols + 2 * i + 1] = bf16_bits((float)sl[r]);
         }
     }
-    std::vector<int> md = balanced256(Mod, t->Dout);
+    std::vector<int> md = balanced128(Mod, t->Dout);
     std::vector<int8_t> md8(t->Dout);
     for (int r = 0; r < t->Dout; r++) md8[r] = (int8_t)md[r];
     GBMM_CUDA_TRY(cudaMalloc(&t->d_mods, sizeof(ModConst) * P));
@@ -950,7 +988,18 @@ static gbmm_status get_tables(crt_cache *c, int P, crt_tables **out) {
     return GBMM_OK;
 }
 
-static constexpr int RES_STAGES = 4, PROD_STAGES = 3, REC_STAGES = 6, TEST_STAGES = 4;
+static constexpr int RES_STAGES = 4, PROD_STAGES = 4, REC_STAGES = 4, TEST_STAGES = 4;
+
+static int num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 148;
+    }
+    return n;
+}
 static size_t smem_bytes(int stages, size_t stage_bytes) { return stages * stage_bytes + sizeof(Barriers) + 1024 + 64; }
 
 static gbmm_status set_smem(const void *fn, size_t bytes) {
@@ -982,19 +1031,21 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     const int nk = dxp / BK;
     const int G = (nk + GROUP_STEPS - 1) / GROUP_STEPS;
     int BN = 256;
-    while (BN * G > 512) BN /= 2;
-    if (BN < 32) return set_error(GBMM_ERR_UNSUPPORTED, "crt: entries too long for the residue kernel");
+    while (BN * G > 256) BN /= 2;
+    if (BN < 64) return set_error(GBMM_ERR_UNSUPPORTED, "crt: entries longer than 16384 bits");
     CUtensorMap tmD, tmT;
     GBMM_TRY(make_map(&tmD, D, dxp, E, dxp, BK, BM));
     GBMM_TRY(make_map(&tmT, T, dxp, 2 * t->P, dxp, BK, BN));
     ResidueArgs a;
     a.sizes = X.sizes; a.rs = X.rs; a.transpose = transpose; a.kdim = kdim; a.E = E; a.nk = nk;
     a.BN = BN; a.G = G; a.P = t->P; a.mods = t->d_mods; a.R = R; a.plane = (int64_t)rowsR * kp; a.kp = kp;
+    a.n_ntiles = (2 * t->P + BN - 1) / BN;
+    a.ntiles = (int64_t)a.n_ntiles * ((E + BM - 1) / BM);
     const size_t sm = smem_bytes(RES_STAGES, BM * 128 + (size_t)BN * 128);
     GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES>, sm));
-    dim3 grid((unsigned)((2 * t->P + BN - 1) / BN), (unsigned)((E + BM - 1) / BM));
+    dim3 grid((unsigned)std::min<int64_t>(a.ntiles, num_sms()));
     LaunchScope ls_("k_crt_residue", s);
-    k_crt_residue<RES_STAGES><<<grid, CTA_THREADS, sm, s>>>(tmD, tmT, a, device_error_word());
+    k_crt_residue<RES_STAGES><<<grid, CTA_THREADS8, sm, s>>>(tmD, tmT, a, device_error_word());
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
 }
@@ -1019,6 +1070,23 @@ static size_t crt_workspace(const gbmm_mat &a, const gbmm_mat &b, const gbmm_mat
            std::max(align256((size_t)m * k * dxa * 2 + 1024), align256((size_t)k * n * dxb * 2 + 1024)) + 8192;
 }
 
+bool crt_feasible(int la, int lb, int k) {
+    const int P = crt_moduli(32LL * la, 32LL * lb, std::min(k, GROUP_STEPS * BK));
+    return P > 0 && P <= 1023 && 4 * std::max(la, lb) <= 4 * GROUP_STEPS * BK;
+}
+
+size_t crt_workspace_bytes(int la, int lb, int m, int k, int n, int cn) {
+    gbmm_mat a, b, c;
+    memset(&a, 0, sizeof a); memset(&b, 0, sizeof b); memset(&c, 0, sizeof c);
+    const int kc = std::min(k, GROUP_STEPS * BK);
+    a.rows = m; a.cols = kc; a.nlimbs = la;
+    b.rows = kc; b.cols = n; b.nlimbs = lb;
+    size_t ws = crt_workspace(a, b, c, 32LL * la, 32LL * lb, 0);
+    // an accumulating chunk adds a product-sized temporary
+    if (k > kc) ws += align256((size_t)m * n * (std::max(cn, la + lb + 4) + 1) * 4) + 8192;
+    return ws;
+}
+
 gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, int64_t bits_a,
                        int64_t bits_b, int nprimes, int accumulate, cudaStream_t s) {
     const int m = a.rows, k = a.cols, n = b.cols;
@@ -1040,10 +1108,19 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         arena_release(h, mark);
         return st;
     }
-    if (k > GROUP_STEPS * BK) return set_error(GBMM_ERR_UNSUPPORTED, "crt: inner dimension %d > 512 per call", k);
+    if (k > GROUP_STEPS * BK) {
+        // inner dimension in chunks of 512: C = A_0 B_0, then C += A_j B_j
+        for (int k0 = 0; k0 < k; k0 += GROUP_STEPS * BK) {
+            const int kc = std::min(GROUP_STEPS * BK, k - k0);
+            gbmm_mat ac = sub_view(a, 0, k0, m, kc), bc = sub_view(b, k0, 0, kc, n);
+            GBMM_TRY(crt_matmul(h, c, ac, bc, bits_a, bits_b, nprimes, k0 > 0, s));
+        }
+        return GBMM_OK;
+    }
     int P = nprimes > 0 ? nprimes : crt_moduli(bits_a, bits_b, k);
-    if (P <= 0 || P > (int)primes_desc().size())
-        return set_error(GBMM_ERR_UNSUPPORTED, "crt: product bound needs more moduli than available");
+    // one exact FP32 accumulation in the reconstruction covers 2P * 2^13 < 2^24
+    if (P <= 0 || P > 1023)
+        return set_error(GBMM_ERR_UNSUPPORTED, "crt: product bound needs %d moduli (at most 1023)", P);
     crt_tables *t = nullptr;
     GBMM_TRY(get_tables(h->crt, P, &t));
     if (!get_encode()) return set_error(GBMM_ERR_CUDA, "crt: no tensor-map encoder");
@@ -1075,25 +1152,28 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     {
         CUtensorMap tmA, tmB;
         GBMM_TRY(make_map(&tmA, RA, kp, (uint64_t)2 * P * m, kp, BK, BM));
-        GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)2 * P * n, kp, BK, BM));
+        GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)2 * P * n, kp, BK, PBX));
         ProductArgs pa;
         pa.m = m; pa.n = n; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.Ep = Ep;
-        const size_t sm = smem_bytes(PROD_STAGES, 4 * BM * 128);
+        pa.nyt = (m + BM - 1) / BM;
+        pa.nxt = (n + PBX - 1) / PBX;
+        pa.ntiles = (int64_t)P * pa.nyt * pa.nxt;
+        const size_t sm = smem_bytes(PROD_STAGES, 2 * BM * 128 + 2 * PBX * 128);
         GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES>, sm));
-        dim3 grid((unsigned)((n + BM - 1) / BM), (unsigned)((m + BM - 1) / BM), (unsigned)P);
+        dim3 grid((unsigned)std::min<int64_t>(pa.ntiles, num_sms()));
         LaunchScope ls_("k_crt_product", s);
-        k_crt_product<PROD_STAGES><<<grid, CTA_THREADS, sm, s>>>(tmA, tmB, pa, err);
+        k_crt_product<PROD_STAGES><<<grid, CTA_THREADS8, sm, s>>>(tmA, tmB, pa, err);
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     {
         CUtensorMap tmY, tmT;
         GBMM_TRY(make_map(&tmY, Y, Ep, (uint64_t)2 * t->Pp, Ep, 64, BK));
-        GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * BM, 2 * t->Pp, BK, BM));
+        GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RBN, 2 * t->Pp, BK, RBN));
         ReconArgs ra;
-        ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.gsplit = (ra.nk + 1) / 2; ra.NT = t->NT; ra.Dout = t->Dout;
+        ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.NT = t->NT; ra.Dout = t->Dout;
         ra.mdig = t->d_mdig; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
         ra.cnlimbs = c.nlimbs;
-        const size_t sm = smem_bytes(REC_STAGES, 2 * BM * 128);
+        const size_t sm = smem_bytes(REC_STAGES, BM * 128 + RBN * 128) + t->Dout + 64;
         GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES>, sm));
         dim3 grid((unsigned)((E + BM - 1) / BM));
         LaunchScope ls_("k_crt_recon", s);

@@ -72,6 +72,10 @@ gbmm_status launch_limb_matmul(const gbmm_mat &c, const gbmm_mat &a, const gbmm_
 gbmm_status launch_mat_zero(const gbmm_mat &c, cudaStream_t s);
 gbmm_status launch_mat_copy(const gbmm_mat &dst, const gbmm_mat &src, cudaStream_t s);
 gbmm_status launch_max_size(const gbmm_mat &a, int32_t *d_out, cudaStream_t s);
+gbmm_status launch_split_sizes(const gbmm_mat &x, int h, int32_t *lo, int32_t *hi, cudaStream_t s);
+gbmm_status launch_add_shifted(const gbmm_mat &w, const gbmm_mat &u, const gbmm_mat &v, int sh, cudaStream_t s);
+// whether the per-entry product kernel handles la x lb limb entries
+bool limb_kernel_fits(int la, int lb);
 
 // ---- CRT path (crt.cu) --------------------------------------------------------------
 struct crt_cache;
@@ -79,6 +83,48 @@ crt_cache *crt_cache_create();
 void crt_cache_destroy(crt_cache *);
 gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b,
                        int64_t bits_a, int64_t bits_b, int nprimes, int accumulate, cudaStream_t s);
+// whether the CRT kernels take la x lb limb entries with inner dimension k directly
+bool crt_feasible(int la, int lb, int k);
+// device workspace one crt_matmul call with these shapes carves from the arena
+size_t crt_workspace_bytes(int la, int lb, int m, int k, int n, int cn);
+
+// ---- persistent batched limb kernel (limb.cu) ---------------------------------------------
+// Host-side plan of one batch of limb-path products: a blob holding the job
+// descriptors and the (job, tile) work items of every block-edge group.
+struct LimbBatchPlan {
+    std::vector<char> blob;
+    struct Group {
+        int R = 0;
+        size_t jobs_off = 0, items_off = 0;
+        int nitems = 0;
+        size_t smem = 0;
+    };
+    std::vector<Group> groups;
+};
+gbmm_status plan_limb_batch(const std::vector<gbmm_mat> &C, const std::vector<gbmm_mat> &A,
+                            const std::vector<gbmm_mat> &B, LimbBatchPlan &plan);
+// d_blob holds plan.blob on the device; d_counters has one int per group
+gbmm_status launch_limb_batch(const LimbBatchPlan &plan, const char *d_blob, int *d_counters, cudaStream_t s);
+
+// ---- dispatch (host.cpp, batch.cpp) ------------------------------------------------------
+struct Plan {
+    int path;     // GBMM_PATH_LIMB or GBMM_PATH_CRT after resolution
+    int method;   // limb path square method
+    int cutoff;   // limb path recursion cutoff
+    int nprimes;  // CRT moduli (0 = from the bound)
+};
+int heuristic_path(int m, int k, int n, int la, int lb);
+// AUTO path choice: learned model when loaded, tuning table, else the heuristic
+int choose_path(gbmm_handle h, int m, int k, int n, int la, int lb, int *cutoff);
+size_t dispatch_ws(const Plan &p, int la, int lb, int m, int k, int n, int cn, int accumulate);
+gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, const Plan &p,
+                     int accumulate, cudaStream_t s);
+gbmm_status resolve_plan(gbmm_handle h, const gbmm_mat &a, const gbmm_mat &b, const gbmm_opts &o, Plan &p);
+void invalidate_graphs(gbmm_handle h);
+void batch_state_destroy(gbmm_handle h);
+// learned cost model (mlp.cu): path for one product, or -1 when no model applies
+int model_choose(gbmm_handle h, int m, int k, int n, int la, int lb, int *cutoff);
+void model_destroy(gbmm_handle h);
 
 // ---- device workspace arena -------------------------------------------------------------
 // One growing allocation per handle, carved out stack-wise; freeing happens in
@@ -99,8 +145,11 @@ struct gbmm_handle_s {
     gbmm::crt_cache *crt = nullptr;
     // tuning knobs (filled from defaults or the autotuner)
     int limb_cutoff = 32;
-    // learned-dispatch model (null when not loaded)
+    // learned-dispatch model (null when not loaded) and whether AUTO consults it
     void *model = nullptr;
+    int use_model = 0;
+    // batched-execution state: tuning table, graph cache, staging (batch.cpp)
+    void *batch = nullptr;
 };
 
 namespace gbmm {

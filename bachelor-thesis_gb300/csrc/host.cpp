@@ -119,6 +119,7 @@ gbmm_status arena_reserve(gbmm_handle h, size_t bytes) {
     size_t want = std::max(bytes, h->ws.cap * 2);
     want = (want + 0xFFFFF) & ~(size_t)0xFFFFF;
     GBMM_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    invalidate_graphs(h);  // captured graphs point into the old block
     if (h->ws.base) GBMM_CUDA_TRY(cudaFree(h->ws.base));
     h->ws.base = nullptr;
     h->ws.cap = 0;
@@ -146,6 +147,7 @@ static bool arena_mat(gbmm_handle h, int rows, int cols, int nlimbs, gbmm_mat &m
     return m.limbs && m.sizes;
 }
 static size_t mat_bytes(int64_t n, int nlimbs) { return (size_t)n * nlimbs * 4 + (size_t)n * 4 + 2 * 256 + 32; }
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 }  // namespace gbmm
 
@@ -210,6 +212,8 @@ extern "C" gbmm_status gbmm_create(gbmm_handle *out) {
 extern "C" gbmm_status gbmm_destroy(gbmm_handle h) {
     if (!h) return GBMM_OK;
     cudaStreamSynchronize(h->stream);
+    batch_state_destroy(h);
+    model_destroy(h);
     if (h->ws.base) cudaFree(h->ws.base);
     crt_cache_destroy(h->crt);
     delete h;
@@ -639,7 +643,9 @@ gbmm_status rec_naive(RecCtx &c, gbmm_mat C, gbmm_mat A, gbmm_mat B, int N, int 
 }
 
 gbmm_status rec_square(RecCtx &c, int method, gbmm_mat C, gbmm_mat A, gbmm_mat B, int N, int levels, int addmul) {
-    if (levels <= 0 || N % 2 != 0 || N / 2 < 1) return launch_limb_matmul(C, A, B, addmul, c.s);
+    // recursion is skipped when the one-limb-longer sums it forms would not fit the per-entry kernel
+    if (levels <= 0 || N % 2 != 0 || N / 2 < 1 || !limb_kernel_fits(c.capSA, c.capSB))
+        return launch_limb_matmul(C, A, B, addmul, c.s);
     if (method == GBMM_METHOD_WINOGRAD) return rec_winograd(c, C, A, B, N, levels, addmul);
     if (addmul) return launch_limb_matmul(C, A, B, 1, c.s);
     if (method == GBMM_METHOD_STRASSEN) return rec_strassen(c, C, A, B, N, levels);
@@ -767,6 +773,110 @@ gbmm_status matmul_limb(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, con
 }
 }  // namespace gbmm
 
+namespace gbmm {
+
+// Plain dispatch heuristic: the CRT form pays off once products are large
+// enough to amortise the residue and reconstruction passes.
+int heuristic_path(int m, int k, int n, int la, int lb) {
+    const int64_t work = (int64_t)m * k * n * la * lb;
+    const bool crt_ok = crt_feasible(std::min(la, 1023), std::min(lb, 1023), k);
+    if (la + lb >= 16 && work >= ((int64_t)1 << 22) && crt_ok) return GBMM_PATH_CRT;
+    return GBMM_PATH_LIMB;
+}
+
+static bool direct_ok(const Plan &p, int la, int lb, int k) {
+    if (p.path == GBMM_PATH_CRT) return crt_feasible(la, lb, k);
+    return limb_kernel_fits(la, lb);
+}
+
+// Upper bound of the device workspace dispatch() carves from the arena.
+size_t dispatch_ws(const Plan &p, int la, int lb, int m, int k, int n, int cn, int accumulate) {
+    if (m == 0 || n == 0 || k == 0) return 0;
+    if (direct_ok(p, la, lb, k)) {
+        if (p.path == GBMM_PATH_CRT) return crt_workspace_bytes(la, lb, m, k, n, cn);
+        if (p.method == GBMM_METHOD_NAIVE) return 0;
+        int levels = levels_for(std::max(std::max(m, k), n), p.cutoff) + 2;
+        int need = limbs_needed(la, lb, k, levels);
+        const int capT = std::max(std::max(la + 1, lb + 1), std::max(need, cn));
+        size_t rec = accumulate ? rec_ws(p.method, m, levels_for(m, p.cutoff), capT)
+                                : squarify_ws(p.method, m, k, n, p.cutoff, capT, std::max(need, cn));
+        return (cn < need ? mat_bytes((int64_t)m * n, need) : 0) + rec + 8192;
+    }
+    const bool sa = la >= lb;
+    const int hl = (sa ? la : lb) / 2;
+    const int64_t xs = sa ? (int64_t)m * k : (int64_t)k * n;
+    const int tn = limbs_needed(sa ? la - hl : la, sa ? lb : lb - hl, k, 0) + 1;
+    size_t own = 2 * (align_up((size_t)xs * 4, 256) + 256) + mat_bytes((int64_t)m * n, tn) + 1024;
+    size_t lo = dispatch_ws(p, sa ? hl : la, sa ? lb : hl, m, k, n, cn, accumulate);
+    size_t hi = dispatch_ws(p, sa ? la - hl : la, sa ? lb : lb - hl, m, k, n, tn, 0);
+    return own + std::max(lo, hi);
+}
+
+// C (+)= A*B with the planned path; operands too long for the chosen kernels
+// are split into low and high limb halves (A = A_hi 2^(32h) + A_lo, the
+// Karatsuba-style split of Knuth 4.3.3 without the middle-product trick):
+// C (+)= A_lo B, T = A_hi B, C += T 2^(32h).
+gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, const Plan &p,
+                     int accumulate, cudaStream_t s) {
+    const int m = a.rows, k = a.cols, n = b.cols;
+    if (m == 0 || n == 0) return GBMM_OK;
+    if (k == 0) return accumulate ? GBMM_OK : launch_mat_zero(c, s);
+    if (direct_ok(p, a.nlimbs, b.nlimbs, k)) {
+        if (p.path == GBMM_PATH_CRT)
+            return crt_matmul(h, c, a, b, 32LL * a.nlimbs, 32LL * b.nlimbs, p.nprimes, accumulate, s);
+        int levels = p.method == GBMM_METHOD_NAIVE ? 0 : levels_for(std::max(std::max(m, k), n), p.cutoff) + 2;
+        int need = limbs_needed(a.nlimbs, b.nlimbs, k, levels);
+        if (c.nlimbs < need && p.method != GBMM_METHOD_NAIVE) {
+            // the recursion needs headroom for intermediate values: run it into a
+            // workspace matrix with enough planes, then copy into C (the copy
+            // flags a capacity error if the exact result does not fit C)
+            size_t mark = arena_mark(h);
+            gbmm_mat T;
+            if (!arena_mat(h, m, n, need, T)) return set_error(GBMM_ERR_NOMEM, "workspace");
+            if (accumulate) GBMM_TRY(launch_mat_copy(T, c, s));
+            gbmm_status st = matmul_limb(h, T, a, b, p.method, p.cutoff, accumulate, s);
+            if (st == GBMM_OK) st = launch_mat_copy(c, T, s);
+            arena_release(h, mark);
+            return st;
+        }
+        return matmul_limb(h, c, a, b, p.method, p.cutoff, accumulate, s);
+    }
+    const bool sa = a.nlimbs >= b.nlimbs;
+    const gbmm_mat &X = sa ? a : b;
+    if (X.nlimbs < 2) return set_error(GBMM_ERR_UNSUPPORTED, "no kernel takes %d x %d limb entries", a.nlimbs, b.nlimbs);
+    const int hl = X.nlimbs / 2;
+    size_t mark = arena_mark(h);
+    const size_t xs = (size_t)(X.rows - 1) * X.rs + X.cols;
+    int32_t *lo = (int32_t *)arena_alloc(h, xs * 4), *hi = (int32_t *)arena_alloc(h, xs * 4);
+    gbmm_mat T;
+    const int tn = limbs_needed(sa ? a.nlimbs - hl : a.nlimbs, sa ? b.nlimbs : b.nlimbs - hl, k, 0) + 1;
+    if (!lo || !hi || !arena_mat(h, m, n, tn, T)) return set_error(GBMM_ERR_NOMEM, "split workspace");
+    GBMM_TRY(launch_split_sizes(X, hl, lo, hi, s));
+    gbmm_mat Xlo = X, Xhi = X;
+    Xlo.nlimbs = hl;
+    Xlo.sizes = lo;
+    Xhi.nlimbs = X.nlimbs - hl;
+    Xhi.limbs = X.limbs + (int64_t)hl * X.ld;
+    Xhi.sizes = hi;
+    GBMM_TRY(dispatch(h, c, sa ? Xlo : a, sa ? b : Xlo, p, accumulate, s));
+    GBMM_TRY(dispatch(h, T, sa ? Xhi : a, sa ? b : Xhi, p, 0, s));
+    GBMM_TRY(launch_add_shifted(c, c, T, hl, s));
+    arena_release(h, mark);
+    return GBMM_OK;
+}
+
+gbmm_status resolve_plan(gbmm_handle h, const gbmm_mat &a, const gbmm_mat &b, const gbmm_opts &o, Plan &p) {
+    p.method = o.method ? o.method : GBMM_METHOD_WINOGRAD;
+    p.cutoff = o.cutoff > 0 ? o.cutoff : h->limb_cutoff;
+    p.nprimes = o.nprimes;
+    p.path = o.path;
+    if (p.path == GBMM_PATH_AUTO) p.path = choose_path(h, a.rows, a.cols, b.cols, a.nlimbs, b.nlimbs, &p.cutoff);
+    if (p.path != GBMM_PATH_CRT && p.path != GBMM_PATH_LIMB) return set_error(GBMM_ERR_INVALID, "unknown path %d", o.path);
+    return GBMM_OK;
+}
+
+}  // namespace gbmm
+
 extern "C" gbmm_status gbmm_matmul(gbmm_handle h, gbmm_mat c, gbmm_mat a, gbmm_mat b, const gbmm_opts *opts) {
     if (!h) return set_error(GBMM_ERR_INVALID, "null handle");
     GBMM_TRY(validate_mat(c, "C"));
@@ -779,37 +889,10 @@ extern "C" gbmm_status gbmm_matmul(gbmm_handle h, gbmm_mat c, gbmm_mat a, gbmm_m
     gbmm_opts o;
     memset(&o, 0, sizeof o);
     if (opts) o = *opts;
-    if (o.method == 0) o.method = GBMM_METHOD_WINOGRAD;
-    const int cutoff = o.cutoff > 0 ? o.cutoff : h->limb_cutoff;
-    int path = o.path;
-    if (path == GBMM_PATH_AUTO) {
-        // plain heuristic: the CRT form pays off once products are large enough
-        // to amortise residue / reconstruction passes
-        int64_t work = (int64_t)a.rows * a.cols * b.cols * a.nlimbs * b.nlimbs;
-        path = (a.nlimbs + b.nlimbs >= 16 && work >= ((int64_t)1 << 22)) ? GBMM_PATH_CRT : GBMM_PATH_LIMB;
-    }
-    if (path == GBMM_PATH_CRT)
-        return crt_matmul(h, c, a, b, 32LL * a.nlimbs, 32LL * b.nlimbs, o.nprimes, o.accumulate, h->stream);
-    int levels = o.method == GBMM_METHOD_NAIVE ? 0 : levels_for(std::max(std::max(a.rows, a.cols), b.cols), cutoff) + 2;
-    int need = limbs_needed(a.nlimbs, b.nlimbs, a.cols, levels);
-    if (c.nlimbs < need && o.method != GBMM_METHOD_NAIVE) {
-        // The recursion needs headroom for intermediate values: run it into a
-        // workspace matrix with enough planes, then copy into C (the copy
-        // flags a capacity error if the exact result does not fit C).
-        const int capT = std::max(std::max(a.nlimbs + 1, b.nlimbs + 1), need);
-        size_t rec = o.accumulate ? rec_ws(o.method, a.rows, levels_for(a.rows, cutoff), capT)
-                                  : squarify_ws(o.method, a.rows, a.cols, b.cols, cutoff, capT, need);
-        GBMM_TRY(arena_reserve(h, mat_bytes((int64_t)c.rows * c.cols, need) + rec + 8192));
-        size_t mark = arena_mark(h);
-        gbmm_mat T;
-        if (!arena_mat(h, c.rows, c.cols, need, T)) return set_error(GBMM_ERR_NOMEM, "workspace");
-        if (o.accumulate) GBMM_TRY(launch_mat_copy(T, c, h->stream));
-        gbmm_status st = matmul_limb(h, T, a, b, o.method, cutoff, o.accumulate, h->stream);
-        if (st == GBMM_OK) st = launch_mat_copy(c, T, h->stream);
-        arena_release(h, mark);
-        return st;
-    }
-    return matmul_limb(h, c, a, b, o.method, cutoff, o.accumulate, h->stream);
+    Plan p;
+    GBMM_TRY(resolve_plan(h, a, b, o, p));
+    GBMM_TRY(arena_reserve(h, dispatch_ws(p, a.nlimbs, b.nlimbs, a.rows, a.cols, b.cols, c.nlimbs, o.accumulate) + 65536));
+    return dispatch(h, c, a, b, p, o.accumulate, h->stream);
 }
 
 extern "C" gbmm_status gbmm_mpn_mul(gbmm_handle h, uint32_t *rp, const uint32_t *up, int32_t un, const uint32_t *vp,
@@ -828,17 +911,3 @@ extern "C" gbmm_status gbmm_mpn_mul(gbmm_handle h, uint32_t *rp, const uint32_t 
     return st;
 }
 
-extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_t njobs, const gbmm_opts *opts) {
-    if (!h || (njobs > 0 && !jobs)) return set_error(GBMM_ERR_INVALID, "null argument");
-    for (int32_t j = 0; j < njobs; j++) {
-        gbmm_opts o;
-        memset(&o, 0, sizeof o);
-        if (opts) o = *opts;
-        o.path = jobs[j].path;
-        if (jobs[j].cutoff) o.cutoff = jobs[j].cutoff;
-        if (jobs[j].nprimes) o.nprimes = jobs[j].nprimes;
-        GBMM_TRY(gbmm_matmul(h, jobs[j].c, jobs[j].a, jobs[j].b, &o));
-        jobs[j].chosen_path = o.path;
-    }
-    return GBMM_OK;
-}

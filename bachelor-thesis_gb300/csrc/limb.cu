@@ -17,6 +17,10 @@
 // §4.3.3); the code is written for GB300, not translated from the reference.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
 
 #include "gbmm_internal.h"
 
@@ -27,14 +31,13 @@ __device__ __forceinline__ int iabs_d(int x) { return x < 0 ? -x : x; }
 
 // 96-bit column accumulator (c0, c1, c2) += a * b.  One 32x32->64 wide multiply
 // accumulating into c0, then the high word and the carry.
+// The three instructions share the carry flag, so they stay in one asm block.
 #define MAC96(c0, c1, c2, a, b)                                                   \
-    do {                                                                          \
-        uint64_t t_ = (uint64_t)(a) * (uint64_t)(b) + (uint64_t)(c0);             \
-        (c0) = (uint32_t)t_;                                                      \
-        uint64_t u_ = (uint64_t)(c1) + (t_ >> 32);                                \
-        (c1) = (uint32_t)u_;                                                      \
-        (c2) += (uint32_t)(u_ >> 32);                                             \
-    } while (0)
+    asm("mad.lo.cc.u32 %0, %3, %4, %0;\n\t"                                      \
+        "madc.hi.cc.u32 %1, %3, %4, %1;\n\t"                                     \
+        "addc.u32 %2, %2, 0;"                                                     \
+        : "+r"(c0), "+r"(c1), "+r"(c2)                                            \
+        : "r"(a), "r"(b))
 
 struct MatArgs {
     uint32_t *limbs;
@@ -468,6 +471,69 @@ __global__ void k_mat_zero(MatArgs C, int64_t count) {
     C.sizes[ic] = 0;
 }
 
+// Sizes of the low (limbs [0,h)) and high (limbs [h, nlimbs)) parts of every
+// entry, same sign as the entry; the limb planes themselves are shared views.
+__global__ void k_split_sizes(MatArgs X, int h, int32_t *lo, int32_t *hi, int64_t count) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    const int64_t ix = ent(X, e);
+    const int s = X.sizes[ix], n = iabs_d(s);
+    int nlo = n < h ? n : h;
+    while (nlo > 0 && X.limbs[(int64_t)(nlo - 1) * X.ld + ix] == 0u) nlo--;
+    const int nhi = n > h ? n - h : 0;  // top limb of the entry is nonzero, so no normalisation needed
+    lo[ix] = s < 0 ? -nlo : nlo;  // same (row stride) layout as the source sizes
+    hi[ix] = s < 0 ? -nhi : nhi;
+}
+
+// W = U + V * 2^(32 sh), elementwise and signed; W may be U.
+__global__ void k_add_shifted(MatArgs W, MatArgs U, MatArgs V, int sh, int64_t count, uint32_t *err) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    const int64_t iw = ent(W, e), iu = ent(U, e), iv = ent(V, e);
+    const int su = U.sizes[iu], sv = V.sizes[iv];
+    const int un = iabs_d(su), vn0 = iabs_d(sv), vn = vn0 ? vn0 + sh : 0;
+    const uint32_t *up = U.limbs + iu, *vp = V.limbs + iv;
+    uint32_t *wp = W.limbs + iw;
+    auto ul = [&](int t) -> uint32_t { return t < un ? up[(int64_t)t * U.ld] : 0u; };
+    auto vl = [&](int t) -> uint32_t { return (t >= sh && t < vn) ? vp[(int64_t)(t - sh) * V.ld] : 0u; };
+    const int mx = un > vn ? un : vn;
+    int len = 0, neg;
+    if (vn0 == 0 || un == 0 || (su < 0) == (sv < 0)) {
+        neg = un ? su < 0 : sv < 0;
+        uint32_t c = 0;
+        for (int t = 0; t < mx; t++) {
+            uint64_t x = (uint64_t)ul(t) + vl(t) + c;
+            if (t >= W.nlimbs) { if ((uint32_t)x) { atomicOr(err, DEVERR_CAPACITY); return; } }
+            else wp[(int64_t)t * W.ld] = (uint32_t)x;
+            c = (uint32_t)(x >> 32);
+            if ((uint32_t)x) len = t + 1;
+        }
+        if (c) {
+            if (mx >= W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
+            wp[(int64_t)mx * W.ld] = c;
+            len = mx + 1;
+        }
+    } else {
+        int cmp = 0;
+        if (un != vn) cmp = un < vn ? -1 : 1;
+        for (int t = mx - 1; t >= 0 && cmp == 0; t--)
+            if (ul(t) != vl(t)) cmp = ul(t) < vl(t) ? -1 : 1;
+        neg = cmp >= 0 ? su < 0 : sv < 0;
+        uint32_t br = 0;
+        for (int t = 0; t < mx; t++) {
+            const uint32_t x = cmp >= 0 ? ul(t) : vl(t), y = cmp >= 0 ? vl(t) : ul(t);
+            uint64_t d = (uint64_t)x - y - br;
+            br = (uint32_t)(d >> 63);
+            if (t >= W.nlimbs) { if ((uint32_t)d) { atomicOr(err, DEVERR_CAPACITY); return; } }
+            else wp[(int64_t)t * W.ld] = (uint32_t)d;
+            if ((uint32_t)d) len = t + 1;
+        }
+    }
+    for (int t = mx + 1; t < W.nlimbs; t++) wp[(int64_t)t * W.ld] = 0u;
+    if (mx < W.nlimbs && len <= mx) wp[(int64_t)mx * W.ld] = 0u;
+    W.sizes[iw] = len == 0 ? 0 : (neg ? -len : len);
+}
+
 // dst = src (entries copied with their sizes; planes beyond the value zeroed)
 __global__ void k_mat_copy(MatArgs D, MatArgs S, int64_t count, uint32_t *err) {
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -522,14 +588,14 @@ struct MMCfg {
 
 // (c0, c1, c2) -= a * b on a 96-bit two's-complement accumulator
 #define MSC96(c0, c1, c2, a, b)                                                   \
-    do {                                                                          \
-        uint64_t t_ = (uint64_t)(a) * (uint64_t)(b);                              \
-        uint64_t l_ = ((uint64_t)(c1) << 32) | (c0);                              \
-        (c2) -= (uint32_t)(l_ < t_);                                              \
-        l_ -= t_;                                                                 \
-        (c0) = (uint32_t)l_;                                                      \
-        (c1) = (uint32_t)(l_ >> 32);                                              \
-    } while (0)
+    asm("{\n\t.reg .u32 lo_, hi_;\n\t"                                          \
+        "mul.lo.u32 lo_, %3, %4;\n\t"                                            \
+        "mul.hi.u32 hi_, %3, %4;\n\t"                                            \
+        "sub.cc.u32 %0, %0, lo_;\n\t"                                            \
+        "subc.cc.u32 %1, %1, hi_;\n\t"                                           \
+        "subc.u32 %2, %2, 0;\n\t}"                                               \
+        : "+r"(c0), "+r"(c1), "+r"(c2)                                            \
+        : "r"(a), "r"(b))
 
 // Writes the signed multi-limb value held in buf[0..L) (two's complement,
 // `neg` = its sign) into entry ic of C as sign-magnitude.
@@ -551,10 +617,11 @@ __device__ void store_signed(uint32_t *buf, int L, bool neg, const MatArgs &C, i
     C.sizes[ic] = neg ? -top : top;
 }
 
+// One CTA tile (TY x TX output entries at tile coordinates by, bx) of the
+// per-entry product; shared by the grid kernel and the persistent batched one.
 template <int R>
-__global__ void __launch_bounds__(MM_THREADS) k_limb_matmul(MatArgs C, MatArgs A, MatArgs B, MMCfg cfg,
-                                                            uint32_t *err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, const MatArgs &B, const MMCfg &cfg,
+                                          int by, int bx, unsigned char *smem_raw, uint32_t *err) {
     const int La = cfg.La, Lb = cfg.Lb, TY = cfg.TY, TX = cfg.TX;
     const int sa_stride = La + 4, sb_stride = Lb + 4;  // +4 words: fewer bank conflicts, 16B aligned rows
     uint32_t *sA = reinterpret_cast<uint32_t *>(smem_raw);                 // [TY][KC][La+4]
@@ -567,7 +634,7 @@ __global__ void __launch_bounds__(MM_THREADS) k_limb_matmul(MatArgs C, MatArgs A
     const int EPC = TY * TX;
     const bool has_entry = g < EPC;
     const int ty = has_entry ? g / TX : 0, tx = has_entry ? g % TX : 0;
-    const int y0 = blockIdx.y * TY, x0 = blockIdx.x * TX;
+    const int y0 = by * TY, x0 = bx * TX;
     const int y = y0 + ty, x = x0 + tx;
     const bool valid = has_entry && y < C.rows && x < C.cols;
     const int nbA = La / R, nbB = Lb / R;
@@ -716,6 +783,40 @@ __global__ void __launch_bounds__(MM_THREADS) k_limb_matmul(MatArgs C, MatArgs A
     store_signed(buf, LB, carry < 0, C, ic, err);
 }
 
+template <int R>
+__global__ void __launch_bounds__(MM_THREADS) k_limb_matmul(MatArgs C, MatArgs A, MatArgs B, MMCfg cfg,
+                                                            uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    limb_tile<R>(C, A, B, cfg, blockIdx.y, blockIdx.x, smem_raw, err);
+}
+
+// Persistent form for batches of uneven products: every CTA takes (job, tile)
+// items from a device work queue (items sorted by cost, largest first, so the
+// tail is short) until the queue is empty.  One launch covers all limb-path
+// jobs of one block edge R.
+struct LimbJob {
+    MatArgs C, A, B;
+    MMCfg cfg;
+};
+
+template <int R>
+__global__ void __launch_bounds__(MM_THREADS) k_limb_batched(const LimbJob *jobs, const int *items, int nitems,
+                                                             int *counter, uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int cur;
+    for (;;) {
+        if (threadIdx.x == 0) cur = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = cur;
+        if (it >= nitems) break;
+        const LimbJob &j = jobs[items[3 * it]];
+        const MatArgs C = j.C, A = j.A, B = j.B;
+        const MMCfg cfg = j.cfg;
+        limb_tile<R>(C, A, B, cfg, items[3 * it + 1], items[3 * it + 2], smem_raw, err);
+        __syncthreads();
+    }
+}
+
 // ---- host launchers ---------------------------------------------------------------------
 static inline int64_t nentries(const gbmm_mat &m) { return (int64_t)m.rows * m.cols; }
 static inline unsigned grid1(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -743,6 +844,24 @@ gbmm_status launch_mat_copy(const gbmm_mat &dst, const gbmm_mat &src, cudaStream
     if (n == 0) return GBMM_OK;
     LaunchScope ls_("k_mat_copy", s);
     k_mat_copy<<<grid1(n, 256), 256, 0, s>>>(margs(dst), margs(src), n, device_error_word());
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+gbmm_status launch_split_sizes(const gbmm_mat &x, int h, int32_t *lo, int32_t *hi, cudaStream_t s) {
+    const int64_t n = nentries(x);
+    if (n == 0) return GBMM_OK;
+    LaunchScope ls_("k_split_sizes", s);
+    k_split_sizes<<<grid1(n, 256), 256, 0, s>>>(margs(x), h, lo, hi, n);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+gbmm_status launch_add_shifted(const gbmm_mat &w, const gbmm_mat &u, const gbmm_mat &v, int sh, cudaStream_t s) {
+    const int64_t n = nentries(w);
+    if (n == 0) return GBMM_OK;
+    LaunchScope ls_("k_add_shifted", s);
+    k_add_shifted<<<grid1(n, 256), 256, 0, s>>>(margs(w), margs(u), margs(v), sh, n, device_error_word());
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
 }
@@ -798,6 +917,11 @@ static bool choose_mm(int la, int lb, MMCfg &cfg) {
     return false;
 }
 
+bool limb_kernel_fits(int la, int lb) {
+    MMCfg cfg;
+    return choose_mm(la, lb, cfg);
+}
+
 static size_t mm_smem(const MMCfg &c) {
     size_t stage = (size_t)c.TY * MM_KC * (c.La + 4) * 4 + (size_t)MM_KC * c.TX * (c.Lb + 4) * 4 +
                    (size_t)(c.TY + c.TX) * MM_KC * 4;
@@ -844,6 +968,105 @@ gbmm_status launch_limb_matmul(const gbmm_mat &c, const gbmm_mat &a, const gbmm_
     }
 #undef LAUNCH_R
     GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+static int occupancy_ctas(const void *fn, size_t smem) {
+    int n = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, MM_THREADS, smem) != cudaSuccess || n < 1) n = 1;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return n * (sms > 0 ? sms : 148);
+}
+
+gbmm_status plan_limb_batch(const std::vector<gbmm_mat> &C, const std::vector<gbmm_mat> &A,
+                            const std::vector<gbmm_mat> &B, LimbBatchPlan &plan) {
+    struct Item {
+        int job, by, bx;
+        double cost;
+    };
+    const int Rs[4] = {1, 2, 4, 8};
+    std::vector<LimbJob> jobs[4];
+    std::vector<Item> items[4];
+    size_t smem[4] = {0, 0, 0, 0};
+    for (size_t i = 0; i < C.size(); i++) {
+        MMCfg cfg;
+        if (!choose_mm(A[i].nlimbs, B[i].nlimbs, cfg))
+            return set_error(GBMM_ERR_UNSUPPORTED, "batched limb job %zu: entries too long", i);
+        const int EPC = cfg.Gp >= MM_THREADS ? 1 : MM_THREADS / cfg.Gp;
+        int TY = 1;
+        while (TY * TY * 4 <= EPC) TY *= 2;
+        cfg.TY = TY;
+        cfg.TX = EPC / TY;
+        cfg.M = A[i].cols;
+        cfg.accumulate = 0;
+        int g = 0;
+        while (Rs[g] != cfg.R) g++;
+        smem[g] = std::max(smem[g], mm_smem(cfg));
+        LimbJob lj;
+        lj.C = margs(C[i]); lj.A = margs(A[i]); lj.B = margs(B[i]); lj.cfg = cfg;
+        const int jid = (int)jobs[g].size();
+        jobs[g].push_back(lj);
+        const int ny = (C[i].rows + cfg.TY - 1) / cfg.TY, nx = (C[i].cols + cfg.TX - 1) / cfg.TX;
+        const double cost = (double)cfg.TY * cfg.TX * cfg.La * cfg.Lb * cfg.M;
+        for (int by = 0; by < ny; by++)
+            for (int bx = 0; bx < nx; bx++) items[g].push_back(Item{jid, by, bx, cost});
+    }
+    plan.blob.clear();
+    plan.groups.clear();
+    for (int g = 0; g < 4; g++) {
+        if (jobs[g].empty()) continue;
+        if (smem[g] > 200 * 1024) return set_error(GBMM_ERR_UNSUPPORTED, "batched limb: shared memory too large");
+        std::stable_sort(items[g].begin(), items[g].end(), [](const Item &x, const Item &y) { return x.cost > y.cost; });
+        LimbBatchPlan::Group gr;
+        gr.R = Rs[g];
+        gr.smem = smem[g];
+        gr.nitems = (int)items[g].size();
+        size_t off = (plan.blob.size() + 255) & ~(size_t)255;
+        gr.jobs_off = off;
+        plan.blob.resize(off + jobs[g].size() * sizeof(LimbJob));
+        memcpy(plan.blob.data() + off, jobs[g].data(), jobs[g].size() * sizeof(LimbJob));
+        off = (plan.blob.size() + 255) & ~(size_t)255;
+        gr.items_off = off;
+        plan.blob.resize(off + items[g].size() * 3 * sizeof(int));
+        int *ip = reinterpret_cast<int *>(plan.blob.data() + off);
+        for (size_t t = 0; t < items[g].size(); t++) {
+            ip[3 * t] = items[g][t].job;
+            ip[3 * t + 1] = items[g][t].by;
+            ip[3 * t + 2] = items[g][t].bx;
+        }
+        plan.groups.push_back(gr);
+    }
+    return GBMM_OK;
+}
+
+gbmm_status launch_limb_batch(const LimbBatchPlan &plan, const char *d_blob, int *d_counters, cudaStream_t s) {
+    if (plan.groups.empty()) return GBMM_OK;
+    GBMM_CUDA_TRY(cudaMemsetAsync(d_counters, 0, sizeof(int) * plan.groups.size(), s));
+    uint32_t *err = device_error_word();
+    for (size_t g = 0; g < plan.groups.size(); g++) {
+        const LimbBatchPlan::Group &gr = plan.groups[g];
+        const LimbJob *jobs = reinterpret_cast<const LimbJob *>(d_blob + gr.jobs_off);
+        const int *items = reinterpret_cast<const int *>(d_blob + gr.items_off);
+#define LAUNCH_B(RR)                                                                                            \
+    do {                                                                                                        \
+        if (gr.smem > 48 * 1024)                                                                                \
+            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_limb_batched<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                               (int)gr.smem));                                                  \
+        const int grid = std::min(gr.nitems, occupancy_ctas((const void *)k_limb_batched<RR>, gr.smem));       \
+        LaunchScope ls_("k_limb_batched", s);                                                                   \
+        k_limb_batched<RR><<<grid, MM_THREADS, gr.smem, s>>>(jobs, items, gr.nitems, d_counters + g, err);     \
+    } while (0)
+        switch (gr.R) {
+            case 1: LAUNCH_B(1); break;
+            case 2: LAUNCH_B(2); break;
+            case 4: LAUNCH_B(4); break;
+            default: LAUNCH_B(8); break;
+        }
+#undef LAUNCH_B
+        GBMM_CUDA_TRY(cudaGetLastError());
+    }
     return GBMM_OK;
 }
 

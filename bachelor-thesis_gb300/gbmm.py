@@ -72,6 +72,18 @@ _SIGS = {
     "gbmm_matmul": [_P, Mat, Mat, Mat, ctypes.POINTER(Opts)],
     "gbmm_mat_mul_naive": [Mat, Mat, Mat, ctypes.c_int32, _P],
     "gbmm_matmul_batched": [_P, ctypes.POINTER(Job), ctypes.c_int32, ctypes.POINTER(Opts)],
+    "gbmm_set_graphs": [_P, ctypes.c_int32],
+    "gbmm_autotune": [_P, ctypes.POINTER(Job), ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p],
+    "gbmm_tune_save": [_P, ctypes.c_char_p],
+    "gbmm_tune_load": [_P, ctypes.c_char_p],
+    "gbmm_model_features": [ctypes.c_int32] * 5 + [_P],
+    "gbmm_model_init": [_P, ctypes.c_uint64],
+    "gbmm_model_set_params": [_P, _P],
+    "gbmm_model_get_params": [_P, _P, _P],
+    "gbmm_model_use": [_P, ctypes.c_int32],
+    "gbmm_model_predict": [_P, _P, ctypes.c_int32, _P],
+    "gbmm_model_gradient": [_P, _P, _P, ctypes.c_int32, _P, _P],
+    "gbmm_model_train": [_P, _P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_float, _P],
     "gbmm_mpn_add_n": [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, _P, _P],
     "gbmm_mpn_sub_n": [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, _P, _P],
     "gbmm_mpn_mul_1": [_P, _P, ctypes.c_int32, _P, ctypes.c_int64, ctypes.c_int64, _P, _P],
@@ -107,6 +119,7 @@ def lib():
     L.gbmm_kernel_launches.restype = ctypes.c_uint64
     L.gbmm_profile.argtypes = [ctypes.c_int32]
     L.gbmm_profile_read.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    L.gbmm_model_nparams.restype = ctypes.c_int32
     L.gbmm_mpn_toom22_mul_itch.restype = ctypes.c_int32
     L.gbmm_mpn_toom22_mul_itch.argtypes = [ctypes.c_int32, ctypes.c_int32]
     _lib = L
@@ -310,9 +323,82 @@ class Handle:
         o = Opts(path, method, cutoff, nprimes, int(bool(accumulate)))
         check(lib().gbmm_matmul(self.h, _m(C), _m(A), _m(B), ctypes.byref(o)))
 
+    @staticmethod
+    def jobs(triples, path=PATH_AUTO):
+        """[(C, A, B), ...] -> ctypes array of gbmm_job."""
+        arr = (Job * len(triples))()
+        for i, (c, a, b) in enumerate(triples):
+            arr[i].c, arr[i].a, arr[i].b = _m(c), _m(a), _m(b)
+            arr[i].path = path
+        return arr
+
+    def matmul_batched(self, jobs, path=PATH_AUTO):
+        """Runs a ctypes array of gbmm_job; returns the paths the dispatcher chose."""
+        self.bind_stream()
+        o = Opts(path, METHOD_WINOGRAD, 0, 0, 0)
+        check(lib().gbmm_matmul_batched(self.h, jobs, len(jobs), ctypes.byref(o)))
+        return [jobs[i].chosen_path for i in range(len(jobs))]
+
+    # ---- learned cost model ----
+    def model_init(self, seed=1):
+        check(lib().gbmm_model_init(self.h, seed))
+
+    def model_params(self):
+        n = lib().gbmm_model_nparams()
+        m = np.zeros(n, dtype=np.float32)
+        b = np.zeros(n, dtype=np.uint16)
+        check(lib().gbmm_model_get_params(self.h, m.ctypes.data, b.ctypes.data))
+        return m, b
+
+    def model_set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        check(lib().gbmm_model_set_params(self.h, p.ctypes.data))
+
+    def model_predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], 3), dtype=np.float32)
+        self.bind_stream()
+        check(lib().gbmm_model_predict(self.h, X.ctypes.data, X.shape[0], Y.ctypes.data))
+        return Y
+
+    def model_gradient(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        g = np.zeros(lib().gbmm_model_nparams(), dtype=np.float32)
+        loss = ctypes.c_float(0)
+        self.bind_stream()
+        check(lib().gbmm_model_gradient(self.h, X.ctypes.data, T.ctypes.data, X.shape[0], g.ctypes.data,
+                                        ctypes.byref(loss)))
+        return g, loss.value
+
+    def model_train(self, X, T, epochs=300, lr=3e-3):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        loss = ctypes.c_float(0)
+        self.bind_stream()
+        check(lib().gbmm_model_train(self.h, X.ctypes.data, T.ctypes.data, X.shape[0], epochs, lr,
+                                     ctypes.byref(loss)))
+        return loss.value
+
+    def model_use(self, enable=True):
+        check(lib().gbmm_model_use(self.h, int(bool(enable))))
+
+    def set_graphs(self, enable):
+        check(lib().gbmm_set_graphs(self.h, int(bool(enable))))
+
+    def autotune(self, jobs, repeats=2, log_path=None):
+        self.bind_stream()
+        check(lib().gbmm_autotune(self.h, jobs, len(jobs), repeats, log_path.encode() if log_path else None))
+
 
 def _m(x):
     return x.mat if isinstance(x, DeviceMatrix) else x
+
+
+def model_features(m, k, n, la, lb):
+    f = np.zeros(8, dtype=np.float32)
+    check(lib().gbmm_model_features(m, k, n, la, lb, f.ctypes.data))
+    return f
 
 
 def limbs_needed(a_nlimbs, b_nlimbs, inner, path=PATH_LIMB, method=METHOD_WINOGRAD, cutoff=0):

@@ -193,6 +193,46 @@ typedef struct gbmm_job {
  * and replayed on later calls with the same job signature.
  * replaces: the unused chunked-stream job DAG (mat-gpu/job.cu:32-338). */
 gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_t njobs, const gbmm_opts *opts);
+/* Turns CUDA-graph capture and replay of batches on (default) or off.
+ * No counterpart in the reference. */
+gbmm_status gbmm_set_graphs(gbmm_handle h, int32_t enable);
+
+/* ---- autotuner / dispatch tables -------------------------------------------
+ * gbmm_autotune times candidate plans (limb naive, limb Winograd, CRT) on each
+ * job's own buffers (C is overwritten), keeps the fastest per shape class for
+ * GBMM_PATH_AUTO, and appends one JSON line per timing to log_path (may be
+ * NULL): the timing record the learned cost model trains on.
+ * replaces: the fixed BASE_SIZE / TRANSFER_SIZE / GPU_BLK_* tuning constants
+ * (mat-gpu/mat-params.h:4-14). */
+gbmm_status gbmm_autotune(gbmm_handle h, const gbmm_job *jobs, int32_t njobs, int32_t repeats,
+                          const char *log_path);
+gbmm_status gbmm_tune_save(gbmm_handle h, const char *path);
+gbmm_status gbmm_tune_load(gbmm_handle h, const char *path);
+
+/* ---- learned cost model ------------------------------------------------------
+ * An 8 -> 64 -> 64 -> 3 MLP (BF16 weights, FP32 accumulation, ReLU) whose three
+ * heads predict log2(ms) of the limb path without recursion, the limb path with
+ * Winograd recursion (cutoff 64) and the CRT path for one product.  When
+ * enabled with gbmm_model_use, GBMM_PATH_AUTO takes the cheapest head; the
+ * plain heuristic (and the autotuner's table) stay the fallback.  Training
+ * runs on the GPU (forward, backward, Adam kernels) on feature rows from
+ * gbmm_model_features and targets from the autotuner's timing log.
+ * No counterpart in the reference. */
+int32_t gbmm_model_nparams(void);
+gbmm_status gbmm_model_features(int32_t m, int32_t k, int32_t n, int32_t la, int32_t lb, float *out8);
+gbmm_status gbmm_model_init(gbmm_handle h, uint64_t seed);
+gbmm_status gbmm_model_set_params(gbmm_handle h, const float *params);
+gbmm_status gbmm_model_get_params(gbmm_handle h, float *master, uint16_t *bf16_params);
+gbmm_status gbmm_model_use(gbmm_handle h, int32_t enable);
+/* X: nsamp x 8 features, Y: nsamp x 3 predictions (host arrays). */
+gbmm_status gbmm_model_predict(gbmm_handle h, const float *X, int32_t nsamp, float *Y);
+/* Mean-squared-error loss and its gradient (gbmm_model_nparams floats) on
+ * (X, T); T entries may be NaN for missing heads. */
+gbmm_status gbmm_model_gradient(gbmm_handle h, const float *X, const float *T, int32_t nsamp, float *grad,
+                                float *loss);
+/* Full-batch Adam for `epochs` steps with learning rate lr. */
+gbmm_status gbmm_model_train(gbmm_handle h, const float *X, const float *T, int32_t nsamp, int32_t epochs,
+                             float lr, float *final_loss);
 
 /* ---- batched mpn layer ----------------------------------------------------
  * Operand b (0 <= b < nb) of a batched call has limb i at ptr[i*ld + b].

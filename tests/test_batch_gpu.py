@@ -1,0 +1,115 @@
+"""Batched uneven products (persistent work-queue kernel + CRT jobs + CUDA
+graph replay), the limb-half split for entries longer than any kernel takes,
+and the autotuner's dispatch table.  Bit-exact against Python integers."""
+import json
+import os
+import random
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def g(built_lib):
+    import gbmm
+    gbmm.default_handle()
+    return gbmm
+
+
+def _rand(rng, n, bits, zero=0.1):
+    return [0 if rng.random() < zero else rng.getrandbits(bits) * rng.choice((-1, 1)) for _ in range(n)]
+
+
+def _exact(K, M, N, A, B):
+    return [sum(A[y * M + k] * B[k * N + x] for k in range(M)) for y in range(K) for x in range(N)]
+
+
+def _make_jobs(g, rng, specs):
+    out = []
+    for K, M, N, ba, bb in specs:
+        A, B = _rand(rng, K * M, ba), _rand(rng, M * N, bb)
+        la, lb = (ba + 31) // 32, (bb + 31) // 32
+        dA = g.DeviceMatrix.from_ints(K, M, A, la)
+        dB = g.DeviceMatrix.from_ints(M, N, B, lb)
+        dC = g.DeviceMatrix(K, N, la + lb + 2)
+        out.append((K, M, N, A, B, dA, dB, dC))
+    return out
+
+
+SPECS = [(16, 16, 16, 64, 64), (37, 5, 19, 200, 900), (64, 64, 64, 1024, 1024), (3, 100, 7, 33, 2000),
+         (50, 20, 40, 4096, 64), (1, 1, 1, 16384, 64), (20, 30, 25, 3000, 2500), (90, 17, 11, 96, 96),
+         (128, 64, 33, 512, 777), (5, 5, 5, 9000, 9000), (17, 129, 33, 2048, 2048), (2, 600, 3, 700, 700)]
+
+
+@pytest.mark.parametrize("path", ["auto", "limb", "crt"])
+def test_batched_uneven_exact(g, path):
+    rng = random.Random(7)
+    jobs = _make_jobs(g, rng, SPECS)
+    h = g.Handle()
+    p = {"auto": g.PATH_AUTO, "limb": g.PATH_LIMB, "crt": g.PATH_CRT}[path]
+    arr = h.jobs([(j[7], j[5], j[6]) for j in jobs], path=p)
+    chosen = h.matmul_batched(arr, path=p)
+    for (K, M, N, A, B, dA, dB, dC), c in zip(jobs, chosen):
+        assert dC.to_ints() == _exact(K, M, N, A, B), (K, M, N, c)
+    h.close()
+
+
+def test_batched_graph_replay_sees_new_inputs(g):
+    """Same buffers, new contents: the eager call, the capturing call and two
+    replays must each compute the product of the current inputs."""
+    rng = random.Random(3)
+    specs = [(33, 40, 21, 300, 500), (64, 64, 64, 2048, 2048), (8, 9, 10, 64, 5000)]
+    jobs = _make_jobs(g, rng, specs)
+    h = g.Handle()
+    arr = h.jobs([(j[7], j[5], j[6]) for j in jobs])
+    for rnd in range(4):
+        if rnd:
+            for idx, (K, M, N, A, B, dA, dB, dC) in enumerate(jobs):
+                A = _rand(rng, K * M, specs[idx][3])
+                B = _rand(rng, M * N, specs[idx][4])
+                dA.upload(*g.ints_to_planes(A, dA.nlimbs))
+                dB.upload(*g.ints_to_planes(B, dB.nlimbs))
+                jobs[idx] = (K, M, N, A, B, dA, dB, dC)
+        h.matmul_batched(arr)
+        for K, M, N, A, B, dA, dB, dC in jobs:
+            assert dC.to_ints() == _exact(K, M, N, A, B), rnd
+    h.close()
+
+
+@pytest.mark.parametrize("path", ["limb", "crt"])
+def test_split_for_very_long_entries(g, path):
+    rng = random.Random(11)
+    K, M, N = 6, 9, 5
+    A, B = _rand(rng, K * M, 12000, 0.0), _rand(rng, M * N, 30000, 0.0)
+    dA = g.DeviceMatrix.from_ints(K, M, A)
+    dB = g.DeviceMatrix.from_ints(M, N, B)
+    dC = g.DeviceMatrix(K, N, dA.nlimbs + dB.nlimbs + 2)
+    g.default_handle().matmul(dC, dA, dB, path={"limb": g.PATH_LIMB, "crt": g.PATH_CRT}[path])
+    assert dC.to_ints() == _exact(K, M, N, A, B)
+
+
+def test_autotune_table_roundtrip(g, tmp_path):
+    rng = random.Random(5)
+    jobs = _make_jobs(g, rng, [(64, 64, 64, 2048, 2048), (8, 8, 8, 64, 64)])
+    h = g.Handle()
+    arr = h.jobs([(j[7], j[5], j[6]) for j in jobs])
+    log = str(tmp_path / "timings.jsonl")
+    h.autotune(arr, repeats=1, log_path=log)
+    rows = [json.loads(l) for l in open(log)]
+    assert len(rows) >= 4 and all(r["ms"] > 0 for r in rows)
+    table = str(tmp_path / "tune.json")
+    g.check(g.lib().gbmm_tune_save(h.h, table.encode()))
+    h2 = g.Handle()
+    g.check(g.lib().gbmm_tune_load(h2.h, table.encode()))
+    chosen = h2.matmul_batched(h2.jobs([(j[7], j[5], j[6]) for j in jobs]))
+    best = {}
+    for r in rows:
+        key = (r["m"], r["la"])
+        if key not in best or r["ms"] < best[key][0]:
+            best[key] = (r["ms"], r["path"])
+    assert chosen == [best[(64, 64)][1], best[(8, 2)][1]]
+    for K, M, N, A, B, dA, dB, dC in jobs:
+        assert dC.to_ints() == _exact(K, M, N, A, B)
+    h.close()
+    h2.close()
