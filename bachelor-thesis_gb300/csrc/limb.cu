@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "gbmm_internal.h"
@@ -1151,6 +1152,60 @@ extern "C" gbmm_status gbmm_mpn_toom22_mul(uint32_t *pp, const uint32_t *ap, int
     if (an < bn || !(0 < s && s <= n && s >= n - 1) || !(0 < t && t <= s))
         return set_error(GBMM_ERR_INVALID, "toom22 preconditions violated (an=%d bn=%d)", an, bn);
     if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_toom22", as_stream(stream));
+    k_mpn_toom22<<<grid1(nb, 128), 128, 0, as_stream(stream)>>>(pp, ap, an, bp, bn, scratch, ld, nb);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+// ---- Toom-2.2 without any allocation ---------------------------------------------------
+// Scratch for gbmm_mpn_toom22_mul_noalloc lives in this file-scope device array:
+// every GPU that loads the library holds it until the process exits, and all
+// calls on a device share it.  Host code must not pass `g_toom22_scratch`
+// itself to a kernel (on the host that name is only a stand-in for the device
+// symbol); its device address is looked up once per device with
+// cudaGetSymbolAddress and cached below.
+static __device__ __align__(256) uint32_t g_toom22_scratch[GBMM_NOALLOC_SCRATCH_BYTES / 4];
+
+static std::mutex g_noalloc_mu;
+static uint32_t *g_noalloc_ptr[64];
+
+// Looks up the device address of the scratch array for the current device
+// (first call on each device; no allocation happens).
+static gbmm_status noalloc_scratch(uint32_t **out) {
+    int dev = 0;
+    GBMM_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(GBMM_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_toom22_scratch);
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_toom22_scratch)");
+        g_noalloc_ptr[dev] = static_cast<uint32_t *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_mpn_toom22_mul_noalloc(uint32_t *pp, const uint32_t *ap, int32_t an, const uint32_t *bp,
+                                                   int32_t bn, int64_t ld, int64_t nb, void *stream) {
+    GBMM_TRY(check_batch(pp, ap, ld, nb, an));
+    if (!bp) return set_error(GBMM_ERR_INVALID, "null pointer");
+    const int s = an >> 1, n = an - s, t = bn - n;
+    if (an < bn || !(0 < s && s <= n && s >= n - 1) || !(0 < t && t <= s))
+        return set_error(GBMM_ERR_INVALID, "toom22 preconditions violated (an=%d bn=%d)", an, bn);
+    const uint64_t need = (uint64_t)gbmm_mpn_toom22_mul_itch(an, bn) * (uint64_t)ld * 4u;
+    if (need > GBMM_NOALLOC_SCRATCH_BYTES)
+        return set_error(GBMM_ERR_CAPACITY,
+                         "toom22 without allocation: scratch of %llu bytes (itch %d limbs x plane stride %lld) exceeds "
+                         "the fixed %d-byte device array",
+                         (unsigned long long)need, gbmm_mpn_toom22_mul_itch(an, bn), (long long)ld,
+                         GBMM_NOALLOC_SCRATCH_BYTES);
+    if (nb == 0) return GBMM_OK;
+    uint32_t *scratch = nullptr;
+    GBMM_TRY(noalloc_scratch(&scratch));
+    // every scratch word the kernel reads it has written first in the same call,
+    // so nothing is cleared between calls
     LaunchScope ls_("k_mpn_toom22", as_stream(stream));
     k_mpn_toom22<<<grid1(nb, 128), 128, 0, as_stream(stream)>>>(pp, ap, an, bp, bn, scratch, ld, nb);
     GBMM_CUDA_TRY(cudaGetLastError());

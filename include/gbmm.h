@@ -269,6 +269,25 @@ int32_t gbmm_mpn_toom22_mul_itch(int32_t an, int32_t bn);
 gbmm_status gbmm_mpn_toom22_mul(uint32_t *pp, const uint32_t *ap, int32_t an,
                                 const uint32_t *bp, int32_t bn, uint32_t *scratch,
                                 int64_t ld, int64_t nb, void *stream);
+/* Bytes of the fixed device array that gbmm_mpn_toom22_mul_noalloc uses as
+ * scratch (one per GPU that loads the library, held until process exit). */
+#define GBMM_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
+/* Same product as gbmm_mpn_toom22_mul, for callers that cannot allocate device
+ * memory: code that runs while another component owns every device allocation
+ * (an embedding runtime with its own pool or allocation accounting), or a
+ * thread that must not enter cudaMalloc / cudaFree because those calls may
+ * synchronise the device or take a global lock.  The caller passes inputs and
+ * outputs only; the scratch is the library's fixed device array, so
+ * gbmm_mpn_toom22_mul_itch(an, bn) * ld * 4 must not exceed
+ * GBMM_NOALLOC_SCRATCH_BYTES (GBMM_ERR_CAPACITY otherwise).  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  Every call shares the one
+ * array, so calls whose kernels may overlap on the GPU (different streams
+ * without ordering between them) race on it.  No allocation of any kind.
+ * No counterpart in the reference. */
+gbmm_status gbmm_mpn_toom22_mul_noalloc(uint32_t *pp, const uint32_t *ap, int32_t an,
+                                        const uint32_t *bp, int32_t bn, int64_t ld, int64_t nb,
+                                        void *stream);
 /* rp (un+vn) = up * vp, un >= vn >= 1, choosing basecase or Toom-2.2 (the
  * Toom-2.2 path uses scratch from the handle).
  * replaces: gpu_mpn_mul (mat-gpu/mul.cu:61-401), gpu_mpn_mul_n (mat-gpu/mul_n.cu:36-111). */
