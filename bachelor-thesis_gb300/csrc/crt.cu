@@ -10,14 +10,15 @@
 //                 per entry (A in row-major order, B in column-major order).
 //  2. residue   : [entries x digits] x [digits x 2P] GEMM with the table
 //                 256^j mod p_i (balanced, split in two signed bytes); the
-//                 epilogue folds the two halves, reduces mod p_i, applies the
-//                 entry's sign and stores the residue as two balanced digits in
-//                 per-modulus planes.
-//  3. product   : for each modulus, [A1;A0] x [B1|B0]^T (two MMAs of
-//                 128x256xK into 512 TMEM columns); the epilogue combines the
-//                 four digit products mod p_i, multiplies by (Mod/p_i)^-1 mod
-//                 p_i (Garner / CRT weight) and stores the balanced result y_i as
-//                 two digits in per-modulus planes.
+//                 epilogue folds the two halves, reduces mod p_i in FP32,
+//                 applies the entry's sign and stores the residue as two
+//                 balanced digits in per-modulus planes.  B's table carries the
+//                 CRT weight w_i = (Mod/p_i)^-1 mod p_i, and B's epilogue also
+//                 stores 256 * residue, so B has four planes per modulus.
+//  3. product   : for each modulus, two accumulators over a K of 2k (A's high
+//                 digits against B's 256-scaled digits, then A's low digits
+//                 against B's plain digits); y_i = 256 * D_hi + D_lo mod p_i,
+//                 stored balanced as two digits in per-modulus planes.
 //  4. reconstruct: [entries x 2P] x [2P x (8 + Dout)] GEMM against the digits
 //                 of Mod/p_i (and 256*Mod/p_i) plus fixed-point digits of
 //                 2^48/p_i; the epilogue gets q = round(sum y_i / p_i), folds
@@ -90,6 +91,28 @@ __device__ __forceinline__ void balanced_digits(int32_t r, int32_t p, float &hi,
     int32_t d1 = (b - d0) >> 8;
     hi = (float)d1;
     lo = (float)d0;
+}
+
+// Balanced representative of x mod p in [-(p-1)/2, (p-1)/2] for an exact
+// integer |x| < 2^24 held in FP32; FMA-pipe only (no int<->float conversion).
+// The quotient is rounded with the 1.5 * 2^23 trick (|x/p| < 2^22); fma gives
+// x - q*p exactly because the result is small; one correction each way covers
+// the quotient's rounding error.
+constexpr float RND_MAGIC = 12582912.0f;  // 1.5 * 2^23
+__device__ __forceinline__ float red_bal(float x, float p, float inv_p) {
+    float q = __fadd_rn(__fmul_rn(x, inv_p), RND_MAGIC);
+    q = __fsub_rn(q, RND_MAGIC);
+    float r = __fmaf_rn(-q, p, x);
+    const float h = 0.5f * p;
+    r = r > h ? r - p : r;
+    r = r < -h ? r + p : r;
+    return r;
+}
+// balanced r (|r| < 2^15) -> two signed byte digits, r = hi * 256 + lo, |hi|, |lo| <= 128
+__device__ __forceinline__ void bal_split(float r, float &hi, float &lo) {
+    float q = __fadd_rn(__fmul_rn(r, 1.0f / 256.0f), RND_MAGIC);
+    hi = __fsub_rn(q, RND_MAGIC);
+    lo = __fmaf_rn(-hi, 256.0f, r);
 }
 
 struct Barriers {
@@ -216,10 +239,12 @@ struct ResidueArgs {
     int32_t nk;               // K steps of 64 digits
     int32_t BN, G;            // table columns per tile, accumulation groups (G * BN <= 256)
     int32_t P;
+    int32_t ncols;            // 2P table columns
     int32_t n_ntiles;
     int64_t ntiles;
+    int32_t scaled;           // B operand: table holds w_i 256^j; also emit 256 * residue
     const ModConst *mods;
-    __nv_bfloat16 *R;  // planes [2P][rowsR][kp]
+    __nv_bfloat16 *R;  // planes [2P or 4P][rowsR][kp]
     int64_t plane;     // rowsR * kp
     int32_t kp;
 };
@@ -259,11 +284,14 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = tc::idesc_bf16_f32(BM, a.BN, 0, 0);
             int it = 0, lt = 0;
             bool ok = true;
             for (int64_t t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x, lt++) {
                 const int b = lt & 1;
+                // the last table tile may be narrow: issue only the columns it has
+                const int n0 = (int)(t % a.n_ntiles) * a.BN;
+                const int nn = min(a.BN, (a.ncols - n0 + 15) & ~15);
+                const uint32_t idesc = tc::idesc_bf16_f32(BM, nn, 0, 0);
                 if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
                 tc::fence_after_sync();
                 for (int s = 0; s < a.nk; s++, it++) {
@@ -286,6 +314,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         const int quad = warp & 3, half = (warp - 2) >> 2;
         const int hcols = a.BN / 2;
         const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
+        const int npl = a.scaled ? 4 : 2;
         int lt = 0;
         for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, lt++) {
             const int b = lt & 1;
@@ -293,48 +322,60 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             const int n0 = (int)(t % a.n_ntiles) * a.BN;
             if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); break; }
             tc::fence_after_sync();
-            int neg = 0;
+            float sgn = 1.f;
             int64_t off = 0;
             if (e < a.E) {
                 const int64_t r = e / a.kdim, c = e % a.kdim;
-                neg = a.sizes[a.transpose ? c * a.rs + r : r * a.rs + c] < 0;
+                sgn = a.sizes[a.transpose ? c * a.rs + r : r * a.rs + c] < 0 ? -1.f : 1.f;
                 off = r * a.kp + c;
             }
             for (int c0 = half * hcols; c0 < (half + 1) * hcols; c0 += 32) {
-                int32_t res[16];
+                float res[16];
 #pragma unroll
-                for (int j = 0; j < 16; j++) res[j] = 0;
+                for (int j = 0; j < 16; j++) res[j] = 0.f;
                 const int mi0 = (n0 + c0) / 2;
+                const bool live_chunk = n0 + c0 < a.ncols;
                 for (int g = 0; g < a.G; g++) {
                     uint32_t v[32];
-                    tc::tmem_ld32(lb + (uint32_t)(256 * b + g * a.BN + c0), v);
-                    tc::tmem_ld_wait();
+                    if (live_chunk) {
+                        tc::tmem_ld32(lb + (uint32_t)(256 * b + g * a.BN + c0), v);
+                        tc::tmem_ld_wait();
+                    }
                     if (g == a.G - 1 && c0 + 32 >= (half + 1) * hcols) {
                         // last TMEM read of this tile by this warp: hand the buffer back
                         tc::fence_before_sync();
                         __syncwarp();
                         if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
                     }
+                    if (!live_chunk) continue;
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
                         const ModConst mc = a.mods[mi0 + j < a.P ? mi0 + j : 0];
+                        const float pf = (float)mc.p;
                         // s0 + 256 * s1 (+ residue of earlier groups), each |s| < 2^24
-                        const int32_t r1 = mod_s32(tc::acc_int(v[2 * j + 1]), mc.p, mc.inv_p);
-                        res[j] = mod_s32(tc::acc_int(v[2 * j]) + 256 * r1 + res[j], mc.p, mc.inv_p);
+                        const float r1 = red_bal(__uint_as_float(v[2 * j + 1]), pf, mc.inv_p);
+                        const float r0 = red_bal(__uint_as_float(v[2 * j]), pf, mc.inv_p);
+                        res[j] = red_bal(__fmaf_rn(256.f, r1, r0) + res[j], pf, mc.inv_p);
                     }
                 }
-                if (e < a.E) {
+                if (e < a.E && live_chunk) {
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
                         const int mi = mi0 + j;
                         if (mi >= a.P) continue;
-                        const int32_t p = a.mods[mi].p;
-                        int32_t r = res[j];
-                        if (neg && r) r = p - r;
+                        const float r = sgn * res[j];
                         float hi, lo;
-                        balanced_digits(r, p, hi, lo);
-                        a.R[(int64_t)(2 * mi) * a.plane + off] = __float2bfloat16_rn(hi);
-                        a.R[(int64_t)(2 * mi + 1) * a.plane + off] = __float2bfloat16_rn(lo);
+                        bal_split(r, hi, lo);
+                        __nv_bfloat16 *dst = a.R + (int64_t)(npl * mi) * a.plane + off;
+                        dst[0] = __float2bfloat16_rn(hi);
+                        dst[a.plane] = __float2bfloat16_rn(lo);
+                        if (a.scaled) {
+                            const ModConst mc = a.mods[mi];
+                            const float r2 = red_bal(256.f * r, (float)mc.p, mc.inv_p);
+                            bal_split(r2, hi, lo);
+                            dst[2 * a.plane] = __float2bfloat16_rn(hi);
+                            dst[3 * a.plane] = __float2bfloat16_rn(lo);
+                        }
                     }
                 }
             }
@@ -344,8 +385,17 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 }
 
 // ======================================================================================
-// 3. per-modulus product GEMM (persistent over (modulus, 128 x 64 output tiles);
+// 3. per-modulus product GEMM (persistent over (modulus, 128 x 128 output tiles);
 //    TMEM double-buffered; 8 epilogue warps)
+//
+// With a = a1*256 + a0 (residues of A, balanced digits) and the B residues
+// pre-multiplied by the CRT weight w = (Mod/p)^-1 mod p in two forms,
+// u = w*b and v = 256*w*b (mod p, balanced digits u1*256+u0, v1*256+v0), the
+// weighted product is
+//     y = a*b*w = 256*(a1*v1 + a0*u1) + (a1*v0 + a0*u0)   (mod p),
+// i.e. two accumulators over a K of 2k: the first k steps pair A1 with
+// [V1 | V0], the next k steps A0 with [U1 | U0].  Each accumulator sums 2k
+// products of magnitude <= 2^14, exact for k <= 512.
 // ======================================================================================
 struct ProductArgs {
     int32_t m, n, nk, P;
@@ -355,7 +405,7 @@ struct ProductArgs {
     __nv_bfloat16 *Y;  // planes [2Pp][Ep]
     int64_t Ep;
 };
-constexpr int PBX = 64;  // output columns per product tile
+constexpr int PBX = 128;  // output columns per product tile
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -368,7 +418,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                   uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
-    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = PBX * 128, STAGE = 2 * A_BYTES + 2 * B_BYTES;
+    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = PBX * 128, STAGE = A_BYTES + 2 * B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     cta_setup(bars, STAGES, 512, 1, 8);
@@ -383,24 +433,27 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             for (int64_t t = blockIdx.x; t < a.ntiles && !aborted(bars); t += gridDim.x) {
                 const int mi = (int)(t / per_mod), r = (int)(t % per_mod);
                 const int y0 = (r / a.nxt) * BM, x0 = (r % a.nxt) * PBX;
-                for (int s = 0; s < a.nk; s++, it++) {
+                for (int s = 0; s < 2 * a.nk; s++, it++) {
                     const int st = it % STAGES;
                     if (it >= STAGES && !tc::mbar_wait(&bars->empty[st], ((it / STAGES) & 1) ^ 1)) {
                         set_abort(bars, err);
                         break;
                     }
+                    const int second = s >= a.nk, ks = (second ? s - a.nk : s) * BK;
                     uint8_t *sa = base + st * STAGE;
                     tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                    tc::tma_load_2d(sa, &tmA, &bars->full[st], s * BK, (2 * mi) * a.m + y0);
-                    tc::tma_load_2d(sa + A_BYTES, &tmA, &bars->full[st], s * BK, (2 * mi + 1) * a.m + y0);
-                    tc::tma_load_2d(sa + 2 * A_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi) * a.n + x0);
-                    tc::tma_load_2d(sa + 2 * A_BYTES + B_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi + 1) * a.n + x0);
+                    // A1 (plane 2i) with V = 256wb (planes 4i+2, 4i+3), then A0 (plane 2i+1) with U = wb (4i, 4i+1)
+                    tc::tma_load_2d(sa, &tmA, &bars->full[st], ks, (2 * mi + second) * a.m + y0);
+                    const int bp = 4 * mi + (second ? 0 : 2);
+                    tc::tma_load_2d(sa + A_BYTES, &tmB, &bars->full[st], ks, bp * a.n + x0);
+                    tc::tma_load_2d(sa + A_BYTES + B_BYTES, &tmB, &bars->full[st], ks, (bp + 1) * a.n + x0);
                 }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            // [B1|B0] is one 128-row operand; A1 -> columns [0,128), A0 -> [128,256) of the buffer
+            // [B hi | B lo] is one 256-row operand: columns [0,128) accumulate the
+            // x256 sum, [128,256) the x1 sum
             const uint32_t idesc = tc::idesc_bf16_f32(BM, 2 * PBX, 0, 0);
             int it = 0, lt = 0;
             bool ok = true;
@@ -409,17 +462,15 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                 if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
                 tc::fence_after_sync();
                 const uint32_t d = tmem + 256u * b;
-                for (int s = 0; s < a.nk; s++, it++) {
+                for (int s = 0; s < 2 * a.nk; s++, it++) {
                     const int st = it % STAGES;
                     if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
                     tc::fence_after_sync();
-                    const uint32_t sa1 = tc::smem_u32(base + st * STAGE), sa0 = sa1 + A_BYTES, sb = sa1 + 2 * A_BYTES;
+                    const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
 #pragma unroll
-                    for (int kk = 0; kk < BK / UK; kk++) {
-                        const uint64_t bd = tc::sdesc_kmajor(sb + kk * 32);
-                        tc::mma_bf16(d, tc::sdesc_kmajor(sa1 + kk * 32), bd, idesc, s != 0 || kk != 0);
-                        tc::mma_bf16(d + 2 * PBX, tc::sdesc_kmajor(sa0 + kk * 32), bd, idesc, s != 0 || kk != 0);
-                    }
+                    for (int kk = 0; kk < BK / UK; kk++)
+                        tc::mma_bf16(d, tc::sdesc_kmajor(sa + kk * 32), tc::sdesc_kmajor(sb + kk * 32), idesc,
+                                     s != 0 || kk != 0);
                     tc::mma_commit(&bars->empty[st]);
                 }
                 if (ok) tc::mma_commit(&bars->tfull[b]);
@@ -433,22 +484,22 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             const int b = lt & 1;
             const int mi = (int)(t / per_mod), r = (int)(t % per_mod);
             const int y = (r / a.nxt) * BM + quad * 32 + lane;
-            const int xh = (r % a.nxt) * PBX + half * 32;  // this warp's 32 output columns
+            const int xh = (r % a.nxt) * PBX + half * 64;  // this warp's 64 output columns
             if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); break; }
             tc::fence_after_sync();
             const ModConst mc = a.mods[mi];
+            const float pf = (float)mc.p;
             __nv_bfloat16 *yhi = a.Y + (int64_t)(2 * mi) * a.Ep + (int64_t)y * a.n + xh;
             __nv_bfloat16 *ylo = a.Y + (int64_t)(2 * mi + 1) * a.Ep + (int64_t)y * a.n + xh;
-            const bool full_row = y < a.m && xh + 32 <= a.n && ((reinterpret_cast<uintptr_t>(yhi) | reinterpret_cast<uintptr_t>(ylo)) & 15) == 0;
-            for (int c = 0; c < 32; c += 16) {
-                uint32_t d11[16], d10[16], d01[16], d00[16];
-                const uint32_t col = 256u * b + half * 32 + c;
-                tc::tmem_ld16(lb + col, d11);
-                tc::tmem_ld16(lb + col + PBX, d10);
-                tc::tmem_ld16(lb + col + 2 * PBX, d01);
-                tc::tmem_ld16(lb + col + 3 * PBX, d00);
+            const bool full_row = y < a.m && xh + 64 <= a.n &&
+                                  ((reinterpret_cast<uintptr_t>(yhi) | reinterpret_cast<uintptr_t>(ylo)) & 15) == 0;
+            for (int c = 0; c < 64; c += 16) {
+                uint32_t dh[16], dl[16];
+                const uint32_t col = 256u * b + half * 64 + c;
+                tc::tmem_ld16(lb + col, dh);
+                tc::tmem_ld16(lb + col + PBX, dl);
                 tc::tmem_ld_wait();
-                if (c == 16) {
+                if (c == 48) {
                     tc::fence_before_sync();
                     __syncwarp();
                     if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
@@ -459,22 +510,20 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                     float h2[2], l2[2];
 #pragma unroll
                     for (int u = 0; u < 2; u++) {
-                        const int32_t r11 = mod_s32(tc::acc_int(d11[j + u]), mc.p, mc.inv_p);
-                        const int32_t r1 = mod_s32(tc::acc_int(d10[j + u]) + tc::acc_int(d01[j + u]), mc.p, mc.inv_p);
-                        const uint32_t t16 = mod_u32((uint32_t)r11 * mc.h16, (uint32_t)mc.p, mc.mu);
-                        const int32_t cc = mod_s32((int32_t)t16 + 256 * r1 + tc::acc_int(d00[j + u]), mc.p, mc.inv_p);
-                        const uint32_t yv = mod_u32((uint32_t)cc * mc.w, (uint32_t)mc.p, mc.mu);
-                        balanced_digits((int32_t)yv, mc.p, h2[u], l2[u]);
+                        const float rh = red_bal(__uint_as_float(dh[j + u]), pf, mc.inv_p);
+                        const float rl = red_bal(__uint_as_float(dl[j + u]), pf, mc.inv_p);
+                        const float yv = red_bal(__fmaf_rn(256.f, rh, rl), pf, mc.inv_p);
+                        bal_split(yv, h2[u], l2[u]);
                     }
                     phi[j / 2] = pack_bf16x2(h2[0], h2[1]);
                     plo[j / 2] = pack_bf16x2(l2[0], l2[1]);
                 }
                 if (full_row) {
-                    uint4 *dh = reinterpret_cast<uint4 *>(yhi + c), *dl = reinterpret_cast<uint4 *>(ylo + c);
-                    dh[0] = make_uint4(phi[0], phi[1], phi[2], phi[3]);
-                    dh[1] = make_uint4(phi[4], phi[5], phi[6], phi[7]);
-                    dl[0] = make_uint4(plo[0], plo[1], plo[2], plo[3]);
-                    dl[1] = make_uint4(plo[4], plo[5], plo[6], plo[7]);
+                    uint4 *dsth = reinterpret_cast<uint4 *>(yhi + c), *dstl = reinterpret_cast<uint4 *>(ylo + c);
+                    dsth[0] = make_uint4(phi[0], phi[1], phi[2], phi[3]);
+                    dsth[1] = make_uint4(phi[4], phi[5], phi[6], phi[7]);
+                    dstl[0] = make_uint4(plo[0], plo[1], plo[2], plo[3]);
+                    dstl[1] = make_uint4(plo[4], plo[5], plo[6], plo[7]);
                 } else if (y < a.m) {
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
@@ -863,7 +912,7 @@ struct crt_tables {
     ModConst *d_mods = nullptr;
     __nv_bfloat16 *d_recon = nullptr;  // [NT*128][2Pp]
     int8_t *d_mdig = nullptr;          // [Dout]
-    std::map<int, __nv_bfloat16 *> residue;  // dxp -> [2P rows][dxp]
+    std::map<int, __nv_bfloat16 *> residue;  // 2 * dxp + scaled -> [2P rows][dxp]
     std::vector<ModConst> h_mods;
 };
 
@@ -950,15 +999,19 @@ static gbmm_status build_tables(crt_tables *t, int P) {
     return GBMM_OK;
 }
 
-static gbmm_status residue_table(crt_tables *t, int dxp, __nv_bfloat16 **out) {
-    auto it = t->residue.find(dxp);
+// Residue table [2P rows][dxp]: rows 2i / 2i+1 hold the low / high balanced
+// byte of 256^j mod p_i (scaled = 0) or of w_i 256^j mod p_i (scaled = 1, the
+// CRT weight w_i = (Mod/p_i)^-1 mod p_i folded into the B operand).
+static gbmm_status residue_table(crt_tables *t, int dxp, int scaled, __nv_bfloat16 **out) {
+    const int key = 2 * dxp + scaled;
+    auto it = t->residue.find(key);
     if (it != t->residue.end()) { *out = it->second; return GBMM_OK; }
     const auto &pr = primes_desc();
     const int rows = 2 * t->P;
     std::vector<uint16_t> tab((size_t)rows * dxp);
     for (int i = 0; i < t->P; i++) {
         const uint32_t p = pr[i];
-        uint32_t v = 1;  // 256^j mod p
+        uint32_t v = scaled ? t->h_mods[i].w : 1u;  // (w) 256^j mod p
         for (int j = 0; j < dxp; j++) {
             int32_t b = v > p / 2 ? (int32_t)v - (int32_t)p : (int32_t)v;
             int32_t d0 = ((b + 128) & 255) - 128;
@@ -971,7 +1024,7 @@ static gbmm_status residue_table(crt_tables *t, int dxp, __nv_bfloat16 **out) {
     __nv_bfloat16 *d = nullptr;
     GBMM_CUDA_TRY(cudaMalloc(&d, tab.size() * 2));
     GBMM_CUDA_TRY(cudaMemcpy(d, tab.data(), tab.size() * 2, cudaMemcpyHostToDevice));
-    t->residue[dxp] = d;
+    t->residue[key] = d;
     *out = d;
     return GBMM_OK;
 }
@@ -1009,9 +1062,10 @@ static gbmm_status set_smem(const void *fn, size_t bytes) {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// digits + residues of one operand into planes [2P][rowsR][kp]
+// digits + residues of one operand into planes [2P][rowsR][kp] (A: a1, a0 per
+// modulus) or, scaled, [4P][rowsR][kp] (B: u1, u0, v1, v0 with u = w b, v = 256 w b)
 static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat &X, int transpose, int rowsR, int kdim,
-                                    int kp, __nv_bfloat16 *R, cudaStream_t s) {
+                                    int kp, int scaled, __nv_bfloat16 *R, cudaStream_t s) {
     const int L = std::max(X.nlimbs, 1);
     const int dxp = (4 * L + 63) / 64 * 64;
     const int64_t E = (int64_t)X.rows * X.cols;
@@ -1027,7 +1081,7 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     __nv_bfloat16 *T = nullptr;
-    GBMM_TRY(residue_table(t, dxp, &T));
+    GBMM_TRY(residue_table(t, dxp, scaled, &T));
     const int nk = dxp / BK;
     const int G = (nk + GROUP_STEPS - 1) / GROUP_STEPS;
     int BN = 256;
@@ -1039,6 +1093,7 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     ResidueArgs a;
     a.sizes = X.sizes; a.rs = X.rs; a.transpose = transpose; a.kdim = kdim; a.E = E; a.nk = nk;
     a.BN = BN; a.G = G; a.P = t->P; a.mods = t->d_mods; a.R = R; a.plane = (int64_t)rowsR * kp; a.kp = kp;
+    a.ncols = 2 * t->P; a.scaled = scaled;
     a.n_ntiles = (2 * t->P + BN - 1) / BN;
     a.ntiles = (int64_t)a.n_ntiles * ((E + BM - 1) / BM);
     const size_t sm = smem_bytes(RES_STAGES, BM * 128 + (size_t)BN * 128);
@@ -1066,7 +1121,7 @@ static size_t crt_workspace(const gbmm_mat &a, const gbmm_mat &b, const gbmm_mat
     const int kp = (k + 63) / 64 * 64;
     const int64_t Ep = ((int64_t)m * n + 63) / 64 * 64;
     const int dxa = (4 * std::max(a.nlimbs, 1) + 63) / 64 * 64, dxb = (4 * std::max(b.nlimbs, 1) + 63) / 64 * 64;
-    return align256((size_t)2 * P * m * kp * 2) + align256((size_t)2 * P * n * kp * 2) + align256((size_t)2 * Pp * Ep * 2) +
+    return align256((size_t)2 * P * m * kp * 2) + align256((size_t)4 * P * n * kp * 2) + align256((size_t)2 * Pp * Ep * 2) +
            std::max(align256((size_t)m * k * dxa * 2 + 1024), align256((size_t)k * n * dxb * 2 + 1024)) + 8192;
 }
 
@@ -1133,32 +1188,32 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     GBMM_TRY(arena_reserve(h, crt_workspace(a, b, c, bits_a, bits_b, P)));
     size_t mark = arena_mark(h);
     __nv_bfloat16 *RA = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * P * m * kp * 2);
-    __nv_bfloat16 *RB = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * P * n * kp * 2);
+    __nv_bfloat16 *RB = (__nv_bfloat16 *)arena_alloc(h, (size_t)4 * P * n * kp * 2);
     __nv_bfloat16 *Y = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * t->Pp * Ep * 2);
     if (!RA || !RB || !Y) return set_error(GBMM_ERR_NOMEM, "crt: workspace");
     if (kp != k) {
         GBMM_CUDA_TRY(cudaMemsetAsync(RA, 0, (size_t)2 * P * m * kp * 2, s));
-        GBMM_CUDA_TRY(cudaMemsetAsync(RB, 0, (size_t)2 * P * n * kp * 2, s));
+        GBMM_CUDA_TRY(cudaMemsetAsync(RB, 0, (size_t)4 * P * n * kp * 2, s));
     }
     if (Ep != E || t->Pp != P) GBMM_CUDA_TRY(cudaMemsetAsync(Y, 0, (size_t)2 * t->Pp * Ep * 2, s));
     {
         size_t mk = arena_mark(h);
-        GBMM_TRY(operand_residues(h, t, a, 0, m, k, kp, RA, s));
+        GBMM_TRY(operand_residues(h, t, a, 0, m, k, kp, 0, RA, s));
         arena_release(h, mk);
-        GBMM_TRY(operand_residues(h, t, b, 1, n, k, kp, RB, s));
+        GBMM_TRY(operand_residues(h, t, b, 1, n, k, kp, 1, RB, s));
         arena_release(h, mk);
     }
     uint32_t *err = device_error_word();
     {
         CUtensorMap tmA, tmB;
         GBMM_TRY(make_map(&tmA, RA, kp, (uint64_t)2 * P * m, kp, BK, BM));
-        GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)2 * P * n, kp, BK, PBX));
+        GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)4 * P * n, kp, BK, PBX));
         ProductArgs pa;
         pa.m = m; pa.n = n; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.Ep = Ep;
         pa.nyt = (m + BM - 1) / BM;
         pa.nxt = (n + PBX - 1) / PBX;
         pa.ntiles = (int64_t)P * pa.nyt * pa.nxt;
-        const size_t sm = smem_bytes(PROD_STAGES, 2 * BM * 128 + 2 * PBX * 128);
+        const size_t sm = smem_bytes(PROD_STAGES, BM * 128 + 2 * PBX * 128);
         GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES>, sm));
         dim3 grid((unsigned)std::min<int64_t>(pa.ntiles, num_sms()));
         LaunchScope ls_("k_crt_product", s);

@@ -509,8 +509,15 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--size", type=int, default=0,
+                    help="override K=M=N of a single-product workload (small cases for profiling)")
+    ap.add_argument("--bits", type=int, default=0, help="override the entry bit length")
     args = ap.parse_args()
     W = WORKLOADS[args.workload]
+    if (args.size or args.bits) and args.workload != "cfg4":
+        S = args.size or W["K"]
+        b = args.bits or W["bits"]
+        W = dict(W, K=S, M=S, N=S, bits=b, label=f"{S}x{S}x{S} {b}-bit signed (resized {args.workload})")
     world, rank, local = dist_init()
     if args.impl == "reference":
         if args.workload == "cfg4":
