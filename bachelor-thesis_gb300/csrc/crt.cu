@@ -19,11 +19,11 @@
 //                 digits against B's 256-scaled digits, then A's low digits
 //                 against B's plain digits); y_i = 256 * D_hi + D_lo mod p_i,
 //                 stored balanced as two digits in per-modulus planes.
-//  4. reconstruct: [entries x 2P] x [2P x (8 + Dout)] GEMM against the digits
+//  4. reconstruct: [entries x 2P] x [2P x (32 + Dout)] GEMM against the digits
 //                 of Mod/p_i (and 256*Mod/p_i) plus fixed-point digits of
-//                 2^48/p_i; the epilogue gets q = round(sum y_i / p_i), folds
-//                 out q*Mod, propagates carries across the digit columns and
-//                 writes sign-magnitude limbs.  C = sum y_i Mod/p_i - q*Mod.
+//                 2^96/p_i; the epilogue gets q = round(sum y_i / p_i) and the
+//                 sign of C, folds out q*Mod, carries across the digit columns
+//                 and writes sign-magnitude limbs.  C = sum y_i Mod/p_i - q*Mod.
 // The CRT itself is the textbook one (HAC 14.5, Knuth 4.3.2); the reference's
 // crt.cpp (split / merge of one integer through a tree of coprime pairs) is
 // unused by the reference and only the idea carries over.
@@ -50,11 +50,11 @@ constexpr int BK = 64;   // bf16 elements per K step (one 128-byte swizzle row)
 constexpr int UK = 16;   // K of one kind::f16 MMA
 constexpr int GROUP_STEPS = 8;  // K steps per exact accumulation group (512 digits)
 constexpr int SROWS = 32;       // columns before the first output digit in the reconstruction table
-constexpr int SUSED = 8;        // of which the fixed-point sum uses the first 8
-constexpr int FIXB = 48;        // fixed-point bits of the 1/p_i weights
+constexpr int SUSED = 14;       // of which the fixed-point sum uses the first 14 (98 bits)
+constexpr int FIXB = 96;        // fixed-point bits of the 1/p_i weights
 constexpr int CTA_THREADS = 192;   // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
 constexpr int CTA_THREADS8 = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue (two per lane quadrant)
-constexpr int RBN = 256;           // reconstruction N tile (output digit columns)
+constexpr int RBN = 128;           // reconstruction N tile (output digit columns)
 }  // namespace
 
 struct ModConst {
@@ -67,52 +67,31 @@ struct ModConst {
 };
 
 // ---- modular helpers (device) ---------------------------------------------------------
-// s mod p for |s| < 2^25 using an FP32 quotient estimate (error <= 1) and two fixes.
-__device__ __forceinline__ int32_t mod_s32(int32_t s, int32_t p, float inv_p) {
-    int32_t q = __float2int_rd(__int2float_rn(s) * inv_p);
-    int32_t r = s - q * p;
-    r += r < 0 ? p : 0;
-    r += r < 0 ? p : 0;
-    r -= r >= p ? p : 0;
-    r -= r >= p ? p : 0;
-    return r;
-}
-// v mod p for any 32-bit unsigned v (Barrett with mu = floor(2^32/p)).
-__device__ __forceinline__ uint32_t mod_u32(uint32_t v, uint32_t p, uint32_t mu) {
-    uint32_t q = __umulhi(v, mu);
-    uint32_t r = v - q * p;
-    return r >= p ? r - p : r;
-}
-// residue r in [0,p) -> balanced value in (-p/2, p/2] split as hi*256 + lo with
-// lo in [-128, 127] and hi in [-128, 128]
-__device__ __forceinline__ void balanced_digits(int32_t r, int32_t p, float &hi, float &lo) {
-    int32_t b = r > (p >> 1) ? r - p : r;
-    int32_t d0 = ((b + 128) & 255) - 128;
-    int32_t d1 = (b - d0) >> 8;
-    hi = (float)d1;
-    lo = (float)d0;
-}
-
-// Balanced representative of x mod p in [-(p-1)/2, (p-1)/2] for an exact
-// integer |x| < 2^24 held in FP32; FMA-pipe only (no int<->float conversion).
-// The quotient is rounded with the 1.5 * 2^23 trick (|x/p| < 2^22); fma gives
-// x - q*p exactly because the result is small; one correction each way covers
-// the quotient's rounding error.
+// Every value below is an exact integer held in FP32 with magnitude < 2^24, so
+// the reductions run on the FMA pipe with no int<->float conversion.
+//
+// red(x) = x - rint(x / p) * p for |x| < 2^24 and 2^15 < p < 2^16.  The quotient
+// is rounded by adding 1.5 * 2^23 inside one FMA (|x / p| < 2^9 keeps the sum in
+// the binade where the ulp is 1); with inv_p = fl(1/p) its error against the
+// true x / p is at most 2^9 * 2^-24 = 2^-15, so the result lies in
+// [-p/2 - 2, p/2 + 2]: congruent to x, not always the balanced representative.
+// The second FMA is exact because the true result is a small integer.
+// Downstream bounds use |red(x)| <= 32772.
 constexpr float RND_MAGIC = 12582912.0f;  // 1.5 * 2^23
-__device__ __forceinline__ float red_bal(float x, float p, float inv_p) {
-    float q = __fadd_rn(__fmul_rn(x, inv_p), RND_MAGIC);
-    q = __fsub_rn(q, RND_MAGIC);
-    float r = __fmaf_rn(-q, p, x);
-    const float h = 0.5f * p;
-    r = r > h ? r - p : r;
-    r = r < -h ? r + p : r;
-    return r;
+__device__ __forceinline__ float red(float x, float p, float inv_p) {
+    const float q = __fadd_rn(__fmaf_rn(x, inv_p, RND_MAGIC), -RND_MAGIC);
+    return __fmaf_rn(-q, p, x);
 }
-// balanced r (|r| < 2^15) -> two signed byte digits, r = hi * 256 + lo, |hi|, |lo| <= 128
+// r (|r| <= 32772) -> two signed byte digits, r = hi * 256 + lo, |hi|, |lo| <= 128
 __device__ __forceinline__ void bal_split(float r, float &hi, float &lo) {
-    float q = __fadd_rn(__fmul_rn(r, 1.0f / 256.0f), RND_MAGIC);
-    hi = __fsub_rn(q, RND_MAGIC);
+    hi = __fadd_rn(__fmaf_rn(r, 1.0f / 256.0f, RND_MAGIC), -RND_MAGIC);
     lo = __fmaf_rn(-hi, 256.0f, r);
+}
+// bf16 bit patterns of two small integers (|v| <= 256 has at most 9 significant
+// bits, so the low 16 bits of its FP32 encoding are zero and truncation is exact):
+// a in the low half, b in the high half
+__device__ __forceinline__ uint32_t bf16x2_bits(float a, float b) {
+    return __byte_perm(__float_as_uint(a), __float_as_uint(b), 0x7632);
 }
 
 struct Barriers {
@@ -123,6 +102,8 @@ struct Barriers {
     uint32_t tmem_base;
     int abort_flag;
 };
+constexpr uint32_t SMEM_BARS = 256;  // bytes reserved for Barriers; per-kernel tables follow
+static_assert(sizeof(Barriers) <= SMEM_BARS, "barrier block");
 
 __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
     uintptr_t v = reinterpret_cast<uintptr_t>(p);
@@ -257,7 +238,13 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
     uint8_t *base = align1024(smem_raw);
     const uint32_t A_BYTES = BM * 128, B_BYTES = (uint32_t)a.BN * 128, STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
+    // (p, 1/p) per modulus, padded to a multiple of 16 with the last modulus
+    float2 *smod = reinterpret_cast<float2 *>(reinterpret_cast<uint8_t *>(bars) + SMEM_BARS);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < (a.P + 15) / 16 * 16; i += blockDim.x) {
+        const ModConst mc = a.mods[i < a.P ? i : a.P - 1];
+        smod[i] = make_float2((float)mc.p, mc.inv_p);
+    }
     cta_setup(bars, STAGES, 512, 1, 8);
     const uint32_t tmem = bars->tmem_base;
 
@@ -329,6 +316,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                 sgn = a.sizes[a.transpose ? c * a.rs + r : r * a.rs + c] < 0 ? -1.f : 1.f;
                 off = r * a.kp + c;
             }
+            const int64_t pstep = (int64_t)npl * a.plane;  // planes of one modulus
             for (int c0 = half * hcols; c0 < (half + 1) * hcols; c0 += 32) {
                 float res[16];
 #pragma unroll
@@ -350,31 +338,29 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                     if (!live_chunk) continue;
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
-                        const ModConst mc = a.mods[mi0 + j < a.P ? mi0 + j : 0];
-                        const float pf = (float)mc.p;
-                        // s0 + 256 * s1 (+ residue of earlier groups), each |s| < 2^24
-                        const float r1 = red_bal(__uint_as_float(v[2 * j + 1]), pf, mc.inv_p);
-                        const float r0 = red_bal(__uint_as_float(v[2 * j]), pf, mc.inv_p);
-                        res[j] = red_bal(__fmaf_rn(256.f, r1, r0) + res[j], pf, mc.inv_p);
+                        const float2 pc = smod[mi0 + j];
+                        // s0 + 256 * s1 (+ residue of earlier groups): |s| <= 2^24 each,
+                        // |256 red(s1) + red(s0) + res| <= 257 * 32772 + 32772 < 2^24
+                        const float r1 = red(__uint_as_float(v[2 * j + 1]), pc.x, pc.y);
+                        const float r0 = red(__uint_as_float(v[2 * j]), pc.x, pc.y);
+                        res[j] = red(__fmaf_rn(256.f, r1, r0) + res[j], pc.x, pc.y);
                     }
                 }
                 if (e < a.E && live_chunk) {
+                    uint16_t *dst = reinterpret_cast<uint16_t *>(a.R + (int64_t)mi0 * pstep + off);
 #pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const int mi = mi0 + j;
-                        if (mi >= a.P) continue;
+                    for (int j = 0; j < 16; j++, dst += pstep) {
+                        if (mi0 + j >= a.P) break;
                         const float r = sgn * res[j];
                         float hi, lo;
                         bal_split(r, hi, lo);
-                        __nv_bfloat16 *dst = a.R + (int64_t)(npl * mi) * a.plane + off;
-                        dst[0] = __float2bfloat16_rn(hi);
-                        dst[a.plane] = __float2bfloat16_rn(lo);
+                        dst[0] = (uint16_t)(__float_as_uint(hi) >> 16);
+                        dst[a.plane] = (uint16_t)(__float_as_uint(lo) >> 16);
                         if (a.scaled) {
-                            const ModConst mc = a.mods[mi];
-                            const float r2 = red_bal(256.f * r, (float)mc.p, mc.inv_p);
-                            bal_split(r2, hi, lo);
-                            dst[2 * a.plane] = __float2bfloat16_rn(hi);
-                            dst[3 * a.plane] = __float2bfloat16_rn(lo);
+                            const float2 pc = smod[mi0 + j];
+                            bal_split(red(256.f * r, pc.x, pc.y), hi, lo);
+                            dst[2 * a.plane] = (uint16_t)(__float_as_uint(hi) >> 16);
+                            dst[3 * a.plane] = (uint16_t)(__float_as_uint(lo) >> 16);
                         }
                     }
                 }
@@ -402,15 +388,11 @@ struct ProductArgs {
     int32_t nyt, nxt;
     int64_t ntiles;
     const ModConst *mods;
-    __nv_bfloat16 *Y;  // planes [2Pp][Ep]
-    int64_t Ep;
+    __nv_bfloat16 *Y;  // blocked [Ep/64][2Pp][64]: 64 entries per row, 2Pp rows per block
+    int64_t yblk;      // elements per 64-entry block (2Pp * 64)
 };
 constexpr int PBX = 128;  // output columns per product tile
 
-__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
-    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<uint32_t *>(&v);
-}
 
 template <int STAGES>
 __global__ void __launch_bounds__(CTA_THREADS8, 1)
@@ -489,10 +471,8 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             tc::fence_after_sync();
             const ModConst mc = a.mods[mi];
             const float pf = (float)mc.p;
-            __nv_bfloat16 *yhi = a.Y + (int64_t)(2 * mi) * a.Ep + (int64_t)y * a.n + xh;
-            __nv_bfloat16 *ylo = a.Y + (int64_t)(2 * mi + 1) * a.Ep + (int64_t)y * a.n + xh;
-            const bool full_row = y < a.m && xh + 64 <= a.n &&
-                                  ((reinterpret_cast<uintptr_t>(yhi) | reinterpret_cast<uintptr_t>(ylo)) & 15) == 0;
+            const int64_t erow = (int64_t)y * a.n + xh;  // entry index of this warp's first column
+            __nv_bfloat16 *yplane = a.Y + (int64_t)(2 * mi) * 64;  // hi plane; lo plane 64 elements on
             for (int c = 0; c < 64; c += 16) {
                 uint32_t dh[16], dl[16];
                 const uint32_t col = 256u * b + half * 64 + c;
@@ -510,27 +490,32 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                     float h2[2], l2[2];
 #pragma unroll
                     for (int u = 0; u < 2; u++) {
-                        const float rh = red_bal(__uint_as_float(dh[j + u]), pf, mc.inv_p);
-                        const float rl = red_bal(__uint_as_float(dl[j + u]), pf, mc.inv_p);
-                        const float yv = red_bal(__fmaf_rn(256.f, rh, rl), pf, mc.inv_p);
-                        bal_split(yv, h2[u], l2[u]);
+                        // |256 red(Dh) + red(Dl)| <= 257 * 32772 < 2^24
+                        const float rh = red(__uint_as_float(dh[j + u]), pf, mc.inv_p);
+                        const float rl = red(__uint_as_float(dl[j + u]), pf, mc.inv_p);
+                        bal_split(red(__fmaf_rn(256.f, rh, rl), pf, mc.inv_p), h2[u], l2[u]);
                     }
-                    phi[j / 2] = pack_bf16x2(h2[0], h2[1]);
-                    plo[j / 2] = pack_bf16x2(l2[0], l2[1]);
+                    phi[j / 2] = bf16x2_bits(h2[0], h2[1]);
+                    plo[j / 2] = bf16x2_bits(l2[0], l2[1]);
                 }
-                if (full_row) {
-                    uint4 *dsth = reinterpret_cast<uint4 *>(yhi + c), *dstl = reinterpret_cast<uint4 *>(ylo + c);
+                if (y >= a.m) continue;
+                const int64_t ec = erow + c;
+                if ((ec & 15) == 0 && xh + c + 16 <= a.n) {
+                    // 16 entries inside one 64-entry block: two 32-byte runs
+                    __nv_bfloat16 *dst = yplane + (ec >> 6) * a.yblk + (ec & 63);
+                    uint4 *dsth = reinterpret_cast<uint4 *>(dst), *dstl = reinterpret_cast<uint4 *>(dst + 64);
                     dsth[0] = make_uint4(phi[0], phi[1], phi[2], phi[3]);
                     dsth[1] = make_uint4(phi[4], phi[5], phi[6], phi[7]);
                     dstl[0] = make_uint4(plo[0], plo[1], plo[2], plo[3]);
                     dstl[1] = make_uint4(plo[4], plo[5], plo[6], plo[7]);
-                } else if (y < a.m) {
+                } else {
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
                         if (xh + c + j >= a.n) break;
-                        const uint32_t wh = phi[j / 2] >> (16 * (j & 1)), wl = plo[j / 2] >> (16 * (j & 1));
-                        reinterpret_cast<uint16_t *>(yhi)[c + j] = (uint16_t)wh;
-                        reinterpret_cast<uint16_t *>(ylo)[c + j] = (uint16_t)wl;
+                        const int64_t e = ec + j;
+                        uint16_t *dst = reinterpret_cast<uint16_t *>(yplane + (e >> 6) * a.yblk + (e & 63));
+                        dst[0] = (uint16_t)(phi[j / 2] >> (16 * (j & 1)));
+                        dst[64] = (uint16_t)(plo[j / 2] >> (16 * (j & 1)));
                     }
                 }
             }
@@ -540,16 +525,23 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 }
 
 // ======================================================================================
-// 4. reconstruction GEMM (one CTA per 128 entries, N tiles of 256 digit columns,
-//    TMEM double-buffered across tiles; base-128 table digits so one FP32
-//    accumulation over all 2P rows stays exact: 2P * 128 * 64 < 2^24)
+// 4. reconstruction GEMM (persistent over tiles of 256 entries; each K step
+//    multiplies two 128-entry subtiles by one tile of RBN table rows, so the
+//    table tile is fetched once per 256 entries; TMEM double-buffered across
+//    N tiles; 8 epilogue warps, each owning 32 entries.  Base-128 table digits
+//    keep one FP32 accumulation over all 2P rows exact: 2P * 128 * 64 < 2^24.)
+//    Y arrives blocked, [E/64][2Pp][64], so each 64-entry x 64-row A box is one
+//    contiguous 8 KB run.
 // ======================================================================================
+constexpr int RME = 2 * BM;  // entries per reconstruction tile
 struct ReconArgs {
     int64_t E;       // entries of C
     int32_t ncols;   // columns of C (entry e -> row e / ncols, col e % ncols)
     int32_t nk;      // K steps over 2Pp
     int32_t NT;      // N tiles of RBN table rows
     int32_t Dout;    // output base-128 digit positions
+    int32_t kpad;    // 2Pp: rows of one 64-entry block of Y
+    int64_t nmt;     // tiles of RME entries
     const int8_t *mdig;  // balanced base-128 digits of Mod, Dout entries
     uint32_t *climbs;
     int32_t *csizes;
@@ -558,18 +550,18 @@ struct ReconArgs {
 };
 
 template <int STAGES>
-__global__ void __launch_bounds__(CTA_THREADS, 1)
+__global__ void __launch_bounds__(CTA_THREADS8, 1)
     k_crt_recon(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmT, ReconArgs a,
                 uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
-    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = RBN * 128, STAGE = A_BYTES + B_BYTES;
+    constexpr uint32_t BOX = 64 * 128;  // one 64-entry x 64-row A box
+    constexpr uint32_t A_BYTES = RME * 128, B_BYTES = RBN * 128, STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
-    int8_t *smdig = reinterpret_cast<int8_t *>(bars + 1);
+    int8_t *smdig = reinterpret_cast<int8_t *>(bars) + SMEM_BARS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t e0 = (int64_t)blockIdx.x * BM;
     for (int i = threadIdx.x; i < a.Dout + 32; i += blockDim.x) smdig[i] = i < a.Dout ? a.mdig[i] : 0;
-    cta_setup(bars, STAGES, 512, 1, 4);
+    cta_setup(bars, STAGES, 512, 1, 8);
     const uint32_t tmem = bars->tmem_base;
 
     if (warp == 0) {
@@ -577,134 +569,177 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
             tc::prefetch_tmap(&tmY);
             tc::prefetch_tmap(&tmT);
             int it = 0;
-            for (int j = 0; j < a.NT && !aborted(bars); j++) {
-                for (int s = 0; s < a.nk; s++, it++) {
-                    const int st = it % STAGES;
-                    if (it >= STAGES && !tc::mbar_wait(&bars->empty[st], ((it / STAGES) & 1) ^ 1)) {
-                        set_abort(bars, err);
-                        break;
+            for (int64_t t = blockIdx.x; t < a.nmt && !aborted(bars); t += gridDim.x) {
+                const int blk0 = (int)(t * (RME / 64));
+                for (int j = 0; j < a.NT && !aborted(bars); j++) {
+                    for (int s = 0; s < a.nk; s++, it++) {
+                        const int st = it % STAGES;
+                        if (it >= STAGES && !tc::mbar_wait(&bars->empty[st], ((it / STAGES) & 1) ^ 1)) {
+                            set_abort(bars, err);
+                            break;
+                        }
+                        uint8_t *sa = base + st * STAGE;
+                        tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                        // A (MN-major): four 64-entry blocks x 64 K-rows; blocks past the
+                        // end of Y read as zeros and still count their full box bytes
+#pragma unroll
+                        for (int q = 0; q < RME / 64; q++)
+                            tc::tma_load_2d(sa + q * BOX, &tmY, &bars->full[st], 0, (blk0 + q) * a.kpad + s * BK);
+                        tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, j * RBN);
                     }
-                    uint8_t *sa = base + st * STAGE;
-                    tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                    // A (MN-major): two boxes of 64 entries x 64 K-rows
-                    tc::tma_load_2d(sa, &tmY, &bars->full[st], (int)e0, s * BK);
-                    tc::tma_load_2d(sa + A_BYTES / 2, &tmY, &bars->full[st], (int)e0 + 64, s * BK);
-                    tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, j * RBN);
                 }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
             const uint32_t idesc = tc::idesc_bf16_f32(BM, RBN, 1, 0);
-            int it = 0;
+            int it = 0, lt = 0;
             bool ok = true;
-            for (int j = 0; j < a.NT && ok; j++) {
-                const int b = j & 1;
-                if (j >= 2 && !tc::mbar_wait(&bars->tempty[b], ((j >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
-                tc::fence_after_sync();
-                const uint32_t d = tmem + 256u * b;
-                for (int s = 0; s < a.nk; s++, it++) {
-                    const int st = it % STAGES;
-                    if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+            for (int64_t t = blockIdx.x; t < a.nmt && ok; t += gridDim.x) {
+                for (int j = 0; j < a.NT && ok; j++, lt++) {
+                    const int b = lt & 1;
+                    if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) {
+                        set_abort(bars, err);
+                        ok = false;
+                        break;
+                    }
                     tc::fence_after_sync();
-                    const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
+                    const uint32_t d = tmem + 256u * b;
+                    for (int s = 0; s < a.nk; s++, it++) {
+                        const int st = it % STAGES;
+                        if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+                        tc::fence_after_sync();
+                        const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
 #pragma unroll
-                    for (int kk = 0; kk < BK / UK; kk++)
-                        tc::mma_bf16(d, tc::sdesc_mnmajor(sa + kk * 2048, A_BYTES / 2), tc::sdesc_kmajor(sb + kk * 32),
-                                     idesc, s != 0 || kk != 0);
-                    tc::mma_commit(&bars->empty[st]);
+                        for (int kk = 0; kk < BK / UK; kk++) {
+                            const uint64_t bdesc = tc::sdesc_kmajor(sb + kk * 32);
+#pragma unroll
+                            for (int sub = 0; sub < 2; sub++)
+                                tc::mma_bf16(d + sub * RBN, tc::sdesc_mnmajor(sa + sub * 2 * BOX + kk * 2048, BOX),
+                                             bdesc, idesc, s != 0 || kk != 0);
+                        }
+                        tc::mma_commit(&bars->empty[st]);
+                    }
+                    if (ok) tc::mma_commit(&bars->tfull[b]);
                 }
-                if (ok) tc::mma_commit(&bars->tfull[b]);
             }
         }
     } else {
-        const int row = epi_row();
-        const int64_t e = e0 + row;
-        const bool live = e < a.E;
-        const int64_t coff = live ? (e / a.ncols) * a.crs + (e % a.ncols) : 0;
-        const uint32_t lb = lane_base(tmem);
-        int32_t carry = 0, q = 0, smask = 0;  // smask = -1 flips every digit column (C < 0)
-        bool ambiguous = false, ok = true;
-        int pos = 0, top = 0;
-        bool drop_nz = false, drop_ones = true;
-        for (int j = 0; j < a.NT; j++) {
-            const int b = j & 1;
-            if (!tc::mbar_wait(&bars->tfull[b], (j >> 1) & 1)) { set_abort(bars, err); ok = false; break; }
-            tc::fence_after_sync();
-            for (int c0 = 0; c0 < RBN; c0 += 32) {
-                uint32_t g[32];
-                tc::tmem_ld32(lb + (uint32_t)(256 * b + c0), g);
-                tc::tmem_ld_wait();
-                if (c0 + 32 >= RBN) {
-                    tc::fence_before_sync();
-                    __syncwarp();
-                    if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
-                }
-                if (j == 0 && c0 == 0) {
-                    // fixed-point sum S = sum y_i 2^48 / p_i from the first SUSED columns (base 128)
-                    __int128 S = 0;
+        // warp (2..9) -> TMEM lane quadrant warp % 4 of subtile (warp - 2) / 4
+        const int quad = warp & 3, sub = (warp - 2) >> 2;
+        const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(sub * RBN);
+        int lt = 0;
+        for (int64_t t = blockIdx.x; t < a.nmt; t += gridDim.x) {
+            const int64_t e = t * RME + sub * BM + quad * 32 + lane;
+            const bool live = e < a.E;
+            const int64_t coff = live ? (e / a.ncols) * a.crs + (e % a.ncols) : 0;
+            // C = sum_u (acc_u - q Mod_u) 128^u; sgn = -1 when C < 0 so that the digits
+            // produce |C|, qs = q * sgn
+            long long carry = 0;
+            int32_t q = 0, sgn = 1, qs = 0;
+            bool ambiguous = false, ok = true;
+            int pos = 0, top = 0;
+            bool drop_nz = false, drop_ones = true;
+            for (int j = 0; j < a.NT; j++, lt++) {
+                const int b = lt & 1;
+                if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); ok = false; break; }
+                tc::fence_after_sync();
+                for (int c0 = 0; c0 < RBN; c0 += 64) {
+                    uint32_t g[64];
+                    tc::tmem_ld32(lb + (uint32_t)(256 * b + c0), *reinterpret_cast<uint32_t(*)[32]>(&g[0]));
+                    tc::tmem_ld32(lb + (uint32_t)(256 * b + c0 + 32), *reinterpret_cast<uint32_t(*)[32]>(&g[32]));
+                    tc::tmem_ld_wait();
+                    if (c0 + 64 >= RBN) {
+                        tc::fence_before_sync();
+                        __syncwarp();
+                        if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
+                    }
 #pragma unroll
-                    for (int t = SUSED - 1; t >= 0; t--) S = S * 128 + tc::acc_int(g[t]);
-                    const __int128 halfw = (__int128)1 << (FIXB - 1);
-                    const __int128 qq = (S + halfw) >> FIXB;
-                    const __int128 frac = S - (qq << FIXB);
-                    q = (int32_t)qq;
-                    const __int128 tol = (__int128)1 << 20;
-                    smask = frac < -tol ? -1 : 0;
-                    ambiguous = frac <= tol && frac >= -tol;
-                    continue;
-                }
-                if (!live || pos >= a.Dout) continue;
-                // 32 base-128 digits = 224 bits = 7 limbs; chunks start on limb boundaries
-                uint64_t bits = 0;
-                int nb = 0, li = pos / 32 * 7;
+                    for (int h = 0; h < 2; h++) {
+                        const uint32_t *gh = g + 32 * h;
+                        if (j == 0 && c0 == 0 && h == 0) {
+                            // fixed-point sum S = sum y_i 2^FIXB / p_i from the first SUSED columns
+                            // (base 128): S = (q + C / Mod) 2^FIXB + err, |err| <= 128 P < 2^17, and
+                            // |C / Mod| < 2^-18, so q = round(S / 2^FIXB) and the sign of
+                            // frac = S - q 2^FIXB is the sign of C unless |C| < Mod 2^(20 - FIXB)
+                            __int128 S = 0;
 #pragma unroll
-                for (int t = 0; t < 32; t++) {
-                    int32_t v = tc::acc_int(g[t]) - q * (int32_t)smdig[pos + t];
-                    v = ((v ^ smask) - smask) + carry;
-                    carry = v >> 7;
-                    bits |= (uint64_t)(uint32_t)(v & 127) << nb;
-                    nb += 7;
-                    if (nb >= 32) {
-                        const uint32_t limb = (uint32_t)bits;
-                        bits >>= 32;
-                        nb -= 32;
-                        if (li < a.cnlimbs) {
-                            a.climbs[(int64_t)li * a.cld + coff] = limb;
-                            if (limb) top = li + 1;
-                        } else {
-                            drop_nz |= limb != 0u;
-                            drop_ones &= limb == 0xFFFFFFFFu;
+                            for (int u = SUSED - 1; u >= 0; u--) S = S * 128 + tc::acc_int(gh[u]);
+                            const __int128 halfw = (__int128)1 << (FIXB - 1);
+                            const __int128 qq = (S + halfw) >> FIXB;
+                            const __int128 frac = S - (qq << FIXB);
+                            q = (int32_t)qq;
+                            const __int128 tol = (__int128)1 << 20;
+                            sgn = frac < -tol ? -1 : 1;
+                            qs = q * sgn;
+                            ambiguous = frac <= tol && frac >= -tol;
+                        } else if (live && pos < a.Dout) {
+                            // 32 base-128 digits = 224 bits = 7 limbs (chunks start on limb
+                            // boundaries).  Each signed digit value x_u (|x_u| < 2^24) enters a
+                            // 64-bit accumulator per limb at its bit offset 7u; one carry pass
+                            // over the 7 limbs follows, so no chain runs through the digits.
+                            long long A[7];
+                            A[0] = carry;
+#pragma unroll
+                            for (int l = 1; l < 7; l++) A[l] = 0;
+#pragma unroll
+                            for (int u = 0; u < 32; u++) {
+                                const int32_t x = tc::acc_int(gh[u]) * sgn - qs * (int32_t)smdig[pos + u];
+                                A[(7 * u) >> 5] += (long long)x * (1LL << ((7 * u) & 31));
+                            }
+                            const int li0 = pos / 32 * 7;
+#pragma unroll
+                            for (int l = 0; l < 7; l++) {
+                                if (l < 6) A[l + 1] += A[l] >> 32;
+                                const uint32_t limb = (uint32_t)A[l];
+                                const int li = li0 + l;
+                                if (li < a.cnlimbs) {
+                                    a.climbs[(int64_t)li * a.cld + coff] = limb;
+                                    if (limb) top = li + 1;
+                                } else {
+                                    drop_nz |= limb != 0u;
+                                    drop_ones &= limb == 0xFFFFFFFFu;
+                                }
+                            }
+                            carry = A[6] >> 32;
+                            pos += 32;
                         }
-                        li++;
                     }
                 }
-                pos += 32;
             }
-        }
-        if (ok && live) {
-            const int nl = pos / 32 * 7;  // limbs produced
-            const int written = nl < a.cnlimbs ? nl : a.cnlimbs;
-            int neg = smask != 0;
-            if (carry < 0) {
-                // only reachable on the ambiguous path: two's complement -> magnitude
-                if (!ambiguous || carry != -1 || (nl > a.cnlimbs && !(drop_ones && top != 0)))
+            if (!ok) break;
+            if (live) {
+                const int nl = pos / 32 * 7;  // limbs produced
+                const int written = nl < a.cnlimbs ? nl : a.cnlimbs;
+                int neg = sgn < 0;
+                if (carry < 0) {
+                    // only reachable on the ambiguous path: two's complement -> magnitude
+                    if (!ambiguous || carry != -1 || (nl > a.cnlimbs && !(drop_ones && top != 0)))
+                        atomicOr(err, DEVERR_CAPACITY);
+                    uint32_t cc = 1;
+                    top = 0;
+                    for (int l0 = 0; l0 < written; l0 += 8) {
+                        uint32_t w[8];
+#pragma unroll
+                        for (int u = 0; u < 8; u++)
+                            w[u] = l0 + u < written ? a.climbs[(int64_t)(l0 + u) * a.cld + coff] : 0u;
+#pragma unroll
+                        for (int u = 0; u < 8; u++) {
+                            if (l0 + u >= written) break;
+                            const uint64_t sum = (uint64_t)(~w[u]) + cc;
+                            const uint32_t r = (uint32_t)sum;
+                            cc = (uint32_t)(sum >> 32);
+                            a.climbs[(int64_t)(l0 + u) * a.cld + coff] = r;
+                            if (r) top = l0 + u + 1;
+                        }
+                    }
+                    neg = 1;
+                } else if (carry != 0 || drop_nz) {
                     atomicOr(err, DEVERR_CAPACITY);
-                uint32_t cc = 1;
-                top = 0;
-                for (int li = 0; li < written; li++) {
-                    uint64_t s = (uint64_t)(~a.climbs[(int64_t)li * a.cld + coff]) + cc;
-                    const uint32_t r = (uint32_t)s;
-                    cc = (uint32_t)(s >> 32);
-                    a.climbs[(int64_t)li * a.cld + coff] = r;
-                    if (r) top = li + 1;
                 }
-                neg = 1;
-            } else if (carry != 0 || drop_nz) {
-                atomicOr(err, DEVERR_CAPACITY);
+                for (int li = written; li < a.cnlimbs; li++) a.climbs[(int64_t)li * a.cld + coff] = 0u;
+                a.csizes[coff] = top == 0 ? 0 : (neg ? -top : top);
             }
-            for (int li = written; li < a.cnlimbs; li++) a.climbs[(int64_t)li * a.cld + coff] = 0u;
-            a.csizes[coff] = top == 0 ? 0 : (neg ? -top : top);
         }
     }
     cta_teardown(bars, 512);
@@ -910,7 +945,7 @@ struct crt_tables {
     int P = 0, Pp = 0;   // moduli, padded 2P/2 (2Pp multiple of 64)
     int Dout = 0, NT = 0;
     ModConst *d_mods = nullptr;
-    __nv_bfloat16 *d_recon = nullptr;  // [NT*128][2Pp]
+    __nv_bfloat16 *d_recon = nullptr;  // [NT * RBN][2Pp]
     int8_t *d_mdig = nullptr;          // [Dout]
     std::map<int, __nv_bfloat16 *> residue;  // 2 * dxp + scaled -> [2P rows][dxp]
     std::vector<ModConst> h_mods;
@@ -976,11 +1011,15 @@ static gbmm_status build_tables(crt_tables *t, int P) {
             tab[(size_t)(SROWS + r) * cols + 2 * i] = bf16_bits((float)dh[r]);
             tab[(size_t)(SROWS + r) * cols + 2 * i + 1] = bf16_bits((float)dl[r]);
         }
-        // fixed-point weights: round(2^56 / p) for the high digit, round(2^48 / p) for the low digit
+        // fixed-point weights: round(2^(FIXB+8) / p) for the high digit, round(2^FIXB / p) for the low digit
         const unsigned __int128 one = 1;
-        uint64_t gh = (uint64_t)(((one << (FIXB + 8)) + p / 2) / p);
-        uint64_t gl = (uint64_t)(((one << FIXB) + p / 2) / p);
-        big bh{(uint32_t)gh, (uint32_t)(gh >> 32)}, bl{(uint32_t)gl, (uint32_t)(gl >> 32)};
+        const unsigned __int128 gh = ((one << (FIXB + 8)) + p / 2) / p;
+        const unsigned __int128 gl = ((one << FIXB) + p / 2) / p;
+        big bh, bl;
+        for (int w = 0; w < 4; w++) {
+            bh.push_back((uint32_t)(gh >> (32 * w)));
+            bl.push_back((uint32_t)(gl >> (32 * w)));
+        }
         std::vector<int> sh = balanced128(bh, SUSED), sl = balanced128(bl, SUSED);
         for (int r = 0; r < SUSED; r++) {
             tab[(size_t)r * cols + 2 * i] = bf16_bits((float)sh[r]);
@@ -1053,7 +1092,7 @@ static int num_sms() {
     }
     return n;
 }
-static size_t smem_bytes(int stages, size_t stage_bytes) { return stages * stage_bytes + sizeof(Barriers) + 1024 + 64; }
+static size_t smem_bytes(int stages, size_t stage_bytes) { return stages * stage_bytes + SMEM_BARS + 1024 + 64; }
 
 static gbmm_status set_smem(const void *fn, size_t bytes) {
     GBMM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -1096,7 +1135,7 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     a.ncols = 2 * t->P; a.scaled = scaled;
     a.n_ntiles = (2 * t->P + BN - 1) / BN;
     a.ntiles = (int64_t)a.n_ntiles * ((E + BM - 1) / BM);
-    const size_t sm = smem_bytes(RES_STAGES, BM * 128 + (size_t)BN * 128);
+    const size_t sm = smem_bytes(RES_STAGES, BM * 128 + (size_t)BN * 128) + (size_t)(t->P + 15) / 16 * 16 * 8;
     GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES>, sm));
     dim3 grid((unsigned)std::min<int64_t>(a.ntiles, num_sms()));
     LaunchScope ls_("k_crt_residue", s);
@@ -1195,7 +1234,12 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         GBMM_CUDA_TRY(cudaMemsetAsync(RA, 0, (size_t)2 * P * m * kp * 2, s));
         GBMM_CUDA_TRY(cudaMemsetAsync(RB, 0, (size_t)4 * P * n * kp * 2, s));
     }
-    if (Ep != E || t->Pp != P) GBMM_CUDA_TRY(cudaMemsetAsync(Y, 0, (size_t)2 * t->Pp * Ep * 2, s));
+    // Y is blocked [Ep/64][2Pp][64]; the padding rows 2P..2Pp-1 of every block meet
+    // zero table columns but must not hold NaN patterns, so they are cleared.  Padding
+    // entries E..Ep-1 only reach accumulator rows that are never stored.
+    if (t->Pp != P)
+        GBMM_CUDA_TRY(cudaMemset2DAsync(Y + (size_t)2 * P * 64, (size_t)2 * t->Pp * 64 * 2, 0,
+                                        (size_t)(2 * t->Pp - 2 * P) * 64 * 2, (size_t)(Ep / 64), s));
     {
         size_t mk = arena_mark(h);
         GBMM_TRY(operand_residues(h, t, a, 0, m, k, kp, 0, RA, s));
@@ -1209,7 +1253,7 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         GBMM_TRY(make_map(&tmA, RA, kp, (uint64_t)2 * P * m, kp, BK, BM));
         GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)4 * P * n, kp, BK, PBX));
         ProductArgs pa;
-        pa.m = m; pa.n = n; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.Ep = Ep;
+        pa.m = m; pa.n = n; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.yblk = (int64_t)2 * t->Pp * 64;
         pa.nyt = (m + BM - 1) / BM;
         pa.nxt = (n + PBX - 1) / PBX;
         pa.ntiles = (int64_t)P * pa.nyt * pa.nxt;
@@ -1222,17 +1266,17 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     }
     {
         CUtensorMap tmY, tmT;
-        GBMM_TRY(make_map(&tmY, Y, Ep, (uint64_t)2 * t->Pp, Ep, 64, BK));
+        GBMM_TRY(make_map(&tmY, Y, 64, (uint64_t)(Ep / 64) * 2 * t->Pp, 64, 64, BK));
         GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RBN, 2 * t->Pp, BK, RBN));
         ReconArgs ra;
         ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.NT = t->NT; ra.Dout = t->Dout;
         ra.mdig = t->d_mdig; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
-        ra.cnlimbs = c.nlimbs;
-        const size_t sm = smem_bytes(REC_STAGES, BM * 128 + RBN * 128) + t->Dout + 64;
+        ra.cnlimbs = c.nlimbs; ra.kpad = 2 * t->Pp; ra.nmt = (E + RME - 1) / RME;
+        const size_t sm = smem_bytes(REC_STAGES, RME * 128 + RBN * 128) + t->Dout + 64;
         GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES>, sm));
-        dim3 grid((unsigned)((E + BM - 1) / BM));
+        dim3 grid((unsigned)std::min<int64_t>(ra.nmt, num_sms()));
         LaunchScope ls_("k_crt_recon", s);
-        k_crt_recon<REC_STAGES><<<grid, CTA_THREADS, sm, s>>>(tmY, tmT, ra, err);
+        k_crt_recon<REC_STAGES><<<grid, CTA_THREADS8, sm, s>>>(tmY, tmT, ra, err);
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     arena_release(h, mark);
