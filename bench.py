@@ -386,7 +386,19 @@ def crt_params(bits_a, bits_b, k):
         mod *= pr[P]
         P += 1
     modbits = 32 * ((mod.bit_length() + 31) // 32)
-    return P, (modbits + 7) // 8 + 2
+    return P, (modbits + 6) // 7 + 2  # base-128 output digits
+
+
+# DRAM bytes (read + write) per launch of each CRT GEMM on 512x512x512 at 4096 bits:
+# one `ncu --set full` capture of the same kernels on 256x256x256 at 4096 bits
+# (profiles/crt_kernels_256x256x256_4096b_ncu.md), times 4 for 4x the entries.
+# The residue figure is the mean of its two launches (A, then B with four planes).
+NCU_DRAM_BYTES_512_4096 = {
+    "k_crt_residue": 4 * (152.548e6 + 284.571e6) / 2,
+    "k_crt_product": 4 * 508.851e6,
+    "k_crt_recon": 4 * 198.109e6,
+}
+FIXED_POINT_COLUMNS = 14  # reconstruction columns that carry the 2^96 / p_i weights
 
 
 def kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof):
@@ -408,12 +420,16 @@ def kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof):
         flops = 2.0 * (K * M + M * N) / 2 * dx * 2 * P  # one launch per operand (square: equal halves)
         note = f"entries x {dx} digits x {2 * P} table columns per operand"
     elif kname == "k_crt_recon":
-        flops = 2.0 * K * N * 2 * P * (8 + Dout)
-        note = f"entries x {2 * P} moduli digits x {8 + Dout} output columns"
+        flops = 2.0 * K * N * 2 * P * (FIXED_POINT_COLUMNS + Dout)
+        note = f"entries x {2 * P} moduli digits x {FIXED_POINT_COLUMNS + Dout} output columns"
     if flops is not None:
         ach = flops / (per_ms * 1e-3) / 1e12
+        traffic = None
+        if (K, M, N, W["bits"]) == (512, 512, 512, 4096) and kname in NCU_DRAM_BYTES_512_4096:
+            traffic = NCU_DRAM_BYTES_512_4096[kname]
+            note += "; traffic: ncu DRAM bytes of the 256^3 capture x 4"
         return {"kernel": kname, "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
-                "frac": ach / bf16, "traffic": None, "peak_source": src + " (bf16 dense, burst)",
+                "frac": ach / bf16, "traffic": traffic, "peak_source": src + " (bf16 dense, burst)",
                 "ms_per_launch": per_ms, "note": note}
     # memory-bound kernels: algorithmic bytes per launch
     if kname == "k_crt_digits":
