@@ -777,10 +777,12 @@ namespace gbmm {
 
 // Plain dispatch heuristic: the CRT form pays off once products are large
 // enough to amortise the residue and reconstruction passes.
+// Plain dispatch rule: the CRT path for products with enough limb work, the limb
+// path otherwise.  Entries too long for one CRT product (more than 1023 moduli)
+// still take the CRT path: dispatch() splits them into limb halves that fit.
 int heuristic_path(int m, int k, int n, int la, int lb) {
     const int64_t work = (int64_t)m * k * n * la * lb;
-    const bool crt_ok = crt_feasible(std::min(la, 1023), std::min(lb, 1023), k);
-    if (la + lb >= 16 && work >= ((int64_t)1 << 22) && crt_ok) return GBMM_PATH_CRT;
+    if (la + lb >= 16 && work >= ((int64_t)1 << 22)) return GBMM_PATH_CRT;
     return GBMM_PATH_LIMB;
 }
 
