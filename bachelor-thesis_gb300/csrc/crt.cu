@@ -13,12 +13,11 @@
 //                 epilogue folds the two halves, reduces mod p_i in FP32,
 //                 applies the entry's sign and stores the residue as two
 //                 balanced digits in per-modulus planes.  B's table carries the
-//                 CRT weight w_i = (Mod/p_i)^-1 mod p_i, and B's epilogue also
-//                 stores 256 * residue, so B has four planes per modulus.
-//  3. product   : for each modulus, two accumulators over a K of 2k (A's high
-//                 digits against B's 256-scaled digits, then A's low digits
-//                 against B's plain digits); y_i = 256 * D_hi + D_lo mod p_i,
-//                 stored balanced as two digits in per-modulus planes.
+//                 CRT weight w_i = (Mod/p_i)^-1 mod p_i.
+//  3. product   : for each modulus, A's two digit planes against B's two
+//                 (pre-weighted) digit planes in four accumulators;
+//                 y_i = 65536 a1 u1 + 256 (a1 u0 + a0 u1) + a0 u0 mod p_i, stored
+//                 balanced as two digits in per-modulus planes.
 //  4. reconstruct: [entries x 2P] x [2P x (32 + Dout)] GEMM against the digits
 //                 of Mod/p_i (and 256*Mod/p_i) plus fixed-point digits of
 //                 2^96/p_i; the epilogue gets q = round(sum y_i / p_i) and the
@@ -54,7 +53,7 @@ constexpr int SUSED = 14;       // of which the fixed-point sum uses the first 1
 constexpr int FIXB = 96;        // fixed-point bits of the 1/p_i weights
 constexpr int CTA_THREADS = 192;   // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
 constexpr int CTA_THREADS8 = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue (two per lane quadrant)
-constexpr int RBN = 128;           // reconstruction N tile (output digit columns)
+constexpr int RTAB = 256;          // reconstruction table rows are padded to a multiple of this
 }  // namespace
 
 struct ModConst {
@@ -223,9 +222,8 @@ struct ResidueArgs {
     int32_t ncols;            // 2P table columns
     int32_t n_ntiles;
     int64_t ntiles;
-    int32_t scaled;           // B operand: table holds w_i 256^j; also emit 256 * residue
     const ModConst *mods;
-    __nv_bfloat16 *R;  // planes [2P or 4P][rowsR][kp]
+    __nv_bfloat16 *R;  // planes [2P][rowsR][kp]
     int64_t plane;     // rowsR * kp
     int32_t kp;
 };
@@ -301,7 +299,6 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         const int quad = warp & 3, half = (warp - 2) >> 2;
         const int hcols = a.BN / 2;
         const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
-        const int npl = a.scaled ? 4 : 2;
         int lt = 0;
         for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, lt++) {
             const int b = lt & 1;
@@ -316,7 +313,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                 sgn = a.sizes[a.transpose ? c * a.rs + r : r * a.rs + c] < 0 ? -1.f : 1.f;
                 off = r * a.kp + c;
             }
-            const int64_t pstep = (int64_t)npl * a.plane;  // planes of one modulus
+            const int64_t pstep = 2 * a.plane;  // planes of one modulus
             for (int c0 = half * hcols; c0 < (half + 1) * hcols; c0 += 32) {
                 float res[16];
 #pragma unroll
@@ -356,12 +353,6 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                         bal_split(r, hi, lo);
                         dst[0] = (uint16_t)(__float_as_uint(hi) >> 16);
                         dst[a.plane] = (uint16_t)(__float_as_uint(lo) >> 16);
-                        if (a.scaled) {
-                            const float2 pc = smod[mi0 + j];
-                            bal_split(red(256.f * r, pc.x, pc.y), hi, lo);
-                            dst[2 * a.plane] = (uint16_t)(__float_as_uint(hi) >> 16);
-                            dst[3 * a.plane] = (uint16_t)(__float_as_uint(lo) >> 16);
-                        }
                     }
                 }
             }
@@ -371,17 +362,17 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 }
 
 // ======================================================================================
-// 3. per-modulus product GEMM (persistent over (modulus, 128 x 128 output tiles);
+// 3. per-modulus product GEMM (persistent over (modulus, 128 x 64 output tiles);
 //    TMEM double-buffered; 8 epilogue warps)
 //
-// With a = a1*256 + a0 (residues of A, balanced digits) and the B residues
-// pre-multiplied by the CRT weight w = (Mod/p)^-1 mod p in two forms,
-// u = w*b and v = 256*w*b (mod p, balanced digits u1*256+u0, v1*256+v0), the
-// weighted product is
-//     y = a*b*w = 256*(a1*v1 + a0*u1) + (a1*v0 + a0*u0)   (mod p),
-// i.e. two accumulators over a K of 2k: the first k steps pair A1 with
-// [V1 | V0], the next k steps A0 with [U1 | U0].  Each accumulator sums 2k
-// products of magnitude <= 2^14, exact for k <= 512.
+// With a = 256 a1 + a0 (residues of A as balanced digits) and u = 256 u1 + u0
+// (residues of B, already multiplied by the CRT weight w = (Mod/p)^-1 mod p),
+// the weighted product is
+//     y = a b w = 65536 a1 u1 + 256 (a1 u0 + a0 u1) + a0 u0   (mod p).
+// Each K step issues two N = 128 MMAs against the stacked operand [U1; U0]:
+// A1 into [a1 u1 | a1 u0] and A0 into [a0 u1 | a0 u0].  Each of the four 64-column
+// accumulators sums k products of magnitude <= 2^14: at most 2^23 for k <= 512,
+// and the middle pair adds to at most 2^24.
 // ======================================================================================
 struct ProductArgs {
     int32_t m, n, nk, P;
@@ -391,8 +382,7 @@ struct ProductArgs {
     __nv_bfloat16 *Y;  // blocked [Ep/64][2Pp][64]: 64 entries per row, 2Pp rows per block
     int64_t yblk;      // elements per 64-entry block (2Pp * 64)
 };
-constexpr int PBX = 128;  // output columns per product tile
-
+constexpr int PBX = 64;  // output columns per product tile
 
 template <int STAGES>
 __global__ void __launch_bounds__(CTA_THREADS8, 1)
@@ -400,7 +390,8 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                   uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
-    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = PBX * 128, STAGE = A_BYTES + 2 * B_BYTES;
+    // A1, A0 (128 rows each), then U1, U0 (64 rows each) = one 128-row B operand
+    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = PBX * 128, STAGE = 2 * A_BYTES + 2 * B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     cta_setup(bars, STAGES, 512, 1, 8);
@@ -415,27 +406,23 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             for (int64_t t = blockIdx.x; t < a.ntiles && !aborted(bars); t += gridDim.x) {
                 const int mi = (int)(t / per_mod), r = (int)(t % per_mod);
                 const int y0 = (r / a.nxt) * BM, x0 = (r % a.nxt) * PBX;
-                for (int s = 0; s < 2 * a.nk; s++, it++) {
+                for (int s = 0; s < a.nk; s++, it++) {
                     const int st = it % STAGES;
                     if (it >= STAGES && !tc::mbar_wait(&bars->empty[st], ((it / STAGES) & 1) ^ 1)) {
                         set_abort(bars, err);
                         break;
                     }
-                    const int second = s >= a.nk, ks = (second ? s - a.nk : s) * BK;
                     uint8_t *sa = base + st * STAGE;
                     tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                    // A1 (plane 2i) with V = 256wb (planes 4i+2, 4i+3), then A0 (plane 2i+1) with U = wb (4i, 4i+1)
-                    tc::tma_load_2d(sa, &tmA, &bars->full[st], ks, (2 * mi + second) * a.m + y0);
-                    const int bp = 4 * mi + (second ? 0 : 2);
-                    tc::tma_load_2d(sa + A_BYTES, &tmB, &bars->full[st], ks, bp * a.n + x0);
-                    tc::tma_load_2d(sa + A_BYTES + B_BYTES, &tmB, &bars->full[st], ks, (bp + 1) * a.n + x0);
+                    tc::tma_load_2d(sa, &tmA, &bars->full[st], s * BK, (2 * mi) * a.m + y0);
+                    tc::tma_load_2d(sa + A_BYTES, &tmA, &bars->full[st], s * BK, (2 * mi + 1) * a.m + y0);
+                    tc::tma_load_2d(sa + 2 * A_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi) * a.n + x0);
+                    tc::tma_load_2d(sa + 2 * A_BYTES + B_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi + 1) * a.n + x0);
                 }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            // [B hi | B lo] is one 256-row operand: columns [0,128) accumulate the
-            // x256 sum, [128,256) the x1 sum
             const uint32_t idesc = tc::idesc_bf16_f32(BM, 2 * PBX, 0, 0);
             int it = 0, lt = 0;
             bool ok = true;
@@ -444,21 +431,25 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                 if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
                 tc::fence_after_sync();
                 const uint32_t d = tmem + 256u * b;
-                for (int s = 0; s < 2 * a.nk; s++, it++) {
+                for (int s = 0; s < a.nk; s++, it++) {
                     const int st = it % STAGES;
                     if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
                     tc::fence_after_sync();
-                    const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
+                    const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + 2 * A_BYTES;
 #pragma unroll
-                    for (int kk = 0; kk < BK / UK; kk++)
-                        tc::mma_bf16(d, tc::sdesc_kmajor(sa + kk * 32), tc::sdesc_kmajor(sb + kk * 32), idesc,
+                    for (int kk = 0; kk < BK / UK; kk++) {
+                        const uint64_t bdesc = tc::sdesc_kmajor(sb + kk * 32);
+                        tc::mma_bf16(d, tc::sdesc_kmajor(sa + kk * 32), bdesc, idesc, s != 0 || kk != 0);
+                        tc::mma_bf16(d + 2 * PBX, tc::sdesc_kmajor(sa + A_BYTES + kk * 32), bdesc, idesc,
                                      s != 0 || kk != 0);
+                    }
                     tc::mma_commit(&bars->empty[st]);
                 }
                 if (ok) tc::mma_commit(&bars->tfull[b]);
             }
         }
     } else {
+        // warp (2..9) -> lane quadrant warp % 4, output columns 32 * ((warp - 2) / 4) + [0, 32)
         const int quad = warp & 3, half = (warp - 2) >> 2;
         const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
         int lt = 0;
@@ -466,20 +457,22 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             const int b = lt & 1;
             const int mi = (int)(t / per_mod), r = (int)(t % per_mod);
             const int y = (r / a.nxt) * BM + quad * 32 + lane;
-            const int xh = (r % a.nxt) * PBX + half * 64;  // this warp's 64 output columns
+            const int xh = (r % a.nxt) * PBX + half * 32;  // this warp's 32 output columns
             if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); break; }
             tc::fence_after_sync();
             const ModConst mc = a.mods[mi];
             const float pf = (float)mc.p;
             const int64_t erow = (int64_t)y * a.n + xh;  // entry index of this warp's first column
             __nv_bfloat16 *yplane = a.Y + (int64_t)(2 * mi) * 64;  // hi plane; lo plane 64 elements on
-            for (int c = 0; c < 64; c += 16) {
-                uint32_t dh[16], dl[16];
-                const uint32_t col = 256u * b + half * 64 + c;
-                tc::tmem_ld16(lb + col, dh);
-                tc::tmem_ld16(lb + col + PBX, dl);
+            for (int c = 0; c < 32; c += 16) {
+                uint32_t d11[16], d10[16], d01[16], d00[16];
+                const uint32_t col = 256u * b + half * 32 + c;
+                tc::tmem_ld16(lb + col, d11);
+                tc::tmem_ld16(lb + col + PBX, d10);
+                tc::tmem_ld16(lb + col + 2 * PBX, d01);
+                tc::tmem_ld16(lb + col + 3 * PBX, d00);
                 tc::tmem_ld_wait();
-                if (c == 48) {
+                if (c == 16) {
                     tc::fence_before_sync();
                     __syncwarp();
                     if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
@@ -490,10 +483,12 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                     float h2[2], l2[2];
 #pragma unroll
                     for (int u = 0; u < 2; u++) {
-                        // |256 red(Dh) + red(Dl)| <= 257 * 32772 < 2^24
-                        const float rh = red(__uint_as_float(dh[j + u]), pf, mc.inv_p);
-                        const float rl = red(__uint_as_float(dl[j + u]), pf, mc.inv_p);
-                        bal_split(red(__fmaf_rn(256.f, rh, rl), pf, mc.inv_p), h2[u], l2[u]);
+                        // |a1 u0 + a0 u1| <= 2^24; each step below stays under 257 * 32772 < 2^24
+                        const float r2 = red(__uint_as_float(d11[j + u]), pf, mc.inv_p);
+                        const float r1 = red(__uint_as_float(d10[j + u]) + __uint_as_float(d01[j + u]), pf, mc.inv_p);
+                        const float r0 = red(__uint_as_float(d00[j + u]), pf, mc.inv_p);
+                        const float tt = red(__fmaf_rn(256.f, r2, r1), pf, mc.inv_p);
+                        bal_split(red(__fmaf_rn(256.f, tt, r0), pf, mc.inv_p), h2[u], l2[u]);
                     }
                     phi[j / 2] = bf16x2_bits(h2[0], h2[1]);
                     plo[j / 2] = bf16x2_bits(l2[0], l2[1]);
@@ -525,15 +520,18 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 }
 
 // ======================================================================================
-// 4. reconstruction GEMM (persistent over tiles of 256 entries; each K step
-//    multiplies two 128-entry subtiles by one tile of RBN table rows, so the
-//    table tile is fetched once per 256 entries; TMEM double-buffered across
-//    N tiles; 8 epilogue warps, each owning 32 entries.  Base-128 table digits
-//    keep one FP32 accumulation over all 2P rows exact: 2P * 128 * 64 < 2^24.)
+// 4. reconstruction GEMM (persistent over tiles of SUBS x 128 entries; each K step
+//    multiplies the SUBS 128-entry subtiles by one tile of 256 / SUBS table
+//    rows, so every MMA has N = 256 / SUBS; TMEM double-buffered across N tiles;
+//    4 * SUBS epilogue warps, each owning 32 entries.  Base-128 table digits keep
+//    one FP32 accumulation over all 2P rows exact: 2P * 128 * 64 < 2^24.)
 //    Y arrives blocked, [E/64][2Pp][64], so each 64-entry x 64-row A box is one
 //    contiguous 8 KB run.
+//    SUBS = 1 issues one N = 256 MMA per K slice: 12 KB of shared-memory
+//    operand reads per 2^20 FLOP against 16 KB for two N = 128 MMAs (SUBS = 2),
+//    which is what bounds the MMA rate of a single-SM tcgen05 tile.
 // ======================================================================================
-constexpr int RME = 2 * BM;  // entries per reconstruction tile
+constexpr int REC_SUBS = 1;
 struct ReconArgs {
     int64_t E;       // entries of C
     int32_t ncols;   // columns of C (entry e -> row e / ncols, col e % ncols)
@@ -549,19 +547,20 @@ struct ReconArgs {
     int32_t cnlimbs;
 };
 
-template <int STAGES>
-__global__ void __launch_bounds__(CTA_THREADS8, 1)
+template <int STAGES, int SUBS>
+__global__ void __launch_bounds__(64 + 128 * SUBS, 1)
     k_crt_recon(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmT, ReconArgs a,
                 uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
+    constexpr int RME = SUBS * BM, RBN = 256 / SUBS;  // entries per tile, table rows per N tile
     constexpr uint32_t BOX = 64 * 128;  // one 64-entry x 64-row A box
     constexpr uint32_t A_BYTES = RME * 128, B_BYTES = RBN * 128, STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
     int8_t *smdig = reinterpret_cast<int8_t *>(bars) + SMEM_BARS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int i = threadIdx.x; i < a.Dout + 32; i += blockDim.x) smdig[i] = i < a.Dout ? a.mdig[i] : 0;
-    cta_setup(bars, STAGES, 512, 1, 8);
+    cta_setup(bars, STAGES, 512, 1, 4 * SUBS);
     const uint32_t tmem = bars->tmem_base;
 
     if (warp == 0) {
@@ -614,7 +613,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                         for (int kk = 0; kk < BK / UK; kk++) {
                             const uint64_t bdesc = tc::sdesc_kmajor(sb + kk * 32);
 #pragma unroll
-                            for (int sub = 0; sub < 2; sub++)
+                            for (int sub = 0; sub < SUBS; sub++)
                                 tc::mma_bf16(d + sub * RBN, tc::sdesc_mnmajor(sa + sub * 2 * BOX + kk * 2048, BOX),
                                              bdesc, idesc, s != 0 || kk != 0);
                         }
@@ -625,7 +624,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             }
         }
     } else {
-        // warp (2..9) -> TMEM lane quadrant warp % 4 of subtile (warp - 2) / 4
+        // warp (2 .. 1 + 4 SUBS) -> TMEM lane quadrant warp % 4 of subtile (warp - 2) / 4
         const int quad = warp & 3, sub = (warp - 2) >> 2;
         const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(sub * RBN);
         int lt = 0;
@@ -945,9 +944,9 @@ struct crt_tables {
     int P = 0, Pp = 0;   // moduli, padded 2P/2 (2Pp multiple of 64)
     int Dout = 0, NT = 0;
     ModConst *d_mods = nullptr;
-    __nv_bfloat16 *d_recon = nullptr;  // [NT * RBN][2Pp]
+    __nv_bfloat16 *d_recon = nullptr;  // [NT * RTAB][2Pp]
     int8_t *d_mdig = nullptr;          // [Dout]
-    std::map<int, __nv_bfloat16 *> residue;  // 2 * dxp + scaled -> [2P rows][dxp]
+    std::map<int, __nv_bfloat16 *> residue;  // 2 * dxp + weighted -> [2P rows][dxp]
     std::vector<ModConst> h_mods;
 };
 
@@ -986,8 +985,8 @@ static gbmm_status build_tables(crt_tables *t, int P) {
     for (int i = 0; i < P; i++) big_mul_small(Mod, pr[i]);
     int modbits = (int)(32 * Mod.size());
     t->Dout = (modbits + 6) / 7 + 2;  // base-128 output digits
-    t->NT = (SROWS + t->Dout + RBN - 1) / RBN;
-    const int rows = t->NT * RBN, cols = 2 * t->Pp;
+    t->NT = (SROWS + t->Dout + RTAB - 1) / RTAB;  // in units of RTAB rows
+    const int rows = t->NT * RTAB, cols = 2 * t->Pp;
     std::vector<uint16_t> tab((size_t)rows * cols, bf16_bits(0.f));
     t->h_mods.resize(P);
     for (int i = 0; i < P; i++) {
@@ -1039,10 +1038,10 @@ static gbmm_status build_tables(crt_tables *t, int P) {
 }
 
 // Residue table [2P rows][dxp]: rows 2i / 2i+1 hold the low / high balanced
-// byte of 256^j mod p_i (scaled = 0) or of w_i 256^j mod p_i (scaled = 1, the
+// byte of 256^j mod p_i (weighted = 0) or of w_i 256^j mod p_i (weighted = 1, the
 // CRT weight w_i = (Mod/p_i)^-1 mod p_i folded into the B operand).
-static gbmm_status residue_table(crt_tables *t, int dxp, int scaled, __nv_bfloat16 **out) {
-    const int key = 2 * dxp + scaled;
+static gbmm_status residue_table(crt_tables *t, int dxp, int weighted, __nv_bfloat16 **out) {
+    const int key = 2 * dxp + weighted;
     auto it = t->residue.find(key);
     if (it != t->residue.end()) { *out = it->second; return GBMM_OK; }
     const auto &pr = primes_desc();
@@ -1050,7 +1049,7 @@ static gbmm_status residue_table(crt_tables *t, int dxp, int scaled, __nv_bfloat
     std::vector<uint16_t> tab((size_t)rows * dxp);
     for (int i = 0; i < t->P; i++) {
         const uint32_t p = pr[i];
-        uint32_t v = scaled ? t->h_mods[i].w : 1u;  // (w) 256^j mod p
+        uint32_t v = weighted ? t->h_mods[i].w : 1u;  // (w) 256^j mod p
         for (int j = 0; j < dxp; j++) {
             int32_t b = v > p / 2 ? (int32_t)v - (int32_t)p : (int32_t)v;
             int32_t d0 = ((b + 128) & 255) - 128;
@@ -1102,9 +1101,9 @@ static gbmm_status set_smem(const void *fn, size_t bytes) {
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // digits + residues of one operand into planes [2P][rowsR][kp] (A: a1, a0 per
-// modulus) or, scaled, [4P][rowsR][kp] (B: u1, u0, v1, v0 with u = w b, v = 256 w b)
+// modulus); B's table is weighted, so B's planes hold u = w b (u1, u0)
 static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat &X, int transpose, int rowsR, int kdim,
-                                    int kp, int scaled, __nv_bfloat16 *R, cudaStream_t s) {
+                                    int kp, int weighted, __nv_bfloat16 *R, cudaStream_t s) {
     const int L = std::max(X.nlimbs, 1);
     const int dxp = (4 * L + 63) / 64 * 64;
     const int64_t E = (int64_t)X.rows * X.cols;
@@ -1120,7 +1119,7 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     __nv_bfloat16 *T = nullptr;
-    GBMM_TRY(residue_table(t, dxp, scaled, &T));
+    GBMM_TRY(residue_table(t, dxp, weighted, &T));
     const int nk = dxp / BK;
     const int G = (nk + GROUP_STEPS - 1) / GROUP_STEPS;
     int BN = 256;
@@ -1132,7 +1131,7 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     ResidueArgs a;
     a.sizes = X.sizes; a.rs = X.rs; a.transpose = transpose; a.kdim = kdim; a.E = E; a.nk = nk;
     a.BN = BN; a.G = G; a.P = t->P; a.mods = t->d_mods; a.R = R; a.plane = (int64_t)rowsR * kp; a.kp = kp;
-    a.ncols = 2 * t->P; a.scaled = scaled;
+    a.ncols = 2 * t->P;
     a.n_ntiles = (2 * t->P + BN - 1) / BN;
     a.ntiles = (int64_t)a.n_ntiles * ((E + BM - 1) / BM);
     const size_t sm = smem_bytes(RES_STAGES, BM * 128 + (size_t)BN * 128) + (size_t)(t->P + 15) / 16 * 16 * 8;
@@ -1160,7 +1159,7 @@ static size_t crt_workspace(const gbmm_mat &a, const gbmm_mat &b, const gbmm_mat
     const int kp = (k + 63) / 64 * 64;
     const int64_t Ep = ((int64_t)m * n + 63) / 64 * 64;
     const int dxa = (4 * std::max(a.nlimbs, 1) + 63) / 64 * 64, dxb = (4 * std::max(b.nlimbs, 1) + 63) / 64 * 64;
-    return align256((size_t)2 * P * m * kp * 2) + align256((size_t)4 * P * n * kp * 2) + align256((size_t)2 * Pp * Ep * 2) +
+    return align256((size_t)2 * P * m * kp * 2) + align256((size_t)2 * P * n * kp * 2) + align256((size_t)2 * Pp * Ep * 2) +
            std::max(align256((size_t)m * k * dxa * 2 + 1024), align256((size_t)k * n * dxb * 2 + 1024)) + 8192;
 }
 
@@ -1227,12 +1226,12 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     GBMM_TRY(arena_reserve(h, crt_workspace(a, b, c, bits_a, bits_b, P)));
     size_t mark = arena_mark(h);
     __nv_bfloat16 *RA = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * P * m * kp * 2);
-    __nv_bfloat16 *RB = (__nv_bfloat16 *)arena_alloc(h, (size_t)4 * P * n * kp * 2);
+    __nv_bfloat16 *RB = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * P * n * kp * 2);
     __nv_bfloat16 *Y = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * t->Pp * Ep * 2);
     if (!RA || !RB || !Y) return set_error(GBMM_ERR_NOMEM, "crt: workspace");
     if (kp != k) {
         GBMM_CUDA_TRY(cudaMemsetAsync(RA, 0, (size_t)2 * P * m * kp * 2, s));
-        GBMM_CUDA_TRY(cudaMemsetAsync(RB, 0, (size_t)4 * P * n * kp * 2, s));
+        GBMM_CUDA_TRY(cudaMemsetAsync(RB, 0, (size_t)2 * P * n * kp * 2, s));
     }
     // Y is blocked [Ep/64][2Pp][64]; the padding rows 2P..2Pp-1 of every block meet
     // zero table columns but must not hold NaN patterns, so they are cleared.  Padding
@@ -1251,13 +1250,13 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     {
         CUtensorMap tmA, tmB;
         GBMM_TRY(make_map(&tmA, RA, kp, (uint64_t)2 * P * m, kp, BK, BM));
-        GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)4 * P * n, kp, BK, PBX));
+        GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)2 * P * n, kp, BK, PBX));
         ProductArgs pa;
         pa.m = m; pa.n = n; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.yblk = (int64_t)2 * t->Pp * 64;
         pa.nyt = (m + BM - 1) / BM;
         pa.nxt = (n + PBX - 1) / PBX;
         pa.ntiles = (int64_t)P * pa.nyt * pa.nxt;
-        const size_t sm = smem_bytes(PROD_STAGES, BM * 128 + 2 * PBX * 128);
+        const size_t sm = smem_bytes(PROD_STAGES, 2 * BM * 128 + 2 * PBX * 128);
         GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES>, sm));
         dim3 grid((unsigned)std::min<int64_t>(pa.ntiles, num_sms()));
         LaunchScope ls_("k_crt_product", s);
@@ -1267,16 +1266,17 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     {
         CUtensorMap tmY, tmT;
         GBMM_TRY(make_map(&tmY, Y, 64, (uint64_t)(Ep / 64) * 2 * t->Pp, 64, 64, BK));
-        GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RBN, 2 * t->Pp, BK, RBN));
+        constexpr int RME = REC_SUBS * BM, RBN = 256 / REC_SUBS;
+        GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RTAB, 2 * t->Pp, BK, RBN));
         ReconArgs ra;
-        ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.NT = t->NT; ra.Dout = t->Dout;
+        ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.NT = (SROWS + t->Dout + RBN - 1) / RBN; ra.Dout = t->Dout;
         ra.mdig = t->d_mdig; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
         ra.cnlimbs = c.nlimbs; ra.kpad = 2 * t->Pp; ra.nmt = (E + RME - 1) / RME;
         const size_t sm = smem_bytes(REC_STAGES, RME * 128 + RBN * 128) + t->Dout + 64;
-        GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES>, sm));
+        GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES, REC_SUBS>, sm));
         dim3 grid((unsigned)std::min<int64_t>(ra.nmt, num_sms()));
         LaunchScope ls_("k_crt_recon", s);
-        k_crt_recon<REC_STAGES><<<grid, CTA_THREADS8, sm, s>>>(tmY, tmT, ra, err);
+        k_crt_recon<REC_STAGES, REC_SUBS><<<grid, 64 + 128 * REC_SUBS, sm, s>>>(tmY, tmT, ra, err);
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     arena_release(h, mark);
