@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
                      "--expt-relaxed-constexpr", "-I" + os.path.join(HERE, "..", "include")]
 
-LIB_SOURCES = ["host.cpp", "limb.cu", "crt.cu", "batch.cpp", "mlp.cu"]
+LIB_SOURCES = ["host.cpp", "limb.cu", "crt.cu", "batch.cpp", "mlp.cu", "pipeline.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 
 

@@ -150,10 +150,13 @@ struct gbmm_handle_s {
     int use_model = 0;
     // batched-execution state: tuning table, graph cache, staging (batch.cpp)
     void *batch = nullptr;
+    // host-buffer pipeline: copy streams, two device slots (pipeline.cpp)
+    void *pipe = nullptr;
 };
 
 namespace gbmm {
 gbmm_status arena_reserve(gbmm_handle h, size_t bytes);
+void pipe_destroy(gbmm_handle h);
 void *arena_alloc(gbmm_handle h, size_t bytes);  // nullptr when the reservation is too small
 static inline size_t arena_mark(gbmm_handle h) { return h->ws.top; }
 static inline void arena_release(gbmm_handle h, size_t mark) { h->ws.top = mark; }

@@ -212,6 +212,7 @@ extern "C" gbmm_status gbmm_create(gbmm_handle *out) {
 extern "C" gbmm_status gbmm_destroy(gbmm_handle h) {
     if (!h) return GBMM_OK;
     cudaStreamSynchronize(h->stream);
+    pipe_destroy(h);
     batch_state_destroy(h);
     model_destroy(h);
     if (h->ws.base) cudaFree(h->ws.base);
@@ -360,6 +361,21 @@ static gbmm_status copy_planes(gbmm_mat m, uint32_t *hl, int32_t *hs, int32_t hn
     if (!hl || !hs) return set_error(GBMM_ERR_INVALID, "null host pointer");
     if (hld < (int64_t)m.rows * m.cols) return set_error(GBMM_ERR_INVALID, "host plane stride too small");
     const cudaMemcpyKind kind = up ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    const int64_t E = (int64_t)m.rows * m.cols;
+    if (m.rs == m.cols && m.ld == E && hld == E) {
+        // dense planes on both sides: one copy for the sizes and one for all shared planes
+        const int np = std::min(hn, m.nlimbs);
+        GBMM_CUDA_TRY(cudaMemcpyAsync(up ? (void *)m.sizes : (void *)hs, up ? (const void *)hs : (const void *)m.sizes,
+                                      (size_t)E * 4, kind, s));
+        if (np > 0)
+            GBMM_CUDA_TRY(cudaMemcpyAsync(up ? (void *)m.limbs : (void *)hl, up ? (const void *)hl : (const void *)m.limbs,
+                                          (size_t)np * E * 4, kind, s));
+        if (up && m.nlimbs > np)
+            GBMM_CUDA_TRY(cudaMemsetAsync(m.limbs + (int64_t)np * E, 0, (size_t)(m.nlimbs - np) * E * 4, s));
+        if (!up && hn > np) memset(hl + (int64_t)np * hld, 0, (size_t)(hn - np) * E * 4);
+        GBMM_CUDA_TRY(cudaStreamSynchronize(s));
+        return GBMM_OK;
+    }
     // sizes: rows with stride rs on the device, contiguous on the host
     GBMM_CUDA_TRY(cudaMemcpy2DAsync(up ? (void *)m.sizes : (void *)hs, (up ? m.rs : m.cols) * 4,
                                     up ? (const void *)hs : (const void *)m.sizes, (up ? m.cols : m.rs) * 4,

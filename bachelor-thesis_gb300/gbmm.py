@@ -47,6 +47,16 @@ class Job(ctypes.Structure):
                 ("nprimes", ctypes.c_int32), ("chosen_path", ctypes.c_int32)]
 
 
+class HostJob(ctypes.Structure):
+    _fields_ = [("K", ctypes.c_int32), ("M", ctypes.c_int32), ("N", ctypes.c_int32),
+                ("a_nlimbs", ctypes.c_int32), ("b_nlimbs", ctypes.c_int32), ("c_nlimbs", ctypes.c_int32),
+                ("a_limbs", ctypes.c_void_p), ("a_sizes", ctypes.c_void_p),
+                ("b_limbs", ctypes.c_void_p), ("b_sizes", ctypes.c_void_p),
+                ("c_limbs", ctypes.c_void_p), ("c_sizes", ctypes.c_void_p),
+                ("path", ctypes.c_int32), ("method", ctypes.c_int32), ("cutoff", ctypes.c_int32),
+                ("nprimes", ctypes.c_int32), ("chosen_path", ctypes.c_int32)]
+
+
 _lib = None
 
 _P = ctypes.c_void_p
@@ -73,6 +83,7 @@ _SIGS = {
     "gbmm_mat_mul_naive": [Mat, Mat, Mat, ctypes.c_int32, _P],
     "gbmm_matmul_batched": [_P, ctypes.POINTER(Job), ctypes.c_int32, ctypes.POINTER(Opts)],
     "gbmm_set_graphs": [_P, ctypes.c_int32],
+    "gbmm_matmul_host": [_P, ctypes.POINTER(HostJob), ctypes.c_int32],
     "gbmm_autotune": [_P, ctypes.POINTER(Job), ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p],
     "gbmm_tune_save": [_P, ctypes.c_char_p],
     "gbmm_tune_load": [_P, ctypes.c_char_p],
@@ -337,6 +348,32 @@ class Handle:
         self.bind_stream()
         o = Opts(path, METHOD_WINOGRAD, 0, 0, 0)
         check(lib().gbmm_matmul_batched(self.h, jobs, len(jobs), ctypes.byref(o)))
+        return [jobs[i].chosen_path for i in range(len(jobs))]
+
+    @staticmethod
+    def host_jobs(specs, path=PATH_AUTO, method=0, cutoff=0):
+        """[(K, M, N, (Al, As), (Bl, Bs), (Cl, Cs)), ...] with numpy planes (limbs
+        [nlimbs, rows*cols] uint32, sizes [rows*cols] int32; C's are filled in) ->
+        ctypes array of gbmm_host_job.  The arrays must stay alive during the call."""
+        arr = (HostJob * len(specs))()
+        for i, (K, M, N, (Al, As), (Bl, Bs), (Cl, Cs)) in enumerate(specs):
+            for a in (Al, As, Bl, Bs, Cl, Cs):
+                if not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError("host planes must be contiguous")
+            q = arr[i]
+            q.K, q.M, q.N = K, M, N
+            q.a_nlimbs, q.b_nlimbs, q.c_nlimbs = Al.shape[0], Bl.shape[0], Cl.shape[0]
+            q.a_limbs, q.a_sizes = Al.ctypes.data, As.ctypes.data
+            q.b_limbs, q.b_sizes = Bl.ctypes.data, Bs.ctypes.data
+            q.c_limbs, q.c_sizes = Cl.ctypes.data, Cs.ctypes.data
+            q.path, q.method, q.cutoff = path, method, cutoff
+        return arr
+
+    def matmul_host(self, jobs):
+        """Runs a ctypes array of gbmm_host_job (pipelined host <-> device copies);
+        returns the paths the dispatcher chose."""
+        self.bind_stream()
+        check(lib().gbmm_matmul_host(self.h, jobs, len(jobs)))
         return [jobs[i].chosen_path for i in range(len(jobs))]
 
     # ---- learned cost model ----

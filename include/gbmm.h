@@ -193,6 +193,33 @@ typedef struct gbmm_job {
  * and replayed on later calls with the same job signature.
  * replaces: the unused chunked-stream job DAG (mat-gpu/job.cu:32-338). */
 gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_t njobs, const gbmm_opts *opts);
+/* One product on host buffers: dense limb planes (limb i of entry e at
+ * [i * rows * cols + e]) and a sizes plane per matrix, C = A * B with C K x N,
+ * A K x M, B M x N.  Pinned host memory lets the copies overlap compute. */
+typedef struct gbmm_host_job {
+    int32_t K, M, N;
+    int32_t a_nlimbs, b_nlimbs, c_nlimbs;
+    const uint32_t *a_limbs;
+    const int32_t *a_sizes;
+    const uint32_t *b_limbs;
+    const int32_t *b_sizes;
+    uint32_t *c_limbs;
+    int32_t *c_sizes;
+    int32_t path;        /* gbmm_path; AUTO lets the dispatcher choose */
+    int32_t method;      /* gbmm_method for the limb path, 0 = Winograd */
+    int32_t cutoff;      /* Winograd cutoff, 0 = default */
+    int32_t nprimes;     /* CRT moduli, 0 = derived from the bit lengths */
+    int32_t chosen_path; /* out: path the dispatcher used */
+} gbmm_host_job;
+
+/* Runs a list of products whose operands and results live in host memory and
+ * returns when every C is back in host memory.  Two device slots and separate
+ * upload / download streams let job j+1's host->device copies and job j-1's
+ * device->host copy overlap job j's compute.
+ * replaces: the blocking host <-> device transfers around each product
+ * (mat-gpu/mat-pregpu.cu:10-96, transfer_recurse; mat-gpu/main.cu:362-381). */
+gbmm_status gbmm_matmul_host(gbmm_handle h, gbmm_host_job *jobs, int32_t njobs);
+
 /* Turns CUDA-graph capture and replay of batches on (default) or off.
  * No counterpart in the reference. */
 gbmm_status gbmm_set_graphs(gbmm_handle h, int32_t enable);
