@@ -33,6 +33,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <utility>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -520,47 +521,94 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 }
 
 // ======================================================================================
-// 4. reconstruction GEMM (persistent over tiles of SUBS x 128 entries; each K step
-//    multiplies the SUBS 128-entry subtiles by one tile of 256 / SUBS table
-//    rows, so every MMA has N = 256 / SUBS; TMEM double-buffered across N tiles;
-//    4 * SUBS epilogue warps, each owning 32 entries.  Base-128 table digits keep
-//    one FP32 accumulation over all 2P rows exact: 2P * 128 * 64 < 2^24.)
+// 4. reconstruction GEMM (persistent over tiles of 128 entries, or 256 entries
+//    for a CTA pair; N tiles of 256 table rows; TMEM double-buffered across N
+//    tiles; 8 epilogue warps per CTA, two per entry splitting the columns.  Base-128 table
+//    digits keep one FP32 accumulation over all 2P rows exact:
+//    2P * 128 * 64 < 2^24.)
 //    Y arrives blocked, [E/64][2Pp][64], so each 64-entry x 64-row A box is one
 //    contiguous 8 KB run.
-//    SUBS = 1 issues one N = 256 MMA per K slice: 12 KB of shared-memory
-//    operand reads per 2^20 FLOP against 16 KB for two N = 128 MMAs (SUBS = 2),
-//    which is what bounds the MMA rate of a single-SM tcgen05 tile.
+//    PAIR: a cluster of two CTAs on two SMs runs one M = 256, N = 256
+//    tcgen05.mma.cta_group::2 per K slice.  Each CTA stages its own 128 entries
+//    and its own 128 of the 256 table rows, so per SM the K step moves 32 KB
+//    through TMA and the MMA reads 8 KB of shared memory per 2^20 FLOP, against
+//    48 KB and 12 KB for one CTA with N = 256: shared-memory bandwidth, which
+//    bounds the single-SM tile, drops by a third.
 // ======================================================================================
-constexpr int REC_SUBS = 1;
 struct ReconArgs {
     int64_t E;       // entries of C
     int32_t ncols;   // columns of C (entry e -> row e / ncols, col e % ncols)
     int32_t nk;      // K steps over 2Pp
-    int32_t NT;      // N tiles of RBN table rows
+    int32_t NT;      // N tiles of 256 table rows
     int32_t Dout;    // output base-128 digit positions
     int32_t kpad;    // 2Pp: rows of one 64-entry block of Y
-    int64_t nmt;     // tiles of RME entries
-    const int8_t *mdig;  // balanced base-128 digits of Mod, Dout entries
+    int64_t nmt;     // entry tiles (128 entries, or 256 for a pair)
+    const uint32_t *vtab;  // per 32-digit chunk n: sum_u Mod_(32n+u) 128^u as 7 two's-complement words + sign word
     uint32_t *climbs;
     int32_t *csizes;
     int64_t cld, crs;
     int32_t cnlimbs;
 };
+constexpr bool REC_PAIR = true;
 
-template <int STAGES, int SUBS>
-__global__ void __launch_bounds__(64 + 128 * SUBS, 1)
+// Hand-off between the two epilogue warps of a TMEM lane quadrant (per entry slots).
+struct ReconXfer {
+    uint64_t to1[4], to0[4], qready[4];  // mbarriers per quadrant: half 0 -> 1, half 1 -> 0, q ready
+    long long carry1[128], carry0[128];  // carry handed to half 1 / to half 0
+    uint32_t ripple1[128], ripple0[128]; // negation ripple handed on
+    int32_t q[128], sgn[128], amb[128];  // fixed-point results of an entry's tile 0
+    int32_t top0[128];                   // half 0's highest nonzero limb + 1
+    uint32_t drop0[128];                 // half 0's dropped-limb flags (bit 0 nonzero, bit 1 all ones)
+};
+
+template <int STAGES, bool PAIR>
+__global__ void __launch_bounds__(CTA_THREADS8, 1)
     k_crt_recon(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmT, ReconArgs a,
                 uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
-    constexpr int RME = SUBS * BM, RBN = 256 / SUBS;  // entries per tile, table rows per N tile
-    constexpr uint32_t BOX = 64 * 128;  // one 64-entry x 64-row A box
-    constexpr uint32_t A_BYTES = RME * 128, B_BYTES = RBN * 128, STAGE = A_BYTES + B_BYTES;
+    constexpr int NP = PAIR ? 2 : 1;
+    constexpr int RBN = 256;                      // accumulator columns (table rows) per N tile
+    constexpr int TROWS = RBN / NP;               // table rows this CTA stages per N tile
+    constexpr uint32_t BOX = 64 * 128;            // one 64-entry x 64-row A box
+    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = TROWS * 128, STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
-    int8_t *smdig = reinterpret_cast<int8_t *>(bars) + SMEM_BARS;
+    uint32_t *svtab = reinterpret_cast<uint32_t *>(reinterpret_cast<uint8_t *>(bars) + SMEM_BARS);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = threadIdx.x; i < a.Dout + 32; i += blockDim.x) smdig[i] = i < a.Dout ? a.mdig[i] : 0;
-    cta_setup(bars, STAGES, 512, 1, 4 * SUBS);
+    const uint32_t rank = PAIR ? tc::cluster_rank() : 0;
+    const int64_t t0 = PAIR ? (blockIdx.x >> 1) : blockIdx.x, tstep = PAIR ? (gridDim.x >> 1) : gridDim.x;
+    for (int i = threadIdx.x; i < (a.Dout + 31) / 32 * 8; i += blockDim.x) svtab[i] = a.vtab[i];
+    ReconXfer *xf = reinterpret_cast<ReconXfer *>(reinterpret_cast<uint8_t *>(svtab) + (a.Dout + 31) / 32 * 32);
+    if (threadIdx.x == 0)
+        for (int qd = 0; qd < 4; qd++) {
+            tc::mbar_init(&xf->to1[qd], 1);
+            tc::mbar_init(&xf->to0[qd], 1);
+            tc::mbar_init(&xf->qready[qd], 1);
+        }
+    if (PAIR) {
+        if (threadIdx.x == 0) {
+            for (int s = 0; s < STAGES; s++) {
+                tc::mbar_init(&bars->full[s], 1);
+                tc::mbar_init(&bars->empty[s], 1);
+            }
+            for (int b = 0; b < 2; b++) {
+                tc::mbar_init(&bars->tfull[b], 1);
+                tc::mbar_init(&bars->tempty[b], 16);  // the even CTA's: 8 epilogue warps of each CTA
+            }
+            bars->abort_flag = 0;
+            tc::fence_mbar_init();
+        }
+        if (warp == 1) {
+            tc::tmem_alloc_pair(&bars->tmem_base, 512);
+            tc::tmem_relinquish_pair();
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::cluster_sync_all();  // both CTAs' barriers exist before any cross-CTA signal
+        tc::fence_after_sync();
+    } else {
+        cta_setup(bars, STAGES, 512, 1, 8);
+    }
     const uint32_t tmem = bars->tmem_base;
 
     if (warp == 0) {
@@ -568,8 +616,8 @@ __global__ void __launch_bounds__(64 + 128 * SUBS, 1)
             tc::prefetch_tmap(&tmY);
             tc::prefetch_tmap(&tmT);
             int it = 0;
-            for (int64_t t = blockIdx.x; t < a.nmt && !aborted(bars); t += gridDim.x) {
-                const int blk0 = (int)(t * (RME / 64));
+            for (int64_t t = t0; t < a.nmt && !aborted(bars); t += tstep) {
+                const int blk0 = (int)(t * (2 * NP) + 2 * rank);  // this CTA's two 64-entry blocks
                 for (int j = 0; j < a.NT && !aborted(bars); j++) {
                     for (int s = 0; s < a.nk; s++, it++) {
                         const int st = it % STAGES;
@@ -578,23 +626,30 @@ __global__ void __launch_bounds__(64 + 128 * SUBS, 1)
                             break;
                         }
                         uint8_t *sa = base + st * STAGE;
-                        tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                        // A (MN-major): four 64-entry blocks x 64 K-rows; blocks past the
-                        // end of Y read as zeros and still count their full box bytes
-#pragma unroll
-                        for (int q = 0; q < RME / 64; q++)
-                            tc::tma_load_2d(sa + q * BOX, &tmY, &bars->full[st], 0, (blk0 + q) * a.kpad + s * BK);
-                        tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, j * RBN);
+                        // A (MN-major): two 64-entry blocks x 64 K-rows; blocks past the end of
+                        // Y read as zeros and still count their full box bytes
+                        if (PAIR) {
+                            const uint32_t full0 = tc::mapa(tc::smem_u32(&bars->full[st]), 0);
+                            if (rank == 0) tc::mbar_arrive_expect_tx(&bars->full[st], 2 * STAGE);
+                            tc::tma_load_2d_pair(sa, &tmY, full0, 0, blk0 * a.kpad + s * BK);
+                            tc::tma_load_2d_pair(sa + BOX, &tmY, full0, 0, (blk0 + 1) * a.kpad + s * BK);
+                            tc::tma_load_2d_pair(sa + A_BYTES, &tmT, full0, s * BK, j * RBN + (int)rank * TROWS);
+                        } else {
+                            tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                            tc::tma_load_2d(sa, &tmY, &bars->full[st], 0, blk0 * a.kpad + s * BK);
+                            tc::tma_load_2d(sa + BOX, &tmY, &bars->full[st], 0, (blk0 + 1) * a.kpad + s * BK);
+                            tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, j * RBN);
+                        }
                     }
                 }
             }
         }
     } else if (warp == 1) {
-        if (lane == 0) {
-            const uint32_t idesc = tc::idesc_bf16_f32(BM, RBN, 1, 0);
+        if (lane == 0 && rank == 0) {
+            const uint32_t idesc = tc::idesc_bf16_f32(NP * BM, RBN, 1, 0);
             int it = 0, lt = 0;
             bool ok = true;
-            for (int64_t t = blockIdx.x; t < a.nmt && ok; t += gridDim.x) {
+            for (int64_t t = t0; t < a.nmt && ok; t += tstep) {
                 for (int j = 0; j < a.NT && ok; j++, lt++) {
                     const int b = lt & 1;
                     if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) {
@@ -611,109 +666,212 @@ __global__ void __launch_bounds__(64 + 128 * SUBS, 1)
                         const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
 #pragma unroll
                         for (int kk = 0; kk < BK / UK; kk++) {
-                            const uint64_t bdesc = tc::sdesc_kmajor(sb + kk * 32);
-#pragma unroll
-                            for (int sub = 0; sub < SUBS; sub++)
-                                tc::mma_bf16(d + sub * RBN, tc::sdesc_mnmajor(sa + sub * 2 * BOX + kk * 2048, BOX),
-                                             bdesc, idesc, s != 0 || kk != 0);
+                            const uint64_t adesc = tc::sdesc_mnmajor(sa + kk * 2048, BOX), bdesc = tc::sdesc_kmajor(sb + kk * 32);
+                            if (PAIR) tc::mma_bf16_pair(d, adesc, bdesc, idesc, s != 0 || kk != 0);
+                            else tc::mma_bf16(d, adesc, bdesc, idesc, s != 0 || kk != 0);
                         }
-                        tc::mma_commit(&bars->empty[st]);
+                        if (PAIR) tc::mma_commit_pair(&bars->empty[st], 0x3);
+                        else tc::mma_commit(&bars->empty[st]);
                     }
-                    if (ok) tc::mma_commit(&bars->tfull[b]);
+                    if (ok) {
+                        if (PAIR) tc::mma_commit_pair(&bars->tfull[b], 0x3);
+                        else tc::mma_commit(&bars->tfull[b]);
+                    }
                 }
             }
         }
     } else {
-        // warp (2 .. 1 + 4 SUBS) -> TMEM lane quadrant warp % 4 of subtile (warp - 2) / 4
-        const int quad = warp & 3, sub = (warp - 2) >> 2;
-        const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(sub * RBN);
-        int lt = 0;
-        for (int64_t t = blockIdx.x; t < a.nmt; t += gridDim.x) {
-            const int64_t e = t * RME + sub * BM + quad * 32 + lane;
+        // 8 epilogue warps.  quad = warp % 4 owns TMEM lanes (entries) quad * 32 .. + 31 and
+        // hf = (warp - 2) / 4 owns accumulator columns hf * 128 .. + 127 of every N tile.  An
+        // entry's digits run through its carry chain in the order (tile 0, half 0), (tile 0,
+        // half 1), (tile 1, half 0), ...  Each half reads its 128 columns at once (so the
+        // TMEM buffer goes back to the MMA immediately), turns them into up to 28 limbs
+        // starting from carry 0, then takes its predecessor's carry and negation ripple from
+        // shared memory, adds them, stores, and hands its own on.  Hand-offs are mbarriers
+        // with bounded waits; the exchange slots are per entry.
+        const int quad = warp & 3, hf = (warp - 2) >> 2, idx = quad * 32 + lane;
+        const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(hf * 128);
+        const uint32_t tempty0 = PAIR ? tc::mapa(tc::smem_u32(&bars->tempty[0]), 0) : 0;
+        int lt = 0, ph1 = 0, ph0 = 0, phq = 0;  // tiles seen; hand-off phases consumed
+        bool first = true, ok = true;
+        for (int64_t t = t0; t < a.nmt && ok; t += tstep) {
+            const int64_t e = t * (NP * BM) + rank * BM + quad * 32 + lane;
             const bool live = e < a.E;
             const int64_t coff = live ? (e / a.ncols) * a.crs + (e % a.ncols) : 0;
-            // C = sum_u (acc_u - q Mod_u) 128^u; sgn = -1 when C < 0 so that the digits
-            // produce |C|, qs = q * sgn
-            long long carry = 0;
-            int32_t q = 0, sgn = 1, qs = 0;
-            bool ambiguous = false, ok = true;
-            int pos = 0, top = 0;
+            // C = sum_u (acc_u - q Mod_u) 128^u; the limbs written are |C| (negated on the
+            // fly when the fixed-point sum says C < 0)
+            int32_t q = 0, sgn = 1, amb = 0;
+            int top = 0;
             bool drop_nz = false, drop_ones = true;
+            long long carry_final = 0;
+            uint32_t nc_final = 1;
+            const bool last_t = t + tstep >= a.nmt;
             for (int j = 0; j < a.NT; j++, lt++) {
                 const int b = lt & 1;
                 if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); ok = false; break; }
                 tc::fence_after_sync();
-                for (int c0 = 0; c0 < RBN; c0 += 64) {
-                    uint32_t g[64];
-                    tc::tmem_ld32(lb + (uint32_t)(256 * b + c0), *reinterpret_cast<uint32_t(*)[32]>(&g[0]));
-                    tc::tmem_ld32(lb + (uint32_t)(256 * b + c0 + 32), *reinterpret_cast<uint32_t(*)[32]>(&g[32]));
-                    tc::tmem_ld_wait();
-                    if (c0 + 64 >= RBN) {
+                // columns 0..63 of this half now, 64..127 after two chunks (then the buffer is released)
+                uint32_t g[64];
+                tc::tmem_ld32(lb + (uint32_t)(256 * b), *reinterpret_cast<uint32_t(*)[32]>(&g[0]));
+                tc::tmem_ld32(lb + (uint32_t)(256 * b + 32), *reinterpret_cast<uint32_t(*)[32]>(&g[32]));
+                tc::tmem_ld_wait();
+                if (j == 0) {
+                    if (hf == 0) {
+                        // fixed-point sum S = sum y_i 2^FIXB / p_i from the first SUSED columns
+                        // (base 128): S = (q + C / Mod) 2^FIXB + err, |err| <= 128 P < 2^17, and
+                        // |C / Mod| < 2^-18, so q = round(S / 2^FIXB) and the sign of
+                        // frac = S - q 2^FIXB is the sign of C unless |C| < Mod 2^(20 - FIXB)
+                        __int128 S = 0;
+#pragma unroll
+                        for (int u = SUSED - 1; u >= 0; u--) S = S * 128 + tc::acc_int(g[u]);
+                        const __int128 halfw = (__int128)1 << (FIXB - 1);
+                        const __int128 qq = (S + halfw) >> FIXB;
+                        const __int128 frac = S - (qq << FIXB);
+                        const __int128 tol = (__int128)1 << 20;
+                        q = (int32_t)qq;
+                        sgn = frac < -tol ? -1 : 1;
+                        amb = frac <= tol && frac >= -tol;
+                        xf->q[idx] = q;
+                        xf->sgn[idx] = sgn;
+                        xf->amb[idx] = amb;
+                        __syncwarp();
+                        if (lane == 0) tc::mbar_arrive(&xf->qready[quad]);
+                    } else {
+                        if (!tc::mbar_wait(&xf->qready[quad], phq & 1)) { set_abort(bars, err); ok = false; break; }
+                        phq++;
+                        q = xf->q[idx];
+                        sgn = xf->sgn[idx];
+                        amb = xf->amb[idx];
+                    }
+                }
+                // this half's limbs from carry 0: chunks k = 0..3 are digit columns
+                // pos = 256 j + 128 hf + 32 k - SROWS (32 digits = 7 limbs, on limb boundaries)
+                uint32_t L[28];
+                long long c = 0;
+                int nl = 0;
+                const int pos0 = 256 * j + 128 * hf - SROWS;
+                const int k0 = pos0 < 0 ? 1 : 0;  // the fixed-point columns precede digit 0
+                const int li0 = (pos0 + 32 * k0) / 32 * 7;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (k == 2) {
+                        tc::tmem_ld32(lb + (uint32_t)(256 * b + 64), *reinterpret_cast<uint32_t(*)[32]>(&g[0]));
+                        tc::tmem_ld32(lb + (uint32_t)(256 * b + 96), *reinterpret_cast<uint32_t(*)[32]>(&g[32]));
+                        tc::tmem_ld_wait();
                         tc::fence_before_sync();
                         __syncwarp();
-                        if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
-                    }
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        const uint32_t *gh = g + 32 * h;
-                        if (j == 0 && c0 == 0 && h == 0) {
-                            // fixed-point sum S = sum y_i 2^FIXB / p_i from the first SUSED columns
-                            // (base 128): S = (q + C / Mod) 2^FIXB + err, |err| <= 128 P < 2^17, and
-                            // |C / Mod| < 2^-18, so q = round(S / 2^FIXB) and the sign of
-                            // frac = S - q 2^FIXB is the sign of C unless |C| < Mod 2^(20 - FIXB)
-                            __int128 S = 0;
-#pragma unroll
-                            for (int u = SUSED - 1; u >= 0; u--) S = S * 128 + tc::acc_int(gh[u]);
-                            const __int128 halfw = (__int128)1 << (FIXB - 1);
-                            const __int128 qq = (S + halfw) >> FIXB;
-                            const __int128 frac = S - (qq << FIXB);
-                            q = (int32_t)qq;
-                            const __int128 tol = (__int128)1 << 20;
-                            sgn = frac < -tol ? -1 : 1;
-                            qs = q * sgn;
-                            ambiguous = frac <= tol && frac >= -tol;
-                        } else if (live && pos < a.Dout) {
-                            // 32 base-128 digits = 224 bits = 7 limbs (chunks start on limb
-                            // boundaries).  Each signed digit value x_u (|x_u| < 2^24) enters a
-                            // 64-bit accumulator per limb at its bit offset 7u; one carry pass
-                            // over the 7 limbs follows, so no chain runs through the digits.
-                            long long A[7];
-                            A[0] = carry;
-#pragma unroll
-                            for (int l = 1; l < 7; l++) A[l] = 0;
-#pragma unroll
-                            for (int u = 0; u < 32; u++) {
-                                const int32_t x = tc::acc_int(gh[u]) * sgn - qs * (int32_t)smdig[pos + u];
-                                A[(7 * u) >> 5] += (long long)x * (1LL << ((7 * u) & 31));
-                            }
-                            const int li0 = pos / 32 * 7;
-#pragma unroll
-                            for (int l = 0; l < 7; l++) {
-                                if (l < 6) A[l + 1] += A[l] >> 32;
-                                const uint32_t limb = (uint32_t)A[l];
-                                const int li = li0 + l;
-                                if (li < a.cnlimbs) {
-                                    a.climbs[(int64_t)li * a.cld + coff] = limb;
-                                    if (limb) top = li + 1;
-                                } else {
-                                    drop_nz |= limb != 0u;
-                                    drop_ones &= limb == 0xFFFFFFFFu;
-                                }
-                            }
-                            carry = A[6] >> 32;
-                            pos += 32;
+                        if (lane == 0) {
+                            if (PAIR) tc::mbar_arrive_cluster(tempty0 + 8u * b);
+                            else tc::mbar_arrive(&bars->tempty[b]);
                         }
+                    }
+                    const int pos = pos0 + 32 * k;
+                    if (k < k0 || !live || pos >= a.Dout) continue;
+                    const uint32_t *W = svtab + (pos >> 5) * 8;
+                    long long A[7];
+                    A[0] = c;
+#pragma unroll
+                    for (int l = 1; l < 7; l++) A[l] = 0;
+#pragma unroll
+                    for (int u = 0; u < 32; u++)
+                        A[(7 * u) >> 5] += (long long)tc::acc_int(g[32 * (k & 1) + u]) * (1LL << ((7 * u) & 31));
+#pragma unroll
+                    for (int l = 0; l < 7; l++) A[l] -= (long long)q * (long long)W[l];
+#pragma unroll
+                    for (int l = 0; l < 7; l++) {
+                        if (l < 6) A[l + 1] += A[l] >> 32;
+                        L[7 * k + l] = (uint32_t)A[l];
+                    }
+                    // the chunk's Mod value is sum W_l 2^(32 l) - s 2^224 (s = sign word)
+                    c = (A[6] >> 32) + (W[7] ? (long long)q : 0LL);
+                    nl = 7 * (k + 1);
+                }
+                // predecessor's carry and negation ripple: half 1 takes half 0's of the same
+                // tile; half 0 takes half 1's of the previous tile (none at an entry's tile 0)
+                long long cin = 0;
+                uint32_t nin = 1;
+                if (hf == 1) {
+                    if (!tc::mbar_wait(&xf->to1[quad], ph1 & 1)) { set_abort(bars, err); ok = false; break; }
+                    ph1++;
+                    cin = xf->carry1[idx];
+                    nin = xf->ripple1[idx];
+                } else if (!first) {
+                    if (!tc::mbar_wait(&xf->to0[quad], ph0 & 1)) { set_abort(bars, err); ok = false; break; }
+                    ph0++;
+                    if (j > 0) {
+                        cin = xf->carry0[idx];
+                        nin = xf->ripple0[idx];
+                    }
+                }
+                first = false;
+                // add the carry in, negate when C < 0, store
+#pragma unroll
+                for (int l = 0; l < 28; l++) {
+                    if (l < k0 * 7 || l >= nl || cin == 0) continue;
+                    const long long s = (long long)L[l] + cin;
+                    L[l] = (uint32_t)s;
+                    cin = s >> 32;
+                }
+                c += cin;
+#pragma unroll
+                for (int l = 0; l < 28; l++) {
+                    if (l < k0 * 7 || l >= nl) continue;
+                    uint32_t limb = L[l];
+                    if (sgn < 0) {
+                        const uint32_t nv = ~limb + nin;
+                        nin &= (uint32_t)(limb == 0u);
+                        limb = nv;
+                    }
+                    const int li = li0 + l - k0 * 7;
+                    if (li < a.cnlimbs) {
+                        a.climbs[(int64_t)li * a.cld + coff] = limb;
+                        if (limb) top = li + 1;
+                    } else {
+                        drop_nz |= limb != 0u;
+                        drop_ones &= limb == 0xFFFFFFFFu;
+                    }
+                }
+                // hand on: half 0 -> half 1 of this tile; half 1 -> half 0 of the next tile
+                // (also after an entry's last tile, except the CTA's very last one, so that
+                // half 0 never runs two hand-offs ahead)
+                if (hf == 0) {
+                    xf->carry1[idx] = c;
+                    xf->ripple1[idx] = nin;
+                    if (j == a.NT - 1) {
+                        xf->top0[idx] = top;
+                        xf->drop0[idx] = (drop_nz ? 1u : 0u) | (drop_ones ? 2u : 0u);
+                    }
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&xf->to1[quad]);
+                } else {
+                    if (j == a.NT - 1) {
+                        carry_final = c;
+                        nc_final = nin;
+                    } else {
+                        xf->carry0[idx] = c;
+                        xf->ripple0[idx] = nin;
+                    }
+                    if (!(last_t && j == a.NT - 1)) {
+                        __syncwarp();
+                        if (lane == 0) tc::mbar_arrive(&xf->to0[quad]);
                     }
                 }
             }
             if (!ok) break;
-            if (live) {
-                const int nl = pos / 32 * 7;  // limbs produced
+            if (hf == 1 && live) {
+                // finalize: half 0's top limb and dropped-limb flags arrived with its last hand-off
+                top = max(top, xf->top0[idx]);
+                const uint32_t d0 = xf->drop0[idx];
+                drop_nz |= (d0 & 1u) != 0;
+                drop_ones &= (d0 & 2u) != 0;
+                const int nl = (a.Dout + 31) / 32 * 7;  // limbs produced
                 const int written = nl < a.cnlimbs ? nl : a.cnlimbs;
                 int neg = sgn < 0;
+                // bits above the produced limbs of the written value: C's own, or -C's
+                long long carry = neg ? -carry_final - 1 + (long long)nc_final : carry_final;
                 if (carry < 0) {
                     // only reachable on the ambiguous path: two's complement -> magnitude
-                    if (!ambiguous || carry != -1 || (nl > a.cnlimbs && !(drop_ones && top != 0)))
+                    if (!amb || carry != -1 || (nl > a.cnlimbs && !(drop_ones && top != 0)))
                         atomicOr(err, DEVERR_CAPACITY);
                     uint32_t cc = 1;
                     top = 0;
@@ -741,7 +899,17 @@ __global__ void __launch_bounds__(64 + 128 * SUBS, 1)
             }
         }
     }
-    cta_teardown(bars, 512);
+    if (PAIR) {
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::cluster_sync_all();  // no CTA leaves while its peer may still signal it or write its TMEM
+        if (warp == 1) {
+            tc::fence_after_sync();
+            tc::tmem_dealloc_pair(tmem, 512);
+        }
+    } else {
+        cta_teardown(bars, 512);
+    }
 }
 
 // ======================================================================================
@@ -821,6 +989,114 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
         }
     }
     cta_teardown(bars, 128);
+}
+
+// ======================================================================================
+// CTA-pair GEMM self-test: D[M x N] (int32) = A * B^T, A K-major [M x K], B
+// K-major [N x K], one 256 x 256 tile per cluster of two CTAs.  The even CTA
+// issues tcgen05.mma.cta_group::2 (M = 256, N = 256): each CTA holds its own 128
+// rows of A and its own 128 rows of B at the same shared-memory offsets, and
+// its TMEM receives its 128 rows of D.  Both CTAs' TMA loads complete on the
+// even CTA's stage barrier; the MMA's commit arrives on both CTAs' barriers.
+// ======================================================================================
+constexpr uint32_t PAIR_TMEM_COLS = 256;
+template <int STAGES>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA_THREADS, 1)
+    k_gemm_test_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TestArgs a,
+                     uint32_t *err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *base = align1024(smem_raw);
+    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = BM * 128, STAGE = A_BYTES + B_BYTES;
+    Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = tc::cluster_rank();
+    const int tile = blockIdx.x >> 1, tiles_x = (a.N + 255) / 256;
+    const int ty = tile / tiles_x, tx = tile % tiles_x;
+    const int m0 = ty * 256 + (int)rank * BM, n0 = tx * 256 + (int)rank * BM;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            tc::mbar_init(&bars->full[s], 1);
+            tc::mbar_init(&bars->empty[s], 1);
+        }
+        tc::mbar_init(&bars->tfull[0], 1);
+        bars->abort_flag = 0;
+        tc::fence_mbar_init();
+    }
+    if (warp == 1) {
+        tc::tmem_alloc_pair(&bars->tmem_base, PAIR_TMEM_COLS);
+        tc::tmem_relinquish_pair();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::cluster_sync_all();  // both CTAs' barriers exist before any cross-CTA signal
+    tc::fence_after_sync();
+    const uint32_t tmem = bars->tmem_base;
+    if (threadIdx.x == 0 && rank == 1) {
+        // the pair's MMA writes D at the even CTA's TMEM address: both must agree
+        uint32_t lead;
+        asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(lead) : "r"(tc::mapa(tc::smem_u32(&bars->tmem_base), 0)));
+        if (lead != tmem) atomicOr(err, DEVERR_BADARG);
+    }
+
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int s = 0; s < a.nk; s++) {
+                const int st = s % STAGES;
+                if (s >= STAGES && !tc::mbar_wait(&bars->empty[st], ((s / STAGES) & 1) ^ 1)) {
+                    set_abort(bars, err);
+                    break;
+                }
+                uint8_t *sa = base + st * STAGE;
+                const uint32_t full_lead = tc::mapa(tc::smem_u32(&bars->full[st]), 0);
+                if (rank == 0) tc::mbar_arrive_expect_tx(&bars->full[st], 2 * STAGE);
+                tc::tma_load_2d_pair(sa, &tmA, full_lead, s * BK, m0);
+                tc::tma_load_2d_pair(sa + A_BYTES, &tmB, full_lead, s * BK, n0);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && rank == 0) {
+            const uint32_t idesc = tc::idesc_bf16_f32(2 * BM, 2 * BM, 0, 0);
+            bool ok = true;
+            for (int s = 0; s < a.nk; s++) {
+                const int st = s % STAGES;
+                if (!tc::mbar_wait(&bars->full[st], (s / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+                tc::fence_after_sync();
+                const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < BK / UK; kk++)
+                    tc::mma_bf16_pair(tmem, tc::sdesc_kmajor(sa + kk * 32), tc::sdesc_kmajor(sb + kk * 32), idesc,
+                                      s != 0 || kk != 0);
+                tc::mma_commit_pair(&bars->empty[st], 0x3);
+            }
+            if (ok) tc::mma_commit_pair(&bars->tfull[0], 0x3);
+        }
+    } else {
+        const int row = (int)rank * BM + epi_row();
+        const int m = ty * 256 + row;
+        const uint32_t lb = lane_base(tmem);
+        if (tc::mbar_wait(&bars->tfull[0], 0)) {
+            tc::fence_after_sync();
+            for (int c0 = 0; c0 < 256; c0 += 32) {
+                uint32_t v[32];
+                tc::tmem_ld32(lb + (uint32_t)c0, v);
+                tc::tmem_ld_wait();
+                if (m < a.M) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++)
+                        if (tx * 256 + c0 + j < a.N) a.D[(int64_t)m * a.N + tx * 256 + c0 + j] = tc::acc_int(v[j]);
+                }
+            }
+        } else {
+            set_abort(bars, err);
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::cluster_sync_all();  // no CTA leaves while its peer may still signal it or write its TMEM
+    if (warp == 1) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc_pair(tmem, PAIR_TMEM_COLS);
+    }
 }
 
 // ======================================================================================
@@ -945,7 +1221,7 @@ struct crt_tables {
     int Dout = 0, NT = 0;
     ModConst *d_mods = nullptr;
     __nv_bfloat16 *d_recon = nullptr;  // [NT * RTAB][2Pp]
-    int8_t *d_mdig = nullptr;          // [Dout]
+    uint32_t *d_vtab = nullptr;        // [ceil(Dout / 32)][8]: Mod's digits per 32-digit chunk
     std::map<int, __nv_bfloat16 *> residue;  // 2 * dxp + weighted -> [2P rows][dxp]
     std::vector<ModConst> h_mods;
 };
@@ -958,7 +1234,7 @@ struct crt_cache {
             crt_tables *t = kv.second;
             cudaFree(t->d_mods);
             cudaFree(t->d_recon);
-            cudaFree(t->d_mdig);
+            cudaFree(t->d_vtab);
             for (auto &r : t->residue) cudaFree(r.second);
             delete t;
         }
@@ -1025,15 +1301,38 @@ static gbmm_status build_tables(crt_tables *t, int P) {
             tab[(size_t)r * cols + 2 * i + 1] = bf16_bits((float)sl[r]);
         }
     }
+    // Mod's balanced base-128 digits, summed per 32-digit chunk n into the 224-bit
+    // value V_n = sum_u Mod_(32n+u) 128^u, kept as 8 words of a 256-bit two's
+    // complement number (|V_n| < 2^223, so word 7 is the sign extension)
     std::vector<int> md = balanced128(Mod, t->Dout);
-    std::vector<int8_t> md8(t->Dout);
-    for (int r = 0; r < t->Dout; r++) md8[r] = (int8_t)md[r];
+    const int nch = (t->Dout + 31) / 32;
+    std::vector<uint32_t> vt((size_t)nch * 8, 0u);
+    for (int n = 0; n < nch; n++) {
+        uint32_t *w = &vt[(size_t)n * 8];
+        for (int u = 0; u < 32; u++) {
+            const int r = 32 * n + u;
+            if (r >= t->Dout || md[r] == 0) continue;
+            const int bit = 7 * u, k = bit / 32;
+            const uint64_t v = (uint64_t)((int64_t)md[r] * ((int64_t)1 << (bit % 32)));  // two's complement
+            uint32_t add[8];
+            for (int kk = 0; kk < 8; kk++) add[kk] = md[r] < 0 ? 0xFFFFFFFFu : 0u;
+            for (int kk = 0; kk < k; kk++) add[kk] = 0u;
+            add[k] = (uint32_t)v;
+            if (k + 1 < 8) add[k + 1] = (uint32_t)(v >> 32);
+            uint64_t c = 0;
+            for (int kk = 0; kk < 8; kk++) {
+                const uint64_t sum = (uint64_t)w[kk] + add[kk] + c;
+                w[kk] = (uint32_t)sum;
+                c = sum >> 32;
+            }
+        }
+    }
     GBMM_CUDA_TRY(cudaMalloc(&t->d_mods, sizeof(ModConst) * P));
     GBMM_CUDA_TRY(cudaMemcpy(t->d_mods, t->h_mods.data(), sizeof(ModConst) * P, cudaMemcpyHostToDevice));
     GBMM_CUDA_TRY(cudaMalloc(&t->d_recon, tab.size() * 2));
     GBMM_CUDA_TRY(cudaMemcpy(t->d_recon, tab.data(), tab.size() * 2, cudaMemcpyHostToDevice));
-    GBMM_CUDA_TRY(cudaMalloc(&t->d_mdig, t->Dout));
-    GBMM_CUDA_TRY(cudaMemcpy(t->d_mdig, md8.data(), t->Dout, cudaMemcpyHostToDevice));
+    GBMM_CUDA_TRY(cudaMalloc(&t->d_vtab, vt.size() * 4));
+    GBMM_CUDA_TRY(cudaMemcpy(t->d_vtab, vt.data(), vt.size() * 4, cudaMemcpyHostToDevice));
     return GBMM_OK;
 }
 
@@ -1080,6 +1379,7 @@ static gbmm_status get_tables(crt_cache *c, int P, crt_tables **out) {
 }
 
 static constexpr int RES_STAGES = 4, PROD_STAGES = 4, REC_STAGES = 4, TEST_STAGES = 4;
+static constexpr int REC_STAGES_T = REC_PAIR ? 6 : REC_STAGES;  // a pair CTA stages 32 KB per K step
 
 static int num_sms() {
     static int n = 0;
@@ -1099,6 +1399,33 @@ static gbmm_status set_smem(const void *fn, size_t bytes) {
 }
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Launch of a persistent kernel in clusters of two CTAs (one CTA per SM): the
+// grid is as many pairs as can be resident at once (GPCs with an odd number of
+// free SMs leave one SM without a partner), capped by the work.
+template <typename... KArgs, typename... Args>
+static gbmm_status launch_pairs(void (*kern)(KArgs...), int threads, int64_t work_pairs, size_t smem, cudaStream_t s,
+                                Args &&...args) {
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3((unsigned)(2 * std::max<int>(1, num_sms() / 2)));
+    int resident = 0;
+    GBMM_CUDA_TRY(cudaOccupancyMaxActiveClusters(&resident, (const void *)kern, &cfg));
+    if (resident < 1) return set_error(GBMM_ERR_UNSUPPORTED, "no CTA pair of this kernel fits on the device");
+    cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(work_pairs, resident)));
+    GBMM_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
+    return GBMM_OK;
+}
 
 // digits + residues of one operand into planes [2P][rowsR][kp] (A: a1, a0 per
 // modulus); B's table is weighted, so B's planes hold u = w b (u1, u0)
@@ -1266,17 +1593,22 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     {
         CUtensorMap tmY, tmT;
         GBMM_TRY(make_map(&tmY, Y, 64, (uint64_t)(Ep / 64) * 2 * t->Pp, 64, 64, BK));
-        constexpr int RME = REC_SUBS * BM, RBN = 256 / REC_SUBS;
-        GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RTAB, 2 * t->Pp, BK, RBN));
+        constexpr int NP = REC_PAIR ? 2 : 1, TROWS = 256 / NP;
+        GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RTAB, 2 * t->Pp, BK, TROWS));
         ReconArgs ra;
-        ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.NT = (SROWS + t->Dout + RBN - 1) / RBN; ra.Dout = t->Dout;
-        ra.mdig = t->d_mdig; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
-        ra.cnlimbs = c.nlimbs; ra.kpad = 2 * t->Pp; ra.nmt = (E + RME - 1) / RME;
-        const size_t sm = smem_bytes(REC_STAGES, RME * 128 + RBN * 128) + t->Dout + 64;
-        GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES, REC_SUBS>, sm));
-        dim3 grid((unsigned)std::min<int64_t>(ra.nmt, num_sms()));
+        ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.NT = (SROWS + t->Dout + 255) / 256; ra.Dout = t->Dout;
+        ra.vtab = t->d_vtab; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
+        ra.cnlimbs = c.nlimbs; ra.kpad = 2 * t->Pp; ra.nmt = (E + NP * BM - 1) / (NP * BM);
+        const size_t sm = smem_bytes(REC_STAGES_T, BM * 128 + TROWS * 128) + (size_t)(t->Dout + 31) / 32 * 32 +
+                          sizeof(ReconXfer) + 64;
+        GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES_T, REC_PAIR>, sm));
         LaunchScope ls_("k_crt_recon", s);
-        k_crt_recon<REC_STAGES, REC_SUBS><<<grid, 64 + 128 * REC_SUBS, sm, s>>>(tmY, tmT, ra, err);
+        if (REC_PAIR) {
+            GBMM_TRY(launch_pairs(k_crt_recon<REC_STAGES_T, REC_PAIR>, CTA_THREADS8, ra.nmt, sm, s, tmY, tmT, ra, err));
+        } else {
+            dim3 grid((unsigned)std::min<int64_t>(ra.nmt, num_sms()));
+            k_crt_recon<REC_STAGES_T, REC_PAIR><<<grid, CTA_THREADS8, sm, s>>>(tmY, tmT, ra, err);
+        }
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     arena_release(h, mark);
@@ -1305,6 +1637,26 @@ extern "C" gbmm_status gbmmx_test_gemm(const void *A, const void *B, int32_t *D,
     dim3 grid((unsigned)((N + BM - 1) / BM), (unsigned)((M + BM - 1) / BM));
     LaunchScope ls_("k_gemm_test", s);
     k_gemm_test<TEST_STAGES><<<grid, CTA_THREADS, sm, s>>>(tmA, tmB, ta, device_error_word());
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return check_device_error(s);
+}
+
+// Internal test hook: the same product through the CTA-pair kernel (A and B
+// K-major only).
+extern "C" gbmm_status gbmmx_test_gemm_pair(const void *A, const void *B, int32_t *D, int32_t M, int32_t N, int32_t K,
+                                            void *stream) {
+    cudaStream_t s = as_stream(stream);
+    if (K % 64 || M % 8 || N % 8) return set_error(GBMM_ERR_INVALID, "test gemm: K % 64, M % 8, N % 8 required");
+    CUtensorMap tmA, tmB;
+    GBMM_TRY(make_map(&tmA, A, K, M, K, BK, BM));
+    GBMM_TRY(make_map(&tmB, B, K, N, K, BK, BM));
+    TestArgs ta;
+    ta.M = M; ta.N = N; ta.nk = K / BK; ta.a_mn = 0; ta.D = D;
+    const size_t sm = smem_bytes(TEST_STAGES, 2 * BM * 128);
+    GBMM_TRY(set_smem((const void *)k_gemm_test_pair<TEST_STAGES>, sm));
+    const unsigned tiles = (unsigned)(((M + 255) / 256) * ((N + 255) / 256));
+    LaunchScope ls_("k_gemm_test_pair", s);
+    k_gemm_test_pair<TEST_STAGES><<<2 * tiles, CTA_THREADS, sm, s>>>(tmA, tmB, ta, device_error_word());
     GBMM_CUDA_TRY(cudaGetLastError());
     return check_device_error(s);
 }

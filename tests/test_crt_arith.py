@@ -157,3 +157,86 @@ def test_fixed_point_sign_and_quotient():
             assert (frac < 0) == (C < 0)
         else:
             assert abs(C) <= Mod >> 75
+
+
+def _balanced128(x, ndig):
+    out, carry = [], 0
+    for t in range(ndig):
+        v = ((x >> (7 * t)) & 127) + carry
+        d = v - 128 if v >= 64 else v
+        carry = (v - d) // 128
+        out.append(d)
+    return out
+
+
+def _chunk_words(md, n):
+    """Mod's digits of 32-digit chunk n as the kernel's table: 7 words of the
+    two's-complement value sum_u Mod_(32n+u) 128^u, plus the sign word."""
+    v = sum(md[32 * n + u] * 128 ** u for u in range(32) if 32 * n + u < len(md))
+    assert abs(v) < 1 << 223
+    w = v & ((1 << 256) - 1)
+    return [(w >> (32 * k)) & 0xFFFFFFFF for k in range(8)]
+
+
+def test_reconstruction_epilogue_emulation():
+    """The reconstruction epilogue restated on exact integers: column sums of
+    y_i against Mod/p_i digits, q and the sign from the fixed-point columns,
+    per-chunk subtraction of q Mod through the 7-word table, on-the-fly negation
+    of negative results and the final carry rule."""
+    rng = random.Random(8)
+    P = 24
+    pr = PRIMES[:P]
+    Mod = 1
+    for p in pr:
+        Mod *= p
+    modbits = 32 * ((Mod.bit_length() + 31) // 32)
+    Dout = (modbits + 6) // 7 + 2
+    md = _balanced128(Mod, Dout)
+    nch = (Dout + 31) // 32
+    vt = [_chunk_words(md, n) for n in range(nch)]
+    tabs = []
+    for p in pr:
+        Mi = Mod // p
+        tabs.append((_balanced128(256 * Mi, Dout), _balanced128(Mi, Dout),
+                     ((1 << (FIXB + 8)) + p // 2) // p, ((1 << FIXB) + p // 2) // p))
+    inv = [pow(Mod // p, -1, p) for p in pr]
+    cases = [0, 1, -1, 5, -(1 << 40)] + [rng.randint(-(Mod >> 19), Mod >> 19) for _ in range(60)]
+    cases += [rng.randint(-(Mod >> 90), Mod >> 90) for _ in range(20)]
+    for C in cases:
+        ys = []
+        for i, p in enumerate(pr):
+            y = (C * inv[i]) % p
+            ys.append(y - p if y > p // 2 else y)
+        dig = [bal_split(F(y)) for y in ys]
+        S = sum(int(h) * tabs[i][2] + int(l) * tabs[i][3] for i, (h, l) in enumerate(dig))
+        acc = [sum(int(h) * tabs[i][0][r] + int(l) * tabs[i][1][r] for i, (h, l) in enumerate(dig)) for r in range(Dout)]
+        acc += [0] * (nch * 32 - Dout)
+        q = (S + (1 << (FIXB - 1))) >> FIXB
+        frac = S - (q << FIXB)
+        sgn = -1 if frac < -(1 << 20) else 1
+        carry, nc, limbs = 0, 1, []
+        for n in range(nch):
+            A = [carry] + [0] * 6
+            for u in range(32):
+                A[(7 * u) >> 5] += acc[32 * n + u] * (1 << ((7 * u) & 31))
+            for k in range(7):
+                A[k] -= q * vt[n][k]
+            for k in range(7):
+                if k < 6:
+                    A[k + 1] += A[k] >> 32
+                limb = A[k] & 0xFFFFFFFF
+                if sgn < 0:
+                    nl = (~limb + nc) & 0xFFFFFFFF
+                    nc &= int(limb == 0)
+                    limb = nl
+                limbs.append(limb)
+            carry = (A[6] >> 32) + (q if vt[n][7] else 0)
+        if sgn < 0:
+            carry = -carry - 1 + nc
+        value = sum(l << (32 * i) for i, l in enumerate(limbs))
+        if carry < 0:  # the undecided-sign path: two's complement, negated in place
+            assert carry == -1 and abs(frac) <= 1 << 20
+            value = value - (1 << (32 * len(limbs)))
+        else:
+            assert carry == 0
+        assert (-value if sgn < 0 else value) == C

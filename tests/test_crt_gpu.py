@@ -46,6 +46,27 @@ def test_tcgen05_gemm_core(g, M, N, K, a_mn):
     assert (got == exp).all(), f"{(got != exp).sum()} mismatches"
 
 
+@pytest.mark.parametrize("M,N,K", [(256, 256, 64), (512, 256, 512), (200, 296, 192), (768, 512, 1024)])
+def test_tcgen05_gemm_pair(g, M, N, K):
+    """The CTA-pair (cta_group::2, M = 256) MMA path: A and D split along M across
+    two SMs, B along N, barriers shared across the pair."""
+    import torch
+    rng = np.random.default_rng(M * 7 + N + K)
+    A = rng.integers(-128, 129, size=(M, K))
+    B = rng.integers(-128, 129, size=(N, K))
+    A[0, :] = -128
+    B[0, :] = -128
+    exp = A @ B.T
+    dA, dB = _bf16(torch, A), _bf16(torch, B)
+    D = torch.zeros(M * N, dtype=torch.int32, device="cuda")
+    L = g.lib()
+    L.gbmmx_test_gemm_pair.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int32] * 3 + [ctypes.c_void_p]
+    g.check(L.gbmmx_test_gemm_pair(dA.data_ptr(), dB.data_ptr(), D.data_ptr(), M, N, K, g.stream_ptr()))
+    torch.cuda.synchronize()
+    got = D.cpu().numpy().reshape(M, N)
+    assert (got == exp).all(), f"{(got != exp).sum()} mismatches"
+
+
 def _crt(g, K, M, N, dA, dB, nl=None, nprimes=0):
     nl = nl or g.limbs_needed(dA.nlimbs, dB.nlimbs, M, path=g.PATH_CRT)
     dC = g.DeviceMatrix(K, N, nl)
