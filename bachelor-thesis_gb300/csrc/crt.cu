@@ -229,13 +229,17 @@ struct ResidueArgs {
     int32_t kp;
 };
 
-template <int STAGES>
+// PAIR: a cluster of two CTAs shares one M = 256 tcgen05.mma.cta_group::2 per K
+// slice (issued by the even CTA); each CTA stages its own 128 entries and half of
+// the tile's table columns, and keeps its own 128 rows of D in its TMEM.
+template <int STAGES, bool PAIR>
 __global__ void __launch_bounds__(CTA_THREADS8, 1)
     k_crt_residue(const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmT, ResidueArgs a,
                   uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
-    const uint32_t A_BYTES = BM * 128, B_BYTES = (uint32_t)a.BN * 128, STAGE = A_BYTES + B_BYTES;
+    constexpr int NP = PAIR ? 2 : 1;
+    const uint32_t A_BYTES = BM * 128, B_BYTES = (uint32_t)(a.BN / NP) * 128, STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
     // (p, 1/p) per modulus, padded to a multiple of 16 with the last modulus
     float2 *smod = reinterpret_cast<float2 *>(reinterpret_cast<uint8_t *>(bars) + SMEM_BARS);
@@ -244,17 +248,46 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         const ModConst mc = a.mods[i < a.P ? i : a.P - 1];
         smod[i] = make_float2((float)mc.p, mc.inv_p);
     }
-    cta_setup(bars, STAGES, 512, 1, 8);
+    const uint32_t rank = PAIR ? tc::cluster_rank() : 0;
+    const int64_t t0 = PAIR ? (blockIdx.x >> 1) : blockIdx.x, tstep = PAIR ? (gridDim.x >> 1) : gridDim.x;
+    if (PAIR) {
+        if (threadIdx.x == 0) {
+            for (int s = 0; s < STAGES; s++) {
+                tc::mbar_init(&bars->full[s], 1);
+                tc::mbar_init(&bars->empty[s], 1);
+            }
+            for (int b = 0; b < 2; b++) {
+                tc::mbar_init(&bars->tfull[b], 1);
+                tc::mbar_init(&bars->tempty[b], 16);  // the even CTA's: 8 epilogue warps of each CTA
+            }
+            bars->abort_flag = 0;
+            tc::fence_mbar_init();
+        }
+        if (warp == 1) {
+            tc::tmem_alloc_pair(&bars->tmem_base, 512);
+            tc::tmem_relinquish_pair();
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::cluster_sync_all();  // both CTAs' barriers exist before any cross-CTA signal
+        tc::fence_after_sync();
+    } else {
+        cta_setup(bars, STAGES, 512, 1, 8);
+    }
     const uint32_t tmem = bars->tmem_base;
+    // the last table tile may be narrow: its MMA has only the columns it needs
+    // (a multiple of 16, of 32 for a pair so that each CTA stages whole 8-row groups)
+    const int ngran = PAIR ? 32 : 16;
 
     if (warp == 0) {
         if (lane == 0) {
             tc::prefetch_tmap(&tmD);
             tc::prefetch_tmap(&tmT);
             int it = 0;
-            for (int64_t t = blockIdx.x; t < a.ntiles && !aborted(bars); t += gridDim.x) {
-                const int64_t e0 = (t / a.n_ntiles) * BM;
+            for (int64_t t = t0; t < a.ntiles && !aborted(bars); t += tstep) {
+                const int64_t e0 = (t / a.n_ntiles) * (NP * BM) + rank * BM;
                 const int n0 = (int)(t % a.n_ntiles) * a.BN;
+                const int nn = min(a.BN, (a.ncols - n0 + ngran - 1) / ngran * ngran);
                 for (int s = 0; s < a.nk; s++, it++) {
                     const int st = it % STAGES;
                     if (it >= STAGES && !tc::mbar_wait(&bars->empty[st], ((it / STAGES) & 1) ^ 1)) {
@@ -262,22 +295,29 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                         break;
                     }
                     uint8_t *sa = base + st * STAGE;
-                    tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                    tc::tma_load_2d(sa, &tmD, &bars->full[st], s * BK, (int)e0);
-                    tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, n0);
+                    if (PAIR) {
+                        // this CTA's half of the tile's columns: n0 + rank * nn / 2 onwards
+                        const uint32_t full0 = tc::mapa(tc::smem_u32(&bars->full[st]), 0);
+                        if (rank == 0) tc::mbar_arrive_expect_tx(&bars->full[st], 2 * STAGE);
+                        tc::tma_load_2d_pair(sa, &tmD, full0, s * BK, (int)e0);
+                        tc::tma_load_2d_pair(sa + A_BYTES, &tmT, full0, s * BK, n0 + (int)rank * (nn / 2));
+                    } else {
+                        tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                        tc::tma_load_2d(sa, &tmD, &bars->full[st], s * BK, (int)e0);
+                        tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, n0);
+                    }
                 }
             }
         }
     } else if (warp == 1) {
-        if (lane == 0) {
+        if (lane == 0 && rank == 0) {
             int it = 0, lt = 0;
             bool ok = true;
-            for (int64_t t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x, lt++) {
+            for (int64_t t = t0; t < a.ntiles && ok; t += tstep, lt++) {
                 const int b = lt & 1;
-                // the last table tile may be narrow: issue only the columns it has
                 const int n0 = (int)(t % a.n_ntiles) * a.BN;
-                const int nn = min(a.BN, (a.ncols - n0 + 15) & ~15);
-                const uint32_t idesc = tc::idesc_bf16_f32(BM, nn, 0, 0);
+                const int nn = min(a.BN, (a.ncols - n0 + ngran - 1) / ngran * ngran);
+                const uint32_t idesc = tc::idesc_bf16_f32(NP * BM, nn, 0, 0);
                 if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
                 tc::fence_after_sync();
                 for (int s = 0; s < a.nk; s++, it++) {
@@ -287,12 +327,18 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                     const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
                     const uint32_t d = tmem + (uint32_t)(256 * b + (s / GROUP_STEPS) * a.BN);
 #pragma unroll
-                    for (int kk = 0; kk < BK / UK; kk++)
-                        tc::mma_bf16(d, tc::sdesc_kmajor(sa + kk * 32), tc::sdesc_kmajor(sb + kk * 32), idesc,
-                                     (s % GROUP_STEPS) != 0 || kk != 0);
-                    tc::mma_commit(&bars->empty[st]);
+                    for (int kk = 0; kk < BK / UK; kk++) {
+                        const uint64_t adesc = tc::sdesc_kmajor(sa + kk * 32), bdesc = tc::sdesc_kmajor(sb + kk * 32);
+                        if (PAIR) tc::mma_bf16_pair(d, adesc, bdesc, idesc, (s % GROUP_STEPS) != 0 || kk != 0);
+                        else tc::mma_bf16(d, adesc, bdesc, idesc, (s % GROUP_STEPS) != 0 || kk != 0);
+                    }
+                    if (PAIR) tc::mma_commit_pair(&bars->empty[st], 0x3);
+                    else tc::mma_commit(&bars->empty[st]);
                 }
-                if (ok) tc::mma_commit(&bars->tfull[b]);
+                if (ok) {
+                    if (PAIR) tc::mma_commit_pair(&bars->tfull[b], 0x3);
+                    else tc::mma_commit(&bars->tfull[b]);
+                }
             }
         }
     } else {
@@ -300,10 +346,11 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         const int quad = warp & 3, half = (warp - 2) >> 2;
         const int hcols = a.BN / 2;
         const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
+        const uint32_t tempty0 = PAIR ? tc::mapa(tc::smem_u32(&bars->tempty[0]), 0) : 0;
         int lt = 0;
-        for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, lt++) {
+        for (int64_t t = t0; t < a.ntiles; t += tstep, lt++) {
             const int b = lt & 1;
-            const int64_t e = (t / a.n_ntiles) * BM + quad * 32 + lane;
+            const int64_t e = (t / a.n_ntiles) * (NP * BM) + rank * BM + quad * 32 + lane;
             const int n0 = (int)(t % a.n_ntiles) * a.BN;
             if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); break; }
             tc::fence_after_sync();
@@ -331,7 +378,10 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                         // last TMEM read of this tile by this warp: hand the buffer back
                         tc::fence_before_sync();
                         __syncwarp();
-                        if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
+                        if (lane == 0) {
+                            if (PAIR) tc::mbar_arrive_cluster(tempty0 + 8u * b);
+                            else tc::mbar_arrive(&bars->tempty[b]);
+                        }
                     }
                     if (!live_chunk) continue;
 #pragma unroll
@@ -359,7 +409,17 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             }
         }
     }
-    cta_teardown(bars, 512);
+    if (PAIR) {
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::cluster_sync_all();  // no CTA leaves while its peer may still signal it or write its TMEM
+        if (warp == 1) {
+            tc::fence_after_sync();
+            tc::tmem_dealloc_pair(tmem, 512);
+        }
+    } else {
+        cta_teardown(bars, 512);
+    }
 }
 
 // ======================================================================================
@@ -1380,6 +1440,8 @@ static gbmm_status get_tables(crt_cache *c, int P, crt_tables **out) {
 
 static constexpr int RES_STAGES = 4, PROD_STAGES = 4, REC_STAGES = 4, TEST_STAGES = 4;
 static constexpr int REC_STAGES_T = REC_PAIR ? 6 : REC_STAGES;  // a pair CTA stages 32 KB per K step
+static constexpr bool RES_PAIR = false;  // pair mode measured 0.32 ms vs 0.28 ms per 512^3 launch: the epilogue holds TMEM
+static constexpr int RES_STAGES_T = RES_PAIR ? 6 : RES_STAGES;
 
 static int num_sms() {
     static int n = 0;
@@ -1454,18 +1516,24 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     if (BN < 64) return set_error(GBMM_ERR_UNSUPPORTED, "crt: entries longer than 16384 bits");
     CUtensorMap tmD, tmT;
     GBMM_TRY(make_map(&tmD, D, dxp, E, dxp, BK, BM));
-    GBMM_TRY(make_map(&tmT, T, dxp, 2 * t->P, dxp, BK, BN));
+    constexpr int NP = RES_PAIR ? 2 : 1;
+    GBMM_TRY(make_map(&tmT, T, dxp, 2 * t->P, dxp, BK, BN / NP));
     ResidueArgs a;
     a.sizes = X.sizes; a.rs = X.rs; a.transpose = transpose; a.kdim = kdim; a.E = E; a.nk = nk;
     a.BN = BN; a.G = G; a.P = t->P; a.mods = t->d_mods; a.R = R; a.plane = (int64_t)rowsR * kp; a.kp = kp;
     a.ncols = 2 * t->P;
     a.n_ntiles = (2 * t->P + BN - 1) / BN;
-    a.ntiles = (int64_t)a.n_ntiles * ((E + BM - 1) / BM);
-    const size_t sm = smem_bytes(RES_STAGES, BM * 128 + (size_t)BN * 128) + (size_t)(t->P + 15) / 16 * 16 * 8;
-    GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES>, sm));
-    dim3 grid((unsigned)std::min<int64_t>(a.ntiles, num_sms()));
+    a.ntiles = (int64_t)a.n_ntiles * ((E + NP * BM - 1) / (NP * BM));
+    const size_t sm = smem_bytes(RES_STAGES_T, BM * 128 + (size_t)(BN / NP) * 128) + (size_t)(t->P + 15) / 16 * 16 * 8;
+    GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES_T, RES_PAIR>, sm));
     LaunchScope ls_("k_crt_residue", s);
-    k_crt_residue<RES_STAGES><<<grid, CTA_THREADS8, sm, s>>>(tmD, tmT, a, device_error_word());
+    if (RES_PAIR) {
+        GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES_T, RES_PAIR>, CTA_THREADS8, a.ntiles, sm, s, tmD, tmT, a,
+                              device_error_word()));
+    } else {
+        dim3 grid((unsigned)std::min<int64_t>(a.ntiles, num_sms()));
+        k_crt_residue<RES_STAGES_T, RES_PAIR><<<grid, CTA_THREADS8, sm, s>>>(tmD, tmT, a, device_error_word());
+    }
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
 }
