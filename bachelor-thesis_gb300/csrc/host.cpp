@@ -14,6 +14,7 @@
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gbmm_internal.h"
@@ -238,98 +239,245 @@ static inline int hexval(unsigned char c) {
 }
 static inline bool is_ws(unsigned char c) { return c == ' ' || c == '\n' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
 
+// ---- host-side parallelism for the text and GMP conversions -----------------------------
+// Large inputs are cut into chunks that threads handle independently; errors are
+// reported for the first offending entry in input order, exactly as the serial path
+// does (the serial path is the same code on one chunk).
+static std::atomic<int> g_host_threads{0};  // 0: the hardware's thread count
+static int host_threads() {
+    static const int hw = std::max(1, (int)std::thread::hardware_concurrency());
+    const int n = g_host_threads.load(std::memory_order_relaxed);
+    return n > 0 ? n : hw;
+}
+template <typename F>
+static void run_chunks(int nchunks, F f) {
+    std::vector<std::thread> th;
+    th.reserve(nchunks > 0 ? nchunks - 1 : 0);
+    for (int c = 1; c < nchunks; c++) th.emplace_back(f, c);
+    if (nchunks > 0) f(0);
+    for (auto &t : th) t.join();
+}
+static constexpr size_t PAR_TEXT_BYTES = 1u << 20;   // text per thread before parsing splits
+static constexpr int64_t PAR_ENTRIES = 1 << 14;       // entries per thread before loops split
+
+// One token "[-]hexdigits" at text[p] (p on a non-space byte) into entry e.
+static gbmm_status parse_one(const char *text, size_t len, size_t &p, int64_t e, uint32_t *limbs, int32_t *sizes,
+                             int32_t nlimbs, int64_t ld, char *msg, size_t msgcap) {
+    bool neg = false;
+    if (p < len && text[p] == '-') { neg = true; p++; }
+    size_t s = p;
+    while (p < len && hexval((unsigned char)text[p]) >= 0) p++;
+    size_t nd = p - s;
+    if (nd == 0) {
+        snprintf(msg, msgcap, "entry %lld: expected a hexadecimal digit at byte %zu", (long long)e, p);
+        return GBMM_ERR_PARSE;
+    }
+    if (p < len && !is_ws((unsigned char)text[p])) {
+        snprintf(msg, msgcap, "entry %lld: invalid character '%c' at byte %zu", (long long)e, text[p], p);
+        return GBMM_ERR_PARSE;
+    }
+    while (nd > 1 && text[s] == '0') { s++; nd--; }  // leading zeros
+    int need = (int)((nd + 7) / 8);
+    if (nd == 1 && text[s] == '0') need = 0;
+    if (need > nlimbs) {
+        snprintf(msg, msgcap, "entry %lld needs %d limbs, capacity %d", (long long)e, need, nlimbs);
+        return GBMM_ERR_CAPACITY;
+    }
+    for (int i = 0; i < nlimbs; i++) limbs[(int64_t)i * ld + e] = 0u;
+    for (size_t i = 0; i < nd; i++) {
+        size_t pos = nd - 1 - i;  // digit index from the least significant end
+        if (pos / 8 < (size_t)nlimbs)
+            limbs[(int64_t)(pos / 8) * ld + e] |= (uint32_t)hexval((unsigned char)text[s + i]) << (4 * (pos % 8));
+    }
+    int n = need;
+    while (n > 0 && limbs[(int64_t)(n - 1) * ld + e] == 0) n--;
+    sizes[e] = neg ? -n : n;
+    return GBMM_OK;
+}
+
 extern "C" gbmm_status gbmm_parse_hex(const char *text, size_t len, int64_t count, uint32_t *limbs, int32_t *sizes,
                                       int32_t nlimbs, int64_t ld, size_t *consumed) {
     if ((!text && len) || (count > 0 && (!limbs || !sizes))) return set_error(GBMM_ERR_INVALID, "null pointer");
     if (count > 0 && nlimbs > 0 && ld < count) return set_error(GBMM_ERR_INVALID, "plane stride %lld < count", (long long)ld);
-    size_t p = 0;
-    for (int64_t e = 0; e < count; e++) {
-        while (p < len && is_ws((unsigned char)text[p])) p++;
-        bool neg = false;
-        if (p < len && text[p] == '-') { neg = true; p++; }
-        size_t s = p;
-        while (p < len && hexval((unsigned char)text[p]) >= 0) p++;
-        size_t nd = p - s;
-        if (nd == 0) {
-            if (consumed) *consumed = p;
-            return set_error(GBMM_ERR_PARSE, "entry %lld: expected a hexadecimal digit at byte %zu", (long long)e, p);
+    char msg[256];
+    const int T = (int)std::min<size_t>((size_t)host_threads(), len / PAR_TEXT_BYTES);
+    if (T < 2 || count < 2 * T) {
+        size_t p = 0;
+        for (int64_t e = 0; e < count; e++) {
+            while (p < len && is_ws((unsigned char)text[p])) p++;
+            gbmm_status st = parse_one(text, len, p, e, limbs, sizes, nlimbs, ld, msg, sizeof msg);
+            if (st != GBMM_OK) {
+                if (consumed) *consumed = p;
+                return set_error(st, "%s", msg);
+            }
         }
-        if (p < len && !is_ws((unsigned char)text[p])) {
-            if (consumed) *consumed = p;
-            return set_error(GBMM_ERR_PARSE, "entry %lld: invalid character '%c' at byte %zu", (long long)e, text[p], p);
-        }
-        // skip leading zeros
-        while (nd > 1 && text[s] == '0') { s++; nd--; }
-        int need = (int)((nd + 7) / 8);
-        if (nd == 1 && text[s] == '0') need = 0;
-        if (need > nlimbs) {
-            if (consumed) *consumed = p;
-            return set_error(GBMM_ERR_CAPACITY, "entry %lld needs %d limbs, capacity %d", (long long)e, need, nlimbs);
-        }
-        for (int i = 0; i < nlimbs; i++) limbs[(int64_t)i * ld + e] = 0u;
-        for (size_t i = 0; i < nd; i++) {
-            size_t pos = nd - 1 - i;  // digit index from the least significant end
-            if (pos / 8 < (size_t)nlimbs)
-                limbs[(int64_t)(pos / 8) * ld + e] |= (uint32_t)hexval((unsigned char)text[s + i]) << (4 * (pos % 8));
-        }
-        int n = need;
-        while (n > 0 && limbs[(int64_t)(n - 1) * ld + e] == 0) n--;
-        sizes[e] = neg ? -n : n;
+        if (consumed) *consumed = p;
+        return GBMM_OK;
     }
-    if (consumed) *consumed = p;
+    // chunk boundaries on whitespace, so no token straddles two chunks
+    std::vector<size_t> bnd(T + 1);
+    bnd[0] = 0;
+    bnd[T] = len;
+    for (int t = 1; t < T; t++) {
+        size_t q = std::max(bnd[t - 1], len / T * t);
+        while (q < len && !is_ws((unsigned char)text[q])) q++;
+        bnd[t] = q;
+    }
+    std::vector<int64_t> ntok(T, 0), first(T + 1, 0);
+    run_chunks(T, [&](int t) {
+        int64_t n = 0;
+        bool in = false;
+        for (size_t q = bnd[t]; q < bnd[t + 1]; q++) {
+            const bool w = is_ws((unsigned char)text[q]);
+            if (!w && !in) n++;
+            in = !w;
+        }
+        ntok[t] = n;
+    });
+    for (int t = 0; t < T; t++) first[t + 1] = first[t] + ntok[t];
+    struct ChunkResult {
+        gbmm_status st = GBMM_OK;
+        int64_t e = -1;
+        size_t pos = 0, end = 0;
+        char msg[256];
+    };
+    std::vector<ChunkResult> res(T);
+    run_chunks(T, [&](int t) {
+        ChunkResult &r = res[t];
+        size_t p = bnd[t];
+        for (int64_t e = first[t]; e < first[t + 1] && e < count; e++) {
+            while (p < bnd[t + 1] && is_ws((unsigned char)text[p])) p++;
+            gbmm_status st = parse_one(text, len, p, e, limbs, sizes, nlimbs, ld, r.msg, sizeof r.msg);
+            if (st != GBMM_OK) {
+                r.st = st;
+                r.e = e;
+                r.pos = p;
+                return;
+            }
+            if (e == count - 1) r.end = p;
+        }
+    });
+    for (int t = 0; t < T; t++)
+        if (res[t].st != GBMM_OK) {
+            if (consumed) *consumed = res[t].pos;
+            return set_error(res[t].st, "%s", res[t].msg);
+        }
+    if (first[T] < count) {
+        if (consumed) *consumed = len;
+        return set_error(GBMM_ERR_PARSE, "entry %lld: expected a hexadecimal digit at byte %zu", (long long)first[T], len);
+    }
+    if (consumed)
+        for (int t = 0; t < T; t++)
+            if (count - 1 >= first[t] && count - 1 < first[t + 1]) *consumed = res[t].end;
     return GBMM_OK;
+}
+
+static const char HEXDIG[] = "0123456789abcdef";
+
+// characters of entry e in the text form ("0", or [-] and hex digits without leading zeros); -1: bad size
+static int64_t hex_len(const uint32_t *limbs, const int32_t *sizes, int32_t nlimbs, int64_t ld, int64_t e) {
+    int s = sizes[e], n = s < 0 ? -s : s;
+    if (n > nlimbs) return -1;
+    while (n > 0 && limbs[(int64_t)(n - 1) * ld + e] == 0) n--;
+    if (n == 0) return 1;
+    uint32_t top = limbs[(int64_t)(n - 1) * ld + e];
+    int d = 8;
+    while (d > 1 && (top >> (4 * (d - 1))) == 0) d--;
+    return (s < 0 ? 1 : 0) + 8 * (int64_t)(n - 1) + d;
+}
+static char *hex_put(const uint32_t *limbs, const int32_t *sizes, int64_t ld, int64_t e, char *o) {
+    int s = sizes[e], n = s < 0 ? -s : s;
+    while (n > 0 && limbs[(int64_t)(n - 1) * ld + e] == 0) n--;
+    if (n == 0) { *o++ = '0'; return o; }
+    if (s < 0) *o++ = '-';
+    bool started = false;
+    for (int i = n - 1; i >= 0; i--) {
+        uint32_t v = limbs[(int64_t)i * ld + e];
+        for (int k = 7; k >= 0; k--) {
+            int d = (v >> (4 * k)) & 15;
+            if (d || started) { *o++ = HEXDIG[d]; started = true; }
+        }
+    }
+    return o;
 }
 
 extern "C" gbmm_status gbmm_format_hex(const uint32_t *limbs, const int32_t *sizes, int32_t nlimbs, int64_t ld,
                                        int32_t rows, int32_t cols, int64_t rs, char *out, size_t cap, size_t *written) {
     if (!sizes || (nlimbs > 0 && !limbs)) return set_error(GBMM_ERR_INVALID, "null pointer");
-    size_t w = 0;
-    auto put = [&](char c) {
-        if (out && w < cap) out[w] = c;
-        w++;
-    };
-    static const char *hx = "0123456789abcdef";
-    for (int32_t r = 0; r < rows; r++) {
-        for (int32_t c = 0; c < cols; c++) {
-            if (c) put(' ');
-            int64_t e = (int64_t)r * rs + c;
-            int s = sizes[e], n = s < 0 ? -s : s;
-            if (n > nlimbs) return set_error(GBMM_ERR_INVALID, "entry (%d,%d): size %d exceeds %d planes", r, c, s, nlimbs);
-            while (n > 0 && limbs[(int64_t)(n - 1) * ld + e] == 0) n--;
-            if (n == 0) { put('0'); continue; }
-            if (s < 0) put('-');
-            bool started = false;
-            for (int i = n - 1; i >= 0; i--) {
-                uint32_t v = limbs[(int64_t)i * ld + e];
-                for (int k = 7; k >= 0; k--) {
-                    int d = (v >> (4 * k)) & 15;
-                    if (d || started) { put(hx[d]); started = true; }
+    // row lengths (entries, separators, newline), in parallel over rows
+    const int T = (int)std::max<int64_t>(1, std::min<int64_t>(host_threads(), (int64_t)rows * cols / PAR_ENTRIES));
+    std::vector<int64_t> rowlen(rows + 1, 0);
+    std::vector<int64_t> bad(T, -1);
+    run_chunks(T, [&](int t) {
+        for (int32_t r = (int32_t)((int64_t)rows * t / T); r < (int32_t)((int64_t)rows * (t + 1) / T); r++) {
+            int64_t L = 1 + (cols > 0 ? cols - 1 : 0);
+            for (int32_t c = 0; c < cols; c++) {
+                int64_t l = hex_len(limbs, sizes, nlimbs, ld, (int64_t)r * rs + c);
+                if (l < 0) {
+                    if (bad[t] < 0) bad[t] = (int64_t)r * cols + c;
+                    l = 0;
                 }
+                L += l;
             }
+            rowlen[r + 1] = L;
         }
-        put('\n');
-    }
-    put('\n');
-    if (out && w < cap) out[w] = 0;
+    });
+    for (int t = 0; t < T; t++)
+        if (bad[t] >= 0) {
+            const int32_t r = (int32_t)(bad[t] / cols), c = (int32_t)(bad[t] % cols);
+            return set_error(GBMM_ERR_INVALID, "entry (%d,%d): size %d exceeds %d planes", r, c, sizes[(int64_t)r * rs + c],
+                             nlimbs);
+        }
+    for (int32_t r = 0; r < rows; r++) rowlen[r + 1] += rowlen[r];  // row offsets
+    const size_t w = (size_t)rowlen[rows] + 1;                          // final empty line
     if (written) *written = w;
-    if (out && w > cap) return set_error(GBMM_ERR_INVALID, "output buffer too small (%zu < %zu)", cap, w);
+    if (!out) return GBMM_OK;
+    if (w > cap) return set_error(GBMM_ERR_INVALID, "output buffer too small (%zu < %zu)", cap, w);
+    run_chunks(T, [&](int t) {
+        for (int32_t r = (int32_t)((int64_t)rows * t / T); r < (int32_t)((int64_t)rows * (t + 1) / T); r++) {
+            char *o = out + rowlen[r];
+            for (int32_t c = 0; c < cols; c++) {
+                if (c) *o++ = ' ';
+                o = hex_put(limbs, sizes, ld, (int64_t)r * rs + c, o);
+            }
+            *o++ = '\n';
+        }
+    });
+    out[w - 1] = '\n';
+    if (w < cap) out[w] = 0;
     return GBMM_OK;
 }
+
+// Internal test hook (not part of the public ABI): threads for the host-side
+// conversions, 0 = hardware default; returns the previous setting.
+extern "C" int32_t gbmmx_host_threads(int32_t n) { return g_host_threads.exchange(n < 0 ? 0 : n); }
 
 extern "C" gbmm_status gbmm_import_gmp(int64_t count, const uint64_t *limbs64, const int64_t *offsets,
                                        const int32_t *sizes64, uint32_t *limbs, int32_t *sizes, int32_t nlimbs,
                                        int64_t ld) {
     if (count > 0 && (!limbs64 || !offsets || !sizes64 || !limbs || !sizes))
         return set_error(GBMM_ERR_INVALID, "null pointer");
-    for (int64_t e = 0; e < count; e++) {
-        int s = sizes64[e], n64 = s < 0 ? -s : s;
-        const uint64_t *d = limbs64 + offsets[e];
-        int n = 2 * n64;
-        while (n > 0 && (uint32_t)(d[(n - 1) / 2] >> (32 * ((n - 1) % 2))) == 0) n--;
-        if (n > nlimbs) return set_error(GBMM_ERR_CAPACITY, "entry %lld needs %d limbs, capacity %d", (long long)e, n, nlimbs);
-        for (int i = 0; i < nlimbs; i++) limbs[(int64_t)i * ld + e] = i < n ? (uint32_t)(d[i / 2] >> (32 * (i % 2))) : 0u;
-        sizes[e] = s < 0 ? -n : n;
-    }
+    const int T = (int)std::max<int64_t>(1, std::min<int64_t>(host_threads(), count / PAR_ENTRIES));
+    std::vector<int64_t> bad(T, -1);
+    std::vector<int> badn(T, 0);
+    run_chunks(T, [&](int t) {
+        for (int64_t e = count * t / T; e < count * (t + 1) / T; e++) {
+            int s = sizes64[e], n64 = s < 0 ? -s : s;
+            const uint64_t *d = limbs64 + offsets[e];
+            int n = 2 * n64;
+            while (n > 0 && (uint32_t)(d[(n - 1) / 2] >> (32 * ((n - 1) % 2))) == 0) n--;
+            if (n > nlimbs) {
+                bad[t] = e;
+                badn[t] = n;
+                return;
+            }
+            for (int i = 0; i < nlimbs; i++) limbs[(int64_t)i * ld + e] = i < n ? (uint32_t)(d[i / 2] >> (32 * (i % 2))) : 0u;
+            sizes[e] = s < 0 ? -n : n;
+        }
+    });
+    for (int t = 0; t < T; t++)
+        if (bad[t] >= 0)
+            return set_error(GBMM_ERR_CAPACITY, "entry %lld needs %d limbs, capacity %d", (long long)bad[t], badn[t], nlimbs);
     return GBMM_OK;
 }
 
@@ -337,18 +485,27 @@ extern "C" gbmm_status gbmm_export_gmp(int64_t count, const uint32_t *limbs, con
                                        int64_t ld, uint64_t *limbs64, const int64_t *offsets, int32_t *sizes64) {
     if (count > 0 && (!limbs64 || !offsets || !sizes64 || !limbs || !sizes))
         return set_error(GBMM_ERR_INVALID, "null pointer");
-    for (int64_t e = 0; e < count; e++) {
-        int s = sizes[e], n = s < 0 ? -s : s;
-        if (n > nlimbs) return set_error(GBMM_ERR_INVALID, "entry %lld: size exceeds planes", (long long)e);
-        int n64 = (n + 1) / 2;
-        uint64_t *d = limbs64 + offsets[e];
-        for (int i = 0; i < n64; i++) {
-            uint64_t lo = limbs[(int64_t)(2 * i) * ld + e];
-            uint64_t hi = 2 * i + 1 < n ? limbs[(int64_t)(2 * i + 1) * ld + e] : 0u;
-            d[i] = lo | (hi << 32);
+    const int T = (int)std::max<int64_t>(1, std::min<int64_t>(host_threads(), count / PAR_ENTRIES));
+    std::vector<int64_t> bad(T, -1);
+    run_chunks(T, [&](int t) {
+        for (int64_t e = count * t / T; e < count * (t + 1) / T; e++) {
+            int s = sizes[e], n = s < 0 ? -s : s;
+            if (n > nlimbs) {
+                bad[t] = e;
+                return;
+            }
+            int n64 = (n + 1) / 2;
+            uint64_t *d = limbs64 + offsets[e];
+            for (int i = 0; i < n64; i++) {
+                uint64_t lo = limbs[(int64_t)(2 * i) * ld + e];
+                uint64_t hi = 2 * i + 1 < n ? limbs[(int64_t)(2 * i + 1) * ld + e] : 0u;
+                d[i] = lo | (hi << 32);
+            }
+            sizes64[e] = s < 0 ? -n64 : n64;
         }
-        sizes64[e] = s < 0 ? -n64 : n64;
-    }
+    });
+    for (int t = 0; t < T; t++)
+        if (bad[t] >= 0) return set_error(GBMM_ERR_INVALID, "entry %lld: size exceeds planes", (long long)bad[t]);
     return GBMM_OK;
 }
 

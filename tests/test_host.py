@@ -58,12 +58,14 @@ def test_parse_errors(built_lib):
     assert e.value.status == gbmm.ERR_CAPACITY
 
 
-def test_gmp_limb_import_export(built_lib):
+@pytest.mark.parametrize("extra,threads", [(50, 0), (40000, 4)])
+def test_gmp_limb_import_export(built_lib, extra, threads):
     import gbmm
     L = gbmm.lib()
     rng = random.Random(2)
     vals = [0, -1, 2**64 - 1, -(2**64), 2**95] + [rng.getrandbits(rng.randint(1, 700)) * rng.choice((-1, 1))
-                                                 for _ in range(50)]
+                                                 for _ in range(extra)]
+    old = _threads(gbmm, threads)
     limbs64, offsets, sizes64 = [], [], []
     for v in vals:
         m = abs(v)
@@ -85,6 +87,7 @@ def test_gmp_limb_import_export(built_lib):
     s_back = np.zeros_like(s64)
     gbmm.check(L.gbmm_export_gmp(n, limbs.ctypes.data, sizes.ctypes.data, nl, n, back.ctypes.data, off.ctypes.data,
                                  s_back.ctypes.data))
+    _threads(gbmm, old)
     assert (back == l64).all() and (s_back == s64).all()
 
 
@@ -113,3 +116,46 @@ def test_cli_generate_matches_oracle_generator(built_lib, oracle):
         a = subprocess.run([cli, "-g"] + args, stdout=subprocess.PIPE, check=True).stdout
         b = subprocess.run([ref, "-g"] + args, stdout=subprocess.PIPE, check=True).stdout
         assert a == b
+
+
+def _threads(gbmm, n):
+    f = gbmm.lib().gbmmx_host_threads
+    f.argtypes = [ctypes.c_int32]
+    f.restype = ctypes.c_int32
+    return f(n)
+
+
+def test_parallel_text_and_gmp_conversions_match_serial(built_lib):
+    """Inputs large enough to split across host threads give the same planes,
+    text, errors and consumed offsets as the single-thread path."""
+    import gbmm
+    rng = random.Random(12)
+    vals = [0 if i % 97 == 0 else rng.getrandbits(rng.choice((4, 64, 900, 3000))) * rng.choice((-1, 1))
+            for i in range(36000)]
+    text = " ".join(format(v, "x") if v >= 0 else "-" + format(-v, "x") for v in vals) + "\n"
+    assert len(text) > 7 << 20  # enough for 7 threads of at least 1 MiB each
+    old = _threads(gbmm, 1)
+    try:
+        ref = gbmm.parse_hex(text, len(vals), 100)
+        for n in (2, 3, 7):
+            _threads(gbmm, n)
+            got = gbmm.parse_hex(text, len(vals), 100)
+            assert (got[0] == ref[0]).all() and (got[1] == ref[1]).all() and got[2] == ref[2]
+            assert gbmm.planes_to_ints(got[0], got[1]) == vals
+            assert gbmm.format_hex(got[0], got[1], 360, 100) == gbmm.format_hex(ref[0], ref[1], 360, 100)
+        # errors: a bad byte in the middle, a token too long, a short text
+        bad = text[:len(text) // 2] + "g" + text[len(text) // 2 + 1:]
+        outcomes = []
+        for n in (1, 4):
+            _threads(gbmm, n)
+            res = []
+            for t, count, nl in ((bad, len(vals), 100), (text, len(vals), 50), (text, len(vals) + 5, 100)):
+                try:
+                    gbmm.parse_hex(t, count, nl)
+                    res.append(None)
+                except gbmm.GbmmError as e:
+                    res.append((e.status, str(e)))
+            outcomes.append(res)
+        assert outcomes[0] == outcomes[1] and all(r is not None for r in outcomes[0])
+    finally:
+        _threads(gbmm, old)
