@@ -285,6 +285,9 @@ extern "C" gbmm_status gbmm_autotune(gbmm_handle h, const gbmm_job *jobs, int32_
         float best = 1e30f;
         TuneEntry te{heuristic_path(m, k, n, la, lb), 0, 0.f};
         for (const Cand &cd : cands) {
+            // limb candidates whose schoolbook work predicts far more than any plan needs
+            // (about 50 ms at 4e12 32-bit MAC/s) are not run; their timing stays unknown
+            if (cd.path == GBMM_PATH_LIMB && (double)m * k * n * la * lb > 2e11) continue;
             gbmm_opts o;
             memset(&o, 0, sizeof o);
             o.path = cd.path;

@@ -48,6 +48,12 @@ WORKLOADS = {
     # matrix log-uniform in [64, 16384], 10% zero entries; one batched call
     "cfg4": dict(K=0, M=0, N=0, bits=0, zero=0.1, short=0.0, short_bits=0, cutoff=32, jobs=64,
                  label="64 uneven products: m,n,k log-uniform [16,512], bits log-uniform [64,16384], 10% zeros"),
+    # learned dispatch: jobs drawn as configuration 4 plus rectangular 1024x64x1024
+    # products at bit lengths log-uniform in [256, 8192]; the model trains on the
+    # autotuner's timings of one such stream and dispatches another
+    "cfg5": dict(K=0, M=0, N=0, bits=0, zero=0.1, short=0.0, short_bits=0, cutoff=32, jobs=64, rect=8,
+                 label="learned dispatch: 64 jobs as cfg4 + 8 rectangular 1024x64x1024 at [256,8192] bits; "
+                       "model trained on the autotuner's timings of a separately drawn stream"),
 }
 DEFAULT_WORKLOAD = "cfg3"
 DEFAULT_PATH = "crt"
@@ -443,19 +449,18 @@ def kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof):
             "traffic": None, "peak_source": src, "ms_per_launch": per_ms, "note": note}
 
 
-def run_batched(args, W, world, rank, local):
-    """Configuration 4: many uneven products through one gbmm_matmul_batched
-    call per step (persistent work-queue kernel, CRT jobs, CUDA-graph replay)."""
-    import torch
-    import gbmm
-    torch.cuda.set_device(local)
-    stream = torch.cuda.current_stream()
-    rng = np.random.default_rng(args.seed)
+def gen_jobs(gbmm, W, seed):
+    """Seeded uneven jobs of configuration 4 (and 5's rectangular ones), uploaded:
+    [(C, A, B, host planes...)], total limb-MACs."""
+    rng = np.random.default_rng(seed)
     lu = lambda lo, hi: int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
-    mats, macs = [], 0
+    shapes = []
     for _ in range(W["jobs"]):
-        K, M, N = lu(16, 512), lu(16, 512), lu(16, 512)
-        ba, bb = lu(64, 16384), lu(64, 16384)
+        shapes.append((lu(16, 512), lu(16, 512), lu(16, 512), lu(64, 16384), lu(64, 16384)))
+    for _ in range(W.get("rect", 0)):
+        shapes.append((1024, 64, 1024, lu(256, 8192), lu(256, 8192)))
+    mats, macs = [], 0
+    for K, M, N, ba, bb in shapes:
         Al, As = gen_planes(rng, K * M, ba, W["zero"], 0, 0)
         Bl, Bs = gen_planes(rng, M * N, bb, W["zero"], 0, 0)
         dA, dB = gbmm.DeviceMatrix(K, M, Al.shape[0]), gbmm.DeviceMatrix(M, N, Bl.shape[0])
@@ -464,10 +469,10 @@ def run_batched(args, W, world, rank, local):
         dC = gbmm.DeviceMatrix(K, N, Al.shape[0] + Bl.shape[0] + 2)
         mats.append((dC, dA, dB, (Al, As, Bl, Bs, K, M, N)))
         macs += limb_macs(K, M, N, As, Bs)
-    h = gbmm.Handle()
-    jobs = h.jobs([(c, a, b) for c, a, b, _ in mats])
-    chosen = h.matmul_batched(jobs)
-    torch.cuda.synchronize()
+    return mats, macs
+
+
+def check_jobs(mats, what):
     srng = np.random.default_rng(3)
     for (dC, dA, dB, (Al, As, Bl, Bs, K, M, N)) in mats[:: max(1, len(mats) // 8)]:
         Cl, Cs = dC.download()
@@ -475,7 +480,112 @@ def run_batched(args, W, world, rank, local):
             y, x = int(srng.integers(K)), int(srng.integers(N))
             exp = sum(entry_int(Al, As, y * M + k) * entry_int(Bl, Bs, k * N + x) for k in range(M))
             if entry_int(Cl, Cs, y * N + x) != exp:
-                raise SystemExit("bench: batched product differs from the exact product")
+                raise SystemExit(f"bench: {what} product differs from the exact product")
+
+
+def time_batched(h, jobs, args, flush, stream):
+    """Warm-up (eager, then capture), then K timed graph replays: mean ms per call."""
+    import torch
+    for _ in range(max(args.warmup, 0)):
+        h.matmul_batched(jobs)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.fill_(i)
+        ev[i][0].record(stream)
+        h.matmul_batched(jobs)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / args.steps
+
+
+def run_learned(args, W, world, rank, local):
+    """Configuration 5: the learned cost model against the plain heuristic.  The
+    autotuner times the candidate plans of one seeded stream; the MLP trains on
+    those timings with its own CUDA kernels; a second, separately drawn stream
+    then runs with the heuristic, with the autotuner's table, and with the model."""
+    import tempfile
+    import torch
+    import gbmm
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    train, _ = gen_jobs(gbmm, W, args.seed + 1)
+    ht = gbmm.Handle()
+    tjobs = ht.jobs([(c, a, b) for c, a, b, _ in train])
+    t0 = time.perf_counter()
+    with tempfile.TemporaryDirectory() as td:
+        log = os.path.join(td, "tune.jsonl")
+        ht.autotune(tjobs, repeats=1, log_path=log)
+        rows = [json.loads(l) for l in open(log)]
+    tune_s = time.perf_counter() - t0
+    head = lambda r: 2 if r["path"] == gbmm.PATH_CRT else (0 if r["method"] == gbmm.METHOD_NAIVE else 1)
+    times = {}
+    for r in rows:
+        times.setdefault((r["m"], r["k"], r["n"], r["la"], r["lb"]), [np.nan] * 3)[head(r)] = r["ms"]
+    keys = sorted(times)
+    X = np.stack([gbmm.model_features(m, k, n, la, lb) for (m, k, n, la, lb) in keys])
+    T = np.log2(np.array([times[k] for k in keys], dtype=np.float64)).astype(np.float32)
+    hl = gbmm.Handle()
+    hl.model_init(seed=5)
+    t0 = time.perf_counter()
+    loss = hl.model_train(X, T, epochs=1500, lr=3e-3)
+    train_s = time.perf_counter() - t0
+    hl.model_use(True)
+    del train, tjobs
+    torch.cuda.empty_cache()
+
+    evals, macs = gen_jobs(gbmm, W, args.seed)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device="cuda")
+    hh = gbmm.Handle()
+    res = {}
+    clocks, launches = None, 0
+    for name, h in (("heuristic", hh), ("autotuned", ht), ("learned", hl)):
+        jobs = h.jobs([(c, a, b) for c, a, b, _ in evals])
+        chosen = h.matmul_batched(jobs)
+        torch.cuda.synchronize()
+        check_jobs(evals, name)
+        if name == "learned":
+            sampler = ClockSampler(local)
+            sampler.start()
+            launches0 = gbmm.kernel_launches()
+        ms = max_over_ranks(world, time_batched(h, jobs, args, flush, stream))
+        if name == "learned":
+            launches = gbmm.kernel_launches() - launches0
+            clocks = sampler.stop()
+        res[name] = (ms, {("crt" if p == gbmm.PATH_CRT else "limb"): chosen.count(p) for p in set(chosen)})
+    if rank != 0:
+        return 0
+    ms = res["learned"][0]
+    line = {
+        "metric": "limb-MAC/s", "value": world * macs / (ms * 1e-3), "unit": "limb-MAC/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16+u32", "data": "synthetic",
+        "config": {"workload": W["label"], "seed": args.seed, "limb_macs_per_step": macs,
+                   "ms_per_stream": {k: v[0] for k, v in res.items()},
+                   "paths": {k: v[1] for k, v in res.items()},
+                   "learned_vs_heuristic": res["heuristic"][0] / ms,
+                   "training": {"timings": len(rows), "shapes": len(keys), "autotune_s": tune_s,
+                                "train_s": train_s, "final_loss": loss},
+                   "l2": "flushed between timed steps (512 MiB write)"},
+        "gpu_launches": int(launches), "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batched(args, W, world, rank, local):
+    """Configuration 4: many uneven products through one gbmm_matmul_batched
+    call per step (persistent work-queue kernel, CRT jobs, CUDA-graph replay)."""
+    import torch
+    import gbmm
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    mats, macs = gen_jobs(gbmm, W, args.seed)
+    h = gbmm.Handle()
+    jobs = h.jobs([(c, a, b) for c, a, b, _ in mats])
+    chosen = h.matmul_batched(jobs)
+    torch.cuda.synchronize()
+    check_jobs(mats, "batched")
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device="cuda")
     for _ in range(max(args.warmup, 0)):
         h.matmul_batched(jobs)
@@ -531,17 +641,19 @@ def main():
     ap.add_argument("--bits", type=int, default=0, help="override the entry bit length")
     args = ap.parse_args()
     W = WORKLOADS[args.workload]
-    if (args.size or args.bits) and args.workload != "cfg4":
+    if (args.size or args.bits) and args.workload not in ("cfg4", "cfg5"):
         S = args.size or W["K"]
         b = args.bits or W["bits"]
         W = dict(W, K=S, M=S, N=S, bits=b, label=f"{S}x{S}x{S} {b}-bit signed (resized {args.workload})")
     world, rank, local = dist_init()
     if args.impl == "reference":
-        if args.workload == "cfg4":
+        if args.workload in ("cfg4", "cfg5"):
             return run_reference(args, WORKLOADS["cfg3"], world, rank)
         return run_reference(args, W, world, rank)
     if args.workload == "cfg4":
         return run_batched(args, W, world, rank, local)
+    if args.workload == "cfg5":
+        return run_learned(args, W, world, rank, local)
     return run_gpu(args, W, world, rank, local)
 
 

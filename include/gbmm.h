@@ -228,7 +228,8 @@ gbmm_status gbmm_set_graphs(gbmm_handle h, int32_t enable);
  * gbmm_autotune times candidate plans (limb naive, limb Winograd, CRT) on each
  * job's own buffers (C is overwritten), keeps the fastest per shape class for
  * GBMM_PATH_AUTO, and appends one JSON line per timing to log_path (may be
- * NULL): the timing record the learned cost model trains on.
+ * NULL): the timing record the learned cost model trains on.  Limb candidates
+ * predicted far slower than any plan needs (m k n la lb > 2e11) are skipped.
  * replaces: the fixed BASE_SIZE / TRANSFER_SIZE / GPU_BLK_* tuning constants
  * (mat-gpu/mat-params.h:4-14). */
 gbmm_status gbmm_autotune(gbmm_handle h, const gbmm_job *jobs, int32_t njobs, int32_t repeats,
