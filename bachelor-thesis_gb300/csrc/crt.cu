@@ -445,17 +445,48 @@ struct ProductArgs {
 };
 constexpr int PBX = 64;  // output columns per product tile
 
-template <int STAGES>
+// PAIR: a cluster of two CTAs shares one M = 256 tcgen05.mma.cta_group::2 per K
+// slice (issued by the even CTA): each CTA stages its own 128 rows of A1 and A0,
+// the even CTA U1's 64 rows and the odd CTA U0's, so per SM a K step moves 40 KB
+// instead of 48 KB and the MMAs read 12 KB of shared memory instead of 16 KB.
+template <int STAGES, bool PAIR>
 __global__ void __launch_bounds__(CTA_THREADS8, 1)
     k_crt_product(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, ProductArgs a,
                   uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
-    // A1, A0 (128 rows each), then U1, U0 (64 rows each) = one 128-row B operand
-    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = PBX * 128, STAGE = 2 * A_BYTES + 2 * B_BYTES;
+    constexpr int NP = PAIR ? 2 : 1;
+    // A1, A0 (128 rows each), then U1, U0 (64 rows each; one of them per CTA of a pair):
+    // together the 128-row B operand [U1; U0]
+    constexpr uint32_t A_BYTES = BM * 128, B_BYTES = PBX * 128, STAGE = 2 * A_BYTES + (3 - NP) * B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    cta_setup(bars, STAGES, 512, 1, 8);
+    const uint32_t rank = PAIR ? tc::cluster_rank() : 0;
+    const int64_t t0 = PAIR ? (blockIdx.x >> 1) : blockIdx.x, tstep = PAIR ? (gridDim.x >> 1) : gridDim.x;
+    if (PAIR) {
+        if (threadIdx.x == 0) {
+            for (int s = 0; s < STAGES; s++) {
+                tc::mbar_init(&bars->full[s], 1);
+                tc::mbar_init(&bars->empty[s], 1);
+            }
+            for (int b = 0; b < 2; b++) {
+                tc::mbar_init(&bars->tfull[b], 1);
+                tc::mbar_init(&bars->tempty[b], 16);  // the even CTA's: 8 epilogue warps of each CTA
+            }
+            bars->abort_flag = 0;
+            tc::fence_mbar_init();
+        }
+        if (warp == 1) {
+            tc::tmem_alloc_pair(&bars->tmem_base, 512);
+            tc::tmem_relinquish_pair();
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::cluster_sync_all();  // both CTAs' barriers exist before any cross-CTA signal
+        tc::fence_after_sync();
+    } else {
+        cta_setup(bars, STAGES, 512, 1, 8);
+    }
     const uint32_t tmem = bars->tmem_base;
     const int64_t per_mod = (int64_t)a.nyt * a.nxt;
 
@@ -464,9 +495,9 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             tc::prefetch_tmap(&tmA);
             tc::prefetch_tmap(&tmB);
             int it = 0;
-            for (int64_t t = blockIdx.x; t < a.ntiles && !aborted(bars); t += gridDim.x) {
+            for (int64_t t = t0; t < a.ntiles && !aborted(bars); t += tstep) {
                 const int mi = (int)(t / per_mod), r = (int)(t % per_mod);
-                const int y0 = (r / a.nxt) * BM, x0 = (r % a.nxt) * PBX;
+                const int y0 = (r / a.nxt) * (NP * BM) + (int)rank * BM, x0 = (r % a.nxt) * PBX;
                 for (int s = 0; s < a.nk; s++, it++) {
                     const int st = it % STAGES;
                     if (it >= STAGES && !tc::mbar_wait(&bars->empty[st], ((it / STAGES) & 1) ^ 1)) {
@@ -474,20 +505,29 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                         break;
                     }
                     uint8_t *sa = base + st * STAGE;
-                    tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                    tc::tma_load_2d(sa, &tmA, &bars->full[st], s * BK, (2 * mi) * a.m + y0);
-                    tc::tma_load_2d(sa + A_BYTES, &tmA, &bars->full[st], s * BK, (2 * mi + 1) * a.m + y0);
-                    tc::tma_load_2d(sa + 2 * A_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi) * a.n + x0);
-                    tc::tma_load_2d(sa + 2 * A_BYTES + B_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi + 1) * a.n + x0);
+                    if (PAIR) {
+                        const uint32_t full0 = tc::mapa(tc::smem_u32(&bars->full[st]), 0);
+                        if (rank == 0) tc::mbar_arrive_expect_tx(&bars->full[st], 2 * STAGE);
+                        tc::tma_load_2d_pair(sa, &tmA, full0, s * BK, (2 * mi) * a.m + y0);
+                        tc::tma_load_2d_pair(sa + A_BYTES, &tmA, full0, s * BK, (2 * mi + 1) * a.m + y0);
+                        tc::tma_load_2d_pair(sa + 2 * A_BYTES, &tmB, full0, s * BK, (2 * mi + (int)rank) * a.n + x0);
+                    } else {
+                        tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                        tc::tma_load_2d(sa, &tmA, &bars->full[st], s * BK, (2 * mi) * a.m + y0);
+                        tc::tma_load_2d(sa + A_BYTES, &tmA, &bars->full[st], s * BK, (2 * mi + 1) * a.m + y0);
+                        tc::tma_load_2d(sa + 2 * A_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi) * a.n + x0);
+                        tc::tma_load_2d(sa + 2 * A_BYTES + B_BYTES, &tmB, &bars->full[st], s * BK,
+                                        (2 * mi + 1) * a.n + x0);
+                    }
                 }
             }
         }
     } else if (warp == 1) {
-        if (lane == 0) {
-            const uint32_t idesc = tc::idesc_bf16_f32(BM, 2 * PBX, 0, 0);
+        if (lane == 0 && rank == 0) {
+            const uint32_t idesc = tc::idesc_bf16_f32(NP * BM, 2 * PBX, 0, 0);
             int it = 0, lt = 0;
             bool ok = true;
-            for (int64_t t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x, lt++) {
+            for (int64_t t = t0; t < a.ntiles && ok; t += tstep, lt++) {
                 const int b = lt & 1;
                 if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
                 tc::fence_after_sync();
@@ -500,44 +540,59 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 #pragma unroll
                     for (int kk = 0; kk < BK / UK; kk++) {
                         const uint64_t bdesc = tc::sdesc_kmajor(sb + kk * 32);
-                        tc::mma_bf16(d, tc::sdesc_kmajor(sa + kk * 32), bdesc, idesc, s != 0 || kk != 0);
-                        tc::mma_bf16(d + 2 * PBX, tc::sdesc_kmajor(sa + A_BYTES + kk * 32), bdesc, idesc,
-                                     s != 0 || kk != 0);
+                        const uint64_t a1 = tc::sdesc_kmajor(sa + kk * 32), a0 = tc::sdesc_kmajor(sa + A_BYTES + kk * 32);
+                        if (PAIR) {
+                            tc::mma_bf16_pair(d, a1, bdesc, idesc, s != 0 || kk != 0);
+                            tc::mma_bf16_pair(d + 2 * PBX, a0, bdesc, idesc, s != 0 || kk != 0);
+                        } else {
+                            tc::mma_bf16(d, a1, bdesc, idesc, s != 0 || kk != 0);
+                            tc::mma_bf16(d + 2 * PBX, a0, bdesc, idesc, s != 0 || kk != 0);
+                        }
                     }
-                    tc::mma_commit(&bars->empty[st]);
+                    if (PAIR) tc::mma_commit_pair(&bars->empty[st], 0x3);
+                    else tc::mma_commit(&bars->empty[st]);
                 }
-                if (ok) tc::mma_commit(&bars->tfull[b]);
+                if (ok) {
+                    if (PAIR) tc::mma_commit_pair(&bars->tfull[b], 0x3);
+                    else tc::mma_commit(&bars->tfull[b]);
+                }
             }
         }
     } else {
-        // warp (2..9) -> lane quadrant warp % 4, output columns 32 * ((warp - 2) / 4) + [0, 32)
+        // warp (2..9) -> lane quadrant warp % 4, output columns 32 * ((warp - 2) / 4) + [0, 32).
+        // All four accumulators' 32 columns are read first, so the buffer goes back to the
+        // MMA before the arithmetic.
         const int quad = warp & 3, half = (warp - 2) >> 2;
         const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
+        const uint32_t tempty0 = PAIR ? tc::mapa(tc::smem_u32(&bars->tempty[0]), 0) : 0;
         int lt = 0;
-        for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, lt++) {
+        for (int64_t t = t0; t < a.ntiles; t += tstep, lt++) {
             const int b = lt & 1;
             const int mi = (int)(t / per_mod), r = (int)(t % per_mod);
-            const int y = (r / a.nxt) * BM + quad * 32 + lane;
+            const int y = (r / a.nxt) * (NP * BM) + (int)rank * BM + quad * 32 + lane;
             const int xh = (r % a.nxt) * PBX + half * 32;  // this warp's 32 output columns
             if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); break; }
             tc::fence_after_sync();
+            uint32_t D11[32], D10[32], D01[32], D00[32];
+            const uint32_t col = 256u * b + half * 32;
+            tc::tmem_ld32(lb + col, D11);
+            tc::tmem_ld32(lb + col + PBX, D10);
+            tc::tmem_ld32(lb + col + 2 * PBX, D01);
+            tc::tmem_ld32(lb + col + 3 * PBX, D00);
+            tc::tmem_ld_wait();
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) {
+                if (PAIR) tc::mbar_arrive_cluster(tempty0 + 8u * b);
+                else tc::mbar_arrive(&bars->tempty[b]);
+            }
             const ModConst mc = a.mods[mi];
             const float pf = (float)mc.p;
             const int64_t erow = (int64_t)y * a.n + xh;  // entry index of this warp's first column
             __nv_bfloat16 *yplane = a.Y + (int64_t)(2 * mi) * 64;  // hi plane; lo plane 64 elements on
+#pragma unroll
             for (int c = 0; c < 32; c += 16) {
-                uint32_t d11[16], d10[16], d01[16], d00[16];
-                const uint32_t col = 256u * b + half * 32 + c;
-                tc::tmem_ld16(lb + col, d11);
-                tc::tmem_ld16(lb + col + PBX, d10);
-                tc::tmem_ld16(lb + col + 2 * PBX, d01);
-                tc::tmem_ld16(lb + col + 3 * PBX, d00);
-                tc::tmem_ld_wait();
-                if (c == 16) {
-                    tc::fence_before_sync();
-                    __syncwarp();
-                    if (lane == 0) tc::mbar_arrive(&bars->tempty[b]);
-                }
+                const uint32_t *d11 = D11 + c, *d10 = D10 + c, *d01 = D01 + c, *d00 = D00 + c;
                 uint32_t phi[8], plo[8];
 #pragma unroll
                 for (int j = 0; j < 16; j += 2) {
@@ -577,7 +632,17 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             }
         }
     }
-    cta_teardown(bars, 512);
+    if (PAIR) {
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::cluster_sync_all();  // no CTA leaves while its peer may still signal it or write its TMEM
+        if (warp == 1) {
+            tc::fence_after_sync();
+            tc::tmem_dealloc_pair(tmem, 512);
+        }
+    } else {
+        cta_teardown(bars, 512);
+    }
 }
 
 // ======================================================================================
@@ -1442,6 +1507,8 @@ static constexpr int RES_STAGES = 4, PROD_STAGES = 4, REC_STAGES = 4, TEST_STAGE
 static constexpr int REC_STAGES_T = REC_PAIR ? 6 : REC_STAGES;  // a pair CTA stages 32 KB per K step
 static constexpr bool RES_PAIR = false;  // pair mode measured 0.32 ms vs 0.28 ms per 512^3 launch: the epilogue holds TMEM
 static constexpr int RES_STAGES_T = RES_PAIR ? 6 : RES_STAGES;
+static constexpr bool PROD_PAIR = true;
+static constexpr int PROD_STAGES_T = PROD_PAIR ? 5 : PROD_STAGES;  // a pair CTA stages 40 KB per K step
 
 static int num_sms() {
     static int n = 0;
@@ -1648,14 +1715,20 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)2 * P * n, kp, BK, PBX));
         ProductArgs pa;
         pa.m = m; pa.n = n; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.yblk = (int64_t)2 * t->Pp * 64;
-        pa.nyt = (m + BM - 1) / BM;
+        constexpr int NP = PROD_PAIR ? 2 : 1;
+        pa.nyt = (m + NP * BM - 1) / (NP * BM);
         pa.nxt = (n + PBX - 1) / PBX;
         pa.ntiles = (int64_t)P * pa.nyt * pa.nxt;
-        const size_t sm = smem_bytes(PROD_STAGES, 2 * BM * 128 + 2 * PBX * 128);
-        GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES>, sm));
-        dim3 grid((unsigned)std::min<int64_t>(pa.ntiles, num_sms()));
+        const size_t sm = smem_bytes(PROD_STAGES_T, 2 * BM * 128 + (3 - NP) * PBX * 128);
+        GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES_T, PROD_PAIR>, sm));
         LaunchScope ls_("k_crt_product", s);
-        k_crt_product<PROD_STAGES><<<grid, CTA_THREADS8, sm, s>>>(tmA, tmB, pa, err);
+        if (PROD_PAIR) {
+            GBMM_TRY(launch_pairs(k_crt_product<PROD_STAGES_T, PROD_PAIR>, CTA_THREADS8, pa.ntiles, sm, s, tmA, tmB, pa,
+                                  err));
+        } else {
+            dim3 grid((unsigned)std::min<int64_t>(pa.ntiles, num_sms()));
+            k_crt_product<PROD_STAGES_T, PROD_PAIR><<<grid, CTA_THREADS8, sm, s>>>(tmA, tmB, pa, err);
+        }
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     {
