@@ -674,8 +674,6 @@ struct ReconArgs {
     int64_t cld, crs;
     int32_t cnlimbs;
 };
-constexpr bool REC_PAIR = true;
-
 // Hand-off between the two epilogue warps of a TMEM lane quadrant (per entry slots).
 struct ReconXfer {
     uint64_t to1[4], to0[4], qready[4];  // mbarriers per quadrant: half 0 -> 1, half 1 -> 0, q ready
@@ -1504,11 +1502,11 @@ static gbmm_status get_tables(crt_cache *c, int P, crt_tables **out) {
 }
 
 static constexpr int RES_STAGES = 4, PROD_STAGES = 4, REC_STAGES = 4, TEST_STAGES = 4;
-static constexpr int REC_STAGES_T = REC_PAIR ? 6 : REC_STAGES;  // a pair CTA stages 32 KB per K step
+static constexpr int REC_STAGES_PAIR = 6;  // a pair CTA stages 32 KB per K step
 static constexpr bool RES_PAIR = false;  // pair mode measured 0.32 ms vs 0.28 ms per 512^3 launch: the epilogue holds TMEM
 static constexpr int RES_STAGES_T = RES_PAIR ? 6 : RES_STAGES;
-static constexpr bool PROD_PAIR = true;
-static constexpr int PROD_STAGES_T = PROD_PAIR ? 5 : PROD_STAGES;  // a pair CTA stages 40 KB per K step
+static constexpr int PROD_STAGES_PAIR = 5;  // a pair CTA stages 40 KB per K step
+static constexpr int PROD_PAIR_MIN_NK = 8;  // K steps (of 64) from which the product runs on CTA pairs
 
 static int num_sms() {
     static int n = 0;
@@ -1715,40 +1713,49 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)2 * P * n, kp, BK, PBX));
         ProductArgs pa;
         pa.m = m; pa.n = n; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.yblk = (int64_t)2 * t->Pp * 64;
-        constexpr int NP = PROD_PAIR ? 2 : 1;
+        // CTA pairs pay off once the K loop is long enough to hide the pair's per-tile
+        // synchronisation (measured: faster at k = 512, slower at k = 256)
+        const bool pair = pa.nk >= PROD_PAIR_MIN_NK;
+        const int NP = pair ? 2 : 1;
         pa.nyt = (m + NP * BM - 1) / (NP * BM);
         pa.nxt = (n + PBX - 1) / PBX;
         pa.ntiles = (int64_t)P * pa.nyt * pa.nxt;
-        const size_t sm = smem_bytes(PROD_STAGES_T, 2 * BM * 128 + (3 - NP) * PBX * 128);
-        GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES_T, PROD_PAIR>, sm));
         LaunchScope ls_("k_crt_product", s);
-        if (PROD_PAIR) {
-            GBMM_TRY(launch_pairs(k_crt_product<PROD_STAGES_T, PROD_PAIR>, CTA_THREADS8, pa.ntiles, sm, s, tmA, tmB, pa,
+        if (pair) {
+            const size_t sm = smem_bytes(PROD_STAGES_PAIR, 2 * BM * 128 + PBX * 128);
+            GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES_PAIR, true>, sm));
+            GBMM_TRY(launch_pairs(k_crt_product<PROD_STAGES_PAIR, true>, CTA_THREADS8, pa.ntiles, sm, s, tmA, tmB, pa,
                                   err));
         } else {
+            const size_t sm = smem_bytes(PROD_STAGES, 2 * BM * 128 + 2 * PBX * 128);
+            GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES, false>, sm));
             dim3 grid((unsigned)std::min<int64_t>(pa.ntiles, num_sms()));
-            k_crt_product<PROD_STAGES_T, PROD_PAIR><<<grid, CTA_THREADS8, sm, s>>>(tmA, tmB, pa, err);
+            k_crt_product<PROD_STAGES, false><<<grid, CTA_THREADS8, sm, s>>>(tmA, tmB, pa, err);
         }
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     {
         CUtensorMap tmY, tmT;
         GBMM_TRY(make_map(&tmY, Y, 64, (uint64_t)(Ep / 64) * 2 * t->Pp, 64, 64, BK));
-        constexpr int NP = REC_PAIR ? 2 : 1, TROWS = 256 / NP;
+        // CTA pairs once the K loop over the 2Pp moduli digits is long enough (see the product)
+        const bool pair = 2 * t->Pp / BK >= PROD_PAIR_MIN_NK;
+        const int NP = pair ? 2 : 1, TROWS = 256 / NP;
         GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RTAB, 2 * t->Pp, BK, TROWS));
         ReconArgs ra;
         ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.NT = (SROWS + t->Dout + 255) / 256; ra.Dout = t->Dout;
         ra.vtab = t->d_vtab; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
         ra.cnlimbs = c.nlimbs; ra.kpad = 2 * t->Pp; ra.nmt = (E + NP * BM - 1) / (NP * BM);
-        const size_t sm = smem_bytes(REC_STAGES_T, BM * 128 + TROWS * 128) + (size_t)(t->Dout + 31) / 32 * 32 +
-                          sizeof(ReconXfer) + 64;
-        GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES_T, REC_PAIR>, sm));
+        const size_t extra = (size_t)(t->Dout + 31) / 32 * 32 + sizeof(ReconXfer) + 64;
         LaunchScope ls_("k_crt_recon", s);
-        if (REC_PAIR) {
-            GBMM_TRY(launch_pairs(k_crt_recon<REC_STAGES_T, REC_PAIR>, CTA_THREADS8, ra.nmt, sm, s, tmY, tmT, ra, err));
+        if (pair) {
+            const size_t sm = smem_bytes(REC_STAGES_PAIR, BM * 128 + TROWS * 128) + extra;
+            GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES_PAIR, true>, sm));
+            GBMM_TRY(launch_pairs(k_crt_recon<REC_STAGES_PAIR, true>, CTA_THREADS8, ra.nmt, sm, s, tmY, tmT, ra, err));
         } else {
+            const size_t sm = smem_bytes(REC_STAGES, BM * 128 + TROWS * 128) + extra;
+            GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES, false>, sm));
             dim3 grid((unsigned)std::min<int64_t>(ra.nmt, num_sms()));
-            k_crt_recon<REC_STAGES_T, REC_PAIR><<<grid, CTA_THREADS8, sm, s>>>(tmY, tmT, ra, err);
+            k_crt_recon<REC_STAGES, false><<<grid, CTA_THREADS8, sm, s>>>(tmY, tmT, ra, err);
         }
         GBMM_CUDA_TRY(cudaGetLastError());
     }

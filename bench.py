@@ -639,12 +639,15 @@ def main():
     ap.add_argument("--size", type=int, default=0,
                     help="override K=M=N of a single-product workload (small cases for profiling)")
     ap.add_argument("--bits", type=int, default=0, help="override the entry bit length")
+    ap.add_argument("--shape", default="", help="override K,M,N (C is KxN, inner dimension M)")
     args = ap.parse_args()
     W = WORKLOADS[args.workload]
-    if (args.size or args.bits) and args.workload not in ("cfg4", "cfg5"):
-        S = args.size or W["K"]
+    if (args.size or args.bits or args.shape) and args.workload not in ("cfg4", "cfg5"):
+        K = M = N = args.size or W["K"]
+        if args.shape:
+            K, M, N = (int(x) for x in args.shape.split(","))
         b = args.bits or W["bits"]
-        W = dict(W, K=S, M=S, N=S, bits=b, label=f"{S}x{S}x{S} {b}-bit signed (resized {args.workload})")
+        W = dict(W, K=K, M=M, N=N, bits=b, label=f"{K}x{M}x{N} {b}-bit signed (resized {args.workload})")
     world, rank, local = dist_init()
     if args.impl == "reference":
         if args.workload in ("cfg4", "cfg5"):
