@@ -396,14 +396,14 @@ def crt_params(bits_a, bits_b, k):
     return P, (modbits + 6) // 7 + 2  # base-128 output digits
 
 
-# DRAM bytes (read + write) per launch of each CRT GEMM on 512x512x512 at 4096 bits:
-# one `ncu --set full` capture of the same kernels on 256x256x256 at 4096 bits
-# (profiles/crt_kernels_256x256x256_4096b_ncu.md), times 4 for 4x the entries.
-# The residue figure is the mean of its two launches (A, then B with four planes).
+# DRAM bytes (read + write) per launch of each CRT GEMM on 512x512x512 at 4096 bits,
+# from a one-pass ncu capture of this workload (dram__bytes_read.sum +
+# dram__bytes_write.sum; profiles/crt_512x512x512_4096b_dram_bytes.md).  The residue
+# figure is the mean of its two launches (A, then B).
 NCU_DRAM_BYTES_512_4096 = {
-    "k_crt_residue": 4 * (152.548e6 + 284.571e6) / 2,
-    "k_crt_product": 4 * 508.851e6,
-    "k_crt_recon": 4 * 198.109e6,
+    "k_crt_residue": (270.619136e6 + 487.326464e6 + 270.627584e6 + 487.481088e6) / 2,
+    "k_crt_product": 1083.063808e6 + 507.890176e6,
+    "k_crt_recon": 586.745088e6 + 241.935104e6,
 }
 FIXED_POINT_COLUMNS = 14  # reconstruction columns that carry the 2^96 / p_i weights
 
@@ -434,7 +434,7 @@ def kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof):
         traffic = None
         if (K, M, N, W["bits"]) == (512, 512, 512, 4096) and kname in NCU_DRAM_BYTES_512_4096:
             traffic = NCU_DRAM_BYTES_512_4096[kname]
-            note += "; traffic: ncu DRAM bytes of the 256^3 capture x 4"
+            note += "; traffic: one-pass ncu DRAM bytes of this launch at 512^3"
         return {"kernel": kname, "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
                 "frac": ach / bf16, "traffic": traffic, "peak_source": src + " (bf16 dense, burst)",
                 "ms_per_launch": per_ms, "note": note}
