@@ -152,6 +152,8 @@ struct gbmm_handle_s {
     void *batch = nullptr;
     // host-buffer pipeline: copy streams, two device slots (pipeline.cpp)
     void *pipe = nullptr;
+    // device bytes a host-buffer product may use before it runs out of core (0: free memory)
+    size_t dev_budget = 0;
 };
 
 namespace gbmm {

@@ -11,11 +11,23 @@
 // The reference moves whole matrices host <-> device around each product with
 // blocking copies (mat-gpu/mat-pregpu.cu:10-96, transfer_recurse); this is the
 // overlapped replacement for a stream of independent products.
+//
+// A product whose device footprint exceeds the handle's device budget (free
+// memory by default) runs out of core: C is cut into row x column blocks and the
+// inner dimension into chunks; each block accumulates its chunk products on the
+// device (C_blk += A_rows,chunk * B_chunk,cols) and goes back to the host once.
+// Sub-blocks move with 2-D copies straight from and to the host planes, two A/B
+// slots and two C blocks keep copies and compute overlapped.  The reference
+// recurses on the host instead (Winograd above 512, mat-gpu/mat-pregpu.cu:273-467,
+// with additions on host memory); here the host only moves blocks and every
+// addition happens on the device.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <vector>
 
 #include "gbmm_internal.h"
 
@@ -93,6 +105,147 @@ gbmm_mat view(int32_t rows, int32_t cols, int32_t nl, uint32_t *limbs, int32_t *
     m.sizes = sizes;
     return m;
 }
+std::atomic<int64_t> g_last_blocks{0};  // block products of the last out-of-core call (test hook)
+
+// host sub-block (rows r0.., cols c0..) of dense planes with plane stride hld and
+// row stride hrs <-> dense device planes (rows x cols per plane)
+gbmm_status copy_block(uint32_t *dev, uint32_t *host, int64_t hld, int64_t hrs, int r0, int c0, int rows, int cols,
+                       int nl, bool up, cudaStream_t s) {
+    if (!rows || !cols) return GBMM_OK;
+    for (int i = 0; i < nl; i++) {
+        uint32_t *d = dev + (int64_t)i * rows * cols, *hp = host + (int64_t)i * hld + (int64_t)r0 * hrs + c0;
+        const cudaError_t e =
+            up ? cudaMemcpy2DAsync(d, (size_t)cols * 4, hp, (size_t)hrs * 4, (size_t)cols * 4, rows, cudaMemcpyHostToDevice, s)
+               : cudaMemcpy2DAsync(hp, (size_t)hrs * 4, d, (size_t)cols * 4, (size_t)cols * 4, rows, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return cuda_error(e, "cudaMemcpy2DAsync");
+    }
+    return GBMM_OK;
+}
+
+gbmm_opts job_opts(const gbmm_host_job &q) {
+    gbmm_opts o;
+    memset(&o, 0, sizeof o);
+    o.path = q.path;
+    o.method = q.method ? q.method : GBMM_METHOD_WINOGRAD;
+    o.cutoff = q.cutoff;
+    o.nprimes = q.nprimes;
+    return o;
+}
+
+// device bytes of one block step: two A and B slots, two C blocks, the product's workspace
+size_t block_footprint(gbmm_handle h, const gbmm_host_job &q, int kb, int mt, int nb) {
+    gbmm_mat A = view(kb, mt, q.a_nlimbs, nullptr, nullptr), B = view(mt, nb, q.b_nlimbs, nullptr, nullptr);
+    Plan p;
+    gbmm_opts o = job_opts(q);
+    if (resolve_plan(h, A, B, o, p) != GBMM_OK) return (size_t)-1;
+    const size_t ws = dispatch_ws(p, q.a_nlimbs, q.b_nlimbs, kb, mt, nb, q.c_nlimbs, 1);
+    return 2 * 4 * ((size_t)kb * mt * (q.a_nlimbs + 1) + (size_t)mt * nb * (q.b_nlimbs + 1) +
+                    (size_t)kb * nb * (q.c_nlimbs + 1)) +
+           ws + ((size_t)4 << 20);
+}
+
+size_t device_budget(gbmm_handle h) {
+    if (h->dev_budget) return h->dev_budget;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return (size_t)-1;
+    return fr / 10 * 9 + h->ws.cap;  // the arena can be reused
+}
+
+// One product too large for the device, in blocks (see the file comment).
+gbmm_status run_blocked(gbmm_handle h, PipeState &ps, gbmm_host_job &q, size_t budget) {
+    int kb = q.K, mt = q.M, nb = q.N;
+    while (block_footprint(h, q, kb, mt, nb) > budget) {
+        int *d = &kb;
+        if (nb > *d) d = &nb;
+        if (mt > *d) d = &mt;
+        if (*d <= 16) return set_error(GBMM_ERR_NOMEM, "product does not fit the device budget even in 16x16x16 blocks");
+        *d = (*d + 1) / 2;
+    }
+    const int la = q.a_nlimbs, lb = q.b_nlimbs, lc = q.c_nlimbs;
+    {
+        gbmm_mat A = view(kb, mt, la, nullptr, nullptr), B = view(mt, nb, lb, nullptr, nullptr);
+        Plan p;
+        gbmm_opts o = job_opts(q);
+        GBMM_TRY(resolve_plan(h, A, B, o, p));
+        q.chosen_path = p.path;
+    }
+    struct Bufs {
+        uint32_t *a[2] = {}, *b[2] = {}, *c[2] = {};
+        int32_t *as[2] = {}, *bs[2] = {}, *cs[2] = {};
+        cudaEvent_t up[2] = {}, comp[2] = {}, down[2] = {}, cdone = nullptr;
+    } bf;
+    gbmm_status st = GBMM_OK;
+    auto alloc = [&](void **p, size_t n) {
+        if (st == GBMM_OK && cudaMalloc(p, std::max<size_t>(n, 256)) != cudaSuccess)
+            st = set_error(GBMM_ERR_NOMEM, "out-of-core block buffers");
+    };
+    for (int i = 0; i < 2; i++) {
+        alloc((void **)&bf.a[i], (size_t)kb * mt * la * 4);
+        alloc((void **)&bf.b[i], (size_t)mt * nb * lb * 4);
+        alloc((void **)&bf.c[i], (size_t)kb * nb * lc * 4);
+        alloc((void **)&bf.as[i], (size_t)kb * mt * 4);
+        alloc((void **)&bf.bs[i], (size_t)mt * nb * 4);
+        alloc((void **)&bf.cs[i], (size_t)kb * nb * 4);
+        if (st == GBMM_OK) st = ck(cudaEventCreateWithFlags(&bf.up[i], cudaEventDisableTiming), "cudaEventCreate");
+        if (st == GBMM_OK) st = ck(cudaEventCreateWithFlags(&bf.comp[i], cudaEventDisableTiming), "cudaEventCreate");
+        if (st == GBMM_OK) st = ck(cudaEventCreateWithFlags(&bf.down[i], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    if (st == GBMM_OK) st = ck(cudaEventCreateWithFlags(&bf.cdone, cudaEventDisableTiming), "cudaEventCreate");
+    const gbmm_opts o0 = job_opts(q);
+    int64_t blk = 0, cblk = 0;
+    for (int r0 = 0; r0 < q.K && st == GBMM_OK; r0 += kb) {
+        for (int c0 = 0; c0 < q.N && st == GBMM_OK; c0 += nb, cblk++) {
+            const int kr = std::min(kb, q.K - r0), nc = std::min(nb, q.N - c0), cs = (int)(cblk & 1);
+            // the C block is free once its previous contents reached the host
+            st = ck(cudaStreamWaitEvent(h->stream, bf.down[cs], 0), "cudaStreamWaitEvent");
+            for (int t0 = 0; st == GBMM_OK && (t0 < q.M || t0 == 0); t0 += mt, blk++) {
+                const int mk = std::min(mt, q.M - t0), s = (int)(blk & 1);
+                st = ck(cudaStreamWaitEvent(ps.up, bf.comp[s], 0), "cudaStreamWaitEvent");
+                if (st == GBMM_OK)
+                    st = copy_block(bf.a[s], const_cast<uint32_t *>(q.a_limbs), (int64_t)q.K * q.M, q.M, r0, t0, kr, mk,
+                                    la, true, ps.up);
+                if (st == GBMM_OK)
+                    st = copy_block((uint32_t *)bf.as[s], (uint32_t *)const_cast<int32_t *>(q.a_sizes), 0, q.M, r0, t0,
+                                    kr, mk, 1, true, ps.up);
+                if (st == GBMM_OK)
+                    st = copy_block(bf.b[s], const_cast<uint32_t *>(q.b_limbs), (int64_t)q.M * q.N, q.N, t0, c0, mk, nc,
+                                    lb, true, ps.up);
+                if (st == GBMM_OK)
+                    st = copy_block((uint32_t *)bf.bs[s], (uint32_t *)const_cast<int32_t *>(q.b_sizes), 0, q.N, t0, c0,
+                                    mk, nc, 1, true, ps.up);
+                if (st == GBMM_OK) st = ck(cudaEventRecord(bf.up[s], ps.up), "cudaEventRecord");
+                if (st == GBMM_OK) st = ck(cudaStreamWaitEvent(h->stream, bf.up[s], 0), "cudaStreamWaitEvent");
+                if (st != GBMM_OK) break;
+                gbmm_opts o = o0;
+                o.accumulate = t0 > 0;
+                st = gbmm_matmul(h, view(kr, nc, lc, bf.c[cs], bf.cs[cs]), view(kr, mk, la, bf.a[s], bf.as[s]),
+                                 view(mk, nc, lb, bf.b[s], bf.bs[s]), &o);
+                if (st == GBMM_OK) st = ck(cudaEventRecord(bf.comp[s], h->stream), "cudaEventRecord");
+                if (q.M == 0) break;
+            }
+            // the finished block goes back to the host on the download stream
+            if (st == GBMM_OK) st = ck(cudaEventRecord(bf.cdone, h->stream), "cudaEventRecord");
+            if (st == GBMM_OK) st = ck(cudaStreamWaitEvent(ps.down, bf.cdone, 0), "cudaStreamWaitEvent");
+            if (st == GBMM_OK) st = copy_block(bf.c[cs], q.c_limbs, (int64_t)q.K * q.N, q.N, r0, c0, kr, nc, lc, false, ps.down);
+            if (st == GBMM_OK)
+                st = copy_block((uint32_t *)bf.cs[cs], (uint32_t *)q.c_sizes, 0, q.N, r0, c0, kr, nc, 1, false, ps.down);
+            if (st == GBMM_OK) st = ck(cudaEventRecord(bf.down[cs], ps.down), "cudaEventRecord");
+        }
+    }
+    cudaStreamSynchronize(ps.up);
+    cudaStreamSynchronize(h->stream);
+    cudaStreamSynchronize(ps.down);
+    for (int i = 0; i < 2; i++) {
+        cudaFree(bf.a[i]); cudaFree(bf.b[i]); cudaFree(bf.c[i]);
+        cudaFree(bf.as[i]); cudaFree(bf.bs[i]); cudaFree(bf.cs[i]);
+        if (bf.up[i]) cudaEventDestroy(bf.up[i]);
+        if (bf.comp[i]) cudaEventDestroy(bf.comp[i]);
+        if (bf.down[i]) cudaEventDestroy(bf.down[i]);
+    }
+    if (bf.cdone) cudaEventDestroy(bf.cdone);
+    g_last_blocks += blk;
+    return st;
+}
 }  // namespace
 
 void pipe_destroy(gbmm_handle h) {
@@ -122,10 +275,17 @@ extern "C" gbmm_status gbmm_matmul_host(gbmm_handle h, gbmm_host_job *jobs, int3
     for (int j = 0; j < njobs; j++) GBMM_TRY(check_job(jobs[j], j));
     GBMM_TRY(pipe_init(h));
     PipeState &ps = *pstate(h);
+    g_last_blocks = 0;
 
-    // size both slots for the largest job; nothing may be in flight while they grow
+    // products whose two-slot footprint exceeds the device budget run out of core
+    const size_t budget = device_budget(h);
+    std::vector<char> blocked(njobs, 0);
+    for (int j = 0; j < njobs; j++) blocked[j] = block_footprint(h, jobs[j], jobs[j].K, jobs[j].M, jobs[j].N) > budget;
+
+    // size both slots for the largest in-core job; nothing may be in flight while they grow
     size_t an = 0, bn = 0, cn = 0, en = 1;
     for (int j = 0; j < njobs; j++) {
+        if (blocked[j]) continue;
         const gbmm_host_job &q = jobs[j];
         an = std::max(an, (size_t)q.a_nlimbs * q.K * q.M * 4);
         bn = std::max(bn, (size_t)q.b_nlimbs * q.M * q.N * 4);
@@ -155,6 +315,14 @@ extern "C" gbmm_status gbmm_matmul_host(gbmm_handle h, gbmm_host_job *jobs, int3
     gbmm_status st = GBMM_OK;
     for (int j = 0; j < njobs && st == GBMM_OK; j++) {
         gbmm_host_job &q = jobs[j];
+        if (blocked[j]) {
+            // drain the in-core pipeline, then run this product in blocks
+            st = ck(cudaStreamSynchronize(ps.up), "upload stream");
+            if (st == GBMM_OK) st = ck(cudaStreamSynchronize(h->stream), "compute stream");
+            if (st == GBMM_OK) st = ck(cudaStreamSynchronize(ps.down), "download stream");
+            if (st == GBMM_OK) st = run_blocked(h, ps, q, budget);
+            continue;
+        }
         PipeSlot &s = ps.slot[j & 1];
         const size_t ea = (size_t)q.K * q.M, eb = (size_t)q.M * q.N, ec = (size_t)q.K * q.N;
         // uploads: the slot's operands are free once the compute two jobs back has run
@@ -203,3 +371,13 @@ extern "C" gbmm_status gbmm_matmul_host(gbmm_handle h, gbmm_host_job *jobs, int3
     GBMM_TRY(ck(e3, "download stream"));
     return check_device_error(h->stream);
 }
+
+extern "C" gbmm_status gbmm_set_device_budget(gbmm_handle h, uint64_t bytes) {
+    if (!h) return set_error(GBMM_ERR_INVALID, "null handle");
+    h->dev_budget = (size_t)bytes;
+    return GBMM_OK;
+}
+
+// Internal test hook (not part of the public ABI): block products run out of core by
+// the last gbmm_matmul_host call.
+extern "C" int64_t gbmmx_host_blocks(void) { return g_last_blocks.load(); }

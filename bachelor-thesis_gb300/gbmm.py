@@ -84,6 +84,7 @@ _SIGS = {
     "gbmm_matmul_batched": [_P, ctypes.POINTER(Job), ctypes.c_int32, ctypes.POINTER(Opts)],
     "gbmm_set_graphs": [_P, ctypes.c_int32],
     "gbmm_matmul_host": [_P, ctypes.POINTER(HostJob), ctypes.c_int32],
+    "gbmm_set_device_budget": [_P, ctypes.c_uint64],
     "gbmm_autotune": [_P, ctypes.POINTER(Job), ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p],
     "gbmm_tune_save": [_P, ctypes.c_char_p],
     "gbmm_tune_load": [_P, ctypes.c_char_p],
@@ -368,6 +369,10 @@ class Handle:
             q.c_limbs, q.c_sizes = Cl.ctypes.data, Cs.ctypes.data
             q.path, q.method, q.cutoff = path, method, cutoff
         return arr
+
+    def set_device_budget(self, nbytes):
+        """Device bytes a host-buffer product may use before it runs out of core (0: free memory)."""
+        check(lib().gbmm_set_device_budget(self.h, int(nbytes)))
 
     def matmul_host(self, jobs):
         """Runs a ctypes array of gbmm_host_job (pipelined host <-> device copies);

@@ -220,6 +220,14 @@ typedef struct gbmm_host_job {
  * (mat-gpu/mat-pregpu.cu:10-96, transfer_recurse; mat-gpu/main.cu:362-381). */
 gbmm_status gbmm_matmul_host(gbmm_handle h, gbmm_host_job *jobs, int32_t njobs);
 
+/* Device memory a gbmm_matmul_host product may use (0, the default: 90% of the free
+ * memory plus the handle's workspace).  A product that needs more runs out of core:
+ * C in row x column blocks, the inner dimension in chunks accumulated on the device,
+ * sub-blocks copied straight from and to the host planes.
+ * replaces: the host-level recursion above the GPU's memory
+ * (mat-gpu/mat-pregpu.cu:273-467). */
+gbmm_status gbmm_set_device_budget(gbmm_handle h, uint64_t bytes);
+
 /* Turns CUDA-graph capture and replay of batches on (default) or off.
  * No counterpart in the reference. */
 gbmm_status gbmm_set_graphs(gbmm_handle h, int32_t enable);

@@ -83,3 +83,27 @@ def test_host_jobs_pinned_buffers(g):
     h.matmul_host(jobs)
     assert g.planes_to_ints(pC, pCs) == exp
     h.close()
+
+
+def test_host_jobs_out_of_core(g):
+    """A device budget below the products' in-core footprint makes gbmm_matmul_host
+    run them in blocks (C tiles, inner chunks accumulated on the device), mixed with
+    in-core jobs in one call."""
+    import ctypes
+    rng = random.Random(31)
+    big = [_spec(g, rng, 150, 130, 110, 1500, 1200), _spec(g, rng, 40, 300, 20, 64, 700)]
+    small = [_spec(g, rng, 8, 8, 8, 64, 64)]
+    h = g.Handle()
+    h.set_device_budget(20 << 20)  # the in-core footprints are 34 MB (limb) and 82 MB (CRT) for the first job
+    f = g.lib().gbmmx_host_blocks
+    f.restype = ctypes.c_int64
+    for path in (g.PATH_AUTO, g.PATH_CRT, g.PATH_LIMB):
+        for spec, _ in big + small:
+            spec[5][0][:] = 0
+            spec[5][1][:] = 0
+        specs = [big[0], small[0], big[1]]
+        h.matmul_host(h.host_jobs([b[0] for b in specs], path=path))
+        assert f() >= 2, f()  # at least one job ran as two or more block products
+        for spec, exp in specs:
+            assert g.planes_to_ints(spec[5][0], spec[5][1]) == exp, (spec[:3], path)
+    h.close()
