@@ -36,7 +36,7 @@ typedef enum gbmm_status {
     GBMM_ERR_PARSE = 4,       /* malformed hexadecimal matrix text */
     GBMM_ERR_NOMEM = 5,       /* host or device allocation failed */
     GBMM_ERR_TIMEOUT = 6,     /* a bounded device-side wait gave up */
-    GBMM_ERR_UNSUPPORTED = 7  /* the request is valid but this build cannot run it */
+    GBMM_ERR_UNSUPPORTED = 7  /* the request is valid but the library cannot run it */
 } gbmm_status;
 
 /* A device matrix view in limb planes (see the file comment). */

@@ -1,7 +1,7 @@
 /*
  * oracle.c -- CPU oracle for gbmm.  TEST INFRASTRUCTURE ONLY: the parity
- * tests, the smoke check and the CPU-baseline leg of the benchmark load it as
- * the checker.  No product code path calls it.
+ * tests, the smoke check and the CPU-baseline leg of the benchmark load it to
+ * compute expected results.  No product code path calls it.
  *
  * It restates, in plain C, the reference's CPU algorithm for exact signed
  * big-integer matrix multiplication (tomsmeding/bachelor-thesis, mat-cpu/):
@@ -18,7 +18,7 @@
  *   - "own": a restatement of GMP's published mpz semantics (sign-magnitude,
  *     normalized sizes) with schoolbook and Karatsuba products on 64-bit limbs;
  *   - "gmp": the system libgmp.so.10 loaded with dlopen, used only as a second
- *     checker and as the CPU baseline when present.
+ *     reference for the tests and as the CPU baseline when present.
  * Batched mpn restatements on 32-bit limbs (add_n, sub_n, mul_1, addmul_1,
  * submul_1, mul_basecase, toom22) mirror the device layer's semantics
  * (GMP's mpn contract) for operation-level tests.
