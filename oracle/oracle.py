@@ -1,6 +1,6 @@
 """ctypes binding of the CPU oracle (oracle.c).  TEST INFRASTRUCTURE ONLY:
 imported by tests/, the smoke check and the benchmark's CPU-baseline leg as the
-checker; never by the product path.
+reference for expected results; never by the product path.
 
 The oracle restates the reference's mat-cpu algorithm (tomsmeding/bachelor-thesis,
 mat-cpu/mat.c, matj.c) over a GMP-semantics big-integer restatement; see the
