@@ -54,6 +54,8 @@ constexpr int SUSED = 14;       // of which the fixed-point sum uses the first 1
 constexpr int FIXB = 96;        // fixed-point bits of the 1/p_i weights
 constexpr int CTA_THREADS = 192;   // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
 constexpr int CTA_THREADS8 = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue (two per lane quadrant)
+constexpr int RES_EPI_WARPS = 16;   // residue GEMM: four epilogue warps per lane quadrant
+constexpr int RES_THREADS = 32 * (2 + RES_EPI_WARPS);
 constexpr int RTAB = 256;          // reconstruction table rows are padded to a multiple of this
 }  // namespace
 
@@ -78,6 +80,12 @@ struct ModConst {
 // The second FMA is exact because the true result is a small integer.
 // Downstream bounds use |red(x)| <= 32772.
 constexpr float RND_MAGIC = 12582912.0f;  // 1.5 * 2^23
+
+// (p, fl(1/p)) of moduli 2i and 2i+1 for the 1024 largest primes below 2^16, in
+// descending order: the moduli of every product are a prefix of this list.  Warps
+// read one modulus at a time (a constant-cache broadcast, no shared-memory traffic).
+constexpr int CMOD_PAIRS = 512;
+__constant__ float4 c_modpair[CMOD_PAIRS];
 __device__ __forceinline__ float red(float x, float p, float inv_p) {
     const float q = __fadd_rn(__fmaf_rn(x, inv_p, RND_MAGIC), -RND_MAGIC);
     return __fmaf_rn(-q, p, x);
@@ -158,8 +166,11 @@ __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: 
 // ======================================================================================
 // 1. digits
 // ======================================================================================
+// The digits carry the entry's sign (a negative entry's digits are negated), so
+// the residue GEMM yields signed residues directly.
 struct DigitArgs {
     const uint32_t *limbs;
+    const int32_t *sizes;  // sizes[r * rs + c]: the entry's sign
     int64_t ld, rs;
     int32_t rows, cols, nlimbs;
     int32_t transpose;  // 0: out row r*cols + c ; 1: out row c*rows + r
@@ -169,10 +180,15 @@ struct DigitArgs {
 
 __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
     __shared__ uint32_t s[128][65];
+    __shared__ uint32_t sflip[128];  // 0x80008000 for a negative entry: flips both bf16 signs of a word
     const int tr = 4, tcn = 32;
     const int r0 = blockIdx.y * tr, c0 = blockIdx.x * tcn;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nchunk = (a.dxp / 4 + 63) / 64;
+    if (threadIdx.x < 128) {
+        const int r = r0 + (threadIdx.x >> 5), c = c0 + (threadIdx.x & 31);
+        sflip[threadIdx.x] = (r < a.rows && c < a.cols && a.sizes[(int64_t)r * a.rs + c] < 0) ? 0x80008000u : 0u;
+    }
     for (int ch = 0; ch < nchunk; ch++) {
         const int l0 = ch * 64;
         __syncthreads();
@@ -198,11 +214,12 @@ __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
             __nv_bfloat162 p1 = __floats2bfloat162_rn((float)((v0 >> 16) & 255u), (float)(v0 >> 24));
             __nv_bfloat162 p2 = __floats2bfloat162_rn((float)(v1 & 255u), (float)((v1 >> 8) & 255u));
             __nv_bfloat162 p3 = __floats2bfloat162_rn((float)((v1 >> 16) & 255u), (float)(v1 >> 24));
+            const uint32_t flip = sflip[ent];
             uint4 pk;
-            pk.x = *reinterpret_cast<uint32_t *>(&p0);
-            pk.y = *reinterpret_cast<uint32_t *>(&p1);
-            pk.z = *reinterpret_cast<uint32_t *>(&p2);
-            pk.w = *reinterpret_cast<uint32_t *>(&p3);
+            pk.x = *reinterpret_cast<uint32_t *>(&p0) ^ flip;
+            pk.y = *reinterpret_cast<uint32_t *>(&p1) ^ flip;
+            pk.z = *reinterpret_cast<uint32_t *>(&p2) ^ flip;
+            pk.w = *reinterpret_cast<uint32_t *>(&p3) ^ flip;
             *reinterpret_cast<uint4 *>(a.out + row * a.dxp + dg) = pk;
         }
     }
@@ -213,41 +230,60 @@ __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
 //    the next tile's MMAs; 8 epilogue warps, two per TMEM lane quadrant)
 // ======================================================================================
 struct ResidueArgs {
-    const int32_t *sizes;  // sizes of the source matrix (for the entry signs)
-    int64_t rs;
-    int32_t transpose, kdim;  // entry e -> (e / kdim, e % kdim) in digit-row order
-    int64_t E;                // entries (digit rows)
-    int32_t nk;               // K steps of 64 digits
-    int32_t BN, G;            // table columns per tile, accumulation groups (G * BN <= 256)
+    int32_t kdim;  // entry e -> (e / kdim, e % kdim) in digit-row order
+    int32_t E;     // entries (digit rows)
+    int32_t nk;    // K steps of 64 digits
+    int32_t BN, G; // table columns per tile, accumulation groups (G * BN <= 256)
     int32_t P;
-    int32_t ncols;            // 2P table columns
+    int32_t ncols;  // 2P table columns
     int32_t n_ntiles;
-    int64_t ntiles;
+    int32_t ntiles;
     const ModConst *mods;
     __nv_bfloat16 *R;  // planes [2P][rowsR][kp]
     int64_t plane;     // rowsR * kp
     int32_t kp;
+    int32_t tma_out;  // kdim % 32 == 0: each warp's 32 entries share a plane row; TMA stores
 };
+
+// shared-memory staging of one epilogue warp's chunk: [32 planes][32 entries] bf16
+constexpr int RES_STG_BYTES = 32 * 32 * 2;
+
+// One chunk of 32 accumulator columns (16 moduli, two table columns each) of
+// group g folded into res: res_j = red(256 red(s1) + red(s0) (+ res_j)).
+// Each term is an integer of magnitude <= 2^24; the sum stays below
+// 257 * 32772 + 32772 < 2^24, so every FP32 step is exact.
+__device__ __forceinline__ void residue_fold(const uint32_t (&v)[32], int mi0, bool first, float (&res)[16]) {
+#pragma unroll
+    for (int j = 0; j < 16; j += 2) {
+        const float4 pc = c_modpair[(mi0 + j) >> 1];  // (p, 1/p) of moduli mi0 + j, mi0 + j + 1
+        float t0 = __fmaf_rn(256.f, red(__uint_as_float(v[2 * j + 1]), pc.x, pc.y),
+                             red(__uint_as_float(v[2 * j]), pc.x, pc.y));
+        float t1 = __fmaf_rn(256.f, red(__uint_as_float(v[2 * j + 3]), pc.z, pc.w),
+                             red(__uint_as_float(v[2 * j + 2]), pc.z, pc.w));
+        if (!first) {
+            t0 += res[j];
+            t1 += res[j + 1];
+        }
+        res[j] = red(t0, pc.x, pc.y);
+        res[j + 1] = red(t1, pc.z, pc.w);
+    }
+}
 
 // PAIR: a cluster of two CTAs shares one M = 256 tcgen05.mma.cta_group::2 per K
 // slice (issued by the even CTA); each CTA stages its own 128 entries and half of
 // the tile's table columns, and keeps its own 128 rows of D in its TMEM.
 template <int STAGES, bool PAIR>
-__global__ void __launch_bounds__(CTA_THREADS8, 1)
-    k_crt_residue(const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmT, ResidueArgs a,
-                  uint32_t *err) {
+__global__ void __launch_bounds__(RES_THREADS, 1)
+    k_crt_residue(const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmT,
+                  const __grid_constant__ CUtensorMap tmR, ResidueArgs a, uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
     constexpr int NP = PAIR ? 2 : 1;
+    constexpr int NBUF = PAIR ? 2 : 1;  // staging buffers per epilogue warp
     const uint32_t A_BYTES = BM * 128, B_BYTES = (uint32_t)(a.BN / NP) * 128, STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
-    // (p, 1/p) per modulus, padded to a multiple of 16 with the last modulus
-    float2 *smod = reinterpret_cast<float2 *>(reinterpret_cast<uint8_t *>(bars) + SMEM_BARS);
+    uint8_t *stage_out = reinterpret_cast<uint8_t *>(bars) + SMEM_BARS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = threadIdx.x; i < (a.P + 15) / 16 * 16; i += blockDim.x) {
-        const ModConst mc = a.mods[i < a.P ? i : a.P - 1];
-        smod[i] = make_float2((float)mc.p, mc.inv_p);
-    }
     const uint32_t rank = PAIR ? tc::cluster_rank() : 0;
     const int64_t t0 = PAIR ? (blockIdx.x >> 1) : blockIdx.x, tstep = PAIR ? (gridDim.x >> 1) : gridDim.x;
     if (PAIR) {
@@ -258,7 +294,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             }
             for (int b = 0; b < 2; b++) {
                 tc::mbar_init(&bars->tfull[b], 1);
-                tc::mbar_init(&bars->tempty[b], 16);  // the even CTA's: 8 epilogue warps of each CTA
+                tc::mbar_init(&bars->tempty[b], 2 * RES_EPI_WARPS);  // the even CTA's: every epilogue warp of both CTAs
             }
             bars->abort_flag = 0;
             tc::fence_mbar_init();
@@ -272,7 +308,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         tc::cluster_sync_all();  // both CTAs' barriers exist before any cross-CTA signal
         tc::fence_after_sync();
     } else {
-        cta_setup(bars, STAGES, 512, 1, 8);
+        cta_setup(bars, STAGES, 512, 1, RES_EPI_WARPS);
     }
     const uint32_t tmem = bars->tmem_base;
     // the last table tile may be narrow: its MMA has only the columns it needs
@@ -284,9 +320,10 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             tc::prefetch_tmap(&tmD);
             tc::prefetch_tmap(&tmT);
             int it = 0;
-            for (int64_t t = t0; t < a.ntiles && !aborted(bars); t += tstep) {
-                const int64_t e0 = (t / a.n_ntiles) * (NP * BM) + rank * BM;
-                const int n0 = (int)(t % a.n_ntiles) * a.BN;
+            for (int t = (int)t0; t < a.ntiles && !aborted(bars); t += (int)tstep) {
+                const int rb = t / a.n_ntiles;
+                const int e0 = rb * (NP * BM) + (int)rank * BM;
+                const int n0 = (t - rb * a.n_ntiles) * a.BN;
                 const int nn = min(a.BN, (a.ncols - n0 + ngran - 1) / ngran * ngran);
                 for (int s = 0; s < a.nk; s++, it++) {
                     const int st = it % STAGES;
@@ -313,9 +350,9 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         if (lane == 0 && rank == 0) {
             int it = 0, lt = 0;
             bool ok = true;
-            for (int64_t t = t0; t < a.ntiles && ok; t += tstep, lt++) {
+            for (int t = (int)t0; t < a.ntiles && ok; t += (int)tstep, lt++) {
                 const int b = lt & 1;
-                const int n0 = (int)(t % a.n_ntiles) * a.BN;
+                const int n0 = (t % a.n_ntiles) * a.BN;
                 const int nn = min(a.BN, (a.ncols - n0 + ngran - 1) / ngran * ngran);
                 const uint32_t idesc = tc::idesc_bf16_f32(NP * BM, nn, 0, 0);
                 if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
@@ -342,72 +379,120 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             }
         }
     } else {
-        // epilogue: warp (2..9) -> lane quadrant warp % 4, column half (warp - 2) / 4
-        const int quad = warp & 3, half = (warp - 2) >> 2;
-        const int hcols = a.BN / 2;
+        // epilogue: warp (2..17) -> lane quadrant warp % 4, column slot (warp - 2) / 4
+        // of cpw chunks of 32 columns.  A warp's work on a tile is its live chunks
+        // times G groups ("units", one 32-column TMEM load each), chunk-major.  Four
+        // warps per scheduler hide the loads' latency.
+        const int quad = warp & 3, slot = (warp - 2) >> 2;
+        const int cpw = max(1, a.BN / 128);                          // chunks per warp
+        const int hcols = slot * cpw * 32;                           // the warp's first column in a tile
+        const int nch = max(0, min(cpw, (a.BN - hcols) / 32)), G = a.G;
         const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
         const uint32_t tempty0 = PAIR ? tc::mapa(tc::smem_u32(&bars->tempty[0]), 0) : 0;
-        int lt = 0;
-        for (int64_t t = t0; t < a.ntiles; t += tstep, lt++) {
+        uint16_t *stg = reinterpret_cast<uint16_t *>(stage_out + (warp - 2) * NBUF * RES_STG_BYTES);
+        const int64_t pstep = 2 * a.plane;  // planes of one modulus
+        const uint32_t kdim = (uint32_t)a.kdim, E = (uint32_t)a.E;
+        int lt = 0, sbuf = 0;
+        for (int t = (int)t0; t < a.ntiles; t += (int)tstep, lt++) {
             const int b = lt & 1;
-            const int64_t e = (t / a.n_ntiles) * (NP * BM) + rank * BM + quad * 32 + lane;
-            const int n0 = (int)(t % a.n_ntiles) * a.BN;
+            const int rb = t / a.n_ntiles;
+            const int n0 = (t - rb * a.n_ntiles) * a.BN;
+            const uint32_t ew = (uint32_t)rb * (NP * BM) + rank * BM + quad * 32;  // the warp's first entry
+            const uint32_t e = ew + lane;
             if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); break; }
             tc::fence_after_sync();
-            float sgn = 1.f;
-            int64_t off = 0;
-            if (e < a.E) {
-                const int64_t r = e / a.kdim, c = e % a.kdim;
-                sgn = a.sizes[a.transpose ? c * a.rs + r : r * a.rs + c] < 0 ? -1.f : 1.f;
-                off = r * a.kp + c;
+            const uint32_t rw = ew / kdim, cw = ew - rw * kdim;  // plane row and column of the warp's box
+            const uint32_t re = e / kdim;
+            const int64_t off = e < E ? (int64_t)re * a.kp + (e - re * kdim) : 0;
+            const int c00 = n0 + hcols;  // the warp's first table column
+            const int nlive = max(0, min(nch, (a.ncols - c00 + 31) / 32));
+            const int nunits = nlive * G;
+            auto release = [&]() {
+                // last TMEM read of this tile by this warp: hand the buffer back
+                tc::fence_before_sync();
+                __syncwarp();
+                if (lane == 0) {
+                    if (PAIR) tc::mbar_arrive_cluster(tempty0 + 8u * b);
+                    else tc::mbar_arrive(&bars->tempty[b]);
+                }
+            };
+            if (nunits == 0) {
+                release();
+                continue;
             }
-            const int64_t pstep = 2 * a.plane;  // planes of one modulus
-            for (int c0 = half * hcols; c0 < (half + 1) * hcols; c0 += 32) {
-                float res[16];
-#pragma unroll
-                for (int j = 0; j < 16; j++) res[j] = 0.f;
-                const int mi0 = (n0 + c0) / 2;
-                const bool live_chunk = n0 + c0 < a.ncols;
-                for (int g = 0; g < a.G; g++) {
-                    uint32_t v[32];
-                    if (live_chunk) {
-                        tc::tmem_ld32(lb + (uint32_t)(256 * b + g * a.BN + c0), v);
-                        tc::tmem_ld_wait();
-                    }
-                    if (g == a.G - 1 && c0 + 32 >= (half + 1) * hcols) {
-                        // last TMEM read of this tile by this warp: hand the buffer back
-                        tc::fence_before_sync();
-                        __syncwarp();
-                        if (lane == 0) {
-                            if (PAIR) tc::mbar_arrive_cluster(tempty0 + 8u * b);
-                            else tc::mbar_arrive(&bars->tempty[b]);
-                        }
-                    }
-                    if (!live_chunk) continue;
+            float res[16];
+            auto store = [&](int mi0) {
+                if (a.tma_out) {
+                    if (ew >= E) return;  // the whole box lies past the last entry
+                    if (lane == 0) tc::bulk_wait_read<NBUF - 1>();
+                    __syncwarp();
+                    uint16_t *buf = stg + sbuf * (RES_STG_BYTES / 2);
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
-                        const float2 pc = smod[mi0 + j];
-                        // s0 + 256 * s1 (+ residue of earlier groups): |s| <= 2^24 each,
-                        // |256 red(s1) + red(s0) + res| <= 257 * 32772 + 32772 < 2^24
-                        const float r1 = red(__uint_as_float(v[2 * j + 1]), pc.x, pc.y);
-                        const float r0 = red(__uint_as_float(v[2 * j]), pc.x, pc.y);
-                        res[j] = red(__fmaf_rn(256.f, r1, r0) + res[j], pc.x, pc.y);
-                    }
-                }
-                if (e < a.E && live_chunk) {
-                    uint16_t *dst = reinterpret_cast<uint16_t *>(a.R + (int64_t)mi0 * pstep + off);
-#pragma unroll
-                    for (int j = 0; j < 16; j++, dst += pstep) {
-                        if (mi0 + j >= a.P) break;
-                        const float r = sgn * res[j];
                         float hi, lo;
-                        bal_split(r, hi, lo);
-                        dst[0] = (uint16_t)(__float_as_uint(hi) >> 16);
-                        dst[a.plane] = (uint16_t)(__float_as_uint(lo) >> 16);
+                        bal_split(res[j], hi, lo);
+                        buf[(2 * j) * 32 + lane] = (uint16_t)(__float_as_uint(hi) >> 16);
+                        buf[(2 * j + 1) * 32 + lane] = (uint16_t)(__float_as_uint(lo) >> 16);
+                    }
+                    tc::fence_proxy_async_smem();
+                    __syncwarp();
+                    if (lane == 0) {
+                        // planes past 2P and rows past the last entry are clipped by the map
+                        tc::tma_store_3d(&tmR, buf, (int)cw, (int)rw, 2 * mi0);
+                        tc::bulk_commit_group();
+                    }
+                    if (NBUF > 1) sbuf ^= 1;
+                } else if (e < E) {
+                    uint16_t *dst = reinterpret_cast<uint16_t *>(a.R + (int64_t)mi0 * pstep + off);
+                    if (mi0 + 16 <= a.P) {
+#pragma unroll
+                        for (int j = 0; j < 16; j++) {
+                            float hi, lo;
+                            bal_split(res[j], hi, lo);
+                            dst[j * pstep] = (uint16_t)(__float_as_uint(hi) >> 16);
+                            dst[j * pstep + a.plane] = (uint16_t)(__float_as_uint(lo) >> 16);
+                        }
+                    } else {
+                        const int nj = a.P - mi0;
+#pragma unroll
+                        for (int j = 0; j < 16; j++) {
+                            if (j >= nj) break;
+                            float hi, lo;
+                            bal_split(res[j], hi, lo);
+                            dst[j * pstep] = (uint16_t)(__float_as_uint(hi) >> 16);
+                            dst[j * pstep + a.plane] = (uint16_t)(__float_as_uint(lo) >> 16);
+                        }
                     }
                 }
+            };
+            int lch = 0, lg = 0;  // the next unit to load
+            auto load_next = [&](uint32_t(&v)[32]) {
+                tc::tmem_ld32(lb + (uint32_t)(256 * b + lg * a.BN + hcols + lch * 32), v);
+                if (++lg == G) {
+                    lg = 0;
+                    lch++;
+                }
+            };
+            int cch = 0, cg = 0;  // the next unit to fold
+            auto consume = [&](const uint32_t(&v)[32]) {
+                const int mi0 = (c00 + cch * 32) >> 1;
+                residue_fold(v, mi0, cg == 0, res);
+                if (cg == G - 1) store(mi0);
+                if (++cg == G) {
+                    cg = 0;
+                    cch++;
+                }
+            };
+            uint32_t va[32];
+            for (int u = 0; u < nunits; u++) {
+                load_next(va);
+                tc::tmem_ld_wait(va);
+                if (u + 1 == nunits) release();
+                consume(va);
             }
         }
+        if (lane == 0) tc::bulk_wait_all();  // staging buffers stay live until the stores finish
+        __syncwarp();
     }
     if (PAIR) {
         tc::fence_before_sync();
@@ -1262,6 +1347,25 @@ static gbmm_status make_map(CUtensorMap *m, const void *ptr, uint64_t inner, uin
     return GBMM_OK;
 }
 
+// Residue planes [nplanes][rows][pitch] bf16 as a 3-D map for the residue epilogue's
+// TMA stores: boxes of 32 entries x 1 row x 32 planes, no swizzle.
+static gbmm_status make_map_planes(CUtensorMap *m, const void *ptr, uint64_t cols, uint64_t rows, uint64_t nplanes,
+                                   uint64_t pitch_elems, uint64_t plane_elems) {
+    PFN_encodeTiled enc = get_encode();
+    if (!enc) return set_error(GBMM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    if ((reinterpret_cast<uintptr_t>(ptr) & 15) || (pitch_elems * 2) % 16 || (plane_elems * 2) % 16)
+        return set_error(GBMM_ERR_INVALID, "tensor map base or pitch not 16-byte aligned");
+    cuuint64_t dims[3] = {cols, rows, nplanes};
+    cuuint64_t strides[2] = {pitch_elems * 2, plane_elems * 2};
+    cuuint32_t box[3] = {32, 1, 32};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(ptr), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(GBMM_ERR_CUDA, "cuTensorMapEncodeTiled (planes) failed (%d)", (int)r);
+    return GBMM_OK;
+}
+
 // ---- host big integers (tables only) ---------------------------------------------------------
 typedef std::vector<uint32_t> big;  // little-endian 32-bit limbs
 static void big_mul_small(big &x, uint32_t m) {
@@ -1450,6 +1554,15 @@ static gbmm_status build_tables(crt_tables *t, int P) {
             }
         }
     }
+    {
+        // the constant (p, 1/p) list: the same for every table, written with each
+        std::vector<float> cm(4 * CMOD_PAIRS);
+        for (int i = 0; i < 2 * CMOD_PAIRS; i++) {
+            cm[2 * i] = (float)pr[i];
+            cm[2 * i + 1] = 1.0f / (float)pr[i];
+        }
+        GBMM_CUDA_TRY(cudaMemcpyToSymbol(c_modpair, cm.data(), cm.size() * sizeof(float)));
+    }
     GBMM_CUDA_TRY(cudaMalloc(&t->d_mods, sizeof(ModConst) * P));
     GBMM_CUDA_TRY(cudaMemcpy(t->d_mods, t->h_mods.data(), sizeof(ModConst) * P, cudaMemcpyHostToDevice));
     GBMM_CUDA_TRY(cudaMalloc(&t->d_recon, tab.size() * 2));
@@ -1503,10 +1616,13 @@ static gbmm_status get_tables(crt_cache *c, int P, crt_tables **out) {
 
 static constexpr int RES_STAGES = 4, PROD_STAGES = 4, REC_STAGES = 4, TEST_STAGES = 4;
 static constexpr int REC_STAGES_PAIR = 6;  // a pair CTA stages 32 KB per K step
-static constexpr bool RES_PAIR = false;  // pair mode measured 0.32 ms vs 0.28 ms per 512^3 launch: the epilogue holds TMEM
-static constexpr int RES_STAGES_T = RES_PAIR ? 6 : RES_STAGES;
+static constexpr int RES_STAGES_PAIR = 5;  // a pair CTA stages 32 KB per K step
 static constexpr int PROD_STAGES_PAIR = 5;  // a pair CTA stages 40 KB per K step
 static constexpr int PROD_PAIR_MIN_NK = 8;  // K steps (of 64) from which the product runs on CTA pairs
+// residue GEMM form: -1 by the K loop's length, 0 single CTAs, 1 CTA pairs
+static int g_residue_mode = -1;
+static constexpr int RES_PAIR_MIN_NK = 1 << 30;  // the pair form of the residue GEMM measured slower at every size
+static bool residue_pair(int nk) { return g_residue_mode < 0 ? nk >= RES_PAIR_MIN_NK : g_residue_mode == 1; }
 
 static int num_sms() {
     static int n = 0;
@@ -1565,7 +1681,7 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     if (!D) return set_error(GBMM_ERR_NOMEM, "crt: workspace for digits");
     {
         DigitArgs a;
-        a.limbs = X.limbs; a.ld = X.ld; a.rs = X.rs; a.rows = X.rows; a.cols = X.cols;
+        a.limbs = X.limbs; a.sizes = X.sizes; a.ld = X.ld; a.rs = X.rs; a.rows = X.rows; a.cols = X.cols;
         a.nlimbs = X.nlimbs; a.transpose = transpose; a.dxp = dxp; a.out = D;
         dim3 grid((unsigned)((X.cols + 31) / 32), (unsigned)((X.rows + 3) / 4));
         LaunchScope ls_("k_crt_digits", s);
@@ -1579,25 +1695,34 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     int BN = 256;
     while (BN * G > 256) BN /= 2;
     if (BN < 64) return set_error(GBMM_ERR_UNSUPPORTED, "crt: entries longer than 16384 bits");
-    CUtensorMap tmD, tmT;
+    const bool pair = residue_pair(nk);
+    const int NP = pair ? 2 : 1;
+    CUtensorMap tmD, tmT, tmR;
     GBMM_TRY(make_map(&tmD, D, dxp, E, dxp, BK, BM));
-    constexpr int NP = RES_PAIR ? 2 : 1;
     GBMM_TRY(make_map(&tmT, T, dxp, 2 * t->P, dxp, BK, BN / NP));
     ResidueArgs a;
-    a.sizes = X.sizes; a.rs = X.rs; a.transpose = transpose; a.kdim = kdim; a.E = E; a.nk = nk;
+    if (E > (int64_t)INT32_MAX - 4 * BM)
+        return set_error(GBMM_ERR_UNSUPPORTED, "crt: more than 2^31 entries in one operand");
+    a.kdim = kdim; a.E = (int32_t)E; a.nk = nk;
     a.BN = BN; a.G = G; a.P = t->P; a.mods = t->d_mods; a.R = R; a.plane = (int64_t)rowsR * kp; a.kp = kp;
     a.ncols = 2 * t->P;
     a.n_ntiles = (2 * t->P + BN - 1) / BN;
-    a.ntiles = (int64_t)a.n_ntiles * ((E + NP * BM - 1) / (NP * BM));
-    const size_t sm = smem_bytes(RES_STAGES_T, BM * 128 + (size_t)(BN / NP) * 128) + (size_t)(t->P + 15) / 16 * 16 * 8;
-    GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES_T, RES_PAIR>, sm));
+    a.ntiles = (int32_t)((int64_t)a.n_ntiles * ((E + NP * BM - 1) / (NP * BM)));
+    // 32-entry boxes of one plane row: [32 planes][1 row][32 entries]
+    a.tma_out = kdim % 32 == 0;
+    if (a.tma_out) GBMM_TRY(make_map_planes(&tmR, R, kdim, rowsR, 2 * t->P, kp, a.plane));
+    else tmR = tmD;  // unused
+    const int stages = pair ? RES_STAGES_PAIR : RES_STAGES;
+    const size_t sm = smem_bytes(stages, BM * 128 + (size_t)(BN / NP) * 128) + (size_t)RES_EPI_WARPS * (pair ? 2 : 1) * RES_STG_BYTES;
     LaunchScope ls_("k_crt_residue", s);
-    if (RES_PAIR) {
-        GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES_T, RES_PAIR>, CTA_THREADS8, a.ntiles, sm, s, tmD, tmT, a,
+    if (pair) {
+        GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES_PAIR, true>, sm));
+        GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES_PAIR, true>, RES_THREADS, a.ntiles, sm, s, tmD, tmT, tmR, a,
                               device_error_word()));
     } else {
+        GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false>, sm));
         dim3 grid((unsigned)std::min<int64_t>(a.ntiles, num_sms()));
-        k_crt_residue<RES_STAGES_T, RES_PAIR><<<grid, CTA_THREADS8, sm, s>>>(tmD, tmT, a, device_error_word());
+        k_crt_residue<RES_STAGES, false><<<grid, RES_THREADS, sm, s>>>(tmD, tmT, tmR, a, device_error_word());
     }
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
@@ -1813,4 +1938,12 @@ extern "C" gbmm_status gbmmx_crt_params(int64_t bits_a, int64_t bits_b, int32_t 
     if (!nmoduli) return set_error(GBMM_ERR_INVALID, "null pointer");
     *nmoduli = crt_moduli(bits_a, bits_b, k);
     return GBMM_OK;
+}
+
+// Test hook: the residue GEMM's form (-1 by the K loop's length, 0 single CTAs,
+// 1 CTA pairs); returns the previous setting.
+extern "C" int32_t gbmmx_residue_mode(int32_t mode) {
+    const int32_t old = g_residue_mode;
+    g_residue_mode = mode < 0 ? -1 : (mode > 0 ? 1 : 0);
+    return old;
 }

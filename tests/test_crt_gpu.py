@@ -118,6 +118,31 @@ def test_crt_matmul_vs_oracle(g, oracle, K, M, N, bits):
     assert (limbs == Cl).all()
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("K,M,N,bits", [(70, 96, 50, 4096), (33, 37, 20, 4096), (20, 64, 24, 8192),
+                                        (5, 64, 7, 16000), (10, 32, 9, 1500), (3, 45, 300, 2048)])
+def test_crt_residue_forms(g, mode, K, M, N, bits):
+    """Both forms of the residue GEMM (single CTAs, CTA pairs), with the epilogue's
+    TMA-store output (inner dimension a multiple of 32) and its per-entry store
+    output (any other), over one to four accumulation groups."""
+    rng = random.Random(K + M * 3 + N * 5 + bits + mode)
+    A = _signed(rng, K * M, bits)
+    B = _signed(rng, M * N, bits)
+    nl = (bits + 31) // 32
+    dA = g.DeviceMatrix.from_ints(K, M, A, nl)
+    dB = g.DeviceMatrix.from_ints(M, N, B, nl)
+    f = g.lib().gbmmx_residue_mode
+    f.argtypes = [ctypes.c_int32]
+    f.restype = ctypes.c_int32
+    old = f(mode)
+    try:
+        dC = _crt(g, K, M, N, dA, dB)
+    finally:
+        f(old)
+    exp = [sum(A[y * M + k] * B[k * N + x] for k in range(M)) for y in range(K) for x in range(N)]
+    assert dC.to_ints() == exp
+
+
 def test_crt_cancellation_and_tiny_results(g):
     # rows of A whose products cancel exactly (C entries 0 or tiny): the sign is
     # then decided on the two's-complement path of the reconstruction
