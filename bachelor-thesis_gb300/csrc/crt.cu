@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
 
 // ======================================================================================
 // 2. residue GEMM (persistent; TMEM double-buffered so a tile's epilogue overlaps
-//    the next tile's MMAs; 8 epilogue warps, two per TMEM lane quadrant)
+//    the next tile's MMAs; 16 epilogue warps, four per TMEM lane quadrant)
 // ======================================================================================
 struct ResidueArgs {
     int32_t kdim;  // entry e -> (e / kdim, e % kdim) in digit-row order

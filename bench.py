@@ -401,9 +401,9 @@ def crt_params(bits_a, bits_b, k):
 # dram__bytes_write.sum; profiles/crt_512x512x512_4096b_dram_bytes.md).  The residue
 # figure is the mean of its two launches (A, then B).
 NCU_DRAM_BYTES_512_4096 = {
-    "k_crt_residue": (270.619136e6 + 487.326464e6 + 270.627584e6 + 487.481088e6) / 2,
-    "k_crt_product": 1083.063808e6 + 507.890176e6,
-    "k_crt_recon": 586.745088e6 + 241.935104e6,
+    "k_crt_residue": (269.560576e6 + 487.791616e6 + 269.612544e6 + 487.564544e6) / 2,
+    "k_crt_product": 1083.505152e6 + 505.784064e6,
+    "k_crt_recon": 586.850304e6 + 241.685760e6,
 }
 FIXED_POINT_COLUMNS = 14  # reconstruction columns that carry the 2^96 / p_i weights
 
