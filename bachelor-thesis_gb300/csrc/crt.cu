@@ -361,13 +361,15 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
                     const int st = it % STAGES;
                     if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
                     tc::fence_after_sync();
-                    const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
+                    const uint32_t sa = tc::smem_u32(base + st * STAGE);
                     const uint32_t d = tmem + (uint32_t)(256 * b + (s / GROUP_STEPS) * a.BN);
+                    const uint64_t ad = tc::sdesc_kmajor(sa), bd = tc::sdesc_kmajor(sa + A_BYTES);
 #pragma unroll
                     for (int kk = 0; kk < BK / UK; kk++) {
-                        const uint64_t adesc = tc::sdesc_kmajor(sa + kk * 32), bdesc = tc::sdesc_kmajor(sb + kk * 32);
-                        if (PAIR) tc::mma_bf16_pair(d, adesc, bdesc, idesc, (s % GROUP_STEPS) != 0 || kk != 0);
-                        else tc::mma_bf16(d, adesc, bdesc, idesc, (s % GROUP_STEPS) != 0 || kk != 0);
+                        const uint64_t adesc = tc::sdesc_advance(ad, kk * 32), bdesc = tc::sdesc_advance(bd, kk * 32);
+                        const uint32_t acc = (s % GROUP_STEPS) != 0 || kk != 0;
+                        if (PAIR) tc::mma_bf16_pair(d, adesc, bdesc, idesc, acc);
+                        else tc::mma_bf16(d, adesc, bdesc, idesc, acc);
                     }
                     if (PAIR) tc::mma_commit_pair(&bars->empty[st], 0x3);
                     else tc::mma_commit(&bars->empty[st]);
@@ -621,17 +623,21 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                     const int st = it % STAGES;
                     if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
                     tc::fence_after_sync();
-                    const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + 2 * A_BYTES;
+                    const uint32_t sa = tc::smem_u32(base + st * STAGE);
+                    // three descriptors per K step; the K slices advance them by 32 bytes
+                    const uint64_t a1d = tc::sdesc_kmajor(sa), a0d = tc::sdesc_kmajor(sa + A_BYTES),
+                                   bd = tc::sdesc_kmajor(sa + 2 * A_BYTES);
 #pragma unroll
                     for (int kk = 0; kk < BK / UK; kk++) {
-                        const uint64_t bdesc = tc::sdesc_kmajor(sb + kk * 32);
-                        const uint64_t a1 = tc::sdesc_kmajor(sa + kk * 32), a0 = tc::sdesc_kmajor(sa + A_BYTES + kk * 32);
+                        const uint64_t bdesc = tc::sdesc_advance(bd, kk * 32);
+                        const uint64_t a1 = tc::sdesc_advance(a1d, kk * 32), a0 = tc::sdesc_advance(a0d, kk * 32);
+                        const uint32_t acc = s != 0 || kk != 0;
                         if (PAIR) {
-                            tc::mma_bf16_pair(d, a1, bdesc, idesc, s != 0 || kk != 0);
-                            tc::mma_bf16_pair(d + 2 * PBX, a0, bdesc, idesc, s != 0 || kk != 0);
+                            tc::mma_bf16_pair(d, a1, bdesc, idesc, acc);
+                            tc::mma_bf16_pair(d + 2 * PBX, a0, bdesc, idesc, acc);
                         } else {
-                            tc::mma_bf16(d, a1, bdesc, idesc, s != 0 || kk != 0);
-                            tc::mma_bf16(d + 2 * PBX, a0, bdesc, idesc, s != 0 || kk != 0);
+                            tc::mma_bf16(d, a1, bdesc, idesc, acc);
+                            tc::mma_bf16(d + 2 * PBX, a0, bdesc, idesc, acc);
                         }
                     }
                     if (PAIR) tc::mma_commit_pair(&bars->empty[st], 0x3);
@@ -871,12 +877,14 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                         const int st = it % STAGES;
                         if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
                         tc::fence_after_sync();
-                        const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
+                        const uint32_t sa = tc::smem_u32(base + st * STAGE);
+                        const uint64_t ad = tc::sdesc_mnmajor(sa, BOX), bd = tc::sdesc_kmajor(sa + A_BYTES);
 #pragma unroll
                         for (int kk = 0; kk < BK / UK; kk++) {
-                            const uint64_t adesc = tc::sdesc_mnmajor(sa + kk * 2048, BOX), bdesc = tc::sdesc_kmajor(sb + kk * 32);
-                            if (PAIR) tc::mma_bf16_pair(d, adesc, bdesc, idesc, s != 0 || kk != 0);
-                            else tc::mma_bf16(d, adesc, bdesc, idesc, s != 0 || kk != 0);
+                            const uint64_t adesc = tc::sdesc_advance(ad, kk * 2048), bdesc = tc::sdesc_advance(bd, kk * 32);
+                            const uint32_t acc = s != 0 || kk != 0;
+                            if (PAIR) tc::mma_bf16_pair(d, adesc, bdesc, idesc, acc);
+                            else tc::mma_bf16(d, adesc, bdesc, idesc, acc);
                         }
                         if (PAIR) tc::mma_commit_pair(&bars->empty[st], 0x3);
                         else tc::mma_commit(&bars->empty[st]);

@@ -84,6 +84,12 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr, uint32_t lbo_byt
 // groups 1024 B apart.  The K offset inside the 128-byte row is added to the
 // start address (16 elements = 32 bytes per MMA step).
 __device__ __forceinline__ uint64_t sdesc_kmajor(uint32_t saddr) { return sdesc_sw128(saddr, 16, 1024); }
+// A descriptor advanced by `bytes` (a multiple of 16) inside its tile: the start
+// address field is the low word's bits [0,14), and tile addresses stay below
+// 2^18 bytes, so one 32-bit add on the low word is exact.
+__device__ __forceinline__ uint64_t sdesc_advance(uint64_t d, uint32_t bytes) {
+    return ((d >> 32) << 32) | (uint32_t)((uint32_t)d + (bytes >> 4));
+}
 // MN-major operand: 64-element (128 B) MN blocks, 8 K-rows per 1024-byte
 // swizzle atom; `mn_block_bytes` is the distance between consecutive 64-wide
 // MN blocks (leading byte offset), 1024 B between 8-row K groups (stride offset).
