@@ -166,6 +166,17 @@ __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: 
 // ======================================================================================
 // 1. digits
 // ======================================================================================
+// bf16 bits of bytes k and k+1 of w, byte k in the low half.  Each byte b
+// becomes the FP32 value 2^23 + b (bits 0x4B000000 | b, built by one byte
+// permute) minus 2^23, which is exact; b has at most 8 significant bits, so the
+// top half of its FP32 encoding is its bf16 encoding.  Integer and FP32-add
+// work only: no int->float conversion instructions.
+__device__ __forceinline__ uint32_t byte_pair_bf16(uint32_t w, int k) {
+    const float lo = __fadd_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + k)), -8388608.0f);
+    const float hi = __fadd_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7541u + k)), -8388608.0f);
+    return bf16x2_bits(lo, hi);
+}
+
 // The digits carry the entry's sign (a negative entry's digits are negated), so
 // the residue GEMM yields signed residues directly.
 struct DigitArgs {
@@ -210,16 +221,12 @@ __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
             int dg = 4 * (l0 + 2 * lane);
             if (dg >= a.dxp) continue;
             uint32_t v0 = s[ent][2 * lane], v1 = s[ent][2 * lane + 1];
-            __nv_bfloat162 p0 = __floats2bfloat162_rn((float)(v0 & 255u), (float)((v0 >> 8) & 255u));
-            __nv_bfloat162 p1 = __floats2bfloat162_rn((float)((v0 >> 16) & 255u), (float)(v0 >> 24));
-            __nv_bfloat162 p2 = __floats2bfloat162_rn((float)(v1 & 255u), (float)((v1 >> 8) & 255u));
-            __nv_bfloat162 p3 = __floats2bfloat162_rn((float)((v1 >> 16) & 255u), (float)(v1 >> 24));
             const uint32_t flip = sflip[ent];
             uint4 pk;
-            pk.x = *reinterpret_cast<uint32_t *>(&p0) ^ flip;
-            pk.y = *reinterpret_cast<uint32_t *>(&p1) ^ flip;
-            pk.z = *reinterpret_cast<uint32_t *>(&p2) ^ flip;
-            pk.w = *reinterpret_cast<uint32_t *>(&p3) ^ flip;
+            pk.x = byte_pair_bf16(v0, 0) ^ flip;
+            pk.y = byte_pair_bf16(v0, 2) ^ flip;
+            pk.z = byte_pair_bf16(v1, 0) ^ flip;
+            pk.w = byte_pair_bf16(v1, 2) ^ flip;
             *reinterpret_cast<uint4 *>(a.out + row * a.dxp + dg) = pk;
         }
     }
