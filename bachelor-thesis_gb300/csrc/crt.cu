@@ -759,6 +759,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 //    bounds the single-SM tile, drops by a third.
 // ======================================================================================
 struct ReconArgs {
+    int64_t mt0;     // first entry tile of this launch (tiles mt0 .. nmt-1)
     int64_t E;       // entries of C
     int32_t ncols;   // columns of C (entry e -> row e / ncols, col e % ncols)
     int32_t nk;      // K steps over 2Pp
@@ -837,7 +838,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             tc::prefetch_tmap(&tmY);
             tc::prefetch_tmap(&tmT);
             int it = 0;
-            for (int64_t t = t0; t < a.nmt && !aborted(bars); t += tstep) {
+            for (int64_t t = a.mt0 + t0; t < a.nmt && !aborted(bars); t += tstep) {
                 const int blk0 = (int)(t * (2 * NP) + 2 * rank);  // this CTA's two 64-entry blocks
                 for (int j = 0; j < a.NT && !aborted(bars); j++) {
                     for (int s = 0; s < a.nk; s++, it++) {
@@ -870,7 +871,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             const uint32_t idesc = tc::idesc_bf16_f32(NP * BM, RBN, 1, 0);
             int it = 0, lt = 0;
             bool ok = true;
-            for (int64_t t = t0; t < a.nmt && ok; t += tstep) {
+            for (int64_t t = a.mt0 + t0; t < a.nmt && ok; t += tstep) {
                 for (int j = 0; j < a.NT && ok; j++, lt++) {
                     const int b = lt & 1;
                     if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) {
@@ -917,7 +918,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         const uint32_t tempty0 = PAIR ? tc::mapa(tc::smem_u32(&bars->tempty[0]), 0) : 0;
         int lt = 0, ph1 = 0, ph0 = 0, phq = 0;  // tiles seen; hand-off phases consumed
         bool first = true, ok = true;
-        for (int64_t t = t0; t < a.nmt && ok; t += tstep) {
+        for (int64_t t = a.mt0 + t0; t < a.nmt && ok; t += tstep) {
             const int64_t e = t * (NP * BM) + rank * BM + quad * 32 + lane;
             const bool live = e < a.E;
             const int64_t coff = live ? (e / a.ncols) * a.crs + (e % a.ncols) : 0;
@@ -1780,9 +1781,19 @@ size_t crt_workspace_bytes(int la, int lb, int m, int k, int n, int cn) {
     return ws;
 }
 
+bool crt_single_pass(int k) { return k <= GROUP_STEPS * BK; }
+
 gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, int64_t bits_a,
                        int64_t bits_b, int nprimes, int accumulate, cudaStream_t s) {
     const int m = a.rows, k = a.cols, n = b.cols;
+    // stage hooks apply to this product only; any branch but the single-pass one
+    // waits for B at once and runs the reconstruction whole
+    crt_stage_hooks *hk = h->stage;
+    h->stage = nullptr;
+    if (hk && (m == 0 || n == 0 || k == 0 || accumulate || k > GROUP_STEPS * BK)) {
+        if (hk->b_ready) GBMM_CUDA_TRY(cudaStreamWaitEvent(s, hk->b_ready, 0));
+        hk = nullptr;
+    }
     if (m == 0 || n == 0) return GBMM_OK;
     if (k == 0) return accumulate ? GBMM_OK : launch_mat_zero(c, s);
     if (accumulate) {
@@ -1843,6 +1854,7 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         size_t mk = arena_mark(h);
         GBMM_TRY(operand_residues(h, t, a, 0, m, k, kp, 0, RA, s));
         arena_release(h, mk);
+        if (hk && hk->b_ready) GBMM_CUDA_TRY(cudaStreamWaitEvent(s, hk->b_ready, 0));
         GBMM_TRY(operand_residues(h, t, b, 1, n, k, kp, 1, RB, s));
         arena_release(h, mk);
     }
@@ -1884,20 +1896,32 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         ReconArgs ra;
         ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.NT = (SROWS + t->Dout + 255) / 256; ra.Dout = t->Dout;
         ra.vtab = t->d_vtab; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
-        ra.cnlimbs = c.nlimbs; ra.kpad = 2 * t->Pp; ra.nmt = (E + NP * BM - 1) / (NP * BM);
+        ra.cnlimbs = c.nlimbs; ra.kpad = 2 * t->Pp;
+        const int64_t nmt = (E + NP * BM - 1) / (NP * BM);
         const size_t extra = (size_t)(t->Dout + 31) / 32 * 32 + sizeof(ReconXfer) + 64;
-        LaunchScope ls_("k_crt_recon", s);
-        if (pair) {
-            const size_t sm = smem_bytes(REC_STAGES_PAIR, BM * 128 + TROWS * 128) + extra;
-            GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES_PAIR, true>, sm));
-            GBMM_TRY(launch_pairs(k_crt_recon<REC_STAGES_PAIR, true>, CTA_THREADS8, ra.nmt, sm, s, tmY, tmT, ra, err));
-        } else {
-            const size_t sm = smem_bytes(REC_STAGES, BM * 128 + TROWS * 128) + extra;
-            GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES, false>, sm));
-            dim3 grid((unsigned)std::min<int64_t>(ra.nmt, num_sms()));
-            k_crt_recon<REC_STAGES, false><<<grid, CTA_THREADS8, sm, s>>>(tmY, tmT, ra, err);
+        const size_t sm = smem_bytes(pair ? REC_STAGES_PAIR : REC_STAGES, BM * 128 + TROWS * 128) + extra;
+        if (pair) GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES_PAIR, true>, sm));
+        else GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES, false>, sm));
+        // one launch, or (stage hooks) entry ranges each followed by an event
+        const int parts = hk ? (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)hk->parts, (int64_t)CRT_MAX_PARTS, nmt})) : 1;
+        for (int pi = 0; pi < parts; pi++) {
+            ra.mt0 = nmt * pi / parts;
+            ra.nmt = nmt * (pi + 1) / parts;
+            LaunchScope ls_("k_crt_recon", s);
+            if (pair) {
+                GBMM_TRY(launch_pairs(k_crt_recon<REC_STAGES_PAIR, true>, CTA_THREADS8, ra.nmt - ra.mt0, sm, s, tmY, tmT,
+                                      ra, err));
+            } else {
+                dim3 grid((unsigned)std::min<int64_t>(ra.nmt - ra.mt0, num_sms()));
+                k_crt_recon<REC_STAGES, false><<<grid, CTA_THREADS8, sm, s>>>(tmY, tmT, ra, err);
+            }
+            GBMM_CUDA_TRY(cudaGetLastError());
+            if (hk && parts > 1) {
+                GBMM_CUDA_TRY(cudaEventRecord(hk->part_ev[pi], s));
+                hk->part_end[pi] = std::min<int64_t>(E, ra.nmt * NP * BM);
+            }
         }
-        GBMM_CUDA_TRY(cudaGetLastError());
+        if (hk && parts > 1) hk->parts_done = parts;
     }
     arena_release(h, mark);
     return GBMM_OK;

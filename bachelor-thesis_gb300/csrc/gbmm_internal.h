@@ -87,6 +87,21 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
 bool crt_feasible(int la, int lb, int k);
 // device workspace one crt_matmul call with these shapes carves from the arena
 size_t crt_workspace_bytes(int la, int lb, int m, int k, int n, int cn);
+// whether crt_matmul covers inner dimension k in one pass (no chunks of k)
+bool crt_single_pass(int k);
+// Stage hooks the host-buffer pipeline hands to one single-pass CRT product
+// (gbmm_handle::stage, consumed and cleared by crt_matmul): B's digits and
+// residues wait for b_ready, so A's run while B is still uploading; the
+// reconstruction runs in `parts` entry ranges, each followed by part_ev[i], so
+// finished ranges of C can go back to the host while the rest is computed.
+constexpr int CRT_MAX_PARTS = 4;
+struct crt_stage_hooks {
+    cudaEvent_t b_ready = nullptr;
+    int parts = 1;
+    cudaEvent_t part_ev[CRT_MAX_PARTS] = {};
+    int64_t part_end[CRT_MAX_PARTS] = {};  // entries of C finished after part i (exclusive end)
+    int parts_done = 0;                    // parts recorded (0: none, C finishes with the stream)
+};
 
 // ---- persistent batched limb kernel (limb.cu) ---------------------------------------------
 // Host-side plan of one batch of limb-path products: a blob holding the job
@@ -154,6 +169,8 @@ struct gbmm_handle_s {
     void *pipe = nullptr;
     // device bytes a host-buffer product may use before it runs out of core (0: free memory)
     size_t dev_budget = 0;
+    // stage hooks for the next CRT product (pipeline.cpp sets them, crt_matmul clears them)
+    gbmm::crt_stage_hooks *stage = nullptr;
 };
 
 namespace gbmm {

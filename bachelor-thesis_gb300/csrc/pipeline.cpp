@@ -6,7 +6,10 @@
 // streams: job j's host->device copies run on the upload stream while job j-1
 // computes on the handle's stream and job j-2's result goes back on the
 // download stream.  Each slot is reused only after the compute that read its
-// operands and the copy that read its result have finished (events).
+// operands and the copy that read its result have finished (events).  A
+// single-pass CRT product starts on A while B is still uploading, and the call's
+// last product goes back in entry ranges as its reconstruction finishes them
+// (crt_stage_hooks).
 //
 // The reference moves whole matrices host <-> device around each product with
 // blocking copies (mat-gpu/mat-pregpu.cu:10-96, transfer_recurse); this is the
@@ -39,11 +42,12 @@ struct PipeSlot {
     int32_t *as = nullptr, *bs = nullptr, *cs = nullptr;
     size_t acap = 0, bcap = 0, ccap = 0;  // plane bytes allocated
     size_t ecap = 0;                      // entries allocated per sizes plane (max of A, B, C)
-    cudaEvent_t uploaded = nullptr, computed = nullptr, downloaded = nullptr;
+    cudaEvent_t a_uploaded = nullptr, uploaded = nullptr, computed = nullptr, downloaded = nullptr;
 };
 struct PipeState {
     cudaStream_t up = nullptr, down = nullptr;
     PipeSlot slot[2];
+    cudaEvent_t part[CRT_MAX_PARTS] = {};  // reconstruction ranges of the call's last product
 };
 
 PipeState *pstate(gbmm_handle h) { return static_cast<PipeState *>(h->pipe); }
@@ -74,7 +78,9 @@ gbmm_status pipe_init(gbmm_handle h) {
     h->pipe = ps;
     GBMM_CUDA_TRY(cudaStreamCreateWithFlags(&ps->up, cudaStreamNonBlocking));
     GBMM_CUDA_TRY(cudaStreamCreateWithFlags(&ps->down, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : ps->part) GBMM_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (PipeSlot &s : ps->slot) {
+        GBMM_CUDA_TRY(cudaEventCreateWithFlags(&s.a_uploaded, cudaEventDisableTiming));
         GBMM_CUDA_TRY(cudaEventCreateWithFlags(&s.uploaded, cudaEventDisableTiming));
         GBMM_CUDA_TRY(cudaEventCreateWithFlags(&s.computed, cudaEventDisableTiming));
         GBMM_CUDA_TRY(cudaEventCreateWithFlags(&s.downloaded, cudaEventDisableTiming));
@@ -253,8 +259,11 @@ void pipe_destroy(gbmm_handle h) {
     if (!ps) return;
     if (ps->up) cudaStreamSynchronize(ps->up);
     if (ps->down) cudaStreamSynchronize(ps->down);
+    for (cudaEvent_t e : ps->part)
+        if (e) cudaEventDestroy(e);
     for (PipeSlot &s : ps->slot) {
         slot_free(s);
+        if (s.a_uploaded) cudaEventDestroy(s.a_uploaded);
         if (s.uploaded) cudaEventDestroy(s.uploaded);
         if (s.computed) cudaEventDestroy(s.computed);
         if (s.downloaded) cudaEventDestroy(s.downloaded);
@@ -325,21 +334,6 @@ extern "C" gbmm_status gbmm_matmul_host(gbmm_handle h, gbmm_host_job *jobs, int3
         }
         PipeSlot &s = ps.slot[j & 1];
         const size_t ea = (size_t)q.K * q.M, eb = (size_t)q.M * q.N, ec = (size_t)q.K * q.N;
-        // uploads: the slot's operands are free once the compute two jobs back has run
-        st = ck(cudaStreamWaitEvent(ps.up, s.computed, 0), "cudaStreamWaitEvent");
-        if (st == GBMM_OK && ea) st = ck(cudaMemcpyAsync(s.as, q.a_sizes, ea * 4, cudaMemcpyHostToDevice, ps.up), "cudaMemcpyAsync");
-        if (st == GBMM_OK && ea && q.a_nlimbs)
-            st = ck(cudaMemcpyAsync(s.a, q.a_limbs, (size_t)q.a_nlimbs * ea * 4, cudaMemcpyHostToDevice, ps.up),
-                            "cudaMemcpyAsync");
-        if (st == GBMM_OK && eb) st = ck(cudaMemcpyAsync(s.bs, q.b_sizes, eb * 4, cudaMemcpyHostToDevice, ps.up), "cudaMemcpyAsync");
-        if (st == GBMM_OK && eb && q.b_nlimbs)
-            st = ck(cudaMemcpyAsync(s.b, q.b_limbs, (size_t)q.b_nlimbs * eb * 4, cudaMemcpyHostToDevice, ps.up),
-                            "cudaMemcpyAsync");
-        if (st == GBMM_OK) st = ck(cudaEventRecord(s.uploaded, ps.up), "cudaEventRecord");
-        // compute: after this job's uploads and after the slot's previous result left
-        if (st == GBMM_OK) st = ck(cudaStreamWaitEvent(h->stream, s.uploaded, 0), "cudaStreamWaitEvent");
-        if (st == GBMM_OK) st = ck(cudaStreamWaitEvent(h->stream, s.downloaded, 0), "cudaStreamWaitEvent");
-        if (st != GBMM_OK) break;
         gbmm_mat A = view(q.K, q.M, q.a_nlimbs, s.a, s.as), B = view(q.M, q.N, q.b_nlimbs, s.b, s.bs),
                  C = view(q.K, q.N, q.c_nlimbs, s.c, s.cs);
         gbmm_opts o;
@@ -352,14 +346,55 @@ extern "C" gbmm_status gbmm_matmul_host(gbmm_handle h, gbmm_host_job *jobs, int3
         st = resolve_plan(h, A, B, o, p);
         if (st != GBMM_OK) break;
         q.chosen_path = p.path;
-        st = gbmm_matmul(h, C, A, B, &o);
-        if (st == GBMM_OK) st = ck(cudaEventRecord(s.computed, h->stream), "cudaEventRecord");
-        // download
-        if (st == GBMM_OK) st = ck(cudaStreamWaitEvent(ps.down, s.computed, 0), "cudaStreamWaitEvent");
-        if (st == GBMM_OK && ec) st = ck(cudaMemcpyAsync(q.c_sizes, s.cs, ec * 4, cudaMemcpyDeviceToHost, ps.down), "cudaMemcpyAsync");
-        if (st == GBMM_OK && ec && q.c_nlimbs)
-            st = ck(cudaMemcpyAsync(q.c_limbs, s.c, (size_t)q.c_nlimbs * ec * 4, cudaMemcpyDeviceToHost, ps.down),
+        // a single-pass CRT product starts on A while B is still uploading, and the call's
+        // last product returns C in entry ranges as its reconstruction finishes them
+        const bool staged = p.path == GBMM_PATH_CRT && crt_feasible(q.a_nlimbs, q.b_nlimbs, q.M) &&
+                            crt_single_pass(q.M) && ec > 0 && q.M > 0;
+        bool last = true;
+        for (int j2 = j + 1; j2 < njobs; j2++) last = last && blocked[j2];
+        // uploads: the slot's operands are free once the compute two jobs back has run
+        st = ck(cudaStreamWaitEvent(ps.up, s.computed, 0), "cudaStreamWaitEvent");
+        if (st == GBMM_OK && ea) st = ck(cudaMemcpyAsync(s.as, q.a_sizes, ea * 4, cudaMemcpyHostToDevice, ps.up), "cudaMemcpyAsync");
+        if (st == GBMM_OK && ea && q.a_nlimbs)
+            st = ck(cudaMemcpyAsync(s.a, q.a_limbs, (size_t)q.a_nlimbs * ea * 4, cudaMemcpyHostToDevice, ps.up),
                             "cudaMemcpyAsync");
+        if (st == GBMM_OK) st = ck(cudaEventRecord(s.a_uploaded, ps.up), "cudaEventRecord");
+        if (st == GBMM_OK && eb) st = ck(cudaMemcpyAsync(s.bs, q.b_sizes, eb * 4, cudaMemcpyHostToDevice, ps.up), "cudaMemcpyAsync");
+        if (st == GBMM_OK && eb && q.b_nlimbs)
+            st = ck(cudaMemcpyAsync(s.b, q.b_limbs, (size_t)q.b_nlimbs * eb * 4, cudaMemcpyHostToDevice, ps.up),
+                            "cudaMemcpyAsync");
+        if (st == GBMM_OK) st = ck(cudaEventRecord(s.uploaded, ps.up), "cudaEventRecord");
+        // compute: after this job's uploads (A's only, when staged) and after the slot's
+        // previous result left
+        if (st == GBMM_OK)
+            st = ck(cudaStreamWaitEvent(h->stream, staged ? s.a_uploaded : s.uploaded, 0), "cudaStreamWaitEvent");
+        if (st == GBMM_OK) st = ck(cudaStreamWaitEvent(h->stream, s.downloaded, 0), "cudaStreamWaitEvent");
+        if (st != GBMM_OK) break;
+        crt_stage_hooks hooks;
+        if (staged) {
+            hooks.b_ready = s.uploaded;
+            hooks.parts = last ? CRT_MAX_PARTS : 1;
+            for (int i = 0; i < CRT_MAX_PARTS; i++) hooks.part_ev[i] = ps.part[i];
+            h->stage = &hooks;
+        }
+        st = gbmm_matmul(h, C, A, B, &o);
+        h->stage = nullptr;
+        if (st == GBMM_OK) st = ck(cudaEventRecord(s.computed, h->stream), "cudaEventRecord");
+        // download: the whole of C after the compute, or each finished entry range
+        const int nparts = hooks.parts_done;
+        int64_t e0 = 0;
+        for (int pi = 0; pi < std::max(nparts, 1) && st == GBMM_OK; pi++) {
+            const int64_t e1 = nparts ? std::min<int64_t>(hooks.part_end[pi], (int64_t)ec) : (int64_t)ec;
+            st = ck(cudaStreamWaitEvent(ps.down, nparts ? ps.part[pi] : s.computed, 0), "cudaStreamWaitEvent");
+            if (st == GBMM_OK && e1 > e0)
+                st = ck(cudaMemcpyAsync(q.c_sizes + e0, s.cs + e0, (size_t)(e1 - e0) * 4, cudaMemcpyDeviceToHost, ps.down),
+                        "cudaMemcpyAsync");
+            if (st == GBMM_OK && e1 > e0 && q.c_nlimbs)
+                st = ck(cudaMemcpy2DAsync(q.c_limbs + e0, ec * 4, s.c + e0, ec * 4, (size_t)(e1 - e0) * 4, q.c_nlimbs,
+                                          cudaMemcpyDeviceToHost, ps.down),
+                        "cudaMemcpy2DAsync");
+            e0 = std::max(e0, e1);
+        }
         if (st == GBMM_OK) st = ck(cudaEventRecord(s.downloaded, ps.down), "cudaEventRecord");
     }
     // drain all three streams whatever happened, then report the first error

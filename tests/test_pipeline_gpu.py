@@ -107,3 +107,27 @@ def test_host_jobs_out_of_core(g):
         for spec, exp in specs:
             assert g.planes_to_ints(spec[5][0], spec[5][1]) == exp, (spec[:3], path)
     h.close()
+
+
+def test_host_jobs_staged_crt_parts(g):
+    """Single-pass CRT products start on A while B uploads, and the call's last
+    product returns C in entry ranges as its reconstruction finishes them.  The
+    first job here (2048-bit entries, 258 moduli) reconstructs on CTA pairs in four
+    ranges when it is last; followed by a limb-path job it runs whole."""
+    rng = random.Random(44)
+    crt = _spec(g, rng, 150, 64, 120, 2048, 2048)
+    small = _spec(g, rng, 12, 9, 14, 96, 64)
+    h = g.Handle()
+    for order in ([crt], [crt, small], [small, crt]):
+        for spec, _ in order:
+            spec[5][0][:] = 0
+            spec[5][1][:] = 0
+        paths = [g.PATH_CRT if s is crt else g.PATH_LIMB for s in order]
+        arr = h.host_jobs([s[0] for s in order], path=g.PATH_AUTO)
+        for i, p in enumerate(paths):
+            arr[i].path = p
+        chosen = h.matmul_host(arr)
+        assert list(chosen) == paths
+        for spec, exp in order:
+            assert g.planes_to_ints(spec[5][0], spec[5][1]) == exp, spec[:3]
+    h.close()
