@@ -939,8 +939,19 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                 tc::tmem_ld32(lb + (uint32_t)(256 * b), *reinterpret_cast<uint32_t(*)[32]>(&g[0]));
                 tc::tmem_ld32(lb + (uint32_t)(256 * b + 32), *reinterpret_cast<uint32_t(*)[32]>(&g[32]));
                 tc::tmem_ld_wait();
+                bool took0 = false;  // half 0: the hand-off from half 1 is already taken
                 if (j == 0) {
                     if (hf == 0) {
+                        // with one N tile per entry tile, the q, top0 and drop0 slots are free
+                        // only once half 1 is done with the previous entry tile (its finalize
+                        // included): take that hand-off before writing them, so that the slots
+                        // and qready never run a tile ahead.  With more N tiles, the hand-off
+                        // at j = 1 already orders them.
+                        if (!first && a.NT == 1) {
+                            if (!tc::mbar_wait(&xf->to0[quad], ph0 & 1)) { set_abort(bars, err); ok = false; break; }
+                            ph0++;
+                            took0 = true;
+                        }
                         // fixed-point sum S = sum y_i 2^FIXB / p_i from the first SUSED columns
                         // (base 128): S = (q + C / Mod) 2^FIXB + err, |err| <= 128 P < 2^17, and
                         // |C / Mod| < 2^-18, so q = round(S / 2^FIXB) and the sign of
@@ -1020,8 +1031,10 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                     cin = xf->carry1[idx];
                     nin = xf->ripple1[idx];
                 } else if (!first) {
-                    if (!tc::mbar_wait(&xf->to0[quad], ph0 & 1)) { set_abort(bars, err); ok = false; break; }
-                    ph0++;
+                    if (!took0) {
+                        if (!tc::mbar_wait(&xf->to0[quad], ph0 & 1)) { set_abort(bars, err); ok = false; break; }
+                        ph0++;
+                    }
                     if (j > 0) {
                         cin = xf->carry0[idx];
                         nin = xf->ripple0[idx];
@@ -1075,7 +1088,9 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                         xf->carry0[idx] = c;
                         xf->ripple0[idx] = nin;
                     }
-                    if (!(last_t && j == a.NT - 1)) {
+                    // after an entry's last N tile the hand-off waits for the finalize when the
+                    // entry tile has only that one (see half 0's early take at j = 0)
+                    if (j < a.NT - 1 || (a.NT > 1 && !last_t)) {
                         __syncwarp();
                         if (lane == 0) tc::mbar_arrive(&xf->to0[quad]);
                     }
@@ -1120,6 +1135,11 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                 }
                 for (int li = written; li < a.cnlimbs; li++) a.climbs[(int64_t)li * a.cld + coff] = 0u;
                 a.csizes[coff] = top == 0 ? 0 : (neg ? -top : top);
+            }
+            if (hf == 1 && !last_t && a.NT == 1) {
+                // the finalize is done with half 0's slots: hand on to half 0's next entry tile
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&xf->to0[quad]);
             }
         }
     }

@@ -211,3 +211,32 @@ def test_crt_full_size_512_4096_sampled_and_linear(g):
         y, x = int(srng.integers(K)), int(srng.integers(N))
         exp = sum(_entry(Al, As, y * M + k) * _entry(B1l, B1s, k * N + x) for k in range(M))
         assert _entry(lc, sc, y * N + x) == exp
+
+
+@pytest.mark.parametrize("bits", [64, 600, 700])
+def test_crt_reconstruction_one_table_tile_many_entry_tiles(g, bits):
+    """Products whose result fits one 256-digit table tile (small entries), with
+    several entry tiles per CTA: the reconstruction's two epilogue halves then hand
+    over the fixed-point quotient, sign and top-limb slots once per entry tile, and
+    a half running a tile ahead would overwrite them.  Repeated runs, compared bit
+    for bit against the limb path and, on a sample, against Python integers."""
+    rng = random.Random(bits)
+    K, M, N = 420, 16, 400
+    A = _signed(rng, K * M, bits)
+    B = _signed(rng, M * N, bits)
+    nl = (bits + 31) // 32
+    dA = g.DeviceMatrix.from_ints(K, M, A, nl)
+    dB = g.DeviceMatrix.from_ints(M, N, B, nl)
+    cn = g.limbs_needed(nl, nl, M, path=g.PATH_CRT)
+    ref = g.DeviceMatrix(K, N, cn)
+    g.default_handle().matmul(ref, dA, dB, path=g.PATH_LIMB, method=g.METHOD_NAIVE)
+    rl, rs = ref.download()
+    srng = random.Random(1)
+    for _ in range(8):
+        y, x = srng.randrange(K), srng.randrange(N)
+        assert _entry(rl, rs, y * N + x) == sum(A[y * M + k] * B[k * N + x] for k in range(M))
+    for rep in range(12):
+        dC = g.DeviceMatrix(K, N, cn)
+        g.default_handle().matmul(dC, dA, dB, path=g.PATH_CRT)
+        cl, cs = dC.download()
+        assert (cs == rs).all() and (cl == rl).all(), rep
