@@ -195,14 +195,14 @@ __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
     const int tr = 4, tcn = 32;
     const int r0 = blockIdx.y * tr, c0 = blockIdx.x * tcn;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nchunk = (a.dxp / 4 + 63) / 64;
     if (threadIdx.x < 128) {
         const int r = r0 + (threadIdx.x >> 5), c = c0 + (threadIdx.x & 31);
         sflip[threadIdx.x] = (r < a.rows && c < a.cols && a.sizes[(int64_t)r * a.rs + c] < 0) ? 0x80008000u : 0u;
     }
-    for (int ch = 0; ch < nchunk; ch++) {
-        const int l0 = ch * 64;
-        __syncthreads();
+    {
+        // one chunk of 64 limbs per block (blockIdx.z): more, shorter blocks keep the
+        // last wave of the grid small
+        const int l0 = blockIdx.z * 64;
         // load limbs [l0, l0+64) of the 4 x 32 entries, coalesced along c
         for (int q = threadIdx.x; q < 64 * 128; q += 256) {
             int cc = q & 31, rr = (q >> 5) & 3, li = q >> 7;
@@ -1719,7 +1719,7 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
         DigitArgs a;
         a.limbs = X.limbs; a.sizes = X.sizes; a.ld = X.ld; a.rs = X.rs; a.rows = X.rows; a.cols = X.cols;
         a.nlimbs = X.nlimbs; a.transpose = transpose; a.dxp = dxp; a.out = D;
-        dim3 grid((unsigned)((X.cols + 31) / 32), (unsigned)((X.rows + 3) / 4));
+        dim3 grid((unsigned)((X.cols + 31) / 32), (unsigned)((X.rows + 3) / 4), (unsigned)((dxp / 4 + 63) / 64));
         LaunchScope ls_("k_crt_digits", s);
         k_crt_digits<<<grid, 256, 0, s>>>(a);
         GBMM_CUDA_TRY(cudaGetLastError());
