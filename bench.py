@@ -401,9 +401,9 @@ def crt_params(bits_a, bits_b, k):
 # dram__bytes_write.sum; profiles/crt_512x512x512_4096b_dram_bytes.md).  The residue
 # figure is the mean of its two launches (A, then B).
 NCU_DRAM_BYTES_512_4096 = {
-    "k_crt_residue": (269.651968e6 + 488.234752e6 + 269.614592e6 + 487.935744e6) / 2,
-    "k_crt_product": 1083.156480e6 + 507.490048e6,
-    "k_crt_recon": 586.886144e6 + 241.744128e6,
+    "k_crt_residue": (269.558528e6 + 487.749376e6 + 269.553408e6 + 487.559680e6) / 2,
+    "k_crt_product": 1083.140608e6 + 506.246400e6,
+    "k_crt_recon": 583.059200e6 + 241.474048e6,
 }
 FIXED_POINT_COLUMNS = 14  # reconstruction columns that carry the 2^96 / p_i weights
 
