@@ -240,3 +240,53 @@ def test_crt_reconstruction_one_table_tile_many_entry_tiles(g, bits):
         g.default_handle().matmul(dC, dA, dB, path=g.PATH_CRT)
         cl, cs = dC.download()
         assert (cs == rs).all() and (cl == rl).all(), rep
+
+
+@pytest.mark.parametrize("mode", ["single", "batched", "host"])
+def test_crt_vs_limb_random_shapes(g, mode):
+    """Differential check over seeded random shapes (log-uniform dimensions, A and B
+    of independent bit lengths in [16, 9000], zero and shortened entries): the CRT
+    path through one entry point equals the limb path bit for bit."""
+    import numpy as np
+    import bench
+    rng = random.Random({"single": 1, "batched": 2, "host": 3}[mode])
+    nprng = np.random.default_rng(rng.randrange(1 << 30))
+    lu = lambda lo, hi: int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
+    jobs = []
+    while len(jobs) < 12:
+        K, M, N = lu(1, 400), lu(1, 600), lu(1, 400)
+        ba, bb = lu(16, 9000), lu(16, 9000)
+        if K * M * N * ((ba + 31) // 32) * ((bb + 31) // 32) > 1e10:
+            continue
+        Al, As = bench.gen_planes(nprng, K * M, ba, 0.1, 0.1, 48)
+        Bl, Bs = bench.gen_planes(nprng, M * N, bb, 0.1, 0.1, 48)
+        dA, dB = g.DeviceMatrix(K, M, Al.shape[0]), g.DeviceMatrix(M, N, Bl.shape[0])
+        dA.upload(Al, As)
+        dB.upload(Bl, Bs)
+        jobs.append((K, M, N, dA, dB, Al.shape[0] + Bl.shape[0] + 2, (Al, As, Bl, Bs)))
+    h = g.Handle()
+    refs = []
+    for K, M, N, dA, dB, cn, _ in jobs:
+        r = g.DeviceMatrix(K, N, cn)
+        h.matmul(r, dA, dB, path=g.PATH_LIMB, method=g.METHOD_NAIVE)
+        refs.append(r.download())
+    if mode == "single":
+        outs = []
+        for K, M, N, dA, dB, cn, _ in jobs:
+            c = g.DeviceMatrix(K, N, cn)
+            h.matmul(c, dA, dB, path=g.PATH_CRT)
+            outs.append(c.download())
+    elif mode == "batched":
+        cs = [g.DeviceMatrix(j[0], j[2], j[5]) for j in jobs]
+        h.matmul_batched(h.jobs([(c, j[3], j[4]) for c, j in zip(cs, jobs)], path=g.PATH_CRT), path=g.PATH_CRT)
+        outs = [c.download() for c in cs]
+    else:
+        specs = []
+        for K, M, N, dA, dB, cn, (Al, As, Bl, Bs) in jobs:
+            specs.append((K, M, N, (Al, As), (Bl, Bs),
+                          (np.zeros((cn, K * N), dtype=np.uint32), np.zeros(K * N, dtype=np.int32))))
+        h.matmul_host(h.host_jobs(specs, path=g.PATH_CRT))
+        outs = [(s[5][0], s[5][1]) for s in specs]
+    for j, (rl, rs), (cl, cs_) in zip(jobs, refs, outs):
+        assert (cs_ == rs).all() and (cl == rl).all(), j[:3]
+    h.close()
