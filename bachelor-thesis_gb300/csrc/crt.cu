@@ -245,7 +245,6 @@ struct ResidueArgs {
     int32_t ncols;  // 2P table columns
     int32_t n_ntiles;
     int32_t ntiles;
-    const ModConst *mods;
     __nv_bfloat16 *R;  // planes [2P][rowsR][kp]
     int64_t plane;     // rowsR * kp
     int32_t kp;
@@ -1740,7 +1739,7 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     if (E > (int64_t)INT32_MAX - 4 * BM)
         return set_error(GBMM_ERR_UNSUPPORTED, "crt: more than 2^31 entries in one operand");
     a.kdim = kdim; a.E = (int32_t)E; a.nk = nk;
-    a.BN = BN; a.G = G; a.P = t->P; a.mods = t->d_mods; a.R = R; a.plane = (int64_t)rowsR * kp; a.kp = kp;
+    a.BN = BN; a.G = G; a.P = t->P; a.R = R; a.plane = (int64_t)rowsR * kp; a.kp = kp;
     a.ncols = 2 * t->P;
     a.n_ntiles = (2 * t->P + BN - 1) / BN;
     a.ntiles = (int32_t)((int64_t)a.n_ntiles * ((E + NP * BM - 1) / (NP * BM)));

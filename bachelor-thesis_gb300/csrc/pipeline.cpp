@@ -377,7 +377,9 @@ extern "C" gbmm_status gbmm_matmul_host(gbmm_handle h, gbmm_host_job *jobs, int3
             for (int i = 0; i < CRT_MAX_PARTS; i++) hooks.part_ev[i] = ps.part[i];
             h->stage = &hooks;
         }
-        st = gbmm_matmul(h, C, A, B, &o);
+        // the plan resolved above runs as is, so the staging decision and the product agree
+        st = arena_reserve(h, dispatch_ws(p, q.a_nlimbs, q.b_nlimbs, q.K, q.M, q.N, q.c_nlimbs, 0) + 65536);
+        if (st == GBMM_OK) st = dispatch(h, C, A, B, p, 0, h->stream);
         h->stage = nullptr;
         if (st == GBMM_OK) st = ck(cudaEventRecord(s.computed, h->stream), "cudaEventRecord");
         // download: the whole of C after the compute, or each finished entry range
