@@ -164,6 +164,34 @@ __global__ void __launch_bounds__(256) k_mpn_addsub_n_cla(uint32_t *rp, const ui
     }
 }
 
+// ---- add_n / sub_n for large batches: one thread per operand, serial over limbs ------
+// Limb i of neighbouring operands is adjacent, so every load and store of a warp is
+// one coalesced 128-byte line; with enough operands to fill the GPU this streams at
+// HBM speed, where the warp carry-lookahead above leaves lanes idle on short operands.
+template <bool SUB>
+__global__ void __launch_bounds__(256) k_mpn_addsub_n_serial(uint32_t *rp, const uint32_t *up, const uint32_t *vp,
+                                                             int n, int64_t ld, int64_t nb, uint32_t *cy) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    uint32_t c = 0;
+#pragma unroll 4
+    for (int i = 0; i < n; i++) {
+        const uint32_t x = up[(int64_t)i * ld + b], y = vp[(int64_t)i * ld + b];
+        if (!SUB) {
+            const uint64_t t = (uint64_t)x + y + c;
+            rp[(int64_t)i * ld + b] = (uint32_t)t;
+            c = (uint32_t)(t >> 32);
+        } else {
+            const uint64_t t = (uint64_t)x - y - c;
+            rp[(int64_t)i * ld + b] = (uint32_t)t;
+            c = (uint32_t)(t >> 63);
+        }
+    }
+    cy[b] = c;
+}
+// batches with at least this many operands take the one-thread-per-operand kernel
+constexpr int64_t ADDSUB_SERIAL_MIN_OPS = 16384;
+
 // ---- mul_1 family: one thread per operand, serial over limbs (coalesced) -----------
 template <int OP>  // 0 mul_1, 1 addmul_1, 2 submul_1
 __global__ void k_mpn_mul1ops(uint32_t *rp, const uint32_t *up, int n, const uint32_t *vl, int64_t ld, int64_t nb,
@@ -346,41 +374,36 @@ __global__ void k_mpz_addsub(MatArgs W, MatArgs U, MatArgs V, int sub, int64_t c
     const int un = iabs_d(su), vn = iabs_d(sv);
     const uint32_t *up = U.limbs + iu, *vp = V.limbs + iv;
     uint32_t *wp = W.limbs + iw;
-    int len = 0, neg = 0;
-    if ((su < 0) == (sv < 0) || un == 0 || vn == 0) {
-        neg = un ? (su < 0) : (sv < 0);
-        const int mx = un > vn ? un : vn;
-        if (mx > W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
-        uint32_t c = 0;
-        for (int i = 0; i < mx; i++) {
-            uint64_t s = (uint64_t)(i < un ? up[(int64_t)i * U.ld] : 0u) + (i < vn ? vp[(int64_t)i * V.ld] : 0u) + c;
-            wp[(int64_t)i * W.ld] = (uint32_t)s;
-            c = (uint32_t)(s >> 32);
+    // equal signs (or a zero operand) add magnitudes; opposite signs subtract the
+    // smaller magnitude from the larger
+    const bool add = (su < 0) == (sv < 0) || un == 0 || vn == 0;
+    const int cmp = add ? 1 : (un != vn ? (un < vn ? -1 : 1) : dev_cmp(up, U.ld, vp, V.ld, un));
+    const bool swap = cmp < 0;
+    const uint32_t *xp = swap ? vp : up, *yp = swap ? up : vp;
+    const int xn = swap ? vn : un, yn = swap ? un : vn;
+    const int64_t xs = swap ? V.ld : U.ld, ys = swap ? U.ld : V.ld;
+    const int neg = add ? (un ? (su < 0) : (sv < 0)) : (swap ? (sv < 0) : (su < 0));
+    // every lane runs over all of W's planes, writing the zero tail in the same pass:
+    // the warp's stores to a plane go out together as whole sectors
+    uint32_t c = 0;  // carry or borrow
+    int len = 0;
+    for (int i = 0; i < W.nlimbs; i++) {
+        const uint32_t x = i < xn ? xp[(int64_t)i * xs] : 0u, y = i < yn ? yp[(int64_t)i * ys] : 0u;
+        uint32_t r;
+        if (add) {
+            const uint64_t t = (uint64_t)x + y + c;
+            r = (uint32_t)t;
+            c = (uint32_t)(t >> 32);
+        } else {
+            const uint64_t t = (uint64_t)x - y - c;
+            r = (uint32_t)t;
+            c = (uint32_t)(t >> 63);
         }
-        len = mx;
-        if (c) {
-            if (mx >= W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
-            wp[(int64_t)mx * W.ld] = c;
-            len = mx + 1;
-        }
-    } else {
-        int cmp = un != vn ? (un < vn ? -1 : 1) : dev_cmp(up, U.ld, vp, V.ld, un);
-        const uint32_t *xp = up, *yp = vp;
-        int xn = un, yn = vn;
-        int64_t xs = U.ld, ys = V.ld;
-        neg = su < 0;
-        if (cmp < 0) { xp = vp; yp = up; xn = vn; yn = un; xs = V.ld; ys = U.ld; neg = sv < 0; }
-        if (xn > W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
-        uint32_t br = 0;
-        for (int i = 0; i < xn; i++) {
-            uint64_t d = (uint64_t)xp[(int64_t)i * xs] - (i < yn ? yp[(int64_t)i * ys] : 0u) - br;
-            uint32_t r = (uint32_t)d;
-            wp[(int64_t)i * W.ld] = r;
-            br = (uint32_t)(d >> 63);
-            if (r) len = i + 1;
-        }
+        wp[(int64_t)i * W.ld] = r;
+        if (r) len = i + 1;
     }
-    for (int i = len; i < W.nlimbs; i++) wp[(int64_t)i * W.ld] = 0u;
+    // a carry out of W's last plane, or operand limbs beyond it: W is too small
+    if ((add && c) || xn > W.nlimbs || yn > W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
     W.sizes[iw] = len == 0 ? 0 : (neg ? -len : len);
 }
 
@@ -1090,8 +1113,13 @@ extern "C" gbmm_status gbmm_mpn_add_n(uint32_t *rp, const uint32_t *up, const ui
     GBMM_TRY(check_batch(rp, up, ld, nb, n));
     if (!vp || !cy) return set_error(GBMM_ERR_INVALID, "null pointer");
     if (nb == 0) return GBMM_OK;
-    LaunchScope ls_("k_mpn_addsub_n_cla", as_stream(stream));
-    k_mpn_addsub_n_cla<false><<<grid1(nb, CLA_OPS), 256, 0, as_stream(stream)>>>(rp, up, vp, n, ld, nb, cy);
+    if (nb >= ADDSUB_SERIAL_MIN_OPS) {
+        LaunchScope ls_("k_mpn_addsub_n_serial", as_stream(stream));
+        k_mpn_addsub_n_serial<false><<<grid1(nb, 256), 256, 0, as_stream(stream)>>>(rp, up, vp, n, ld, nb, cy);
+    } else {
+        LaunchScope ls_("k_mpn_addsub_n_cla", as_stream(stream));
+        k_mpn_addsub_n_cla<false><<<grid1(nb, CLA_OPS), 256, 0, as_stream(stream)>>>(rp, up, vp, n, ld, nb, cy);
+    }
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
 }
@@ -1100,8 +1128,13 @@ extern "C" gbmm_status gbmm_mpn_sub_n(uint32_t *rp, const uint32_t *up, const ui
     GBMM_TRY(check_batch(rp, up, ld, nb, n));
     if (!vp || !cy) return set_error(GBMM_ERR_INVALID, "null pointer");
     if (nb == 0) return GBMM_OK;
-    LaunchScope ls_("k_mpn_addsub_n_cla", as_stream(stream));
-    k_mpn_addsub_n_cla<true><<<grid1(nb, CLA_OPS), 256, 0, as_stream(stream)>>>(rp, up, vp, n, ld, nb, cy);
+    if (nb >= ADDSUB_SERIAL_MIN_OPS) {
+        LaunchScope ls_("k_mpn_addsub_n_serial", as_stream(stream));
+        k_mpn_addsub_n_serial<true><<<grid1(nb, 256), 256, 0, as_stream(stream)>>>(rp, up, vp, n, ld, nb, cy);
+    } else {
+        LaunchScope ls_("k_mpn_addsub_n_cla", as_stream(stream));
+        k_mpn_addsub_n_cla<true><<<grid1(nb, CLA_OPS), 256, 0, as_stream(stream)>>>(rp, up, vp, n, ld, nb, cy);
+    }
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
 }

@@ -54,6 +54,10 @@ WORKLOADS = {
     "cfg5": dict(K=0, M=0, N=0, bits=0, zero=0.1, short=0.0, short_bits=0, cutoff=32, jobs=64, rect=8,
                  label="learned dispatch: 64 jobs as cfg4 + 8 rectangular 1024x64x1024 at [256,8192] bits; "
                        "model trained on the autotuner's timings of a separately drawn stream"),
+    # the limb form's batched mpn / mpz kernels one by one, on batches larger than L2
+    "limbkernels": dict(K=0, M=0, N=0, bits=0, zero=0.0, short=0.0, short_bits=0, cutoff=32,
+                        label="limb-form kernels: batched mpn_add_n/sub_n/mul_1/addmul_1/submul_1, "
+                              "mul_basecase, toom22_mul, mpz_add/sub/mul/addmul over 2^21-operand batches"),
 }
 DEFAULT_WORKLOAD = "cfg3"
 DEFAULT_PATH = "crt"
@@ -573,6 +577,107 @@ def run_learned(args, W, world, rank, local):
     return 0
 
 
+def run_limb_kernels(args, W, world, rank, local):
+    """Each limb-form kernel through the public API on a batch larger than L2 (so
+    every call streams from HBM): mean CUDA-event time per call, algorithmic bytes
+    (inputs read once, outputs written once) and GB/s against the measured HBM copy
+    peak; the product kernels also report 32x32-bit limb MACs per second.  One JSON
+    line with a record per kernel."""
+    import torch
+    import gbmm
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    dev = "cuda"
+    rnd = lambda *shape: torch.randint(-2 ** 31, 2 ** 31 - 1, shape, dtype=torch.int32, device=dev)
+    nb, n = 1 << 21, 32                       # operands per batch, limbs per operand
+    up, vp, rp = rnd(n, nb), rnd(n, nb), rnd(n, nb)
+    vl, cy = rnd(nb), torch.zeros(nb, dtype=torch.int32, device=dev)
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(max(1, args.steps)):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / max(1, args.steps)
+
+    out = {}
+
+    def rec(name, kernel, ms, nbytes, macs=None):
+        r = {"kernel": kernel, "ms": ms, "bytes": nbytes, "GB/s": nbytes / (ms * 1e-3) / 1e9,
+             "frac_hbm": nbytes / (ms * 1e-3) / 1e9 / hbm}
+        if macs:
+            r["limb_macs_32"] = macs
+            r["MAC/s"] = macs / (ms * 1e-3)
+        out[name] = r
+
+    L4 = 4 * n * nb                           # bytes of one operand batch
+    rec("mpn_add_n", "k_mpn_addsub_n_serial", timed(lambda: gbmm.mpn_add_n(rp, up, vp, n, nb, nb, cy)),
+        3 * L4 + 4 * nb)
+    rec("mpn_sub_n", "k_mpn_addsub_n_serial", timed(lambda: gbmm.mpn_sub_n(rp, up, vp, n, nb, nb, cy)),
+        3 * L4 + 4 * nb)
+    rec("mpn_mul_1", "k_mpn_mul1ops", timed(lambda: gbmm.mpn_mul_1(rp, up, n, vl, nb, nb, cy)),
+        2 * L4 + 8 * nb, n * nb)
+    rec("mpn_addmul_1", "k_mpn_mul1ops", timed(lambda: gbmm.mpn_addmul_1(rp, up, n, vl, nb, nb, cy)),
+        3 * L4 + 8 * nb, n * nb)
+    rec("mpn_submul_1", "k_mpn_mul1ops", timed(lambda: gbmm.mpn_submul_1(rp, up, n, vl, nb, nb, cy)),
+        3 * L4 + 8 * nb, n * nb)
+    del rp
+    # products: 2^18 operand pairs of 32 x 32 limbs (basecase) and 64 x 64 limbs (Toom-2.2)
+    pb = 1 << 18
+    ua, va = rnd(32, pb), rnd(32, pb)
+    ra = torch.zeros(64, pb, dtype=torch.int32, device=dev)
+    rec("mpn_mul_basecase", "k_mpn_mul_basecase", timed(lambda: gbmm.mpn_mul_basecase(ra, ua, 32, va, 32, pb, pb)),
+        4 * pb * (32 + 32 + 64), 32 * 32 * pb)
+    ub, vb = rnd(64, pb), rnd(64, pb)
+    rb = torch.zeros(128, pb, dtype=torch.int32, device=dev)
+    scratch = torch.zeros(int(gbmm.mpn_toom22_mul_itch(64, 64)), pb, dtype=torch.int32, device=dev)
+    rec("mpn_toom22_mul", "k_mpn_toom22",
+        timed(lambda: gbmm.mpn_toom22_mul(rb, ub, 64, vb, 64, scratch, pb, pb)),
+        4 * pb * (64 + 64 + 128), 64 * 64 * pb)
+    del ua, va, ra, ub, vb, rb, scratch, up, vp
+    # signed entries of matrices: 1024 x 2048 entries, 32-limb operands (16 for products)
+    rng = np.random.default_rng(args.seed)
+    R, Cc = 1024, 2048
+    E = R * Cc
+    mats = {}
+    for key, bits in (("u", 1024), ("v", 1024), ("s", 512), ("t", 512)):
+        Lp, Sp = gen_planes(rng, E, bits, 0.0, 0.0, 0)
+        m = gbmm.DeviceMatrix(R, Cc, Lp.shape[0])
+        m.upload(Lp, Sp)
+        mats[key] = m
+    w = gbmm.DeviceMatrix(R, Cc, 33)
+    rec("mpz_add", "k_mpz_addsub", timed(lambda: gbmm.mpz_add(w, mats["u"], mats["v"])), E * (4 * (32 + 32 + 33) + 12))
+    rec("mpz_sub", "k_mpz_addsub", timed(lambda: gbmm.mpz_sub(w, mats["u"], mats["v"])), E * (4 * (32 + 32 + 33) + 12))
+    p = gbmm.DeviceMatrix(R, Cc, 33)
+    rec("mpz_mul", "k_mpz_mulops", timed(lambda: gbmm.mpz_mul(p, mats["s"], mats["t"])),
+        E * (4 * (16 + 16 + 32) + 12), 16 * 16 * E)
+    rec("mpz_addmul", "k_mpz_mulops", timed(lambda: gbmm.mpz_addmul(p, mats["s"], mats["t"])),
+        E * (4 * (16 + 16 + 33 + 33) + 16), 16 * 16 * E)
+    if rank != 0:
+        return 0
+    line = {
+        "metric": "GB/s per limb-form kernel", "value": max(r["GB/s"] for r in out.values()), "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": W["label"], "hbm_peak_gbs": hbm, "operands": nb, "limbs": n,
+                   "l2": "every batch is larger than L2"},
+        "kernels": out,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_batched(args, W, world, rank, local):
     """Configuration 4: many uneven products through one gbmm_matmul_batched
     call per step (persistent work-queue kernel, CRT jobs, CUDA-graph replay)."""
@@ -650,13 +755,15 @@ def main():
         W = dict(W, K=K, M=M, N=N, bits=b, label=f"{K}x{M}x{N} {b}-bit signed (resized {args.workload})")
     world, rank, local = dist_init()
     if args.impl == "reference":
-        if args.workload in ("cfg4", "cfg5"):
+        if args.workload in ("cfg4", "cfg5", "limbkernels"):
             return run_reference(args, WORKLOADS["cfg3"], world, rank)
         return run_reference(args, W, world, rank)
     if args.workload == "cfg4":
         return run_batched(args, W, world, rank, local)
     if args.workload == "cfg5":
         return run_learned(args, W, world, rank, local)
+    if args.workload == "limbkernels":
+        return run_limb_kernels(args, W, world, rank, local)
     return run_gpu(args, W, world, rank, local)
 
 

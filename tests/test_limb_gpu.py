@@ -33,12 +33,12 @@ def _host(t):
     return t.cpu().numpy().view(np.uint32)
 
 
+@pytest.mark.parametrize("nb", [70, 20000])  # warp carry-lookahead; one thread per operand
 @pytest.mark.parametrize("n", [1, 3, 31, 32, 128, 129, 300])
 @pytest.mark.parametrize("sub", [False, True])
-def test_mpn_add_sub_n_cla(g, oracle, n, sub):
+def test_mpn_add_sub_n_cla(g, oracle, n, sub, nb):
     import torch
-    rng = np.random.default_rng(n + 7 * sub)
-    nb = 70
+    rng = np.random.default_rng(n + 7 * sub + nb)
     u = _rand_planes(rng, n, nb, "ones")
     v = _rand_planes(rng, n, nb)
     v[:, :8] = 0 if sub else 1          # long carry / borrow chains
