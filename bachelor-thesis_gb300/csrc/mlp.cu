@@ -91,58 +91,74 @@ __global__ void __launch_bounds__(MLP_THREADS) k_mlp_forward(const __nv_bfloat16
 // targets T may be NaN for heads without a measurement (masked out).  Each
 // CTA sums its samples' contributions in shared memory, then adds them to the
 // global FP32 gradient with atomics.  loss receives sum of squared errors / count.
-__global__ void __launch_bounds__(MLP_THREADS) k_mlp_backward(const __nv_bfloat16 *w, const float *X, const float *T,
-                                                              const float *H1, const float *H2, const float *Y,
-                                                              int nsamp, float inv_count, float *grad, float *loss) {
-    __shared__ float sw[NPARAM];
-    __shared__ float sg[NPARAM];
-    for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) {
-        sw[i] = __bfloat162float(w[i]);
-        sg[i] = 0.f;
-    }
+// Backward pass in two kernels, with no atomics on the gradient: k_mlp_delta gives
+// every sample's error terms (one thread per sample), k_mlp_wgrad sums them into
+// each parameter's gradient (one thread per parameter, a loop over the samples).
+// The sums run in sample order, so the gradient is the same on every run.
+__global__ void __launch_bounds__(MLP_THREADS) k_mlp_delta(const __nv_bfloat16 *w, const float *T, const float *H1,
+                                                           const float *H2, const float *Y, int nsamp,
+                                                           float inv_count, float *D1, float *D2, float *D3,
+                                                           float *loss) {
+    __shared__ float sw[NW2 + NW3];  // W2 and W3, the weights the error terms pass back through
+    for (int i = threadIdx.x; i < NW2 + NW3; i += blockDim.x)
+        sw[i] = __bfloat162float(w[i < NW2 ? OFF_W2 + i : OFF_W3 + (i - NW2)]);
     __syncthreads();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     float lsum = 0.f;
     if (s < nsamp) {
-        float dy[NO], dh2[NH], dh1[NH];
+        float dy[NO], dh2[NH];
         for (int o = 0; o < NO; o++) {
             const float t = T[(int64_t)s * NO + o];
             const float e = isnan(t) ? 0.f : Y[(int64_t)s * NO + o] - t;
             lsum += e * e;
             dy[o] = 2.f * e * inv_count;
-            atomicAdd(&sg[OFF_B3 + o], dy[o]);
+            D3[(int64_t)s * NO + o] = dy[o];
         }
         for (int i = 0; i < NH; i++) {
-            const float h = H2[(int64_t)s * NH + i];
             float a = 0.f;
-            for (int o = 0; o < NO; o++) {
-                atomicAdd(&sg[OFF_W3 + i * NO + o], h * dy[o]);
-                a += dy[o] * sw[OFF_W3 + i * NO + o];
-            }
-            dh2[i] = h > 0.f ? a : 0.f;
+            for (int o = 0; o < NO; o++) a += dy[o] * sw[NW2 + i * NO + o];
+            dh2[i] = H2[(int64_t)s * NH + i] > 0.f ? a : 0.f;
+            D2[(int64_t)s * NH + i] = dh2[i];
         }
-        for (int j = 0; j < NH; j++) atomicAdd(&sg[OFF_B2 + j], dh2[j]);
         for (int i = 0; i < NH; i++) {
-            const float h = H1[(int64_t)s * NH + i];
             float a = 0.f;
-            for (int j = 0; j < NH; j++) {
-                if (h != 0.f) atomicAdd(&sg[OFF_W2 + i * NH + j], h * dh2[j]);
-                a += dh2[j] * sw[OFF_W2 + i * NH + j];
-            }
-            dh1[i] = h > 0.f ? a : 0.f;
-        }
-        for (int j = 0; j < NH; j++) atomicAdd(&sg[OFF_B1 + j], dh1[j]);
-        for (int i = 0; i < NF; i++) {
-            const float x = X[(int64_t)s * NF + i];
-            for (int j = 0; j < NH; j++) atomicAdd(&sg[OFF_W1 + i * NH + j], x * dh1[j]);
+            for (int j = 0; j < NH; j++) a += dh2[j] * sw[i * NH + j];
+            D1[(int64_t)s * NH + i] = H1[(int64_t)s * NH + i] > 0.f ? a : 0.f;
         }
     }
     // warp-reduce the loss, one atomic per warp
     for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xFFFFFFFFu, lsum, o);
     if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, lsum * inv_count);
-    __syncthreads();
-    for (int i = threadIdx.x; i < NPARAM; i += blockDim.x)
-        if (sg[i] != 0.f) atomicAdd(&grad[i], sg[i]);
+}
+
+// grad[p] for every parameter p: a weight from unit i into unit j of the next layer
+// sums (input activation i) x (error term j) over the samples; a bias sums error j.
+__global__ void k_mlp_wgrad(const float *X, const float *H1, const float *H2, const float *D1, const float *D2,
+                            const float *D3, int nsamp, float *grad) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= NPARAM) return;
+    const float *in = nullptr, *d;
+    int nin = 0, nd, i = 0, j;
+    if (p < OFF_B1) {
+        in = X; nin = NF; d = D1; nd = NH; i = p / NH; j = p % NH;
+    } else if (p < OFF_W2) {
+        d = D1; nd = NH; j = p - OFF_B1;
+    } else if (p < OFF_B2) {
+        in = H1; nin = NH; d = D2; nd = NH; i = (p - OFF_W2) / NH; j = (p - OFF_W2) % NH;
+    } else if (p < OFF_W3) {
+        d = D2; nd = NH; j = p - OFF_B2;
+    } else if (p < OFF_B3) {
+        in = H2; nin = NH; d = D3; nd = NO; i = (p - OFF_W3) / NO; j = (p - OFF_W3) % NO;
+    } else {
+        d = D3; nd = NO; j = p - OFF_B3;
+    }
+    float g = 0.f;
+    if (in) {
+        for (int s = 0; s < nsamp; s++) g += in[(int64_t)s * nin + i] * d[(int64_t)s * nd + j];
+    } else {
+        for (int s = 0; s < nsamp; s++) g += d[(int64_t)s * nd + j];
+    }
+    grad[p] = g;
 }
 
 // Adam step on the FP32 master parameters; the BF16 copy is refreshed.
@@ -326,6 +342,23 @@ extern "C" gbmm_status gbmm_model_predict(gbmm_handle h, const float *X, int32_t
     return st;
 }
 
+// Backward pass: per-sample error terms, then every parameter's gradient into d_grad.
+static cudaError_t launch_backward(Model *md, const float *dX, const float *dT, const float *dH1, const float *dH2,
+                                   const float *dY, float *dD1, float *dD2, float *dD3, int nsamp, int count, float *dL,
+                                   cudaStream_t s) {
+    const int grid = (nsamp + MLP_THREADS - 1) / MLP_THREADS;
+    {
+        LaunchScope ls_("k_mlp_delta", s);
+        k_mlp_delta<<<grid, MLP_THREADS, 0, s>>>(md->d_w16, dT, dH1, dH2, dY, nsamp, 1.f / (float)std::max(count, 1),
+                                                 dD1, dD2, dD3, dL);
+    }
+    {
+        LaunchScope ls_("k_mlp_wgrad", s);
+        k_mlp_wgrad<<<(NPARAM + 127) / 128, 128, 0, s>>>(dX, dH1, dH2, dD1, dD2, dD3, nsamp, md->d_grad);
+    }
+    return cudaGetLastError();
+}
+
 // Loss and parameter gradient of the current model on (X, T) (host arrays;
 // T rows may hold NaN for missing heads).  grad receives NPARAM floats.
 extern "C" gbmm_status gbmm_model_gradient(gbmm_handle h, const float *X, const float *T, int32_t nsamp, float *grad,
@@ -336,8 +369,9 @@ extern "C" gbmm_status gbmm_model_gradient(gbmm_handle h, const float *X, const 
     cudaStream_t s = h->stream;
     float *buf = nullptr;
     const size_t nX = (size_t)nsamp * NF, nT = (size_t)nsamp * NO, nH = (size_t)nsamp * NH;
-    GBMM_CUDA_TRY(cudaMalloc(&buf, (nX + nT + 2 * nH + nT + 1) * 4));
+    GBMM_CUDA_TRY(cudaMalloc(&buf, (nX + nT + 2 * nH + nT + 1 + 2 * nH + nT) * 4));
     float *dX = buf, *dT = dX + nX, *dH1 = dT + nT, *dH2 = dH1 + nH, *dY = dH2 + nH, *dL = dY + nT;
+    float *dD1 = dL + 1, *dD2 = dD1 + nH, *dD3 = dD2 + nH;  // error terms per sample
     int count = 0;
     for (size_t i = 0; i < nT; i++) count += !std::isnan(T[i]);
     gbmm_status st = GBMM_OK;
@@ -351,10 +385,7 @@ extern "C" gbmm_status gbmm_model_gradient(gbmm_handle h, const float *X, const 
             LaunchScope ls_("k_mlp_forward", s);
             k_mlp_forward<<<grid, MLP_THREADS, 0, s>>>(md->d_w16, dX, nsamp, dH1, dH2, dY);
         }
-        LaunchScope ls2_("k_mlp_backward", s);
-        k_mlp_backward<<<grid, MLP_THREADS, 0, s>>>(md->d_w16, dX, dT, dH1, dH2, dY, nsamp,
-                                                    1.f / (float)std::max(count, 1), md->d_grad, dL);
-        e = cudaGetLastError();
+        e = launch_backward(md, dX, dT, dH1, dH2, dY, dD1, dD2, dD3, nsamp, count, dL, s);
     }
     if (e == cudaSuccess && grad) e = cudaMemcpyAsync(grad, md->d_grad, NPARAM * 4, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, dL, 4, cudaMemcpyDeviceToHost, s);
@@ -373,8 +404,9 @@ extern "C" gbmm_status gbmm_model_train(gbmm_handle h, const float *X, const flo
     cudaStream_t s = h->stream;
     float *buf = nullptr;
     const size_t nX = (size_t)nsamp * NF, nT = (size_t)nsamp * NO, nH = (size_t)nsamp * NH;
-    GBMM_CUDA_TRY(cudaMalloc(&buf, (nX + nT + 2 * nH + nT + 1) * 4));
+    GBMM_CUDA_TRY(cudaMalloc(&buf, (nX + nT + 2 * nH + nT + 1 + 2 * nH + nT) * 4));
     float *dX = buf, *dT = dX + nX, *dH1 = dT + nT, *dH2 = dH1 + nH, *dY = dH2 + nH, *dL = dY + nT;
+    float *dD1 = dL + 1, *dD2 = dD1 + nH, *dD3 = dD2 + nH;  // error terms per sample
     int count = 0;
     for (size_t i = 0; i < nT; i++) count += !std::isnan(T[i]);
     cudaError_t e = cudaMemcpyAsync(dX, X, nX * 4, cudaMemcpyHostToDevice, s);
@@ -382,17 +414,12 @@ extern "C" gbmm_status gbmm_model_train(gbmm_handle h, const float *X, const flo
     const int grid = (nsamp + MLP_THREADS - 1) / MLP_THREADS;
     const float b1 = 0.9f, b2 = 0.999f;
     for (int ep = 0; ep < epochs && e == cudaSuccess; ep++) {
-        e = cudaMemsetAsync(md->d_grad, 0, NPARAM * 4, s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(dL, 0, 4, s);
+        e = cudaMemsetAsync(dL, 0, 4, s);
         {
             LaunchScope ls_("k_mlp_forward", s);
             k_mlp_forward<<<grid, MLP_THREADS, 0, s>>>(md->d_w16, dX, nsamp, dH1, dH2, dY);
         }
-        {
-            LaunchScope ls_("k_mlp_backward", s);
-            k_mlp_backward<<<grid, MLP_THREADS, 0, s>>>(md->d_w16, dX, dT, dH1, dH2, dY, nsamp,
-                                                        1.f / (float)std::max(count, 1), md->d_grad, dL);
-        }
+        if (e == cudaSuccess) e = launch_backward(md, dX, dT, dH1, dH2, dY, dD1, dD2, dD3, nsamp, count, dL, s);
         md->step++;
         const float c1 = 1.f - powf(b1, (float)md->step), c2 = 1.f - powf(b2, (float)md->step);
         {
