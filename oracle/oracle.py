@@ -20,13 +20,22 @@ REF_CLI = os.path.join(HERE, "_ref", "mat-cpu")
 _lib = None
 
 
+def reference_dir():
+    """Root of a checkout of the reference (the directory holding mat-cpu/), taken
+    from the GBMM_REFERENCE_DIR environment variable; None when unset or absent."""
+    d = os.environ.get("GBMM_REFERENCE_DIR", "")
+    return d if d and os.path.isdir(os.path.join(d, "mat-cpu")) else None
+
+
 def build(with_ref=None):
-    """Compiles the oracle (and, when the reference tree is mounted, _ref/mat-cpu)."""
+    """Compiles the oracle, and _ref/mat-cpu from the reference's own sources when
+    GBMM_REFERENCE_DIR names a checkout of the reference (skipped otherwise)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    ref = reference_dir()
     if with_ref is None:
-        with_ref = os.path.isdir("/root/reference/mat-cpu")
-    if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        with_ref = ref is not None
+    if with_ref and ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + ref], check=True)
 
 
 def lib():

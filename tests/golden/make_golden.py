@@ -8,8 +8,9 @@ by `make -C oracle ref`, method -m 1 = naive GMP triple loop, cross-checked
 with -m 35 Winograd), and independently by Python integers; the fixture is
 written only if all agree.  Output: <case>.in.gz and <case>.out.gz.
 
-Run in a container where the reference tree is mounted:
-    python tests/golden/make_golden.py
+Run with GBMM_REFERENCE_DIR naming a checkout of the reference (make -C oracle
+ref reads its mat-cpu sources from there):
+    GBMM_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py
 """
 import gzip
 import os
