@@ -1163,6 +1163,11 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 struct TestArgs {
     int32_t M, N, nk, a_mn;
     int32_t *D;
+    // failure-path test knobs: the producer leaves K step `skip_step` unloaded and
+    // its stage barrier unarmed (-1: none), and every wait gives up after
+    // `wait_limit` SM clocks
+    int32_t skip_step;
+    long long wait_limit;
 };
 
 template <int STAGES>
@@ -1177,14 +1182,18 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BM;
     cta_setup(bars, STAGES, 128, 1, 1);
     const uint32_t tmem = bars->tmem_base;
+    const long long lim = a.wait_limit;
     if (warp == 0) {
         if (lane == 0) {
+            int issued = 0;  // K steps whose loads were issued: steps [0, issued) except skip_step
             for (int s = 0; s < a.nk; s++) {
                 const int st = s % STAGES;
-                if (s >= STAGES && !tc::mbar_wait(&bars->empty[st], ((s / STAGES) & 1) ^ 1)) {
+                if (s >= STAGES && !tc::mbar_wait(&bars->empty[st], ((s / STAGES) & 1) ^ 1, lim)) {
                     set_abort(bars, err);
                     break;
                 }
+                issued = s + 1;
+                if (s == a.skip_step) continue;  // nothing arms this stage: its consumer's wait runs out
                 uint8_t *sa = base + st * STAGE;
                 tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
                 if (a.a_mn) {
@@ -1195,14 +1204,22 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
                 }
                 tc::tma_load_2d(sa + A_BYTES, &tmB, &bars->full[st], s * BK, n0);
             }
+            if (aborted(bars)) {
+                // before the CTA's shared memory goes away: wait (bounded) until the
+                // copies of the last stages issued have landed
+                for (int s = issued - 1; s >= 0 && s >= issued - STAGES; s--)
+                    if (s != a.skip_step) tc::mbar_wait(&bars->full[s % STAGES], (s / STAGES) & 1, lim);
+            }
         }
     } else if (warp == 1) {
         if (lane == 0) {
             const uint32_t idesc = tc::idesc_bf16_f32(BM, BM, a.a_mn, 0);
             bool ok = true;
+            int mma_steps = 0;
             for (int s = 0; s < a.nk; s++) {
                 const int st = s % STAGES;
-                if (!tc::mbar_wait(&bars->full[st], (s / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
+                if (!tc::mbar_wait(&bars->full[st], (s / STAGES) & 1, lim)) { set_abort(bars, err); ok = false; break; }
+                mma_steps++;
                 tc::fence_after_sync();
                 const uint32_t sa = tc::smem_u32(base + st * STAGE), sb = sa + A_BYTES;
 #pragma unroll
@@ -1214,10 +1231,15 @@ __global__ void __launch_bounds__(CTA_THREADS, 1)
                 tc::mma_commit(&bars->empty[st]);
             }
             if (ok) tc::mma_commit(&bars->tfull[0]);
+            else if (mma_steps > 0) {
+                // MMAs already issued still write TMEM: wait (bounded) for them before teardown frees it
+                tc::mma_commit(&bars->tfull[1]);
+                tc::mbar_wait(&bars->tfull[1], 0, lim);
+            }
         }
     } else {
         const int row = epi_row();
-        bool ok = tc::mbar_wait(&bars->tfull[0], 0);
+        bool ok = tc::mbar_wait(&bars->tfull[0], 0, lim);
         if (!ok) set_abort(bars, err);
         tc::fence_after_sync();
         const uint32_t lb = lane_base(tmem);
@@ -1963,11 +1985,40 @@ extern "C" gbmm_status gbmmx_test_gemm(const void *A, const void *B, int32_t *D,
     GBMM_TRY(make_map(&tmB, B, K, N, K, BK, BM));
     TestArgs ta;
     ta.M = M; ta.N = N; ta.nk = K / BK; ta.a_mn = a_mn; ta.D = D;
+    ta.skip_step = -1;
+    ta.wait_limit = tc::WAIT_LIMIT_CLOCKS;
     const size_t sm = smem_bytes(TEST_STAGES, 2 * BM * 128);
     GBMM_TRY(set_smem((const void *)k_gemm_test<TEST_STAGES>, sm));
     dim3 grid((unsigned)((N + BM - 1) / BM), (unsigned)((M + BM - 1) / BM));
     LaunchScope ls_("k_gemm_test", s);
     k_gemm_test<TEST_STAGES><<<grid, CTA_THREADS, sm, s>>>(tmA, tmB, ta, device_error_word());
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return check_device_error(s);
+}
+
+// Internal test hook for the failure path: the same single-CTA pipeline (M = N =
+// 128, one CTA) with K step `skip_step` never loaded (its stage barrier is never
+// armed, so the MMA issuer's wait for it cannot complete) and every wait bounded
+// by `wait_limit_clocks`.  Each role gives up when its wait runs out, records
+// DEVERR_TIMEOUT, lets its in-flight copies and MMAs finish (bounded waits), and
+// the CTA frees its TMEM and exits; the status comes back as GBMM_ERR_TIMEOUT.
+extern "C" gbmm_status gbmmx_test_gemm_timeout(const void *A, const void *B, int32_t *D, int32_t K, int32_t skip_step,
+                                               int64_t wait_limit_clocks, void *stream) {
+    cudaStream_t s = as_stream(stream);
+    if (K % 64 || K < 64 || skip_step < 0 || skip_step >= K / BK || wait_limit_clocks < 1000 ||
+        wait_limit_clocks > tc::WAIT_LIMIT_CLOCKS)
+        return set_error(GBMM_ERR_INVALID, "test gemm timeout: bad arguments");
+    CUtensorMap tmA, tmB;
+    GBMM_TRY(make_map(&tmA, A, K, BM, K, BK, BM));
+    GBMM_TRY(make_map(&tmB, B, K, BM, K, BK, BM));
+    TestArgs ta;
+    ta.M = BM; ta.N = BM; ta.nk = K / BK; ta.a_mn = 0; ta.D = D;
+    ta.skip_step = skip_step;
+    ta.wait_limit = wait_limit_clocks;
+    const size_t sm = smem_bytes(TEST_STAGES, 2 * BM * 128);
+    GBMM_TRY(set_smem((const void *)k_gemm_test<TEST_STAGES>, sm));
+    LaunchScope ls_("k_gemm_test", s);
+    k_gemm_test<TEST_STAGES><<<dim3(1, 1), CTA_THREADS, sm, s>>>(tmA, tmB, ta, device_error_word());
     GBMM_CUDA_TRY(cudaGetLastError());
     return check_device_error(s);
 }
@@ -1983,6 +2034,8 @@ extern "C" gbmm_status gbmmx_test_gemm_pair(const void *A, const void *B, int32_
     GBMM_TRY(make_map(&tmB, B, K, N, K, BK, BM));
     TestArgs ta;
     ta.M = M; ta.N = N; ta.nk = K / BK; ta.a_mn = 0; ta.D = D;
+    ta.skip_step = -1;
+    ta.wait_limit = tc::WAIT_LIMIT_CLOCKS;
     const size_t sm = smem_bytes(TEST_STAGES, 2 * BM * 128);
     GBMM_TRY(set_smem((const void *)k_gemm_test_pair<TEST_STAGES>, sm));
     const unsigned tiles = (unsigned)(((M + 255) / 256) * ((N + 255) / 256));

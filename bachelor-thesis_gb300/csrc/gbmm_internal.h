@@ -77,6 +77,26 @@ gbmm_status launch_add_shifted(const gbmm_mat &w, const gbmm_mat &u, const gbmm_
 // whether the per-entry product kernel handles la x lb limb entries
 bool limb_kernel_fits(int la, int lb);
 
+// Breadth-first Winograd recursion: the whole tree of one square product laid out
+// in workspace arrays (see limb.cu).  Level d = 1..levels holds 4 * 7^(d-1) A-side
+// and B-side sums and 7^d products, each a dense (N >> d)^2 matrix stored back to
+// back (capSA / capSB / capP planes); level 0's output is C.
+constexpr int WINO_MAX_LEVELS = 8;
+struct WinoTree {
+    gbmm_mat A, B, C;
+    int N = 0, levels = 0;
+    int capSA = 0, capSB = 0, capP = 0;
+    uint32_t *sa_limbs[WINO_MAX_LEVELS + 1] = {}, *sb_limbs[WINO_MAX_LEVELS + 1] = {},
+             *p_limbs[WINO_MAX_LEVELS + 1] = {};
+    int32_t *sa_sizes[WINO_MAX_LEVELS + 1] = {}, *sb_sizes[WINO_MAX_LEVELS + 1] = {},
+            *p_sizes[WINO_MAX_LEVELS + 1] = {};
+};
+// level d's sums from level d - 1's operands; all leaf products; level d's
+// products combined into level d - 1's outputs
+gbmm_status launch_wino_sums(const WinoTree &t, int d, cudaStream_t s);
+gbmm_status launch_wino_leaves(const WinoTree &t, cudaStream_t s);
+gbmm_status launch_wino_combine(const WinoTree &t, int d, cudaStream_t s);
+
 // ---- CRT path (crt.cu) --------------------------------------------------------------
 struct crt_cache;
 crt_cache *crt_cache_create();
@@ -110,6 +130,7 @@ struct LimbBatchPlan {
     std::vector<char> blob;
     struct Group {
         int R = 0;
+        int NT = 0;  // threads per CTA
         size_t jobs_off = 0, items_off = 0;
         int nitems = 0;
         size_t smem = 0;
@@ -160,6 +181,8 @@ struct gbmm_handle_s {
     gbmm::crt_cache *crt = nullptr;
     // tuning knobs (filled from defaults or the autotuner)
     int limb_cutoff = 32;
+    // Winograd products as one breadth-first tree (1, default) or depth first (0)
+    int wino_breadth_first = 1;
     // learned-dispatch model (null when not loaded) and whether AUTO consults it
     void *model = nullptr;
     int use_model = 0;

@@ -222,6 +222,16 @@ extern "C" gbmm_status gbmm_destroy(gbmm_handle h) {
     return GBMM_OK;
 }
 
+// Internal switch (not part of the public ABI): Winograd products through the
+// breadth-first tree (1, default) or the depth-first recursion (0); returns the
+// previous setting, or -1 for a null handle.
+extern "C" int32_t gbmmx_wino_breadth_first(gbmm_handle h, int32_t enable) {
+    if (!h) return -1;
+    const int32_t old = h->wino_breadth_first;
+    h->wino_breadth_first = enable != 0;
+    return old;
+}
+
 extern "C" gbmm_status gbmm_set_stream(gbmm_handle h, void *stream) {
     if (!h) return set_error(GBMM_ERR_INVALID, "null handle");
     h->stream = as_stream(stream);
@@ -660,6 +670,7 @@ struct RecCtx {
     int cutoff;
     int capSA, capSB;  // capacities of A-side and B-side sums
     int capP;          // capacity of products / C quadrants
+    bool breadth_first;  // Winograd products through the breadth-first tree when it fits
 };
 
 static unsigned ilog2u(unsigned n) { unsigned r = 0; while (n >>= 1) r++; return r; }
@@ -815,14 +826,80 @@ gbmm_status rec_naive(RecCtx &c, gbmm_mat C, gbmm_mat A, gbmm_mat B, int N, int 
     return GBMM_OK;
 }
 
+// Workspace of the breadth-first Winograd tree (sums and products of every level).
+static size_t wino_bf_ws(int N, int levels, int capSA, int capSB, int capP) {
+    size_t total = 0;
+    int64_t np = 1;  // parents at level d - 1
+    for (int d = 1; d <= levels; d++) {
+        const int64_t h = N >> d, e = h * h;
+        total += align_up((size_t)(4 * np * e) * capSA * 4, 256) + align_up((size_t)(4 * np * e) * 4, 256);
+        total += align_up((size_t)(4 * np * e) * capSB * 4, 256) + align_up((size_t)(4 * np * e) * 4, 256);
+        total += align_up((size_t)(7 * np * e) * capP * 4, 256) + align_up((size_t)(7 * np * e) * 4, 256);
+        np *= 7;
+    }
+    return total + 6 * 256 * (size_t)levels;
+}
+
+// The breadth-first tree is used for a top-level Winograd product (not C += A*B)
+// whose workspace stays below a fixed share of the device: 7^levels leaf products
+// need (7/4)^levels times the product's own planes.
+static constexpr size_t WINO_BF_MAX_BYTES = (size_t)24 << 30;
+static bool wino_bf_ok(int method, int N, int levels, int addmul, int capSA, int capSB, int capP) {
+    if (method != GBMM_METHOD_WINOGRAD || addmul || levels < 1 || levels > WINO_MAX_LEVELS) return false;
+    if (N % (1 << levels) != 0 || !limb_kernel_fits(capSA, capSB)) return false;
+    return wino_bf_ws(N, levels, capSA, capSB, capP) <= WINO_BF_MAX_BYTES;
+}
+
+// Breadth-first Winograd: sums of every level, then all leaf products in one
+// launch, then the combinations of every level bottom up (kernels in limb.cu).
+// Same products and sums as rec_winograd, so the same exact result.
+gbmm_status rec_winograd_bf(RecCtx &c, gbmm_mat C, gbmm_mat A, gbmm_mat B, int N, int levels) {
+    WinoTree t;
+    t.A = A;
+    t.B = B;
+    t.C = C;
+    t.N = N;
+    t.levels = levels;
+    t.capSA = c.capSA;
+    t.capSB = c.capSB;
+    t.capP = c.capP;
+    const size_t mark = arena_mark(c.h);
+    int64_t np = 1;
+    for (int d = 1; d <= levels; d++) {
+        const int64_t h = N >> d, e = h * h;
+        t.sa_limbs[d] = (uint32_t *)arena_alloc(c.h, (size_t)(4 * np * e) * t.capSA * 4);
+        t.sa_sizes[d] = (int32_t *)arena_alloc(c.h, (size_t)(4 * np * e) * 4);
+        t.sb_limbs[d] = (uint32_t *)arena_alloc(c.h, (size_t)(4 * np * e) * t.capSB * 4);
+        t.sb_sizes[d] = (int32_t *)arena_alloc(c.h, (size_t)(4 * np * e) * 4);
+        t.p_limbs[d] = (uint32_t *)arena_alloc(c.h, (size_t)(7 * np * e) * t.capP * 4);
+        t.p_sizes[d] = (int32_t *)arena_alloc(c.h, (size_t)(7 * np * e) * 4);
+        if (!t.sa_limbs[d] || !t.sa_sizes[d] || !t.sb_limbs[d] || !t.sb_sizes[d] || !t.p_limbs[d] || !t.p_sizes[d]) {
+            arena_release(c.h, mark);
+            return set_error(GBMM_ERR_NOMEM, "winograd tree exceeds the reserved workspace");
+        }
+        np *= 7;
+    }
+    gbmm_status st = GBMM_OK;
+    for (int d = 1; d <= levels && st == GBMM_OK; d++) st = launch_wino_sums(t, d, c.s);
+    if (st == GBMM_OK) st = launch_wino_leaves(t, c.s);
+    for (int d = levels; d >= 1 && st == GBMM_OK; d--) st = launch_wino_combine(t, d, c.s);
+    arena_release(c.h, mark);
+    return st;
+}
+
 gbmm_status rec_square(RecCtx &c, int method, gbmm_mat C, gbmm_mat A, gbmm_mat B, int N, int levels, int addmul) {
     // recursion is skipped when the one-limb-longer sums it forms would not fit the per-entry kernel
     if (levels <= 0 || N % 2 != 0 || N / 2 < 1 || !limb_kernel_fits(c.capSA, c.capSB))
         return launch_limb_matmul(C, A, B, addmul, c.s);
-    if (method == GBMM_METHOD_WINOGRAD) return rec_winograd(c, C, A, B, N, levels, addmul);
+    if (c.breadth_first && wino_bf_ok(method, N, levels, addmul, c.capSA, c.capSB, c.capP))
+        return rec_winograd_bf(c, C, A, B, N, levels);
+    // depth first from here down (the workspace was sized for that)
+    RecCtx dc = c;
+    dc.breadth_first = false;
+    if (method == GBMM_METHOD_WINOGRAD) return rec_winograd(dc, C, A, B, N, levels, addmul);
     if (addmul) return launch_limb_matmul(C, A, B, 1, c.s);
-    if (method == GBMM_METHOD_STRASSEN) return rec_strassen(c, C, A, B, N, levels);
-    if (method == GBMM_METHOD_NAIVE_REC) return rec_naive(c, C, A, B, N, levels);
+    if (method == GBMM_METHOD_STRASSEN) return rec_strassen(dc, C, A, B, N, levels);
+    if (method == GBMM_METHOD_NAIVE_REC) return rec_naive(dc, C, A, B, N, levels);
     return launch_limb_matmul(C, A, B, 0, c.s);
 }
 
@@ -833,8 +910,11 @@ static int levels_for(int N, int cutoff) {
     return l;
 }
 
-// Workspace bytes for a square recursion of `levels` levels on N.
-static size_t rec_ws(int method, int N, int levels, int capT) {
+// Workspace bytes for a square recursion of `levels` levels on N (sums with
+// capSA / capSB planes, products with capP); `bf`: the breadth-first tree may be used.
+static size_t rec_ws(int method, int N, int levels, int addmul, int capSA, int capSB, int capP, bool bf) {
+    if (bf && wino_bf_ok(method, N, levels, addmul, capSA, capSB, capP)) return wino_bf_ws(N, levels, capSA, capSB, capP);
+    const int capT = std::max(std::max(capSA, capSB), capP);
     size_t total = 0;
     int n = N;
     for (int l = 0; l < levels; l++) {
@@ -882,11 +962,11 @@ gbmm_status squarify(RecCtx &c, int method, gbmm_mat C, gbmm_mat A, gbmm_mat B) 
     return GBMM_OK;
 }
 
-static size_t squarify_ws(int method, int K, int M, int N, int base, int capT, int capP) {
+static size_t squarify_ws(int method, int K, int M, int N, int base, int capSA, int capSB, int capP, bool bf) {
     if (K == 0 || M == 0 || N == 0) return 0;
     if (method == GBMM_METHOD_NAIVE || K <= base || M <= base || N <= base) return 0;
     if (K == M && M == N && remove_factors((unsigned)K, 2) <= (unsigned)base)
-        return rec_ws(method, K, levels_for(K, base), capT);
+        return rec_ws(method, K, levels_for(K, base), 0, capSA, capSB, capP, bf);
     int mindim = std::min(std::min(K, M), N);
     int pt = 1 << ilog2u((unsigned)mindim);
     size_t own = mat_bytes((int64_t)K * N, capP);
@@ -894,7 +974,8 @@ static size_t squarify_ws(int method, int K, int M, int N, int base, int capT, i
     int ks[2] = {pt, K - pt}, ms[2] = {pt, M - pt}, ns[2] = {pt, N - pt};
     for (int r = 0; r < 2; r++)
         for (int cc = 0; cc < 2; cc++)
-            for (int kk = 0; kk < 2; kk++) sub = std::max(sub, squarify_ws(method, ks[r], ms[kk], ns[cc], base, capT, capP));
+            for (int kk = 0; kk < 2; kk++)
+                sub = std::max(sub, squarify_ws(method, ks[r], ms[kk], ns[cc], base, capSA, capSB, capP, bf));
     return own + sub;
 }
 
@@ -937,9 +1018,10 @@ gbmm_status matmul_limb(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, con
     ctx.capSA = a.nlimbs + 1;
     ctx.capSB = b.nlimbs + 1;
     ctx.capP = c.nlimbs;
-    const int capT = std::max(std::max(ctx.capSA, ctx.capSB), ctx.capP);
-    size_t ws = accumulate ? rec_ws(method, a.rows, levels_for(a.rows, cutoff), capT)
-                           : squarify_ws(method, a.rows, a.cols, b.cols, cutoff, capT, ctx.capP);
+    ctx.breadth_first = h->wino_breadth_first != 0;
+    size_t ws = accumulate ? rec_ws(method, a.rows, levels_for(a.rows, cutoff), 1, ctx.capSA, ctx.capSB, ctx.capP, false)
+                           : squarify_ws(method, a.rows, a.cols, b.cols, cutoff, ctx.capSA, ctx.capSB, ctx.capP,
+                                         ctx.breadth_first);
     if (ws) GBMM_TRY(arena_reserve(h, ws + 4096));
     if (accumulate) return rec_square(ctx, method, c, a, b, a.rows, levels_for(a.rows, cutoff), 1);
     return squarify(ctx, method, c, a, b);
@@ -972,9 +1054,10 @@ size_t dispatch_ws(const Plan &p, int la, int lb, int m, int k, int n, int cn, i
         if (p.method == GBMM_METHOD_NAIVE) return 0;
         int levels = levels_for(std::max(std::max(m, k), n), p.cutoff) + 2;
         int need = limbs_needed(la, lb, k, levels);
-        const int capT = std::max(std::max(la + 1, lb + 1), std::max(need, cn));
-        size_t rec = accumulate ? rec_ws(p.method, m, levels_for(m, p.cutoff), capT)
-                                : squarify_ws(p.method, m, k, n, p.cutoff, capT, std::max(need, cn));
+        const int capP = std::max(need, cn);
+        // the breadth-first tree's workspace is counted whether or not the handle uses it
+        size_t rec = accumulate ? rec_ws(p.method, m, levels_for(m, p.cutoff), 1, la + 1, lb + 1, capP, false)
+                                : squarify_ws(p.method, m, k, n, p.cutoff, la + 1, lb + 1, capP, true);
         return (cn < need ? mat_bytes((int64_t)m * n, need) : 0) + rec + 8192;
     }
     const bool sa = la >= lb;
@@ -1077,7 +1160,9 @@ extern "C" gbmm_status gbmm_mpn_mul(gbmm_handle h, uint32_t *rp, const uint32_t 
     const int s = un >> 1, n = un - s, t = vn - n;
     const bool toom = vn >= 32 && 4 * un < 5 * vn && 0 < t && t <= s;  // balanced and large enough
     if (!toom) return gbmm_mpn_mul_basecase(rp, up, un, vp, vn, ld, nb, h->stream);
-    size_t need = (size_t)gbmm_mpn_toom22_mul_itch(un, vn) * (size_t)ld * 4;
+    const int32_t itch = gbmm_mpn_toom22_mul_itch(un, vn);
+    if (itch < 0) return set_error(GBMM_ERR_INVALID, "mpn_mul: un=%d is too long", un);
+    size_t need = (size_t)itch * (size_t)ld * 4;
     GBMM_TRY(arena_reserve(h, need + 4096));
     size_t mark = arena_mark(h);
     uint32_t *scratch = (uint32_t *)arena_alloc(h, need);

@@ -46,7 +46,7 @@ struct MatArgs {
     int64_t rs, ld;
     int32_t rows, cols, nlimbs;
 };
-static inline MatArgs margs(const gbmm_mat &m) {
+__host__ __device__ static inline MatArgs margs(const gbmm_mat &m) {
     MatArgs a;
     a.limbs = m.limbs; a.sizes = m.sizes; a.rs = m.rs; a.ld = m.ld;
     a.rows = m.rows; a.cols = m.cols; a.nlimbs = m.nlimbs;
@@ -219,6 +219,95 @@ __global__ void k_mpn_mul1ops(uint32_t *rp, const uint32_t *up, int n, const uin
     cy[b] = (uint32_t)c;
 }
 
+// ---- the rest of the mpn layer: one thread per operand, serial over coalesced limbs -----
+// Neighbouring threads take neighbouring operands, so every limb access of a warp
+// is one 128-byte line.  GMP semantics (mat-gpu/addsub.cu:187-326, com.cu:35-42).
+
+// rp = up +/- vp with un >= vn limbs (vp zero-extended to un); carry / borrow out
+template <bool SUB>
+__global__ void __launch_bounds__(256) k_mpn_addsub(uint32_t *rp, const uint32_t *up, int un, const uint32_t *vp,
+                                                    int vn, int64_t ld, int64_t nb, uint32_t *cy) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    uint32_t c = 0;
+    int i = 0;
+#pragma unroll 4
+    for (; i < vn; i++) {
+        const uint32_t x = up[(int64_t)i * ld + b], y = vp[(int64_t)i * ld + b];
+        const uint64_t t = SUB ? (uint64_t)x - y - c : (uint64_t)x + y + c;
+        rp[(int64_t)i * ld + b] = (uint32_t)t;
+        c = SUB ? (uint32_t)(t >> 63) : (uint32_t)(t >> 32);
+    }
+    for (; i < un; i++) {
+        const uint32_t x = up[(int64_t)i * ld + b];
+        const uint32_t r = SUB ? x - c : x + c;
+        rp[(int64_t)i * ld + b] = r;
+        c = SUB ? (uint32_t)(x < c) : (uint32_t)(r < c);
+    }
+    cy[b] = c;
+}
+
+// rp = up +/- vl[b] (a single limb per operand), n >= 1; carry / borrow out
+template <bool SUB>
+__global__ void __launch_bounds__(256) k_mpn_addsub_1(uint32_t *rp, const uint32_t *up, int n, const uint32_t *vl,
+                                                      int64_t ld, int64_t nb, uint32_t *cy) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    uint32_t c = vl[b];
+#pragma unroll 4
+    for (int i = 0; i < n; i++) {
+        const uint32_t x = up[(int64_t)i * ld + b];
+        const uint32_t r = SUB ? x - c : x + c;
+        rp[(int64_t)i * ld + b] = r;
+        c = SUB ? (uint32_t)(x < c) : (uint32_t)(r < c);
+    }
+    cy[b] = c;
+}
+
+// res[b] = sign(up - vp) over n limbs, compared from the top
+__global__ void __launch_bounds__(256) k_mpn_cmp(const uint32_t *up, const uint32_t *vp, int n, int64_t ld,
+                                                 int64_t nb, int32_t *res) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    int r = 0;
+    for (int i = n - 1; i >= 0; i--) {
+        const uint32_t x = up[(int64_t)i * ld + b], y = vp[(int64_t)i * ld + b];
+        if (x != y) {
+            r = x > y ? 1 : -1;
+            break;
+        }
+    }
+    res[b] = r;
+}
+
+// res[b] = 1 when all n limbs of operand b are zero, else 0
+__global__ void __launch_bounds__(256) k_mpn_zero_p(const uint32_t *up, int n, int64_t ld, int64_t nb, int32_t *res) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    uint32_t any = 0;
+#pragma unroll 4
+    for (int i = 0; i < n; i++) any |= up[(int64_t)i * ld + b];
+    res[b] = any == 0;
+}
+
+// NEG: rp = -up mod B^n (~up + 1), cy[b] = 1 unless up is zero;  COM: rp = ~up
+template <bool NEG>
+__global__ void __launch_bounds__(256) k_mpn_neg_com(uint32_t *rp, const uint32_t *up, int n, int64_t ld, int64_t nb,
+                                                     uint32_t *cy) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    uint32_t c = NEG ? 1u : 0u, any = 0;
+#pragma unroll 4
+    for (int i = 0; i < n; i++) {
+        const uint32_t x = up[(int64_t)i * ld + b];
+        const uint32_t r = ~x + c;
+        c = NEG ? (uint32_t)(r < c) : 0u;
+        any |= x;
+        rp[(int64_t)i * ld + b] = r;
+    }
+    if (NEG) cy[b] = any != 0;
+}
+
 // ---- per-thread strided mpn helpers (operand stride `s`) ------------------------------
 // r[0..un+vn) = u * v by product scanning: column t is summed in a 96-bit
 // accumulator and written once.
@@ -363,15 +452,16 @@ __device__ __forceinline__ int64_t ent(const MatArgs &m, int64_t e) {
     return r * m.rs + c;
 }
 
-// w = u + sgn * v, one thread per entry.  For opposite signs the magnitudes
-// are compared from the top before the subtraction (GMP mpz_add semantics).
-__global__ void k_mpz_addsub(MatArgs W, MatArgs U, MatArgs V, int sub, int64_t count, uint32_t *err) {
-    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= count) return;
-    const int64_t iw = ent(W, e), iu = ent(U, e), iv = ent(V, e);
+// w = u + sgn * v for one entry (W's entry at offset iw, U's at iu, V's at iv).
+// For opposite signs the magnitudes are compared from the top before the
+// subtraction (GMP mpz_add semantics).  W may be U or V (in place).
+__device__ void addsub_entry(const MatArgs &W, int64_t iw, const MatArgs &U, int64_t iu, const MatArgs &V, int64_t iv,
+                             int sub, uint32_t *err) {
     int su = U.sizes[iu], sv = V.sizes[iv];
     if (sub) sv = -sv;
     const int un = iabs_d(su), vn = iabs_d(sv);
+    // a size beyond its operand's planes is malformed input: nothing past the planes is read
+    if (un > U.nlimbs || vn > V.nlimbs) { atomicOr(err, DEVERR_BADARG); W.sizes[iw] = 0; return; }
     const uint32_t *up = U.limbs + iu, *vp = V.limbs + iv;
     uint32_t *wp = W.limbs + iw;
     // equal signs (or a zero operand) add magnitudes; opposite signs subtract the
@@ -383,6 +473,10 @@ __global__ void k_mpz_addsub(MatArgs W, MatArgs U, MatArgs V, int sub, int64_t c
     const int xn = swap ? vn : un, yn = swap ? un : vn;
     const int64_t xs = swap ? V.ld : U.ld, ys = swap ? U.ld : V.ld;
     const int neg = add ? (un ? (su < 0) : (sv < 0)) : (swap ? (sv < 0) : (su < 0));
+    // operand limbs beyond W's planes: rejected before anything is written, so an
+    // in-place call (W aliasing U or V) keeps its operand; only a carry out of W's
+    // last plane (found after the pass) leaves W's limbs undefined
+    if (xn > W.nlimbs || yn > W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); W.sizes[iw] = 0; return; }
     // every lane runs over all of W's planes, writing the zero tail in the same pass:
     // the warp's stores to a plane go out together as whole sectors
     uint32_t c = 0;  // carry or borrow
@@ -402,9 +496,17 @@ __global__ void k_mpz_addsub(MatArgs W, MatArgs U, MatArgs V, int sub, int64_t c
         wp[(int64_t)i * W.ld] = r;
         if (r) len = i + 1;
     }
-    // a carry out of W's last plane, or operand limbs beyond it: W is too small
-    if ((add && c) || xn > W.nlimbs || yn > W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
+    // a carry out of W's last plane: W is too small (its size is set to 0 so a
+    // later reader of W stays inside its planes)
+    if (add && c) { atomicOr(err, DEVERR_CAPACITY); W.sizes[iw] = 0; return; }
     W.sizes[iw] = len == 0 ? 0 : (neg ? -len : len);
+}
+
+// w = u + sgn * v, one thread per entry.
+__global__ void k_mpz_addsub(MatArgs W, MatArgs U, MatArgs V, int sub, int64_t count, uint32_t *err) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    addsub_entry(W, ent(W, e), U, ent(U, e), V, ent(V, e), sub, err);
 }
 
 // w = u * v (op 0), w += u * v (op 1), w -= u * v (op 2); one thread per entry.
@@ -597,7 +699,8 @@ __global__ void k_max_size(MatArgs A, int64_t count, int32_t *out) {
 // as 128-bit vectors and reused by every thread of the CTA's TY x TX entries.
 // ======================================================================================
 namespace {
-constexpr int MM_THREADS = 256;
+constexpr int MM_THREADS = 256;       // CTA size when groups of <= 256 threads share a CTA
+constexpr int MM_THREADS_WIDE = 512;  // largest CTA: one group of up to 512 threads
 constexpr int MM_KC = 8;
 }
 
@@ -605,6 +708,9 @@ struct MMCfg {
     int R;        // block edge in limbs
     int La, Lb;   // padded limb counts (multiples of R)
     int G, Gp;    // threads per entry (active, padded)
+    int NT;       // threads per CTA (entries x Gp, at most MM_THREADS; Gp for one wide group)
+    int thinA, thinB;  // the operand has one limb past a multiple of R: its last block row
+                       // (column) holds that single limb and is multiplied as 1 x R (R x 1)
     int TY, TX;   // entries per CTA
     int M;        // inner dimension
     int accumulate;
@@ -620,6 +726,152 @@ struct MMCfg {
         "subc.u32 %2, %2, 0;\n\t}"                                               \
         : "+r"(c0), "+r"(c1), "+r"(c2)                                            \
         : "r"(a), "r"(b))
+
+// Block (I, J) of the La x Lb limb square that thread lt of a group owns: the full
+// R x R blocks first, then the thin blocks of a one-limb last block row / column
+// (so thin blocks share warps and their shorter loop does not hold up full ones).
+__device__ __forceinline__ void block_of(int lt, int nbA, int nbB, int thinA, int thinB, int &I, int &J) {
+    const int ma = nbA - thinA, mb = nbB - thinB, nmain = ma * mb;
+    if (lt < nmain) { I = lt / mb; J = lt % mb; return; }
+    int r = lt - nmain;
+    if (thinA) {
+        if (r < mb) { I = nbA - 1; J = r; return; }
+        r -= mb;
+    }
+    if (thinB) {
+        if (r < ma) { I = r; J = nbB - 1; return; }
+    }
+    I = nbA - 1;
+    J = nbB - 1;
+}
+
+// P (+|-)= a-block x b-block; a thin row (column) block has only a[0] (b[0]).
+template <int R, bool NEG>
+__device__ __forceinline__ void block_mac(uint32_t (&P)[2 * R - 1][3], const uint32_t (&a)[R], const uint32_t (&b)[R],
+                                          bool rthin, bool cthin) {
+#define OP_(c, x, y)                                          \
+    do {                                                      \
+        if (NEG) MSC96(P[c][0], P[c][1], P[c][2], x, y);      \
+        else MAC96(P[c][0], P[c][1], P[c][2], x, y);          \
+    } while (0)
+    if (!rthin && !cthin) {
+#pragma unroll
+        for (int i = 0; i < R; i++)
+#pragma unroll
+            for (int j = 0; j < R; j++) OP_(i + j, a[i], b[j]);
+    } else if (!cthin) {
+#pragma unroll
+        for (int j = 0; j < R; j++) OP_(j, a[0], b[j]);
+    } else if (!rthin) {
+#pragma unroll
+        for (int i = 0; i < R; i++) OP_(i, a[i], b[0]);
+    } else {
+        OP_(0, a[0], b[0]);
+    }
+#undef OP_
+}
+
+// Signed carry resolution of one entry's column sums by the 32 lanes of a warp
+// (all lanes call it).  col[t] = (s0, s1, s2) for t < Lc is column t's value
+// s0 + s1 2^32 + s2 2^64 (s2 signed); buf has LB = Lc + 2 words.  Lane l takes
+// the limbs [l S, l S + S), S >= 2: it forms them from carry-in 0 and notes its
+// carry-out q.  A carry-in c (|c| < 2^53) then changes the carry-out by
+// floor((r + c) / 2^(32 len)) in {-1, 0, 1} (r: the segment's limbs), which a
+// 31-step shuffle chain resolves from the segment's low 64 bits and whether its
+// upper limbs are all ones / all zeros.  Then the sign, the two's-complement
+// negation (the +1 reaches a lane when every lower limb is zero: one ballot),
+// the normalized size and the store of entry ic of C (plus the old C for C += A*B).
+__device__ void resolve_store_warp(const unsigned long long *col, uint32_t *buf, int Lc, int LB, const MatArgs &C,
+                                   int64_t ic, int accumulate, uint32_t *err) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    int sc = 0, cn = 0;
+    if (accumulate) {
+        sc = C.sizes[ic];
+        cn = iabs_d(sc);
+    }
+    if (cn > LB || cn > C.nlimbs) {
+        if (lane == 0) atomicOr(err, DEVERR_CAPACITY);
+        return;
+    }
+    const int S = max(2, (LB + 31) / 32);
+    const int t0 = min(lane * S, LB), t1 = min(t0 + S, LB);
+    const bool empty = t0 >= t1;
+    long long q = 0;
+    for (int t = t0; t < t1; t++) {
+        unsigned long long w0 = 0, w1 = 0;
+        long long w2 = 0;
+        if (t < Lc) {
+            w0 = col[t * 3];
+            w1 = col[t * 3 + 1];
+            w2 = (long long)col[t * 3 + 2];
+        }
+        long long extra = 0;
+        if (t < cn) {
+            const long long v = (long long)C.limbs[(int64_t)t * C.ld + ic];
+            extra = sc < 0 ? -v : v;
+        }
+        const long long lo = (long long)(w0 & 0xFFFFFFFFull) + (q & 0xFFFFFFFFll) + extra;
+        buf[t] = (uint32_t)lo;
+        q = (lo >> 32) + (q >> 32) + (long long)(w0 >> 32) + (long long)w1 + (w2 << 32);
+    }
+    bool hi_ones = true, hi_zero = true;
+    for (int t = t0 + 2; t < t1; t++) {
+        hi_ones &= buf[t] == 0xFFFFFFFFu;
+        hi_zero &= buf[t] == 0u;
+    }
+    const unsigned long long low64 =
+        empty ? 0ull : ((unsigned long long)buf[t0] | (t0 + 1 < t1 ? (unsigned long long)buf[t0 + 1] << 32 : 0ull));
+    auto carry_out = [&](long long c) -> long long {
+        if (empty) return c;
+        if (t1 - t0 == 1) return q + (((long long)buf[t0] + c) >> 32);
+        if (c >= 0) return q + ((low64 + (unsigned long long)c < low64 && hi_ones) ? 1 : 0);
+        return q - ((low64 < (unsigned long long)(-c) && hi_zero) ? 1 : 0);
+    };
+    long long cin = 0;
+    for (int l = 0; l < 31; l++) {
+        const long long v = __shfl_sync(FULL, carry_out(cin), l);
+        if (lane == l + 1) cin = v;
+    }
+    const long long fin = __shfl_sync(FULL, carry_out(cin), 31);
+    // the exact sum fits LB limbs, so what is left is the sign extension (0 or -1)
+    if (fin != 0 && fin != -1) {
+        if (lane == 0) atomicOr(err, DEVERR_CAPACITY);
+        return;
+    }
+    long long c = cin;
+    for (int t = t0; t < t1; t++) {
+        const long long lo = (long long)buf[t] + (c & 0xFFFFFFFFll);
+        buf[t] = (uint32_t)lo;
+        c = (lo >> 32) + (c >> 32);
+    }
+    const bool neg = fin < 0;
+    if (neg) {
+        bool z = true;
+        for (int t = t0; t < t1; t++) z &= buf[t] == 0u;
+        const unsigned zmask = __ballot_sync(FULL, z);
+        const unsigned lower = lane == 0 ? 0u : (FULL >> (32 - lane));
+        uint32_t c1 = ((~zmask) & lower) == 0u ? 1u : 0u;
+        for (int t = t0; t < t1; t++) {
+            const uint32_t v = ~buf[t] + c1;
+            c1 = (c1 && v == 0u) ? 1u : 0u;
+            buf[t] = v;
+        }
+    }
+    int top = 0;
+    for (int t = t0; t < t1; t++)
+        if (buf[t]) top = t + 1;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) top = max(top, __shfl_xor_sync(FULL, top, o));
+    if (top > C.nlimbs) {
+        if (lane == 0) atomicOr(err, DEVERR_CAPACITY);
+        return;
+    }
+    uint32_t *cl = C.limbs + ic;
+    for (int t = t0; t < t1 && t < C.nlimbs; t++) cl[(int64_t)t * C.ld] = t < top ? buf[t] : 0u;
+    for (int t = LB + lane; t < C.nlimbs; t += 32) cl[(int64_t)t * C.ld] = 0u;
+    if (lane == 0) C.sizes[ic] = neg ? -top : top;
+}
 
 // Writes the signed multi-limb value held in buf[0..L) (two's complement,
 // `neg` = its sign) into entry ic of C as sign-magnitude.
@@ -653,7 +905,7 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
     int32_t *ssA = reinterpret_cast<int32_t *>(sB + MM_KC * TX * sb_stride);  // [TY][KC]
     int32_t *ssB = ssA + TY * MM_KC;                                       // [KC][TX]
 
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, nt = cfg.NT;
     const int g = tid / cfg.Gp, lt = tid % cfg.Gp;
     const int EPC = TY * TX;
     const bool has_entry = g < EPC;
@@ -663,7 +915,9 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
     const bool valid = has_entry && y < C.rows && x < C.cols;
     const int nbA = La / R, nbB = Lb / R;
     const bool active = valid && lt < cfg.G;
-    const int I0 = active ? lt / nbB : 0, J0 = active ? lt % nbB : 0;
+    int I0 = 0, J0 = 0;
+    if (active) block_of(lt, nbA, nbB, cfg.thinA, cfg.thinB, I0, J0);
+    const bool rthin = cfg.thinA && I0 == nbA - 1, cthin = cfg.thinB && J0 == nbB - 1;
 
     uint32_t P[2 * R - 1][3];
 #pragma unroll
@@ -674,7 +928,7 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
         const int kc = min(MM_KC, M - k0);
         __syncthreads();
         // stage A[y0..y0+TY)[k0..k0+kc) : consecutive threads walk k (contiguous in a plane row)
-        for (int q = tid; q < TY * La * MM_KC; q += MM_THREADS) {
+        for (int q = tid; q < TY * La * MM_KC; q += nt) {
             int kk = q % MM_KC, rest = q / MM_KC, i = rest % La, tyy = rest / La;
             int yy = y0 + tyy;
             uint32_t v = 0;
@@ -682,18 +936,18 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
             sA[(tyy * MM_KC + kk) * sa_stride + i] = v;
         }
         // stage B[k0..k0+kc)[x0..x0+TX) : consecutive threads walk x
-        for (int q = tid; q < MM_KC * Lb * TX; q += MM_THREADS) {
+        for (int q = tid; q < MM_KC * Lb * TX; q += nt) {
             int txx = q % TX, rest = q / TX, i = rest % Lb, kk = rest / Lb;
             int xx = x0 + txx;
             uint32_t v = 0;
             if (kk < kc && xx < B.cols && i < B.nlimbs) v = B.limbs[(int64_t)i * B.ld + (int64_t)(k0 + kk) * B.rs + xx];
             sB[(kk * TX + txx) * sb_stride + i] = v;
         }
-        for (int q = tid; q < TY * MM_KC; q += MM_THREADS) {
+        for (int q = tid; q < TY * MM_KC; q += nt) {
             int kk = q % MM_KC, tyy = q / MM_KC, yy = y0 + tyy;
             ssA[q] = (kk < kc && yy < A.rows) ? A.sizes[(int64_t)yy * A.rs + k0 + kk] : 0;
         }
-        for (int q = tid; q < MM_KC * TX; q += MM_THREADS) {
+        for (int q = tid; q < MM_KC * TX; q += nt) {
             int txx = q % TX, kk = q / TX, xx = x0 + txx;
             ssB[q] = (kk < kc && xx < B.cols) ? B.sizes[(int64_t)(k0 + kk) * B.rs + xx] : 0;
         }
@@ -718,17 +972,8 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
 #pragma unroll
                     for (int v = 0; v < R; v++) { a[v] = pa[v]; b[v] = pb[v]; }
                 }
-                if ((sa ^ sb) >= 0) {
-#pragma unroll
-                    for (int i = 0; i < R; i++)
-#pragma unroll
-                        for (int j = 0; j < R; j++) MAC96(P[i + j][0], P[i + j][1], P[i + j][2], a[i], b[j]);
-                } else {
-#pragma unroll
-                    for (int i = 0; i < R; i++)
-#pragma unroll
-                        for (int j = 0; j < R; j++) MSC96(P[i + j][0], P[i + j][1], P[i + j][2], a[i], b[j]);
-                }
+                if ((sa ^ sb) >= 0) block_mac<R, false>(P, a, b, rthin, cthin);
+                else block_mac<R, true>(P, a, b, rthin, cthin);
             }
         }
     }
@@ -743,7 +988,7 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
     unsigned long long *cs = reinterpret_cast<unsigned long long *>(part + ((part_words + 1) & ~(size_t)1));  // [EPC][Lc][3]
     uint32_t *res = reinterpret_cast<uint32_t *>(cs + (size_t)EPC * Lc * 3);                                  // [EPC][LB]
     if (active) {
-        uint32_t *dst = part + ((size_t)g * cfg.G + lt) * NC * 3;
+        uint32_t *dst = part + ((size_t)g * cfg.G + I0 * nbB + J0) * NC * 3;
 #pragma unroll
         for (int c = 0; c < NC; c++) {
             dst[c * 3 + 0] = P[c][0];
@@ -754,7 +999,7 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
     __syncthreads();
     // column t of entry gg gathers block diagonal d = t / R at offset t % R and
     // diagonal d - 1 at offset t % R + R
-    for (int item = tid; item < EPC * Lc; item += MM_THREADS) {
+    for (int item = tid; item < EPC * Lc; item += nt) {
         const int gg = item / Lc, t = item % Lc;
         unsigned long long s0 = 0, s1 = 0;
         long long s2 = 0;
@@ -775,6 +1020,13 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
         o[2] = (unsigned long long)s2;
     }
     __syncthreads();
+    if (cfg.Gp >= 32) {
+        // one warp per entry: the group's first 32 threads (a whole warp, as Gp is a multiple of 32)
+        if (!(valid && lt < 32)) return;
+        resolve_store_warp(cs + (size_t)g * Lc * 3, res + (size_t)g * LB, Lc, LB, C, (int64_t)y * C.rs + x,
+                           cfg.accumulate, err);
+        return;
+    }
     if (!(valid && lt == 0)) return;
 
     // ---- signed carry propagation, optional C += , write back (one thread per entry) --------
@@ -807,9 +1059,8 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
     store_signed(buf, LB, carry < 0, C, ic, err);
 }
 
-template <int R>
-__global__ void __launch_bounds__(MM_THREADS) k_limb_matmul(MatArgs C, MatArgs A, MatArgs B, MMCfg cfg,
-                                                            uint32_t *err) {
+template <int R, int NT>
+__global__ void __launch_bounds__(NT) k_limb_matmul(MatArgs C, MatArgs A, MatArgs B, MMCfg cfg, uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     limb_tile<R>(C, A, B, cfg, blockIdx.y, blockIdx.x, smem_raw, err);
 }
@@ -823,9 +1074,9 @@ struct LimbJob {
     MMCfg cfg;
 };
 
-template <int R>
-__global__ void __launch_bounds__(MM_THREADS) k_limb_batched(const LimbJob *jobs, const int *items, int nitems,
-                                                             int *counter, uint32_t *err) {
+template <int R, int NT>
+__global__ void __launch_bounds__(NT) k_limb_batched(const LimbJob *jobs, const int *items, int nitems, int *counter,
+                                                     uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int cur;
     for (;;) {
@@ -839,6 +1090,177 @@ __global__ void __launch_bounds__(MM_THREADS) k_limb_batched(const LimbJob *jobs
         limb_tile<R>(C, A, B, cfg, items[3 * it + 1], items[3 * it + 2], smem_raw, err);
         __syncthreads();
     }
+}
+
+// ======================================================================================
+// Breadth-first Winograd recursion.
+//
+// The depth-first recursion (host.cpp) issues a level's seven products and
+// fifteen additions one after another, each a small launch.  Here the whole
+// tree is laid out in workspace arrays and every level is one launch: one for
+// all sums of a level, one for all leaf products of the tree (one CTA per leaf
+// tile), one for all combinations of a level.  Nodes are numbered from the
+// root (level 0); node q at level d has children 7q + j at level d + 1, the
+// products of Winograd's scheme in the reference's operation order
+// (mat-gpu/mat-defines.h:144-164, mat-cpu/mat.c:193-251):
+//   j = 0: M1  = A11 B11        j = 4: M5 = S1 T1
+//   j = 1: M2  = A12 B21        j = 5: M6 = S2 T2
+//   j = 2: M3  = S4 B22         j = 6: M7 = S3 T3
+//   j = 3: M4' = A22 T4'
+// with S1 = A21 + A22, S2 = S1 - A11, S3 = A11 - A21, S4 = A12 - S2 and
+// T1 = B12 - B11, T2 = B22 - T1, T3 = B22 - B12, T4' = B21 - T2, and
+//   C11 = M1 + M2, C12 = M1 + M6 + M5 + M3,
+//   C21 = M1 + M6 + M7 + M4', C22 = M1 + M6 + M7 + M5.
+// The sums of parent q at level d - 1 are matrices 4q + s (s = 0..3: S1..S4,
+// T1..T4') of level d's sum arrays; the products of level d are matrices
+// 0..7^d - 1 of its product array; level 0's output is the caller's C.
+// Every operand view is computed on the device from the node's index path, so
+// a launch takes no job table and the sequence can be captured in a graph.
+// ======================================================================================
+__device__ __forceinline__ MatArgs wt_quad(MatArgs m, int qr, int qc, int h) {
+    const int64_t off = (int64_t)qr * h * m.rs + (int64_t)qc * h;
+    m.limbs += off;
+    m.sizes += off;
+    m.rows = h;
+    m.cols = h;
+    return m;
+}
+__device__ __forceinline__ MatArgs wt_dense(uint32_t *limbs, int32_t *sizes, int64_t q, int h, int cap) {
+    MatArgs m;
+    const int64_t e = (int64_t)h * h;
+    m.limbs = limbs + q * e * cap;
+    m.sizes = sizes + q * e;
+    m.rs = h;
+    m.ld = e;
+    m.rows = h;
+    m.cols = h;
+    m.nlimbs = cap;
+    return m;
+}
+// Operand `which` (0: A, 1: B) of node `node` at level d.
+__device__ MatArgs wt_operand(const WinoTree &t, int which, int d, int64_t node) {
+    MatArgs v = margs(which ? t.B : t.A);
+    int h = t.N;
+    int64_t pw = 1;
+    for (int l = 1; l < d; l++) pw *= 7;
+    for (int l = 1; l <= d; l++) {
+        const int64_t self = node / pw;  // this node's ancestor at level l
+        const int j = (int)(self % 7);
+        const int64_t parent = self / 7;
+        h >>= 1;
+        int s = -1;
+        if (which == 0) {
+            if (j == 0) v = wt_quad(v, 0, 0, h);
+            else if (j == 1) v = wt_quad(v, 0, 1, h);
+            else if (j == 3) v = wt_quad(v, 1, 1, h);
+            else s = j == 2 ? 3 : j - 4;
+        } else {
+            if (j == 0) v = wt_quad(v, 0, 0, h);
+            else if (j == 1) v = wt_quad(v, 1, 0, h);
+            else if (j == 2) v = wt_quad(v, 1, 1, h);
+            else s = j == 3 ? 3 : j - 4;
+        }
+        if (s >= 0)
+            v = which ? wt_dense(t.sb_limbs[l], t.sb_sizes[l], 4 * parent + s, h, t.capSB)
+                      : wt_dense(t.sa_limbs[l], t.sa_sizes[l], 4 * parent + s, h, t.capSA);
+        pw /= 7;
+    }
+    return v;
+}
+
+// Level d's sums: one thread per (operand side, parent, entry of the h x h quadrants).
+__global__ void k_wino_sums(WinoTree t, int d, int64_t nparents, int h, uint32_t *err) {
+    const int64_t hh = (int64_t)h * h;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 2 * nparents * hh) return;
+    const int64_t e = idx % hh, rest = idx / hh;
+    const int64_t p = rest % nparents;
+    const int which = (int)(rest / nparents);
+    const MatArgs par = wt_operand(t, which, d - 1, p);
+    const int64_t ip = (e / h) * par.rs + e % h;  // the entry inside each quadrant of the parent
+    const MatArgs x11 = wt_quad(par, 0, 0, h), x12 = wt_quad(par, 0, 1, h), x21 = wt_quad(par, 1, 0, h),
+                  x22 = wt_quad(par, 1, 1, h);
+    uint32_t *L = which ? t.sb_limbs[d] : t.sa_limbs[d];
+    int32_t *S = which ? t.sb_sizes[d] : t.sa_sizes[d];
+    const int cap = which ? t.capSB : t.capSA;
+    const MatArgs o0 = wt_dense(L, S, 4 * p + 0, h, cap), o1 = wt_dense(L, S, 4 * p + 1, h, cap),
+                  o2 = wt_dense(L, S, 4 * p + 2, h, cap), o3 = wt_dense(L, S, 4 * p + 3, h, cap);
+    if (!which) {
+        addsub_entry(o0, e, x21, ip, x22, ip, 0, err);  // S1 = A21 + A22
+        addsub_entry(o1, e, o0, e, x11, ip, 1, err);    // S2 = S1 - A11
+        addsub_entry(o2, e, x11, ip, x21, ip, 1, err);  // S3 = A11 - A21
+        addsub_entry(o3, e, x12, ip, o1, e, 1, err);    // S4 = A12 - S2
+    } else {
+        addsub_entry(o0, e, x12, ip, x11, ip, 1, err);  // T1 = B12 - B11
+        addsub_entry(o1, e, x22, ip, o0, e, 1, err);    // T2 = B22 - T1
+        addsub_entry(o2, e, x22, ip, x12, ip, 1, err);  // T3 = B22 - B12
+        addsub_entry(o3, e, x21, ip, o1, e, 1, err);    // T4' = B21 - T2
+    }
+}
+
+// All leaf products of the tree: one CTA per (leaf, TY x TX tile of its output).
+template <int R, int NT>
+__global__ void __launch_bounds__(NT) k_wino_leaves(WinoTree t, MMCfg cfg, int ny, int nx, uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int64_t tiles = (int64_t)ny * nx;
+    const int64_t node = blockIdx.x / tiles;
+    const int rem = (int)(blockIdx.x % tiles);
+    const int L = t.levels, h = t.N >> L;
+    const MatArgs A = wt_operand(t, 0, L, node), B = wt_operand(t, 1, L, node);
+    const MatArgs C = wt_dense(t.p_limbs[L], t.p_sizes[L], node, h, t.capP);
+    limb_tile<R>(C, A, B, cfg, rem / nx, rem % nx, smem_raw, err);
+}
+
+// Level d's products combined into their parents' outputs (level d - 1): one
+// thread per (parent, entry of the h x h quadrants).  Quadrant entries are
+// written in place in the order that needs no temporary.
+__global__ void k_wino_combine(WinoTree t, int d, int64_t nparents, int h, uint32_t *err) {
+    const int64_t hh = (int64_t)h * h;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nparents * hh) return;
+    const int64_t e = idx % hh, p = idx / hh;
+    const MatArgs Cp = d == 1 ? margs(t.C) : wt_dense(t.p_limbs[d - 1], t.p_sizes[d - 1], p, 2 * h, t.capP);
+    const int64_t ic = (e / h) * Cp.rs + e % h;
+    const MatArgs c11 = wt_quad(Cp, 0, 0, h), c12 = wt_quad(Cp, 0, 1, h), c21 = wt_quad(Cp, 1, 0, h),
+                  c22 = wt_quad(Cp, 1, 1, h);
+    MatArgs M[7];
+#pragma unroll
+    for (int j = 0; j < 7; j++) M[j] = wt_dense(t.p_limbs[d], t.p_sizes[d], 7 * p + j, h, t.capP);
+    addsub_entry(c11, ic, M[0], e, M[1], e, 0, err);    // C11 = M1 + M2
+    addsub_entry(c12, ic, M[0], e, M[5], e, 0, err);    // U2 = M1 + M6
+    addsub_entry(c21, ic, c12, ic, M[6], e, 0, err);    // U3 = U2 + M7
+    addsub_entry(c22, ic, c21, ic, M[4], e, 0, err);    // C22 = U3 + M5
+    addsub_entry(c21, ic, c21, ic, M[3], e, 0, err);    // C21 = U3 + M4'
+    addsub_entry(c12, ic, c12, ic, M[4], e, 0, err);    // U4 = U2 + M5
+    addsub_entry(c12, ic, c12, ic, M[2], e, 0, err);    // C12 = U4 + M3
+}
+
+// Throughput probe for the per-entry product kernels' roofline: every thread runs
+// the 8 x 8 block of 96-bit column multiply-accumulates (MAC96, the inner step of
+// limb_tile at R = 8) on register operands, `iters` times, with no memory traffic.
+// blocks x 256 x iters x 64 MACs per launch; the rate it reaches is the best the
+// product kernels' MAC sequence can do on this GPU.
+__global__ void __launch_bounds__(256) k_mac_peak(uint32_t *out, int iters, uint32_t seed) {
+    uint32_t a[8], b[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        a[i] = seed * (threadIdx.x + 1) + (uint32_t)i * 0x9E3779B9u;
+        b[i] = (seed ^ blockIdx.x) * 0x85EBCA6Bu + (uint32_t)i * 0xC2B2AE35u;
+    }
+    uint32_t P[15][3];
+#pragma unroll
+    for (int c = 0; c < 15; c++) P[c][0] = P[c][1] = P[c][2] = 0;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) MAC96(P[i + j][0], P[i + j][1], P[i + j][2], a[i], b[j]);
+        a[0] ^= P[0][0];
+    }
+    uint32_t acc = 0;
+#pragma unroll
+    for (int c = 0; c < 15; c++) acc ^= P[c][0] ^ P[c][1] ^ P[c][2];
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = acc;
 }
 
 // ---- host launchers ---------------------------------------------------------------------
@@ -911,10 +1333,21 @@ gbmm_status launch_mpz_mulops(const gbmm_mat &w, const gbmm_mat &u, const gbmm_m
 
 static int roundup(int x, int m) { return (x + m - 1) / m * m; }
 
-// Picks the block edge R and group size for limb counts la x lb.
+// Picks the block edge R and group size for limb counts la x lb.  Groups of up
+// to 256 threads share 256-thread CTAs; a group of 257..512 threads (entries of
+// up to 181 x 181 limbs, e.g. the one-limb-longer operands a Winograd level
+// forms from 128-limb entries) gets a CTA of its own.
+static bool choose_mm_blocks(int la, int lb, MMCfg &cfg);
 static bool choose_mm(int la, int lb, MMCfg &cfg) {
     la = la < 1 ? 1 : la;
     lb = lb < 1 ? 1 : lb;
+    if (!choose_mm_blocks(la, lb, cfg)) return false;
+    cfg.thinA = cfg.R > 1 && la % cfg.R == 1;
+    cfg.thinB = cfg.R > 1 && lb % cfg.R == 1;
+    return true;
+}
+static bool choose_mm_blocks(int la, int lb, MMCfg &cfg) {
+    cfg.NT = MM_THREADS;
     const int cand[3] = {8, 4, 2};
     for (int ci = 0; ci < 3; ci++) {
         int R = cand[ci];
@@ -938,7 +1371,28 @@ static bool choose_mm(int la, int lb, MMCfg &cfg) {
             return true;
         }
     }
+    {
+        int R = 8, pa = roundup(la, R), pb = roundup(lb, R), G = (pa / R) * (pb / R);
+        if (G <= MM_THREADS_WIDE) {
+            cfg.R = R; cfg.La = pa; cfg.Lb = pb; cfg.G = G; cfg.Gp = roundup(G, 32);
+            cfg.NT = cfg.Gp;
+            return true;
+        }
+    }
     return false;
+}
+
+// Entries per CTA and their TY x TX arrangement for a chosen group size; the CTA
+// has exactly EPC x Gp threads.
+static void finish_cfg(MMCfg &cfg, int M, int accumulate) {
+    const int EPC = cfg.Gp >= cfg.NT ? 1 : cfg.NT / cfg.Gp;
+    if (cfg.Gp < cfg.NT) cfg.NT = EPC * cfg.Gp;
+    int TY = 1;
+    while (TY * TY * 4 <= EPC) TY *= 2;
+    cfg.TY = TY;
+    cfg.TX = EPC / TY;
+    cfg.M = M;
+    cfg.accumulate = accumulate;
 }
 
 bool limb_kernel_fits(int la, int lb) {
@@ -965,39 +1419,37 @@ gbmm_status launch_limb_matmul(const gbmm_mat &c, const gbmm_mat &a, const gbmm_
     if (!choose_mm(a.nlimbs, b.nlimbs, cfg))
         return set_error(GBMM_ERR_UNSUPPORTED, "limb matmul: %d x %d limb entries exceed the per-entry kernel", a.nlimbs,
                          b.nlimbs);
-    const int EPC = cfg.Gp >= MM_THREADS ? 1 : MM_THREADS / cfg.Gp;
-    int TY = 1;
-    while (TY * TY * 4 <= EPC) TY *= 2;
-    cfg.TY = TY;
-    cfg.TX = EPC / TY;
-    cfg.M = a.cols;
-    cfg.accumulate = accumulate;
+    finish_cfg(cfg, a.cols, accumulate);
     size_t smem = mm_smem(cfg);
     if (smem > 200 * 1024) return set_error(GBMM_ERR_UNSUPPORTED, "limb matmul: shared memory %zu too large", smem);
     dim3 grid((unsigned)((c.cols + cfg.TX - 1) / cfg.TX), (unsigned)((c.rows + cfg.TY - 1) / cfg.TY));
     uint32_t *err = device_error_word();
-#define LAUNCH_R(RR)                                                                                   \
+#define LAUNCH_R(RR, NTT)                                                                              \
     do {                                                                                               \
         if (smem > 48 * 1024)                                                                          \
-            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_limb_matmul<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                               (int)smem));                                            \
+            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_limb_matmul<RR, NTT>,                                 \
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
         LaunchScope ls_("k_limb_matmul", s);                                                            \
-        k_limb_matmul<RR><<<grid, MM_THREADS, smem, s>>>(margs(c), margs(a), margs(b), cfg, err);     \
+        k_limb_matmul<RR, NTT><<<grid, cfg.NT, smem, s>>>(margs(c), margs(a), margs(b), cfg, err);    \
     } while (0)
-    switch (cfg.R) {
-        case 1: LAUNCH_R(1); break;
-        case 2: LAUNCH_R(2); break;
-        case 4: LAUNCH_R(4); break;
-        default: LAUNCH_R(8); break;
+    if (cfg.NT > MM_THREADS) {
+        LAUNCH_R(8, MM_THREADS_WIDE);
+    } else {
+        switch (cfg.R) {
+            case 1: LAUNCH_R(1, MM_THREADS); break;
+            case 2: LAUNCH_R(2, MM_THREADS); break;
+            case 4: LAUNCH_R(4, MM_THREADS); break;
+            default: LAUNCH_R(8, MM_THREADS); break;
+        }
     }
 #undef LAUNCH_R
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
 }
 
-static int occupancy_ctas(const void *fn, size_t smem) {
+static int occupancy_ctas(const void *fn, int nt, size_t smem) {
     int n = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, MM_THREADS, smem) != cudaSuccess || n < 1) n = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, nt, smem) != cudaSuccess || n < 1) n = 1;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1010,23 +1462,26 @@ gbmm_status plan_limb_batch(const std::vector<gbmm_mat> &C, const std::vector<gb
         int job, by, bx;
         double cost;
     };
-    const int Rs[4] = {1, 2, 4, 8};
-    std::vector<LimbJob> jobs[4];
-    std::vector<Item> items[4];
-    size_t smem[4] = {0, 0, 0, 0};
+    // groups: block edge 1, 2, 4, 8 on 256-thread CTAs, and 8 with one wide group per CTA
+    constexpr int NG = 5;
+    const int Rs[NG] = {1, 2, 4, 8, 8};
+    std::vector<LimbJob> jobs[NG];
+    std::vector<Item> items[NG];
+    size_t smem[NG] = {0, 0, 0, 0, 0};
+    int nts[NG] = {MM_THREADS, MM_THREADS, MM_THREADS, MM_THREADS, 0};
     for (size_t i = 0; i < C.size(); i++) {
         MMCfg cfg;
         if (!choose_mm(A[i].nlimbs, B[i].nlimbs, cfg))
             return set_error(GBMM_ERR_UNSUPPORTED, "batched limb job %zu: entries too long", i);
-        const int EPC = cfg.Gp >= MM_THREADS ? 1 : MM_THREADS / cfg.Gp;
-        int TY = 1;
-        while (TY * TY * 4 <= EPC) TY *= 2;
-        cfg.TY = TY;
-        cfg.TX = EPC / TY;
-        cfg.M = A[i].cols;
-        cfg.accumulate = 0;
+        finish_cfg(cfg, A[i].cols, 0);
         int g = 0;
-        while (Rs[g] != cfg.R) g++;
+        if (cfg.NT > MM_THREADS) {
+            // one launch of the wide group kernel runs with a single CTA size
+            g = NG - 1;
+            nts[g] = std::max(nts[g], cfg.NT);
+        } else {
+            while (Rs[g] != cfg.R) g++;
+        }
         smem[g] = std::max(smem[g], mm_smem(cfg));
         LimbJob lj;
         lj.C = margs(C[i]); lj.A = margs(A[i]); lj.B = margs(B[i]); lj.cfg = cfg;
@@ -1039,12 +1494,14 @@ gbmm_status plan_limb_batch(const std::vector<gbmm_mat> &C, const std::vector<gb
     }
     plan.blob.clear();
     plan.groups.clear();
-    for (int g = 0; g < 4; g++) {
+    for (int g = 0; g < NG; g++) {
         if (jobs[g].empty()) continue;
         if (smem[g] > 200 * 1024) return set_error(GBMM_ERR_UNSUPPORTED, "batched limb: shared memory too large");
         std::stable_sort(items[g].begin(), items[g].end(), [](const Item &x, const Item &y) { return x.cost > y.cost; });
         LimbBatchPlan::Group gr;
         gr.R = Rs[g];
+        gr.NT = nts[g];
+        for (auto &j : jobs[g]) j.cfg.NT = nts[g];
         gr.smem = smem[g];
         gr.nitems = (int)items[g].size();
         size_t off = (plan.blob.size() + 255) & ~(size_t)255;
@@ -1073,24 +1530,91 @@ gbmm_status launch_limb_batch(const LimbBatchPlan &plan, const char *d_blob, int
         const LimbBatchPlan::Group &gr = plan.groups[g];
         const LimbJob *jobs = reinterpret_cast<const LimbJob *>(d_blob + gr.jobs_off);
         const int *items = reinterpret_cast<const int *>(d_blob + gr.items_off);
-#define LAUNCH_B(RR)                                                                                            \
-    do {                                                                                                        \
-        if (gr.smem > 48 * 1024)                                                                                \
-            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_limb_batched<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                               (int)gr.smem));                                                  \
-        const int grid = std::min(gr.nitems, occupancy_ctas((const void *)k_limb_batched<RR>, gr.smem));       \
-        LaunchScope ls_("k_limb_batched", s);                                                                   \
-        k_limb_batched<RR><<<grid, MM_THREADS, gr.smem, s>>>(jobs, items, gr.nitems, d_counters + g, err);     \
+#define LAUNCH_B(RR, NTT)                                                                                 \
+    do {                                                                                                  \
+        if (gr.smem > 48 * 1024)                                                                          \
+            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_limb_batched<RR, NTT>,                                   \
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gr.smem)); \
+        const int grid =                                                                                  \
+            std::min(gr.nitems, occupancy_ctas((const void *)k_limb_batched<RR, NTT>, gr.NT, gr.smem));  \
+        LaunchScope ls_("k_limb_batched", s);                                                             \
+        k_limb_batched<RR, NTT><<<grid, gr.NT, gr.smem, s>>>(jobs, items, gr.nitems, d_counters + g, err); \
     } while (0)
-        switch (gr.R) {
-            case 1: LAUNCH_B(1); break;
-            case 2: LAUNCH_B(2); break;
-            case 4: LAUNCH_B(4); break;
-            default: LAUNCH_B(8); break;
+        if (gr.NT > MM_THREADS) {
+            LAUNCH_B(8, MM_THREADS_WIDE);
+        } else {
+            switch (gr.R) {
+                case 1: LAUNCH_B(1, MM_THREADS); break;
+                case 2: LAUNCH_B(2, MM_THREADS); break;
+                case 4: LAUNCH_B(4, MM_THREADS); break;
+                default: LAUNCH_B(8, MM_THREADS); break;
+            }
         }
 #undef LAUNCH_B
         GBMM_CUDA_TRY(cudaGetLastError());
     }
+    return GBMM_OK;
+}
+
+static int64_t pow7(int d) {
+    int64_t r = 1;
+    while (d-- > 0) r *= 7;
+    return r;
+}
+
+gbmm_status launch_wino_sums(const WinoTree &t, int d, cudaStream_t s) {
+    const int64_t np = pow7(d - 1);
+    const int h = t.N >> d;
+    const int64_t n = 2 * np * h * h;
+    LaunchScope ls_("k_wino_sums", s);
+    k_wino_sums<<<grid1(n, 128), 128, 0, s>>>(t, d, np, h, device_error_word());
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+gbmm_status launch_wino_combine(const WinoTree &t, int d, cudaStream_t s) {
+    const int64_t np = pow7(d - 1);
+    const int h = t.N >> d;
+    const int64_t n = np * h * h;
+    LaunchScope ls_("k_wino_combine", s);
+    k_wino_combine<<<grid1(n, 128), 128, 0, s>>>(t, d, np, h, device_error_word());
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+gbmm_status launch_wino_leaves(const WinoTree &t, cudaStream_t s) {
+    const int h = t.N >> t.levels;
+    MMCfg cfg;
+    if (!choose_mm(t.capSA, t.capSB, cfg))
+        return set_error(GBMM_ERR_UNSUPPORTED, "winograd leaves: %d x %d limb operands exceed the per-entry kernel",
+                         t.capSA, t.capSB);
+    finish_cfg(cfg, h, 0);
+    const size_t smem = mm_smem(cfg);
+    if (smem > 200 * 1024) return set_error(GBMM_ERR_UNSUPPORTED, "winograd leaves: shared memory %zu too large", smem);
+    const int ny = (h + cfg.TY - 1) / cfg.TY, nx = (h + cfg.TX - 1) / cfg.TX;
+    const int64_t blocks = pow7(t.levels) * ny * nx;
+    if (blocks > 0x7FFFFFFF) return set_error(GBMM_ERR_UNSUPPORTED, "winograd leaves: %lld tiles", (long long)blocks);
+    uint32_t *err = device_error_word();
+#define LAUNCH_W(RR, NTT)                                                                              \
+    do {                                                                                               \
+        if (smem > 48 * 1024)                                                                          \
+            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_wino_leaves<RR, NTT>,                                 \
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+        LaunchScope ls_("k_wino_leaves", s);                                                            \
+        k_wino_leaves<RR, NTT><<<(unsigned)blocks, cfg.NT, smem, s>>>(t, cfg, ny, nx, err);           \
+    } while (0)
+    if (cfg.NT > MM_THREADS) {
+        LAUNCH_W(8, MM_THREADS_WIDE);
+    } else {
+        switch (cfg.R) {
+            case 1: LAUNCH_W(1, MM_THREADS); break;
+            case 2: LAUNCH_W(2, MM_THREADS); break;
+            case 4: LAUNCH_W(4, MM_THREADS); break;
+            default: LAUNCH_W(8, MM_THREADS); break;
+        }
+    }
+#undef LAUNCH_W
+    GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
 }
 
@@ -1161,6 +1685,99 @@ extern "C" gbmm_status gbmm_mpn_submul_1(uint32_t *rp, const uint32_t *up, int32
                                          int64_t nb, uint32_t *cy, void *stream) {
     return mul1_entry<2>(rp, up, n, vl, ld, nb, cy, stream);
 }
+// Internal probe (not part of the public ABI): one launch of k_mac_peak, blocks x 256
+// threads, each doing iters x 64 MACs; out holds blocks x 256 words.
+extern "C" gbmm_status gbmmx_mac_peak(uint32_t *out, int32_t blocks, int32_t iters, void *stream) {
+    if (!out || blocks < 1 || iters < 1) return set_error(GBMM_ERR_INVALID, "mac peak: bad arguments");
+    LaunchScope ls_("k_mac_peak", as_stream(stream));
+    k_mac_peak<<<blocks, 256, 0, as_stream(stream)>>>(out, iters, 0x2545F491u);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+extern "C" gbmm_status gbmm_mpn_add(uint32_t *rp, const uint32_t *up, int32_t un, const uint32_t *vp, int32_t vn,
+                                    int64_t ld, int64_t nb, uint32_t *cy, void *stream) {
+    GBMM_TRY(check_batch(rp, up, ld, nb, un));
+    if ((!vp && vn > 0) || !cy) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (un < vn || vn < 0 || un < 1) return set_error(GBMM_ERR_INVALID, "mpn_add needs un >= vn >= 0, un >= 1");
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_addsub", as_stream(stream));
+    k_mpn_addsub<false><<<grid1(nb, 256), 256, 0, as_stream(stream)>>>(rp, up, un, vp, vn, ld, nb, cy);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+extern "C" gbmm_status gbmm_mpn_sub(uint32_t *rp, const uint32_t *up, int32_t un, const uint32_t *vp, int32_t vn,
+                                    int64_t ld, int64_t nb, uint32_t *cy, void *stream) {
+    GBMM_TRY(check_batch(rp, up, ld, nb, un));
+    if ((!vp && vn > 0) || !cy) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (un < vn || vn < 0 || un < 1) return set_error(GBMM_ERR_INVALID, "mpn_sub needs un >= vn >= 0, un >= 1");
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_addsub", as_stream(stream));
+    k_mpn_addsub<true><<<grid1(nb, 256), 256, 0, as_stream(stream)>>>(rp, up, un, vp, vn, ld, nb, cy);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+template <bool SUB>
+static gbmm_status addsub_1_entry(uint32_t *rp, const uint32_t *up, int32_t n, const uint32_t *vl, int64_t ld,
+                                  int64_t nb, uint32_t *cy, void *stream) {
+    GBMM_TRY(check_batch(rp, up, ld, nb, n));
+    if (!vl || !cy) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (n < 1) return set_error(GBMM_ERR_INVALID, "mpn_add_1 / mpn_sub_1 need n >= 1");
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_addsub_1", as_stream(stream));
+    k_mpn_addsub_1<SUB><<<grid1(nb, 256), 256, 0, as_stream(stream)>>>(rp, up, n, vl, ld, nb, cy);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+extern "C" gbmm_status gbmm_mpn_add_1(uint32_t *rp, const uint32_t *up, int32_t n, const uint32_t *vl, int64_t ld,
+                                      int64_t nb, uint32_t *cy, void *stream) {
+    return addsub_1_entry<false>(rp, up, n, vl, ld, nb, cy, stream);
+}
+extern "C" gbmm_status gbmm_mpn_sub_1(uint32_t *rp, const uint32_t *up, int32_t n, const uint32_t *vl, int64_t ld,
+                                      int64_t nb, uint32_t *cy, void *stream) {
+    return addsub_1_entry<true>(rp, up, n, vl, ld, nb, cy, stream);
+}
+extern "C" gbmm_status gbmm_mpn_cmp(const uint32_t *up, const uint32_t *vp, int32_t n, int64_t ld, int64_t nb,
+                                    int32_t *result, void *stream) {
+    GBMM_TRY(check_batch(up, vp, ld, nb, n));
+    if (!result) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_cmp", as_stream(stream));
+    k_mpn_cmp<<<grid1(nb, 256), 256, 0, as_stream(stream)>>>(up, vp, n, ld, nb, result);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+extern "C" gbmm_status gbmm_mpn_zero_p(const uint32_t *up, int32_t n, int64_t ld, int64_t nb, int32_t *result,
+                                       void *stream) {
+    GBMM_TRY(check_batch(up, result, ld, nb, n));
+    if (n < 1) return set_error(GBMM_ERR_INVALID, "mpn_zero_p needs n >= 1");
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_zero_p", as_stream(stream));
+    k_mpn_zero_p<<<grid1(nb, 256), 256, 0, as_stream(stream)>>>(up, n, ld, nb, result);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+extern "C" gbmm_status gbmm_mpn_neg(uint32_t *rp, const uint32_t *up, int32_t n, int64_t ld, int64_t nb, uint32_t *cy,
+                                    void *stream) {
+    GBMM_TRY(check_batch(rp, up, ld, nb, n));
+    if (!cy) return set_error(GBMM_ERR_INVALID, "null pointer");
+    if (n < 1) return set_error(GBMM_ERR_INVALID, "mpn_neg needs n >= 1");
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_neg_com", as_stream(stream));
+    k_mpn_neg_com<true><<<grid1(nb, 256), 256, 0, as_stream(stream)>>>(rp, up, n, ld, nb, cy);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+extern "C" gbmm_status gbmm_mpn_com(uint32_t *rp, const uint32_t *up, int32_t n, int64_t ld, int64_t nb,
+                                    void *stream) {
+    GBMM_TRY(check_batch(rp, up, ld, nb, n));
+    if (n < 1) return set_error(GBMM_ERR_INVALID, "mpn_com needs n >= 1");
+    if (nb == 0) return GBMM_OK;
+    LaunchScope ls_("k_mpn_neg_com", as_stream(stream));
+    k_mpn_neg_com<false><<<grid1(nb, 256), 256, 0, as_stream(stream)>>>(rp, up, n, ld, nb, nullptr);
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
 extern "C" gbmm_status gbmm_mpn_mul_basecase(uint32_t *rp, const uint32_t *up, int32_t un, const uint32_t *vp,
                                              int32_t vn, int64_t ld, int64_t nb, void *stream) {
     GBMM_TRY(check_batch(rp, up, ld, nb, un));
@@ -1172,10 +1789,16 @@ extern "C" gbmm_status gbmm_mpn_mul_basecase(uint32_t *rp, const uint32_t *up, i
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
 }
+// 6n + 2 scratch limbs per operand (n = an - floor(an/2)), or -1 when that count
+// does not fit an int32 (an above about 7.1e8 limbs): callers reject those sizes.
+static int64_t toom22_itch64(int32_t an) {
+    const int64_t n = (int64_t)an - (an >> 1);
+    return 6 * n + 2;
+}
 extern "C" int32_t gbmm_mpn_toom22_mul_itch(int32_t an, int32_t bn) {
     (void)bn;
-    int32_t n = an - (an >> 1);
-    return 6 * n + 2;
+    const int64_t itch = toom22_itch64(an);
+    return itch > INT32_MAX ? -1 : (int32_t)itch;
 }
 extern "C" gbmm_status gbmm_mpn_toom22_mul(uint32_t *pp, const uint32_t *ap, int32_t an, const uint32_t *bp, int32_t bn,
                                            uint32_t *scratch, int64_t ld, int64_t nb, void *stream) {
@@ -1184,6 +1807,7 @@ extern "C" gbmm_status gbmm_mpn_toom22_mul(uint32_t *pp, const uint32_t *ap, int
     const int s = an >> 1, n = an - s, t = bn - n;
     if (an < bn || !(0 < s && s <= n && s >= n - 1) || !(0 < t && t <= s))
         return set_error(GBMM_ERR_INVALID, "toom22 preconditions violated (an=%d bn=%d)", an, bn);
+    if (toom22_itch64(an) > INT32_MAX) return set_error(GBMM_ERR_INVALID, "toom22: an=%d is too long", an);
     if (nb == 0) return GBMM_OK;
     LaunchScope ls_("k_mpn_toom22", as_stream(stream));
     k_mpn_toom22<<<grid1(nb, 128), 128, 0, as_stream(stream)>>>(pp, ap, an, bp, bn, scratch, ld, nb);
@@ -1227,12 +1851,14 @@ extern "C" gbmm_status gbmm_mpn_toom22_mul_noalloc(uint32_t *pp, const uint32_t 
     const int s = an >> 1, n = an - s, t = bn - n;
     if (an < bn || !(0 < s && s <= n && s >= n - 1) || !(0 < t && t <= s))
         return set_error(GBMM_ERR_INVALID, "toom22 preconditions violated (an=%d bn=%d)", an, bn);
-    const uint64_t need = (uint64_t)gbmm_mpn_toom22_mul_itch(an, bn) * (uint64_t)ld * 4u;
+    const int64_t itch = toom22_itch64(an);  // 64-bit: no wrap for any int32 an
+    const double need_d = (double)itch * (double)ld * 4.0;
+    const uint64_t need = need_d > 1e18 ? UINT64_MAX : (uint64_t)itch * (uint64_t)ld * 4u;
     if (need > GBMM_NOALLOC_SCRATCH_BYTES)
         return set_error(GBMM_ERR_CAPACITY,
-                         "toom22 without allocation: scratch of %llu bytes (itch %d limbs x plane stride %lld) exceeds "
+                         "toom22 without allocation: scratch of %llu bytes (itch %lld limbs x plane stride %lld) exceeds "
                          "the fixed %d-byte device array",
-                         (unsigned long long)need, gbmm_mpn_toom22_mul_itch(an, bn), (long long)ld,
+                         (unsigned long long)need, (long long)itch, (long long)ld,
                          GBMM_NOALLOC_SCRATCH_BYTES);
     if (nb == 0) return GBMM_OK;
     uint32_t *scratch = nullptr;

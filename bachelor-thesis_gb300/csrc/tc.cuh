@@ -45,11 +45,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // Spin-wait with an upper bound on elapsed SM clocks (~1 s at 2 GHz).  Returns
 // false when the bound expires; callers then record DEVERR_TIMEOUT and unwind.
 constexpr long long WAIT_LIMIT_CLOCKS = 2000000000LL;
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit = WAIT_LIMIT_CLOCKS) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > WAIT_LIMIT_CLOCKS) return false;
+        if (clock64() - t0 > limit) return false;
     }
     return true;
 }

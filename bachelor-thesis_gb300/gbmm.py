@@ -98,6 +98,14 @@ _SIGS = {
     "gbmm_model_train": [_P, _P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_float, _P],
     "gbmm_mpn_add_n": [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, _P, _P],
     "gbmm_mpn_sub_n": [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, _P, _P],
+    "gbmm_mpn_add": [_P, _P, ctypes.c_int32, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, _P, _P],
+    "gbmm_mpn_sub": [_P, _P, ctypes.c_int32, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, _P, _P],
+    "gbmm_mpn_add_1": [_P, _P, ctypes.c_int32, _P, ctypes.c_int64, ctypes.c_int64, _P, _P],
+    "gbmm_mpn_sub_1": [_P, _P, ctypes.c_int32, _P, ctypes.c_int64, ctypes.c_int64, _P, _P],
+    "gbmm_mpn_cmp": [_P, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, _P, _P],
+    "gbmm_mpn_zero_p": [_P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, _P, _P],
+    "gbmm_mpn_neg": [_P, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, _P, _P],
+    "gbmm_mpn_com": [_P, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, _P],
     "gbmm_mpn_mul_1": [_P, _P, ctypes.c_int32, _P, ctypes.c_int64, ctypes.c_int64, _P, _P],
     "gbmm_mpn_addmul_1": [_P, _P, ctypes.c_int32, _P, ctypes.c_int64, ctypes.c_int64, _P, _P],
     "gbmm_mpn_submul_1": [_P, _P, ctypes.c_int32, _P, ctypes.c_int64, ctypes.c_int64, _P, _P],
@@ -428,6 +436,14 @@ class Handle:
     def set_graphs(self, enable):
         check(lib().gbmm_set_graphs(self.h, int(bool(enable))))
 
+    def set_breadth_first(self, enable):
+        """Winograd products as one breadth-first tree (default) or depth first;
+        returns the previous setting (internal switch, for tests and benchmarks)."""
+        f = lib().gbmmx_wino_breadth_first
+        f.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+        f.restype = ctypes.c_int32
+        return bool(f(self.h, int(bool(enable))))
+
     def autotune(self, jobs, repeats=2, log_path=None):
         self.bind_stream()
         check(lib().gbmm_autotune(self.h, jobs, len(jobs), repeats, log_path.encode() if log_path else None))
@@ -526,6 +542,38 @@ def mpn_add_n(rp, up, vp, n, ld, nb, cy):
 
 def mpn_sub_n(rp, up, vp, n, ld, nb, cy):
     check(lib().gbmm_mpn_sub_n(_dp(rp), _dp(up), _dp(vp), n, ld, nb, _dp(cy), stream_ptr()))
+
+
+def mpn_add(rp, up, un, vp, vn, ld, nb, cy):
+    check(lib().gbmm_mpn_add(_dp(rp), _dp(up), un, _dp(vp), vn, ld, nb, _dp(cy), stream_ptr()))
+
+
+def mpn_sub(rp, up, un, vp, vn, ld, nb, cy):
+    check(lib().gbmm_mpn_sub(_dp(rp), _dp(up), un, _dp(vp), vn, ld, nb, _dp(cy), stream_ptr()))
+
+
+def mpn_add_1(rp, up, n, vl, ld, nb, cy):
+    check(lib().gbmm_mpn_add_1(_dp(rp), _dp(up), n, _dp(vl), ld, nb, _dp(cy), stream_ptr()))
+
+
+def mpn_sub_1(rp, up, n, vl, ld, nb, cy):
+    check(lib().gbmm_mpn_sub_1(_dp(rp), _dp(up), n, _dp(vl), ld, nb, _dp(cy), stream_ptr()))
+
+
+def mpn_cmp(up, vp, n, ld, nb, result):
+    check(lib().gbmm_mpn_cmp(_dp(up), _dp(vp), n, ld, nb, _dp(result), stream_ptr()))
+
+
+def mpn_zero_p(up, n, ld, nb, result):
+    check(lib().gbmm_mpn_zero_p(_dp(up), n, ld, nb, _dp(result), stream_ptr()))
+
+
+def mpn_neg(rp, up, n, ld, nb, cy):
+    check(lib().gbmm_mpn_neg(_dp(rp), _dp(up), n, ld, nb, _dp(cy), stream_ptr()))
+
+
+def mpn_com(rp, up, n, ld, nb):
+    check(lib().gbmm_mpn_com(_dp(rp), _dp(up), n, ld, nb, stream_ptr()))
 
 
 def mpn_mul_1(rp, up, n, vl, ld, nb, cy):

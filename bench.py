@@ -184,34 +184,81 @@ def max_over_ranks(world, x):
 
 
 # ------------------------------------------------------------------------------------
-# CPU leg (reference algorithm on the host cores)
+# CPU leg (the reference's algorithm on the host cores)
 # ------------------------------------------------------------------------------------
-def cpu_rows_sample(W, Al, As, Bl, Bs, target_s, nthreads):
-    """Times the CPU implementation on the first r rows of C = A*B, r chosen so
-    the sample takes about target_s seconds.  Returns (limb-MACs/s, seconds, rows, kind)."""
-    import oracle as orc
-    K, M, N = W["K"], W["M"], W["N"]
-    kind = "port"
-    use_gmp = orc.gmp_available()
-    if use_gmp:
-        orc.set_backend(1)
-    cn = 2 * ((W["bits"] + 31) // 32) + 4
+CPU_JOBSZ, CPU_BASESZ = 128, 32   # mat-cpu's -J / -B for -m 31 (its defaults in BASELINE's timing plan)
 
-    def run(rows):
-        Ar = (Al[:, :rows * M], As[:rows * M])
-        t0 = time.perf_counter()
-        orc.matmul_planes(rows, M, N, Ar, (Bl, Bs), cn, method=1, nthreads=nthreads)
-        return time.perf_counter() - t0
 
-    probe = max(1, min(K, nthreads))
-    t = run(probe)
-    rows = int(min(K, max(probe, probe * target_s / max(t, 1e-6))))
-    t = run(rows)
-    macs = limb_macs(rows, M, N, As[:rows * M], Bs)
-    orc.set_backend(0)
-    sample = (f"first {rows} of {K} rows of C ({rows}x{M}x{N}), naive mat_mul order (mat-cpu -m 1), "
-              f"{'libgmp.so.10' if use_gmp else 'restated GMP'} arithmetic, {nthreads} threads")
-    return macs / t, t, rows, kind, sample
+def workload_config(W, seed):
+    """The `config` both arms print (identical dicts, so the two lines compare)."""
+    return {"workload": W["label"], "seed": seed,
+            "l2": "GPU arm: flushed between timed steps (512 MiB write); CPU arm: host caches as they are"}
+
+
+class CpuSampler:
+    """Bounded samples of C = A*B by the reference's methods on the host cores,
+    timing the multiplication only (mat-cpu's "Multiplication took"):
+      -m 1  : the naive mat_mul order (mat-cpu/mat.c:72-82) on the first `rows` rows;
+      -m 31 : jobsz-block products with Winograd leaves (mat-cpu/matj.c:571-660)
+              on the first block row of C.
+    A sample's share of the full product is rows / K, so its limb-MAC/s is the
+    full product's rate; `calibrate` times each method once and keeps the faster.
+    (-m 35, the full-depth Winograd job DAG of mat-cpu/matj.c:214-417, cannot be cut
+    into row samples; the reference's own timings put it behind -m 31 on this
+    workload: 75.7 s against 42.6 s on 8 x86 cores.)"""
+
+    def __init__(self, W, Al, As, Bl, Bs, nthreads, target_s):
+        import oracle as orc
+        self.orc = orc
+        self.W, self.A, self.B = W, (Al, As), (Bl, Bs)
+        self.nthreads, self.target_s = nthreads, target_s
+        self.gmp = orc.gmp_available()
+        self.rows = {}
+        self.cn = 2 * max(Al.shape[0], Bl.shape[0]) + 4
+
+    def _run(self, method, rows):
+        K, M, N = self.W["K"], self.W["M"], self.W["N"]
+        self.orc.set_backend(1 if self.gmp else 0)
+        try:
+            secs, _ = self.orc.sample_rows(K, M, N, self.A, self.B, 0, rows, method=method, basesz=CPU_BASESZ,
+                                           jobsz=CPU_JOBSZ, nthreads=self.nthreads, cn=self.cn)
+        finally:
+            self.orc.set_backend(0)
+        macs = limb_macs(rows, M, N, self.A[1][:rows * M], self.B[1])
+        return macs / secs, secs
+
+    def methods(self):
+        K, M, N = self.W["K"], self.W["M"], self.W["N"]
+        out = [1]
+        if K % CPU_JOBSZ == 0 and M % CPU_JOBSZ == 0 and N % CPU_JOBSZ == 0:
+            out.append(31)
+        return out
+
+    def sample(self, method):
+        """(limb-MAC/s, seconds, rows) of one sample; the first call per method sizes it."""
+        K = self.W["K"]
+        if method not in self.rows:
+            if method == 31:
+                self.rows[method] = CPU_JOBSZ
+            else:
+                probe = max(1, min(K, self.nthreads))
+                _, t = self._run(1, probe)
+                self.rows[1] = int(min(K, max(probe, probe * self.target_s / max(t, 1e-6))))
+        rate, secs = self._run(method, self.rows[method])
+        return rate, secs, self.rows[method]
+
+    def calibrate(self):
+        rates = {m: self.sample(m) for m in self.methods()}
+        best = max(rates, key=lambda m: rates[m][0])
+        return best, rates
+
+    def describe(self, method):
+        K, M, N = self.W["K"], self.W["M"], self.W["N"]
+        r = self.rows[method]
+        how = ("naive mat_mul order (mat-cpu -m 1)" if method == 1 else
+               f"mat-cpu -m 31: {CPU_JOBSZ}-blocks with Winograd leaves to {CPU_BASESZ}")
+        return (f"rows 0-{r - 1} of {K} of C ({r}x{M}x{N}), {how}, "
+                f"{'libgmp.so.10' if self.gmp else 'restated GMP'} arithmetic, {self.nthreads} threads")
 
 
 def run_reference(args, W, world, rank):
@@ -221,9 +268,11 @@ def run_reference(args, W, world, rank):
     Al, As = gen_planes(rng, W["K"] * W["M"], W["bits"], W["zero"], W["short"], W["short_bits"])
     Bl, Bs = gen_planes(rng, W["M"] * W["N"], W["bits"], W["zero"], W["short"], W["short_bits"])
     nthreads = os.cpu_count() or 1
+    cs = CpuSampler(W, Al, As, Bl, Bs, nthreads, args.cpu_seconds)
+    best, cal = cs.calibrate()
     vals, secs = [], []
     for i in range(args.warmup + args.steps):
-        v, t, rows, kind, sample = cpu_rows_sample(W, Al, As, Bl, Bs, args.cpu_seconds, nthreads)
+        v, t, _ = cs.sample(best)
         if i >= args.warmup:
             vals.append(v)
             secs.append(t)
@@ -231,10 +280,14 @@ def run_reference(args, W, world, rank):
     full_s = limb_macs(W["K"], W["M"], W["N"], As, Bs) / value
     line = {
         "impl": "reference", "metric": "limb-MAC/s", "value": value, "unit": "limb-MAC/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * full_s, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": W["label"], "seed": args.seed, "extrapolated_full_product_s": full_s},
-        "cpu_baseline": {"value": value, "unit": "limb-MAC/s", "cores": nthreads, "kind": kind, "sample": sample},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": workload_config(W, args.seed),
+        "run": {"step": "one bounded sample: " + cs.describe(best), "method": f"-m {best}",
+                "methods_timed": {f"-m {m}": {"limb-MAC/s": r[0], "s": r[1]} for m, r in cal.items()},
+                "full_product_s_at_this_rate": full_s},
+        "cpu_baseline": {"value": value, "unit": "limb-MAC/s", "cores": nthreads, "kind": "port",
+                         "sample": cs.describe(best)},
         "e2e": {"value": value, "unit": "limb-MAC/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -348,6 +401,9 @@ def run_gpu(args, W, world, rank, local):
     except (OSError, ValueError):
         pass
     roof = kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof)
+    limb = None
+    if path == gbmm.PATH_CRT and not args.no_limb:
+        limb = measure_limb_path(gbmm, h, dA, dB, dC, K, M, N, nl, args, flush, stream)
 
     if rank != 0:
         return 0
@@ -356,10 +412,9 @@ def run_gpu(args, W, world, rank, local):
         "metric": "limb-MAC/s", "value": value, "unit": "limb-MAC/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16" if path == gbmm.PATH_CRT else "u32", "data": "synthetic",
-        "config": {"workload": W["label"], "path": args.path, "method": args.method, "cutoff": cutoff,
-                   "seed": args.seed, "limb_macs_per_step": macs, "l2": "flushed between timed steps (512 MiB write)",
-                   "check": f"{args.check} entries bit-exact vs Python integers",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(W, args.seed),
+        "run": {"path": args.path, "method": args.method, "cutoff": cutoff, "limb_macs_per_step": macs,
+                "check": f"{args.check} entries bit-exact vs Python integers", "parallelism": f"replicas x{world}"},
         "roofline": roof,
         "kernels": {k: {"launches": v[0], "ms_total": round(v[1], 4)} for k, v in sorted(prof.items())},
         "e2e": {"value": world * macs / e2e_s, "unit": "limb-MAC/s", "h2d_bytes_per_step": h2d,
@@ -368,10 +423,15 @@ def run_gpu(args, W, world, rank, local):
         "gpu_launches": int(launches // max(1, args.steps)) * args.steps,
         "clocks": clocks,
     }
+    if limb is not None:
+        line["limb_path"] = limb
+        line["crt_over_limb"] = limb["ms_per_step"] / ms
     if not args.no_cpu and world == 1:
-        v, t, rows, kind, sample = cpu_rows_sample(W, Al, As, Bl, Bs, args.cpu_seconds, os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": v, "unit": "limb-MAC/s", "cores": os.cpu_count() or 1, "kind": kind,
-                                "sample": sample}
+        cs = CpuSampler(W, Al, As, Bl, Bs, os.cpu_count() or 1, args.cpu_seconds)
+        best, cal = cs.calibrate()
+        line["cpu_baseline"] = {"value": cal[best][0], "unit": "limb-MAC/s", "cores": os.cpu_count() or 1,
+                                "kind": "port", "sample": cs.describe(best),
+                                "methods_timed": {f"-m {m}": r[0] for m, r in cal.items()}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -451,6 +511,101 @@ def kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof):
     ach = bytes_ / (per_ms * 1e-3) / 1e9
     return {"kernel": kname, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
             "traffic": None, "peak_source": src, "ms_per_launch": per_ms, "note": note}
+
+
+def mac_peak(gbmm, stream):
+    """Measured 32x32-bit MAC rate of the product kernels' inner step (k_mac_peak:
+    MAC96 on register operands, 8 CTAs per SM); best of 5 launches."""
+    import ctypes
+    import torch
+    f = gbmm.lib().gbmmx_mac_peak
+    f.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]
+    blocks = 8 * torch.cuda.get_device_properties(0).multi_processor_count
+    iters = 4000
+    out = torch.zeros(blocks * 256, dtype=torch.int32, device="cuda")
+    for _ in range(2):
+        gbmm.check(f(out.data_ptr(), blocks, iters, stream.cuda_stream))
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        gbmm.check(f(out.data_ptr(), blocks, iters, stream.cuda_stream))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return blocks * 256 * iters * 64 / (best * 1e-3)
+
+
+def winograd_leaf_macs(N, levels, la, lb):
+    """32x32-bit MACs of the breadth-first tree's leaf products: 7^levels products of
+    h = N / 2^levels; a leaf's A operand is a quadrant of A (la limbs) when its path
+    takes only the A11 / A12 / A22 children (3 of 7), else a sum of la + 1 limbs;
+    likewise B with B11 / B21 / B22."""
+    h = N >> levels
+    n_all, n_a, n_b, n_ab = 7 ** levels, 3 ** levels, 3 ** levels, 2 ** levels
+    macs = ((n_all - n_a - n_b + n_ab) * (la + 1) * (lb + 1) + (n_a - n_ab) * la * (lb + 1) +
+            (n_b - n_ab) * (la + 1) * lb + n_ab * la * lb)
+    return macs * h ** 3
+
+
+def measure_limb_path(gbmm, h, dA, dB, dC_crt, K, M, N, nl, args, flush, stream):
+    """The plain limb form on the same inputs (the >= 10x comparison of the CRT form is
+    against this): Winograd's breadth-first tree to the cutoff, or the per-entry kernel
+    alone for --limb-method naive.  Its result must equal the CRT result bit for bit.
+    Returns the record for the bench line."""
+    import torch
+    method = gbmm.METHOD_WINOGRAD if args.limb_method == "winograd" else gbmm.METHOD_NAIVE
+    cutoff = args.limb_cutoff
+    cn = max(gbmm.limbs_needed(nl, nl, M, path=gbmm.PATH_LIMB, method=method, cutoff=cutoff), dC_crt.nlimbs)
+    dL = gbmm.DeviceMatrix(K, N, cn)
+
+    def step():
+        h.matmul(dL, dA, dB, path=gbmm.PATH_LIMB, method=method, cutoff=cutoff)
+
+    step()
+    torch.cuda.synchronize()
+    same = bool(torch.equal(dL.sizes_t, dC_crt.sizes_t)) and bool(
+        torch.equal(dL.limbs_t[:dC_crt.nlimbs * K * N], dC_crt.limbs_t[:dC_crt.nlimbs * K * N])) and not bool(
+        dL.limbs_t[dC_crt.nlimbs * K * N:].any())
+    if not same:
+        raise SystemExit("bench: the limb path and the CRT path differ")
+    times = []
+    l0 = gbmm.kernel_launches()
+    for i in range(args.limb_steps):
+        flush.fill_(i)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    launches = (gbmm.kernel_launches() - l0) // max(1, args.limb_steps)
+    gbmm.profile(True)
+    flush.fill_(7)
+    step()
+    torch.cuda.synchronize()
+    prof = gbmm.profile_read()
+    gbmm.profile(False)
+    levels = 0
+    if method == gbmm.METHOD_WINOGRAD and K == M == N and K > cutoff:
+        # the recursion depth the library uses: floor(log2(N / cutoff)), lowered until 2^levels divides N
+        levels = (K // cutoff).bit_length() - 1
+        while levels > 0 and K % (1 << levels):
+            levels -= 1
+    lk = "k_wino_leaves" if "k_wino_leaves" in prof else "k_limb_matmul"
+    lms = prof.get(lk, (1, 0.0))[1]
+    macs = winograd_leaf_macs(K, levels, nl, nl) if lk == "k_wino_leaves" else K * M * N * nl * nl
+    peak = mac_peak(gbmm, stream)
+    ach = macs / (lms * 1e-3)
+    return {"ms_per_step": statistics.median(times), "steps": args.limb_steps, "method": args.limb_method,
+            "cutoff": cutoff if method == gbmm.METHOD_WINOGRAD else None, "levels": levels,
+            "launches_per_step": int(launches), "equals_crt_result": same,
+            "kernels": {k: {"launches": v[0], "ms_total": round(v[1], 3)} for k, v in sorted(prof.items())},
+            "roofline": {"kernel": lk, "bound": "int-mul", "achieved": ach, "peak": peak, "unit": "MAC/s",
+                         "frac": ach / peak,
+                         "note": "32x32-bit limb MACs of the leaf products / leaf kernel time; peak: measured "
+                                 "rate of the same 96-bit column MAC step on register operands (k_mac_peak)"}}
 
 
 def gen_jobs(gbmm, W, seed):
@@ -739,8 +894,12 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--check", type=int, default=16)
     ap.add_argument("--profile-steps", type=int, default=2)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-limb", action="store_true", help="skip the plain limb form's figure")
+    ap.add_argument("--limb-method", default="winograd", choices=["winograd", "naive"])
+    ap.add_argument("--limb-cutoff", type=int, default=64)
+    ap.add_argument("--limb-steps", type=int, default=2)
     ap.add_argument("--size", type=int, default=0,
                     help="override K=M=N of a single-product workload (small cases for profiling)")
     ap.add_argument("--bits", type=int, default=0, help="override the entry bit length")

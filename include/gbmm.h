@@ -17,6 +17,13 @@
  * sign of the value.  Limbs at positions >= |size| must be zero.  This is the
  * interleaved layout of the reference (mat-gpu/gmp-es-mpz.h:38-42,
  * mat-gpu/main.cu:137-156) with the fixed NUM_SIZE capacity removed.
+ *
+ * Per-device state.  The library keeps a small amount of state per device
+ * ordinal for the life of the process (the device error word kernels report
+ * capacity overflow and expired waits in, and the device address of the fixed
+ * scratch array of gbmm_mpn_toom22_mul_noalloc).  cudaDeviceReset destroys it
+ * behind the library's back: do not call the library on a device after
+ * resetting it in the same process.
  */
 #ifndef GBMM_H
 #define GBMM_H
@@ -282,6 +289,35 @@ gbmm_status gbmm_mpn_add_n(uint32_t *rp, const uint32_t *up, const uint32_t *vp,
 /* rp = up - vp (n limbs), cy[b] = borrow.  replaces: gpu_mpn_sub_n (mat-gpu/sub_n.cu:36-59). */
 gbmm_status gbmm_mpn_sub_n(uint32_t *rp, const uint32_t *up, const uint32_t *vp, int32_t n,
                            int64_t ld, int64_t nb, uint32_t *cy, void *stream);
+/* rp (un limbs) = up (un) + vp (vn), un >= vn >= 0, un >= 1; cy[b] = carry.
+ * replaces: gpu_mpn_add (mat-gpu/addsub.cu:187-192). */
+gbmm_status gbmm_mpn_add(uint32_t *rp, const uint32_t *up, int32_t un, const uint32_t *vp, int32_t vn,
+                         int64_t ld, int64_t nb, uint32_t *cy, void *stream);
+/* rp (un limbs) = up (un) - vp (vn), un >= vn >= 0, un >= 1; cy[b] = borrow.
+ * replaces: gpu_mpn_sub (mat-gpu/addsub.cu:284-289). */
+gbmm_status gbmm_mpn_sub(uint32_t *rp, const uint32_t *up, int32_t un, const uint32_t *vp, int32_t vn,
+                         int64_t ld, int64_t nb, uint32_t *cy, void *stream);
+/* rp = up + vl[b] (one limb per operand), n >= 1; cy[b] = carry.
+ * replaces: gpu_mpn_add_1 (mat-gpu/addsub.cu:236-242). */
+gbmm_status gbmm_mpn_add_1(uint32_t *rp, const uint32_t *up, int32_t n, const uint32_t *vl, int64_t ld,
+                           int64_t nb, uint32_t *cy, void *stream);
+/* rp = up - vl[b], n >= 1; cy[b] = borrow.  replaces: gpu_mpn_sub_1 (mat-gpu/addsub.cu:302-308). */
+gbmm_status gbmm_mpn_sub_1(uint32_t *rp, const uint32_t *up, int32_t n, const uint32_t *vl, int64_t ld,
+                           int64_t nb, uint32_t *cy, void *stream);
+/* result[b] = -1, 0 or 1: the sign of up - vp over n limbs (device int32 array).
+ * replaces: gpu_mpn_cmp (mat-gpu/addsub.cu:244-250). */
+gbmm_status gbmm_mpn_cmp(const uint32_t *up, const uint32_t *vp, int32_t n, int64_t ld, int64_t nb,
+                         int32_t *result, void *stream);
+/* result[b] = 1 when all n >= 1 limbs of operand b are zero, else 0.
+ * replaces: gpu_mpn_zero_p (mat-gpu/addsub.cu:260-270). */
+gbmm_status gbmm_mpn_zero_p(const uint32_t *up, int32_t n, int64_t ld, int64_t nb, int32_t *result,
+                            void *stream);
+/* rp = -up mod 2^(32n), n >= 1; cy[b] = 1 unless up is zero (GMP's borrow).
+ * replaces: gpu_mpn_neg (mat-gpu/addsub.cu:310-326). */
+gbmm_status gbmm_mpn_neg(uint32_t *rp, const uint32_t *up, int32_t n, int64_t ld, int64_t nb, uint32_t *cy,
+                         void *stream);
+/* rp = ~up (one's complement of every limb), n >= 1.  replaces: gpu_mpn_com (mat-gpu/com.cu:35-42). */
+gbmm_status gbmm_mpn_com(uint32_t *rp, const uint32_t *up, int32_t n, int64_t ld, int64_t nb, void *stream);
 /* rp = up * vl[b], cy[b] = high limb.  replaces: gpu_mpn_mul_1 (mat-gpu/mul_1.cu:37-58). */
 gbmm_status gbmm_mpn_mul_1(uint32_t *rp, const uint32_t *up, int32_t n, const uint32_t *vl,
                            int64_t ld, int64_t nb, uint32_t *cy, void *stream);
@@ -296,7 +332,9 @@ gbmm_status gbmm_mpn_submul_1(uint32_t *rp, const uint32_t *up, int32_t n, const
 gbmm_status gbmm_mpn_mul_basecase(uint32_t *rp, const uint32_t *up, int32_t un,
                                   const uint32_t *vp, int32_t vn, int64_t ld, int64_t nb,
                                   void *stream);
-/* Scratch limbs per operand that gbmm_mpn_toom22_mul needs (times ld planes). */
+/* Scratch limbs per operand that gbmm_mpn_toom22_mul needs (times ld planes):
+ * 6n + 2 with n = an - floor(an/2), or -1 when that does not fit an int32
+ * (an above about 7.1e8 limbs; the Toom-2.2 entry points reject such an). */
 int32_t gbmm_mpn_toom22_mul_itch(int32_t an, int32_t bn);
 /* pp (an+bn limbs) = ap * bp by one Karatsuba (Toom-2.2) split; preconditions
  * as GMP: an >= bn, with s = an/2, n = an - s, t = bn - n: 0 < t <= s.
@@ -317,9 +355,12 @@ gbmm_status gbmm_mpn_toom22_mul(uint32_t *pp, const uint32_t *ap, int32_t an,
  * gbmm_mpn_toom22_mul_itch(an, bn) * ld * 4 must not exceed
  * GBMM_NOALLOC_SCRATCH_BYTES (GBMM_ERR_CAPACITY otherwise).  The first call on
  * a device looks up the array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture.  Every call shares the one
- * array, so calls whose kernels may overlap on the GPU (different streams
- * without ordering between them) race on it.  No allocation of any kind.
+ * that first call before any stream capture.  The address is cached per
+ * device ordinal for the life of the process: after cudaDeviceReset (or any
+ * teardown of the primary context) it is stale, so do not call this entry
+ * point after a reset.  Every call shares the one array, so calls whose
+ * kernels may overlap on the GPU (different streams without ordering between
+ * them) race on it.  No allocation of any kind.
  * No counterpart in the reference. */
 gbmm_status gbmm_mpn_toom22_mul_noalloc(uint32_t *pp, const uint32_t *ap, int32_t an,
                                         const uint32_t *bp, int32_t bn, int64_t ld, int64_t nb,

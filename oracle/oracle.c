@@ -733,6 +733,101 @@ int oracle_matmul_planes(int K, int M, int N,
     return rc;
 }
 
+/* ---- bounded CPU samples of the reference's multiplication (benchmark leg) ------
+ * Rows [r0, r0 + rb) of C = A*B by one of mat-cpu's methods, with only the
+ * multiplication timed (like mat-cpu's "Multiplication took", mat-cpu/main.c).
+ *   method 1: the naive order (mat.c:72-82), rows spread over the threads;
+ *   method 31: mat-cpu -m 31's decomposition (matj.c:571-660): bs x bs block
+ *     products (bs = jobsz) each run mat_mul_winograd with
+ *     nlevels = floor(log2(bs / basesz)) (matj.c:583-586, util.c:24-26); the
+ *     sample is one block row of C (rb = bs), its N/bs x M/bs block products
+ *     spread over the threads, then summed per output block.
+ * The sample's share of the full product is rb / K for both methods. */
+typedef struct {
+    unsigned bs, nbj, nkb, nlevels;
+    const onum *A; long Ars; const onum *B; long Brs;
+    mat_t *P;   /* nbj * nkb block products */
+    int next; pthread_mutex_t mu;
+} rowblock_job;
+static void *rowblock_worker(void *arg) {
+    rowblock_job *J = (rowblock_job *)arg;
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        int t = J->next++;
+        pthread_mutex_unlock(&J->mu);
+        if (t >= (int)(J->nbj * J->nkb)) break;
+        unsigned bj = (unsigned)t / J->nkb, kb = (unsigned)t % J->nkb, bs = J->bs;
+        J->P[t] = mat_init(bs, bs);
+        mat_mul_winograd(bs, J->P[t], bs, J->A + (long)kb * bs, J->Ars, J->B + (long)kb * bs * J->Brs + (long)bj * bs,
+                         J->Brs, J->nlevels);
+    }
+    return NULL;
+}
+double oracle_sample_rows(int K, int M, int N, const uint32_t *Al, const int32_t *As, int64_t lda,
+                          const uint32_t *Bl, const int32_t *Bs, int64_t ldb, uint32_t *Cl, int32_t *Cs, int32_t cn,
+                          int64_t ldc, int r0, int rb, int method, int basesz, int jobsz, int nthreads) {
+    if (r0 < 0 || rb < 1 || r0 + rb > K || M < 1 || N < 1) return -1.0;
+    if (basesz <= 0) basesz = 32;
+    if (jobsz <= 0) jobsz = 128;
+    const int blocked = method == 31 && rb == jobsz && M % jobsz == 0 && N % jobsz == 0;
+    if (method != 1 && !blocked) return -1.0;
+    const num_ops *saved = g_ops;
+    const int use_gmp = g_ops == &g_gmp_ops;
+    g_ops = &g_own_ops;
+    mat_t A = mat_init((unsigned)M, (unsigned)rb), B = mat_init((unsigned)N, (unsigned)M);
+    for (int64_t e = 0; e < (int64_t)rb * M; e++) planes_to_own(&A[e], Al, As, lda, (int64_t)r0 * M + e);
+    for (int64_t e = 0; e < (int64_t)M * N; e++) planes_to_own(&B[e], Bl, Bs, ldb, e);
+    if (use_gmp) {
+        /* move the operands into GMP-managed numbers (same struct shape) */
+        g_ops = &g_gmp_ops;
+        mat_t A2 = mat_init((unsigned)M, (unsigned)rb), B2 = mat_init((unsigned)N, (unsigned)M);
+        for (int64_t e = 0; e < (int64_t)rb * M; e++) g_gmp_ops.set(&A2[e], &A[e]);
+        for (int64_t e = 0; e < (int64_t)M * N; e++) g_gmp_ops.set(&B2[e], &B[e]);
+        g_ops = &g_own_ops;
+        mat_free((unsigned)M, (unsigned)rb, A); mat_free((unsigned)N, (unsigned)M, B);
+        A = A2; B = B2;
+        g_ops = &g_gmp_ops;
+    }
+    mat_t C = mat_init((unsigned)N, (unsigned)rb);
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    if (!blocked) {
+        naive_threaded((unsigned)rb, (unsigned)M, (unsigned)N, C, N, A, M, B, N, nthreads, 0);
+    } else {
+        rowblock_job J;
+        J.bs = (unsigned)jobsz; J.nbj = (unsigned)(N / jobsz); J.nkb = (unsigned)(M / jobsz);
+        J.nlevels = jobsz <= basesz ? 0 : ilog2u((unsigned)(jobsz / basesz));
+        J.A = A; J.Ars = M; J.B = B; J.Brs = N;
+        J.P = (mat_t *)calloc((size_t)J.nbj * J.nkb, sizeof(mat_t));
+        J.next = 0;
+        pthread_mutex_init(&J.mu, NULL);
+        int nt = nthreads < 1 ? 1 : nthreads;
+        pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nt);
+        for (int i = 0; i < nt; i++) pthread_create(&th[i], NULL, rowblock_worker, &J);
+        for (int i = 0; i < nt; i++) pthread_join(th[i], NULL);
+        free(th);
+        pthread_mutex_destroy(&J.mu);
+        for (unsigned bj = 0; bj < J.nbj; bj++) {
+            onum *Cb = C + (long)bj * J.bs;
+            mat_t *Pb = J.P + (size_t)bj * J.nkb;
+            mat_add(J.bs, J.bs, Cb, N, Pb[0], J.bs, Pb[J.nkb > 1 ? 1 : 0], J.bs);
+            if (J.nkb == 1) mat_sub(J.bs, J.bs, Cb, N, Cb, N, Pb[0], J.bs);  /* C = P0 + P0 - P0 */
+            for (unsigned kb = 2; kb < J.nkb; kb++) mat_add(J.bs, J.bs, Cb, N, Cb, N, Pb[kb], J.bs);
+        }
+        for (unsigned i = 0; i < J.nbj * J.nkb; i++) mat_free(J.bs, J.bs, J.P[i]);
+        free(J.P);
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    const double secs = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+    int rc = 0;
+    if (Cl)
+        for (int64_t e = 0; e < (int64_t)rb * N; e++)
+            if (own_to_planes(&C[e], Cl, Cs, cn, ldc, e)) rc = -1;
+    mat_free((unsigned)M, (unsigned)rb, A); mat_free((unsigned)N, (unsigned)M, B); mat_free((unsigned)N, (unsigned)rb, C);
+    g_ops = saved;
+    return rc ? -1.0 : secs;
+}
+
 /* Elementwise signed add (sub = 0) or subtract (sub = 1) of n entries. */
 int oracle_addsub_planes(int64_t n, const uint32_t *Al, const int32_t *As, int64_t lda,
                          const uint32_t *Bl, const int32_t *Bs, int64_t ldb,
@@ -822,6 +917,78 @@ void oracle_mpn_mul_basecase(uint32_t *rp, const uint32_t *up, int un, const uin
             }
             rp[(j + un) * ld + b] = (uint32_t)c;
         }
+    }
+}
+
+/* The rest of the mpn layer the reference exposes (mat-gpu/addsub.cu:187-326,
+ * mat-gpu/com.cu:35-42), GMP semantics, batched over operands with plane stride
+ * ld.  rp = up + vp with un >= vn >= 0 limbs (vp zero-extended), carry out;
+ * rp = up - vp, borrow out (addsub.cu:187-192, 284-289). */
+void oracle_mpn_addsub(int sub, uint32_t *rp, const uint32_t *up, int un, const uint32_t *vp, int vn, int64_t ld,
+                       int64_t nb, uint32_t *cy) {
+    for (int64_t b = 0; b < nb; b++) {
+        uint64_t c = 0;
+        for (int i = 0; i < un; i++) {
+            uint64_t y = i < vn ? vp[i * ld + b] : 0;
+            if (!sub) {
+                uint64_t s = (uint64_t)up[i * ld + b] + y + c;
+                rp[i * ld + b] = (uint32_t)s; c = s >> 32;
+            } else {
+                uint64_t d = (uint64_t)up[i * ld + b] - y - c;
+                rp[i * ld + b] = (uint32_t)d; c = (d >> 32) & 1;
+            }
+        }
+        cy[b] = (uint32_t)c;
+    }
+}
+/* rp = up +/- vl[b] (one limb), n >= 1; carry / borrow out (addsub.cu:236-242, 302-308) */
+void oracle_mpn_addsub_1(int sub, uint32_t *rp, const uint32_t *up, int n, const uint32_t *vl, int64_t ld, int64_t nb,
+                         uint32_t *cy) {
+    for (int64_t b = 0; b < nb; b++) {
+        uint64_t c = vl[b];
+        for (int i = 0; i < n; i++) {
+            if (!sub) {
+                uint64_t s = (uint64_t)up[i * ld + b] + c;
+                rp[i * ld + b] = (uint32_t)s; c = s >> 32;
+            } else {
+                uint64_t d = (uint64_t)up[i * ld + b] - c;
+                rp[i * ld + b] = (uint32_t)d; c = (d >> 32) & 1;
+            }
+        }
+        cy[b] = (uint32_t)c;
+    }
+}
+/* res[b] = sign of up - vp over n limbs: -1, 0, 1 (addsub.cu:244-250) */
+void oracle_mpn_cmp(const uint32_t *up, const uint32_t *vp, int n, int64_t ld, int64_t nb, int32_t *res) {
+    for (int64_t b = 0; b < nb; b++) {
+        int r = 0;
+        for (int i = n - 1; i >= 0 && !r; i--) {
+            uint32_t x = up[i * ld + b], y = vp[i * ld + b];
+            if (x != y) r = x > y ? 1 : -1;
+        }
+        res[b] = r;
+    }
+}
+/* res[b] = 1 when all n limbs are zero (addsub.cu:260-270) */
+void oracle_mpn_zero_p(const uint32_t *up, int n, int64_t ld, int64_t nb, int32_t *res) {
+    for (int64_t b = 0; b < nb; b++) {
+        int z = 1;
+        for (int i = 0; i < n; i++) z &= up[i * ld + b] == 0;
+        res[b] = z;
+    }
+}
+/* rp = -up mod B^n, cy = 1 unless up is zero (addsub.cu:310-326); rp = ~up (com.cu:35-42) */
+void oracle_mpn_neg_com(int com, uint32_t *rp, const uint32_t *up, int n, int64_t ld, int64_t nb, uint32_t *cy) {
+    for (int64_t b = 0; b < nb; b++) {
+        uint64_t c = com ? 0 : 1;
+        int nz = 0;
+        for (int i = 0; i < n; i++) {
+            uint32_t u = up[i * ld + b];
+            nz |= u != 0;
+            uint64_t s = (uint64_t)(uint32_t)~u + c;
+            rp[i * ld + b] = (uint32_t)s; c = s >> 32;
+        }
+        if (cy) cy[b] = (uint32_t)nz;
     }
 }
 

@@ -60,6 +60,15 @@ def lib():
         L.oracle_mpn_sub_n.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, P]
         L.oracle_mpn_mul1ops.argtypes = [ctypes.c_int, P, P, ctypes.c_int, P, ctypes.c_int64, ctypes.c_int64, P]
         L.oracle_mpn_mul_basecase.argtypes = [P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int64, ctypes.c_int64]
+        L.oracle_sample_rows.restype = ctypes.c_double
+        L.oracle_sample_rows.argtypes = [ctypes.c_int] * 3 + [P, P, ctypes.c_int64] * 2 + \
+            [P, P, ctypes.c_int32, ctypes.c_int64] + [ctypes.c_int] * 6
+        L.oracle_mpn_addsub.argtypes = [ctypes.c_int, P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int64,
+                                        ctypes.c_int64, P]
+        L.oracle_mpn_addsub_1.argtypes = [ctypes.c_int, P, P, ctypes.c_int, P, ctypes.c_int64, ctypes.c_int64, P]
+        L.oracle_mpn_cmp.argtypes = [P, P, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, P]
+        L.oracle_mpn_zero_p.argtypes = [P, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, P]
+        L.oracle_mpn_neg_com.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, P]
         _lib = L
     return _lib
 
@@ -107,6 +116,23 @@ def matmul_planes(K, M, N, A, B, cn, method=1, basesz=32, jobsz=128, nthreads=1,
     if rc != 0:
         raise ValueError("oracle: C capacity too small")
     return Cl, Cs
+
+
+def sample_rows(K, M, N, A, B, r0, rb, method=1, basesz=32, jobsz=128, nthreads=1, cn=None):
+    """Rows [r0, r0 + rb) of C = A*B by mat-cpu's method 1 (naive order) or 31
+    (jobsz-blocks with Winograd leaves; rb must equal jobsz), timing only the
+    multiplication.  Returns (seconds, (C limbs [cn, rb*N], C sizes [rb*N]))."""
+    Al, As = _c(A[0], np.uint32), _c(A[1], np.int32)
+    Bl, Bs = _c(B[0], np.uint32), _c(B[1], np.int32)
+    cn = cn or (Al.shape[0] + Bl.shape[0] + 2)
+    Cl = np.zeros((cn, rb * N), dtype=np.uint32)
+    Cs = np.zeros(rb * N, dtype=np.int32)
+    secs = lib().oracle_sample_rows(K, M, N, Al.ctypes.data, As.ctypes.data, K * M, Bl.ctypes.data, Bs.ctypes.data,
+                                    M * N, Cl.ctypes.data, Cs.ctypes.data, cn, rb * N, r0, rb, method, basesz, jobsz,
+                                    nthreads)
+    if secs < 0:
+        raise ValueError("oracle: bad sample request or C capacity too small")
+    return secs, (Cl, Cs)
 
 
 def addsub_planes(A, B, cn, sub):
@@ -163,6 +189,52 @@ def mpn_mul_basecase(u, v):
     r = np.zeros((un + vn, nb), dtype=np.uint32)
     lib().oracle_mpn_mul_basecase(r.ctypes.data, u.ctypes.data, un, v.ctypes.data, vn, nb, nb)
     return r
+
+
+def mpn_addsub(u, v, sub=False):
+    """u [un, nb], v [vn, nb] (un >= vn) -> (r [un, nb], carry / borrow [nb])."""
+    u, v = _c(u, np.uint32), _c(v, np.uint32)
+    un, nb = u.shape
+    vn = v.shape[0]
+    r = np.zeros_like(u)
+    cy = np.zeros(nb, dtype=np.uint32)
+    lib().oracle_mpn_addsub(int(sub), r.ctypes.data, u.ctypes.data, un, v.ctypes.data, vn, nb, nb, cy.ctypes.data)
+    return r, cy
+
+
+def mpn_addsub_1(u, vl, sub=False):
+    u, vl = _c(u, np.uint32), _c(vl, np.uint32)
+    n, nb = u.shape
+    r = np.zeros_like(u)
+    cy = np.zeros(nb, dtype=np.uint32)
+    lib().oracle_mpn_addsub_1(int(sub), r.ctypes.data, u.ctypes.data, n, vl.ctypes.data, nb, nb, cy.ctypes.data)
+    return r, cy
+
+
+def mpn_cmp(u, v):
+    u, v = _c(u, np.uint32), _c(v, np.uint32)
+    n, nb = u.shape
+    res = np.zeros(nb, dtype=np.int32)
+    lib().oracle_mpn_cmp(u.ctypes.data, v.ctypes.data, n, nb, nb, res.ctypes.data)
+    return res
+
+
+def mpn_zero_p(u):
+    u = _c(u, np.uint32)
+    n, nb = u.shape
+    res = np.zeros(nb, dtype=np.int32)
+    lib().oracle_mpn_zero_p(u.ctypes.data, n, nb, nb, res.ctypes.data)
+    return res
+
+
+def mpn_neg_com(u, com=False):
+    """-u mod B^n with the nonzero flag (neg), or ~u (com)."""
+    u = _c(u, np.uint32)
+    n, nb = u.shape
+    r = np.zeros_like(u)
+    cy = np.zeros(nb, dtype=np.uint32)
+    lib().oracle_mpn_neg_com(int(com), r.ctypes.data, u.ctypes.data, n, nb, nb, cy.ctypes.data)
+    return r, cy
 
 
 def ref_cli_available():

@@ -290,3 +290,32 @@ def test_crt_vs_limb_random_shapes(g, mode):
     for j, (rl, rs), (cl, cs_) in zip(jobs, refs, outs):
         assert (cs_ == rs).all() and (cl == rl).all(), j[:3]
     h.close()
+
+
+@pytest.mark.parametrize("skip_step", [0, 3, 7])
+def test_bounded_wait_expires_and_context_survives(g, skip_step):
+    """The failure path of the tensor-core pipelines, made to happen: in the
+    single-CTA test GEMM (K = 512: 8 K steps through 4 stages) the producer leaves
+    one K step unloaded, so nothing arms that stage's barrier and the MMA issuer's
+    wait for it cannot complete.  With every wait bounded to 2e7 SM clocks (about
+    10 ms), each role must give up, let its in-flight copies and MMAs finish, free
+    TMEM and exit: the call returns GBMM_ERR_TIMEOUT instead of hanging, and the
+    same context then computes a correct product."""
+    import torch
+    rng = np.random.default_rng(skip_step)
+    A = rng.integers(-128, 128, size=(128, 512))
+    B = rng.integers(-128, 128, size=(128, 512))
+    dA, dB = _bf16(torch, A), _bf16(torch, B)
+    D = torch.zeros(128 * 128, dtype=torch.int32, device="cuda")
+    L = g.lib()
+    f = L.gbmmx_test_gemm_timeout
+    f.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    st = f(dA.data_ptr(), dB.data_ptr(), D.data_ptr(), 512, skip_step, 20_000_000, g.stream_ptr())
+    assert st == g.ERR_TIMEOUT, (st, L.gbmm_last_error_string())
+    assert b"wait expired" in L.gbmm_last_error_string()
+    # the device error word was read and cleared; the context still runs kernels correctly
+    L.gbmmx_test_gemm.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int32] * 4 + [ctypes.c_void_p]
+    g.check(L.gbmmx_test_gemm(dA.data_ptr(), dB.data_ptr(), D.data_ptr(), 128, 128, 512, 0, g.stream_ptr()))
+    torch.cuda.synchronize()
+    assert (D.cpu().numpy().reshape(128, 128) == A @ B.T).all()

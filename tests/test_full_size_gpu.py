@@ -3,7 +3,8 @@ sizes, bit for bit against the CPU oracle (the reference's naive mat_mul order,
 mat-cpu/mat.c:72-82, over GMP arithmetic on all host cores).
 
 - 512 x 512 x 512 at 4096 bits (the headline workload) through gbmm_matmul on
-  the CRT path and through gbmm_matmul_host (host buffers, pipelined copies);
+  the CRT path, on the limb path (Winograd, cutoffs 32 and 64) and through
+  gbmm_matmul_host (host buffers, pipelined copies);
 - 256 x 256 x 256 at 2048 bits with 5% zero and 5% 64-bit entries on the limb
   path (Winograd, cutoff 32) and on the CRT path;
 - one seeded 64-product draw of the uneven workload (m, n, k log-uniform in
@@ -71,6 +72,19 @@ def test_cfg3_crt_device_full_output(g, cfg3):
     dB.upload(*B)
     dC = g.DeviceMatrix(K, N, cn)
     g.default_handle().matmul(dC, dA, dB, path=g.PATH_CRT)
+    _same(dC.download(), exp)
+
+
+@pytest.mark.parametrize("cutoff", [32, 64])
+def test_cfg3_limb_winograd_full_output(g, cfg3, cutoff):
+    """The plain limb form the CRT path is compared against: Winograd's tree on
+    one-limb-longer sums (129 limbs) down to the cutoff."""
+    K, M, N, A, B, cn, exp = cfg3
+    dA, dB = g.DeviceMatrix(K, M, 128), g.DeviceMatrix(M, N, 128)
+    dA.upload(*A)
+    dB.upload(*B)
+    dC = g.DeviceMatrix(K, N, cn)
+    g.default_handle().matmul(dC, dA, dB, path=g.PATH_LIMB, method=g.METHOD_WINOGRAD, cutoff=cutoff)
     _same(dC.download(), exp)
 
 

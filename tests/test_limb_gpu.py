@@ -72,6 +72,77 @@ def test_mpn_mul1ops(g, oracle, op):
     assert (_host(cy) == exp_c).all()
 
 
+@pytest.mark.parametrize("un,vn", [(1, 0), (1, 1), (7, 3), (33, 33), (130, 2)])
+@pytest.mark.parametrize("sub", [False, True])
+def test_mpn_add_sub_unequal(g, oracle, un, vn, sub):
+    import torch
+    rng = np.random.default_rng(un * 13 + vn + sub)
+    nb = 700
+    u = _rand_planes(rng, un, nb, "ones")
+    v = _rand_planes(rng, max(vn, 1), nb)[:vn]
+    if sub:
+        u[:, nb // 2: nb // 2 + 20] = 0       # borrow through zero limbs
+    exp_r, exp_c = oracle.mpn_addsub(u, v, sub=sub)
+    dr, cy = torch.zeros(un * nb, dtype=torch.int32, device="cuda"), torch.zeros(nb, dtype=torch.int32, device="cuda")
+    dv = _dev(torch, v) if vn else torch.zeros(1, dtype=torch.int32, device="cuda")
+    (g.mpn_sub if sub else g.mpn_add)(dr, _dev(torch, u), un, dv, vn, nb, nb, cy)
+    torch.cuda.synchronize()
+    assert (_host(dr).reshape(un, nb) == exp_r).all()
+    assert (_host(cy) == exp_c).all()
+
+
+@pytest.mark.parametrize("n", [1, 5, 64])
+@pytest.mark.parametrize("sub", [False, True])
+def test_mpn_add_sub_1(g, oracle, n, sub):
+    import torch
+    rng = np.random.default_rng(n + 100 * sub)
+    nb = 500
+    u = _rand_planes(rng, n, nb, "ones")
+    u[:, 300:350] = 0
+    vl = rng.integers(0, 2**32, size=nb, dtype=np.uint64).astype(np.uint32)
+    vl[:7] = 0
+    vl[250:260] = 0xFFFFFFFF
+    exp_r, exp_c = oracle.mpn_addsub_1(u, vl, sub=sub)
+    du = _dev(torch, u)
+    cy = torch.zeros(nb, dtype=torch.int32, device="cuda")
+    (g.mpn_sub_1 if sub else g.mpn_add_1)(du, du, n, _dev(torch, vl), nb, nb, cy)   # in place, as GMP allows
+    torch.cuda.synchronize()
+    assert (_host(du).reshape(n, nb) == exp_r).all()
+    assert (_host(cy) == exp_c).all()
+
+
+@pytest.mark.parametrize("n", [1, 3, 129])
+def test_mpn_cmp_zero_p_neg_com(g, oracle, n):
+    import torch
+    rng = np.random.default_rng(n)
+    nb = 600
+    u = _rand_planes(rng, n, nb, "ones")
+    u[:, 400:450] = 0
+    u[0, 420:430] = 5
+    w = u.copy()
+    w[n - 1, 1::4] ^= 8
+    w[0, 2::4] += 1
+    exp_cmp = oracle.mpn_cmp(u, w)
+    exp_z = oracle.mpn_zero_p(u)
+    exp_neg, exp_nz = oracle.mpn_neg_com(u)
+    exp_com, _ = oracle.mpn_neg_com(u, com=True)
+    du, dw = _dev(torch, u), _dev(torch, w)
+    res = torch.zeros(nb, dtype=torch.int32, device="cuda")
+    g.mpn_cmp(du, dw, n, nb, nb, res)
+    torch.cuda.synchronize()
+    assert (res.cpu().numpy() == exp_cmp).all()
+    g.mpn_zero_p(du, n, nb, nb, res)
+    torch.cuda.synchronize()
+    assert (res.cpu().numpy() == exp_z).all()
+    dr, cy = torch.zeros(n * nb, dtype=torch.int32, device="cuda"), torch.zeros(nb, dtype=torch.int32, device="cuda")
+    g.mpn_neg(dr, du, n, nb, nb, cy)
+    torch.cuda.synchronize()
+    assert (_host(dr).reshape(n, nb) == exp_neg).all() and (_host(cy) == exp_nz).all()
+    g.mpn_com(dr, du, n, nb, nb)
+    torch.cuda.synchronize()
+    assert (_host(dr).reshape(n, nb) == exp_com).all()
+
+
 @pytest.mark.parametrize("un,vn", [(1, 1), (5, 3), (32, 32), (64, 17), (100, 100)])
 def test_mpn_mul_basecase(g, oracle, un, vn):
     import torch
@@ -234,3 +305,52 @@ def test_empty_shapes(g):
     dC = g.DeviceMatrix.from_ints(2, 2, [5, 6, 7, 8], 3)
     g.mat_mul(2, 0, 2, dC, dA, dB, method=g.METHOD_NAIVE)
     assert dC.to_ints() == [0, 0, 0, 0]
+
+
+@pytest.mark.parametrize("N,bits,cutoff", [(64, 4096, 16), (32, 1024, 4), (96, 300, 12), (128, 64, 8),
+                                           (48, 5000, 12)])
+def test_winograd_breadth_first_vs_depth_first_and_oracle(g, oracle, N, bits, cutoff):
+    """The breadth-first Winograd tree (all sums of a level, all leaf products,
+    all combinations of a level: one launch each) against the depth-first
+    recursion and the oracle.  4096- and 5000-bit entries make one-limb-longer
+    sums (129 and 158 limbs) that take the per-entry kernel's one-group-per-CTA
+    form (more than 256 threads per entry)."""
+    rng = random.Random(N * 7 + bits + cutoff)
+    A = _signed(rng, N * N, bits, 0.05)
+    B = _signed(rng, N * N, bits, 0.05)
+    nl = (bits + 31) // 32
+    dA = g.DeviceMatrix.from_ints(N, N, A, nl)
+    dB = g.DeviceMatrix.from_ints(N, N, B, nl)
+    cn = g.limbs_needed(nl, nl, N, method=g.METHOD_WINOGRAD, cutoff=cutoff)
+    Cl, Cs = oracle.matmul_planes(N, N, N, g.ints_to_planes(A, nl), g.ints_to_planes(B, nl), cn, method=1,
+                                  nthreads=8)
+    h = g.Handle()
+    for bf in (True, False):
+        h.set_breadth_first(bf)
+        dC = g.DeviceMatrix(N, N, cn)
+        dC.limbs_t.fill_(-1)
+        h.matmul(dC, dA, dB, path=g.PATH_LIMB, method=g.METHOD_WINOGRAD, cutoff=cutoff)
+        limbs, sizes = dC.download()
+        assert (sizes == Cs).all(), bf
+        assert (limbs == Cl).all(), bf
+    h.close()
+
+
+def test_winograd_breadth_first_rectangular_and_small_output(g, oracle):
+    """Squarify around breadth-first square cores, with C holding fewer planes
+    than the recursion's headroom (the product then runs into a workspace
+    matrix and is copied)."""
+    rng = random.Random(21)
+    K, M, N, bits = 70, 96, 66, 700
+    A = _signed(rng, K * M, bits, 0.05)
+    B = _signed(rng, M * N, bits, 0.05)
+    nl = (bits + 31) // 32
+    dA = g.DeviceMatrix.from_ints(K, M, A, nl)
+    dB = g.DeviceMatrix.from_ints(M, N, B, nl)
+    cn = 2 * nl + 1
+    Cl, Cs = oracle.matmul_planes(K, M, N, g.ints_to_planes(A, nl), g.ints_to_planes(B, nl), cn, method=1,
+                                  nthreads=8)
+    dC = g.DeviceMatrix(K, N, cn)
+    g.default_handle().matmul(dC, dA, dB, path=g.PATH_LIMB, method=g.METHOD_WINOGRAD, cutoff=8)
+    limbs, sizes = dC.download()
+    assert (sizes == Cs).all() and (limbs == Cl).all()
