@@ -1,10 +1,11 @@
 // Batched products of uneven shape and bit length, the path dispatcher, the
 // autotuner and CUDA-graph replay.
 //
-// gbmm_matmul_batched splits the jobs by path.  Limb-path jobs are cut into
-// (job, tile) items, sorted largest first, and run by ONE persistent kernel
-// per block edge R that drains a device work queue.  CRT jobs run their
-// residue / product / reconstruction kernels back to back.  The whole launch
+// gbmm_matmul_batched splits the jobs by plan.  Limb jobs planned without
+// recursion are cut into (job, tile) items, sorted largest first, and run by ONE
+// persistent kernel per group (block edge, CTA form, thin operands) that drains a
+// device work queue.  The other jobs (CRT products, Winograd trees) run through
+// dispatch() on four side streams, side by side.  The whole launch
 // sequence of a batch is captured into a CUDA graph the second time a batch
 // with the same signature (shapes, pointers, paths) is seen, and replayed from
 // then on.  This replaces the reference's chunked multi-stream job DAG
@@ -32,8 +33,7 @@ static uint64_t tune_key(int m, int k, int n, int la, int lb) {
 }
 
 struct TuneEntry {
-    int path;
-    int cutoff;
+    int plan;  // gbmm_plan
     float ms;
 };
 
@@ -42,8 +42,13 @@ struct GraphEntry {
     char *d_blob = nullptr;  // work-queue blob owned by this graph
 };
 
+constexpr int NSIDE = 4;  // side streams a batch's dispatched jobs are spread over
+
 struct BatchState {
     std::map<uint64_t, TuneEntry> tune;
+    // side streams and the events that fork them from and join them to the handle's stream
+    cudaStream_t side[NSIDE] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[NSIDE] = {};
     // graph cache
     std::map<std::string, GraphEntry> graphs;
     std::map<std::string, int> seen;
@@ -52,7 +57,7 @@ struct BatchState {
     char *h_stage = nullptr;
     size_t h_cap = 0;
     cudaEvent_t staged = nullptr;
-    int *d_counter = nullptr;  // one per block-edge group
+    int *d_counter = nullptr;  // one per work-queue group (LimbBatchPlan::MAX_GROUPS)
 };
 
 static BatchState &bstate(gbmm_handle h) {
@@ -68,6 +73,11 @@ void batch_state_destroy(gbmm_handle h) {
         cudaFree(kv.second.d_blob);
     }
     if (b->staged) cudaEventDestroy(b->staged);
+    for (int i = 0; i < NSIDE; i++) {
+        if (b->side[i]) cudaStreamDestroy(b->side[i]);
+        if (b->join_ev[i]) cudaEventDestroy(b->join_ev[i]);
+    }
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
     if (b->h_stage) cudaFreeHost(b->h_stage);
     if (b->d_counter) cudaFree(b->d_counter);
     delete b;
@@ -85,24 +95,17 @@ void invalidate_graphs(gbmm_handle h) {
     b.seen.clear();
 }
 
-int choose_path(gbmm_handle h, int m, int k, int n, int la, int lb, int *cutoff) {
+int choose_plan(gbmm_handle h, int m, int k, int n, int la, int lb) {
     if (h->model && h->use_model) {
-        int c = *cutoff;
-        int p = model_choose(h, m, k, n, la, lb, &c);
-        if (p == GBMM_PATH_LIMB || p == GBMM_PATH_CRT) {
-            *cutoff = c;
-            return p;
-        }
+        const int p = model_choose(h, m, k, n, la, lb);
+        if (p >= 0 && p < GBMM_NPLANS) return p;
     }
     if (h->batch) {
         BatchState &b = bstate(h);
         auto it = b.tune.find(tune_key(m, k, n, la, lb));
-        if (it != b.tune.end()) {
-            if (it->second.cutoff > 0) *cutoff = it->second.cutoff;
-            return it->second.path;
-        }
+        if (it != b.tune.end()) return it->second.plan;
     }
-    return heuristic_path(m, k, n, la, lb);
+    return heuristic_plan(m, k, n, la, lb);
 }
 
 }  // namespace gbmm
@@ -115,38 +118,92 @@ static std::string job_signature(const gbmm_job *jobs, int njobs, const std::vec
     char buf[256];
     for (int j = 0; j < njobs; j++) {
         const gbmm_job &q = jobs[j];
-        snprintf(buf, sizeof buf, "%p,%p,%p,%p,%p,%p,%d,%d,%d,%d,%d,%d,%lld,%lld,%lld,%lld,%lld,%lld,%d,%d,%d;",
+        snprintf(buf, sizeof buf, "%p,%p,%p,%p,%p,%p,%d,%d,%d,%d,%d,%d,%lld,%lld,%lld,%lld,%lld,%lld,%d,%d,%d,%d,%d;",
                  (void *)q.c.limbs, (void *)q.c.sizes, (void *)q.a.limbs, (void *)q.a.sizes, (void *)q.b.limbs,
                  (void *)q.b.sizes, q.a.rows, q.a.cols, q.b.cols, q.a.nlimbs, q.b.nlimbs, q.c.nlimbs, (long long)q.a.rs,
                  (long long)q.a.ld, (long long)q.b.rs, (long long)q.b.ld, (long long)q.c.rs, (long long)q.c.ld,
-                 plans[j].path, plans[j].cutoff, plans[j].method);
+                 plans[j].path, plans[j].cutoff, plans[j].method, plans[j].tiles, plans[j].split);
         sig += buf;
     }
     return sig;
 }
 
-// Splits a batch: limb-path jobs that fit the per-entry kernel go to the
-// persistent work-queue kernel, everything else through dispatch().
+// Splits a batch: limb-path jobs planned without recursion that fit the
+// per-entry kernel go to the persistent work-queue kernel, everything else
+// (Winograd trees, CRT products) through dispatch().
 static void split_batch(const gbmm_job *jobs, int njobs, const std::vector<Plan> &plans, std::vector<int> &queue_jobs,
                         std::vector<int> &other) {
     for (int j = 0; j < njobs; j++) {
         const gbmm_job &q = jobs[j];
-        if (plans[j].path == GBMM_PATH_LIMB && limb_kernel_fits(q.a.nlimbs, q.b.nlimbs) && q.a.rows && q.b.cols &&
-            q.a.cols)
+        if (plans[j].path == GBMM_PATH_LIMB && plans[j].method == GBMM_METHOD_NAIVE &&
+            limb_kernel_fits(q.a.nlimbs, q.b.nlimbs) && q.a.rows && q.b.cols && q.a.cols)
             queue_jobs.push_back(j);
         else
             other.push_back(j);
     }
 }
 
-// Enqueues one batch on the handle's stream.  d_blob holds the work-queue plan
-// on the device (already filled); the remaining jobs go through dispatch().
-static gbmm_status enqueue_batch(gbmm_handle h, const gbmm_job *jobs, const std::vector<Plan> &plans,
-                                 const LimbBatchPlan &lp, const char *d_blob, const std::vector<int> &other) {
-    BatchState &bs = bstate(h);
-    if (!lp.groups.empty()) GBMM_TRY(launch_limb_batch(lp, d_blob, bs.d_counter, h->stream));
-    for (int j : other) GBMM_TRY(dispatch(h, jobs[j].c, jobs[j].a, jobs[j].b, plans[j], 0, h->stream));
+// Side streams for batches (created on first use).
+static gbmm_status side_streams(BatchState &bs) {
+    if (bs.fork_ev) return GBMM_OK;
+    for (int i = 0; i < NSIDE; i++) {
+        GBMM_CUDA_TRY(cudaStreamCreateWithFlags(&bs.side[i], cudaStreamNonBlocking));
+        GBMM_CUDA_TRY(cudaEventCreateWithFlags(&bs.join_ev[i], cudaEventDisableTiming));
+    }
+    GBMM_CUDA_TRY(cudaEventCreateWithFlags(&bs.fork_ev, cudaEventDisableTiming));
     return GBMM_OK;
+}
+
+// Side streams a batch with these dispatched jobs uses.
+static int nside_for(size_t njobs) { return (int)std::min<size_t>(NSIDE, njobs); }
+
+// Enqueues one batch on the handle's stream.  d_blob holds the work-queue plan
+// on the device (already filled); the persistent limb kernel runs on the
+// handle's stream.  The remaining jobs go through dispatch() on side streams
+// forked from it (largest estimated work first, each to the least loaded
+// stream), so independent products run side by side; every side stream carves
+// its workspace from its own slice of the arena (`slice` bytes each, above the
+// current top) and the handle's stream waits for all of them at the end.
+static gbmm_status enqueue_batch(gbmm_handle h, const gbmm_job *jobs, const std::vector<Plan> &plans,
+                                 const LimbBatchPlan &lp, const char *d_blob, const std::vector<int> &other,
+                                 size_t slice) {
+    BatchState &bs = bstate(h);
+    const int ns = nside_for(other.size());
+    if (ns > 0) {
+        GBMM_TRY(side_streams(bs));
+        GBMM_CUDA_TRY(cudaEventRecord(bs.fork_ev, h->stream));
+        for (int i = 0; i < ns; i++) GBMM_CUDA_TRY(cudaStreamWaitEvent(bs.side[i], bs.fork_ev, 0));
+    }
+    if (!lp.groups.empty()) GBMM_TRY(launch_limb_batch(lp, d_blob, bs.d_counter, h->stream));
+    std::vector<int> order(other);
+    auto work = [&](int j) {
+        const gbmm_job &q = jobs[j];
+        return (double)q.a.rows * q.a.cols * q.b.cols * std::max(q.a.nlimbs, 1) * std::max(q.b.nlimbs, 1);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work(x) > work(y); });
+    std::vector<double> load(ns, 0.0);
+    // slices start above 0, so a reservation inside dispatch() that did not fit its
+    // slice fails ("grow while in use") instead of reallocating the arena under
+    // work still queued on the other side streams
+    const size_t base = ((arena_mark(h) + 255) & ~(size_t)255) + 256;
+    gbmm_status st = GBMM_OK;
+    for (int j : order) {
+        int i = 0;
+        for (int t = 1; t < ns; t++)
+            if (load[t] < load[i]) i = t;
+        load[i] += work(j);
+        const size_t mark = arena_mark(h);
+        h->ws.top = base + (size_t)i * slice;
+        st = dispatch(h, jobs[j].c, jobs[j].a, jobs[j].b, plans[j], 0, bs.side[i]);
+        arena_release(h, mark);
+        if (st != GBMM_OK) break;
+    }
+    for (int i = 0; i < ns; i++) {
+        // joined even after an error, so a capture in progress can end cleanly
+        GBMM_CUDA_TRY(cudaEventRecord(bs.join_ev[i], bs.side[i]));
+        GBMM_CUDA_TRY(cudaStreamWaitEvent(h->stream, bs.join_ev[i], 0));
+    }
+    return st;
 }
 
 extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_t njobs, const gbmm_opts *opts) {
@@ -172,6 +229,7 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
         if (q.nprimes) oj.nprimes = q.nprimes;
         GBMM_TRY(resolve_plan(h, q.a, q.b, oj, plans[j]));
         jobs[j].chosen_path = plans[j].path;
+        jobs[j].chosen_plan = plans[j].id;
         ws = std::max(ws, dispatch_ws(plans[j], q.a.nlimbs, q.b.nlimbs, q.a.rows, q.a.cols, q.b.cols, q.c.nlimbs, 0));
     }
     if (njobs == 0) return GBMM_OK;
@@ -188,9 +246,12 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
         GBMM_TRY(plan_limb_batch(C, A, B, lp));
     }
     BatchState &bs = bstate(h);
-    if (!bs.d_counter) GBMM_CUDA_TRY(cudaMalloc(&bs.d_counter, 4 * sizeof(int)));
+    if (!bs.d_counter) GBMM_CUDA_TRY(cudaMalloc(&bs.d_counter, LimbBatchPlan::MAX_GROUPS * sizeof(int)));
     if (!bs.staged) GBMM_CUDA_TRY(cudaEventCreateWithFlags(&bs.staged, cudaEventDisableTiming));
-    GBMM_TRY(arena_reserve(h, ws + lp.blob.size() + 65536));
+    // one arena slice per side stream, each large enough for any dispatched job
+    const size_t slice = (ws + 65536 + 255) & ~(size_t)255;
+    const int ns = nside_for(other.size());
+    GBMM_TRY(arena_reserve(h, (size_t)std::max(ns, 1) * slice + lp.blob.size() + 65536 + 1024));
 
     const std::string sig = bs.use_graphs ? job_signature(jobs, njobs, plans) : std::string();
     if (bs.use_graphs) {
@@ -221,7 +282,7 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
             GBMM_CUDA_TRY(cudaMemcpyAsync(d_blob, bs.h_stage, lp.blob.size(), cudaMemcpyHostToDevice, h->stream));
             GBMM_CUDA_TRY(cudaEventRecord(bs.staged, h->stream));
         }
-        gbmm_status st = enqueue_batch(h, jobs, plans, lp, d_blob, other);
+        gbmm_status st = enqueue_batch(h, jobs, plans, lp, d_blob, other, slice);
         arena_release(h, mark);
         return st;
     }
@@ -233,7 +294,7 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
     }
     cudaGraph_t graph = nullptr;
     GBMM_CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    gbmm_status st = enqueue_batch(h, jobs, plans, lp, ge.d_blob, other);
+    gbmm_status st = enqueue_batch(h, jobs, plans, lp, ge.d_blob, other, slice);
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     if (st == GBMM_OK && e != cudaSuccess) st = cuda_error(e, "cudaStreamEndCapture");
     if (st == GBMM_OK) {
@@ -271,33 +332,22 @@ extern "C" gbmm_status gbmm_autotune(gbmm_handle h, const gbmm_job *jobs, int32_
     cudaEvent_t e0, e1;
     GBMM_CUDA_TRY(cudaEventCreate(&e0));
     GBMM_CUDA_TRY(cudaEventCreate(&e1));
-    struct Cand {
-        int path, method, cutoff;
-    };
-    const Cand cands[] = {{GBMM_PATH_LIMB, GBMM_METHOD_NAIVE, 0},
-                          {GBMM_PATH_LIMB, GBMM_METHOD_WINOGRAD, 64},
-                          {GBMM_PATH_CRT, GBMM_METHOD_WINOGRAD, 0}};
     gbmm_status st = GBMM_OK;
     for (int j = 0; j < njobs && st == GBMM_OK; j++) {
         const gbmm_job &q = jobs[j];
         const int m = q.a.rows, k = q.a.cols, n = q.b.cols, la = q.a.nlimbs, lb = q.b.nlimbs;
         if (!m || !k || !n) continue;
         float best = 1e30f;
-        TuneEntry te{heuristic_path(m, k, n, la, lb), 0, 0.f};
-        for (const Cand &cd : cands) {
-            // limb candidates whose schoolbook work predicts far more than any plan needs
-            // (about 50 ms at 4e12 32-bit MAC/s) are not run; their timing stays unknown
-            if (cd.path == GBMM_PATH_LIMB && (double)m * k * n * la * lb > 2e11) continue;
+        TuneEntry te{heuristic_plan(m, k, n, la, lb), 0.f};
+        for (int id = 0; id < GBMM_NPLANS; id++) {
+            const Plan cd = plan_of(id);
+            // limb candidates with far more schoolbook work than any plan needs, Winograd
+            // cutoffs that give no recursion and splits of one-limb operands are not run;
+            // their timing stays unknown
+            if (!plan_admissible(id, m, k, n, la, lb)) continue;
             gbmm_opts o;
             memset(&o, 0, sizeof o);
-            o.path = cd.path;
-            o.method = cd.method;
-            o.cutoff = cd.cutoff;
-            int32_t need = 0;
-            gbmm_matmul_limbs_needed(la, lb, k, &o, &need);
-            if (q.c.nlimbs < need && cd.method != GBMM_METHOD_NAIVE && cd.path == GBMM_PATH_LIMB) {
-                // the tuner only runs candidates whose workspace rules hold for this C
-            }
+            o.plan = 1 + id;
             float tot = 0.f;
             bool ok = true;
             for (int r = 0; r <= repeats && ok; r++) {
@@ -315,13 +365,12 @@ extern "C" gbmm_status gbmm_autotune(gbmm_handle h, const gbmm_job *jobs, int32_
             const float ms = tot / std::max(1, repeats);
             if (log)
                 fprintf(log,
-                        "{\"m\": %d, \"k\": %d, \"n\": %d, \"la\": %d, \"lb\": %d, \"path\": %d, \"method\": %d, "
-                        "\"cutoff\": %d, \"ms\": %.6f}\n",
-                        m, k, n, la, lb, cd.path, cd.method, cd.cutoff, ms);
+                        "{\"m\": %d, \"k\": %d, \"n\": %d, \"la\": %d, \"lb\": %d, \"plan\": %d, \"path\": %d, "
+                        "\"method\": %d, \"cutoff\": %d, \"tiles\": %d, \"split\": %d, \"ms\": %.6f}\n",
+                        m, k, n, la, lb, id, cd.path, cd.method, cd.cutoff, cd.tiles, cd.split, ms);
             if (ms < best) {
                 best = ms;
-                te.path = cd.path;
-                te.cutoff = cd.method == GBMM_METHOD_NAIVE ? 1 << 30 : cd.cutoff;
+                te.plan = id;
                 te.ms = ms;
             }
         }
@@ -340,8 +389,8 @@ extern "C" gbmm_status gbmm_tune_save(gbmm_handle h, const char *path) {
     fprintf(f, "[\n");
     bool first = true;
     for (auto &kv : bstate(h).tune) {
-        fprintf(f, "%s  {\"key\": %llu, \"path\": %d, \"cutoff\": %d, \"ms\": %.6f}", first ? "" : ",\n",
-                (unsigned long long)kv.first, kv.second.path, kv.second.cutoff, kv.second.ms);
+        fprintf(f, "%s  {\"key\": %llu, \"plan\": %d, \"ms\": %.6f}", first ? "" : ",\n",
+                (unsigned long long)kv.first, kv.second.plan, kv.second.ms);
         first = false;
     }
     fprintf(f, "\n]\n");
@@ -357,12 +406,12 @@ extern "C" gbmm_status gbmm_tune_load(gbmm_handle h, const char *path) {
     int loaded = 0;
     while (fgets(line, sizeof line, f)) {
         unsigned long long key = 0;
-        int p = 0, c = 0;
+        int p = 0;
         float ms = 0.f;
         const char *q = strstr(line, "\"key\"");
         if (!q) continue;
-        if (sscanf(q, "\"key\": %llu, \"path\": %d, \"cutoff\": %d, \"ms\": %f", &key, &p, &c, &ms) == 4) {
-            bstate(h).tune[key] = TuneEntry{p, c, ms};
+        if (sscanf(q, "\"key\": %llu, \"plan\": %d, \"ms\": %f", &key, &p, &ms) == 3 && p >= 0 && p < GBMM_NPLANS) {
+            bstate(h).tune[key] = TuneEntry{p, ms};
             loaded++;
         }
     }

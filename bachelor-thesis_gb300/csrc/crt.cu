@@ -1907,8 +1907,9 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         ProductArgs pa;
         pa.m = m; pa.n = n; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.yblk = (int64_t)2 * t->Pp * 64;
         // CTA pairs pay off once the K loop is long enough to hide the pair's per-tile
-        // synchronisation (measured: faster at k = 512, slower at k = 256)
-        const bool pair = pa.nk >= PROD_PAIR_MIN_NK;
+        // synchronisation (measured: faster at k = 512, slower at k = 256); a plan may
+        // fix the form (h->crt_tiles: 1 one-CTA tiles, 2 CTA pairs)
+        const bool pair = h->crt_tiles == 0 ? pa.nk >= PROD_PAIR_MIN_NK : h->crt_tiles == 2;
         const int NP = pair ? 2 : 1;
         pa.nyt = (m + NP * BM - 1) / (NP * BM);
         pa.nxt = (n + PBX - 1) / PBX;
@@ -1930,8 +1931,9 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     {
         CUtensorMap tmY, tmT;
         GBMM_TRY(make_map(&tmY, Y, 64, (uint64_t)(Ep / 64) * 2 * t->Pp, 64, 64, BK));
-        // CTA pairs once the K loop over the 2Pp moduli digits is long enough (see the product)
-        const bool pair = 2 * t->Pp / BK >= PROD_PAIR_MIN_NK;
+        // CTA pairs once the K loop over the 2Pp moduli digits is long enough (see the
+        // product), unless the plan fixes the form
+        const bool pair = h->crt_tiles == 0 ? 2 * t->Pp / BK >= PROD_PAIR_MIN_NK : h->crt_tiles == 2;
         const int NP = pair ? 2 : 1, TROWS = 256 / NP;
         GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RTAB, 2 * t->Pp, BK, TROWS));
         ReconArgs ra;

@@ -127,10 +127,12 @@ struct crt_stage_hooks {
 // Host-side plan of one batch of limb-path products: a blob holding the job
 // descriptors and the (job, tile) work items of every block-edge group.
 struct LimbBatchPlan {
+    static constexpr int MAX_GROUPS = 10;  // launches per batch at most (block edge x CTA form x thin)
     std::vector<char> blob;
     struct Group {
         int R = 0;
-        int NT = 0;  // threads per CTA
+        int NT = 0;    // threads per CTA
+        int thin = 0;  // jobs with a one-limb-longer operand (edge threads fold in its top limb)
         size_t jobs_off = 0, items_off = 0;
         int nitems = 0;
         size_t smem = 0;
@@ -144,22 +146,31 @@ gbmm_status launch_limb_batch(const LimbBatchPlan &plan, const char *d_blob, int
 
 // ---- dispatch (host.cpp, batch.cpp) ------------------------------------------------------
 struct Plan {
-    int path;     // GBMM_PATH_LIMB or GBMM_PATH_CRT after resolution
-    int method;   // limb path square method
-    int cutoff;   // limb path recursion cutoff
-    int nprimes;  // CRT moduli (0 = from the bound)
+    int path = GBMM_PATH_LIMB;  // GBMM_PATH_LIMB or GBMM_PATH_CRT after resolution
+    int method = GBMM_METHOD_NAIVE;  // limb path square method
+    int cutoff = 32;   // limb path recursion cutoff
+    int nprimes = 0;   // CRT moduli (0 = from the bound)
+    int tiles = 0;     // CRT GEMM tiles: 0 by size, 1 one-CTA (128 entries), 2 CTA pairs (256 entries)
+    int split = 0;     // limb-half splits forced before the kernels (fewer moduli per CRT product)
+    int id = -1;       // the gbmm_plan it stands for, -1 for options given field by field
 };
-int heuristic_path(int m, int k, int n, int la, int lb);
-// AUTO path choice: learned model when loaded, tuning table, else the heuristic
-int choose_path(gbmm_handle h, int m, int k, int n, int la, int lb, int *cutoff);
+// the gbmm_plan `id` as a Plan
+Plan plan_of(int id);
+// whether the autotuner times plan `id` for this product (and so whether the
+// learned model may pick it): limb plans only below a schoolbook-work bound,
+// Winograd cutoffs only when they give recursion, splits only of multi-limb operands
+bool plan_admissible(int id, int m, int k, int n, int la, int lb);
+int heuristic_plan(int m, int k, int n, int la, int lb);
+// AUTO choice: learned model when loaded, tuning table, else the heuristic (a gbmm_plan)
+int choose_plan(gbmm_handle h, int m, int k, int n, int la, int lb);
 size_t dispatch_ws(const Plan &p, int la, int lb, int m, int k, int n, int cn, int accumulate);
 gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, const Plan &p,
                      int accumulate, cudaStream_t s);
 gbmm_status resolve_plan(gbmm_handle h, const gbmm_mat &a, const gbmm_mat &b, const gbmm_opts &o, Plan &p);
 void invalidate_graphs(gbmm_handle h);
 void batch_state_destroy(gbmm_handle h);
-// learned cost model (mlp.cu): path for one product, or -1 when no model applies
-int model_choose(gbmm_handle h, int m, int k, int n, int la, int lb, int *cutoff);
+// learned cost model (mlp.cu): the gbmm_plan it picks, or -1 when no model applies
+int model_choose(gbmm_handle h, int m, int k, int n, int la, int lb);
 void model_destroy(gbmm_handle h);
 
 // ---- device workspace arena -------------------------------------------------------------
@@ -183,6 +194,9 @@ struct gbmm_handle_s {
     int limb_cutoff = 32;
     // Winograd products as one breadth-first tree (1, default) or depth first (0)
     int wino_breadth_first = 1;
+    // CRT GEMM tile form for the next product (set around each CRT call by dispatch):
+    // 0 by size, 1 one-CTA tiles, 2 CTA-pair tiles for the product and reconstruction
+    int crt_tiles = 0;
     // learned-dispatch model (null when not loaded) and whether AUTO consults it
     void *model = nullptr;
     int use_model = 0;

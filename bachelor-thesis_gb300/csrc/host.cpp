@@ -1030,18 +1030,43 @@ gbmm_status matmul_limb(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, con
 
 namespace gbmm {
 
-// Plain dispatch heuristic: the CRT form pays off once products are large
-// enough to amortise the residue and reconstruction passes.
-// Plain dispatch rule: the CRT path for products with enough limb work, the limb
-// path otherwise.  Entries too long for one CRT product (more than 1023 moduli)
-// still take the CRT path: dispatch() splits them into limb halves that fit.
-int heuristic_path(int m, int k, int n, int la, int lb) {
+Plan plan_of(int id) {
+    Plan p;
+    p.id = id;
+    switch (id) {
+        case GBMM_PLAN_LIMB_NAIVE: p.path = GBMM_PATH_LIMB; p.method = GBMM_METHOD_NAIVE; break;
+        case GBMM_PLAN_LIMB_W32: p.path = GBMM_PATH_LIMB; p.method = GBMM_METHOD_WINOGRAD; p.cutoff = 32; break;
+        case GBMM_PLAN_LIMB_W64: p.path = GBMM_PATH_LIMB; p.method = GBMM_METHOD_WINOGRAD; p.cutoff = 64; break;
+        case GBMM_PLAN_LIMB_W128: p.path = GBMM_PATH_LIMB; p.method = GBMM_METHOD_WINOGRAD; p.cutoff = 128; break;
+        case GBMM_PLAN_CRT_SINGLE: p.path = GBMM_PATH_CRT; p.tiles = 1; break;
+        case GBMM_PLAN_CRT_PAIR: p.path = GBMM_PATH_CRT; p.tiles = 2; break;
+        case GBMM_PLAN_CRT_SPLIT: p.path = GBMM_PATH_CRT; p.split = 1; break;
+        default: p.path = GBMM_PATH_CRT; p.id = GBMM_PLAN_CRT; break;
+    }
+    return p;
+}
+
+bool plan_admissible(int id, int m, int k, int n, int la, int lb) {
+    const Plan p = plan_of(id);
+    // about 50 ms of schoolbook work at 4e12 32-bit MAC/s: limb plans beyond it are not timed
+    if (p.path == GBMM_PATH_LIMB && (double)m * k * n * la * lb > 2e11) return false;
+    if (p.method == GBMM_METHOD_WINOGRAD && std::min(std::min(m, k), n) <= p.cutoff) return false;
+    if (p.split && std::max(la, lb) < 2) return false;
+    return true;
+}
+
+// Plain dispatch rule: the CRT form for products with enough limb work (it pays
+// off once the residue and reconstruction passes are amortised), the per-entry
+// limb kernel otherwise.  Entries too long for one CRT product (more than 1023
+// moduli) still take the CRT path: dispatch() splits them into limb halves that fit.
+int heuristic_plan(int m, int k, int n, int la, int lb) {
     const int64_t work = (int64_t)m * k * n * la * lb;
-    if (la + lb >= 16 && work >= ((int64_t)1 << 22)) return GBMM_PATH_CRT;
-    return GBMM_PATH_LIMB;
+    if (la + lb >= 16 && work >= ((int64_t)1 << 22)) return GBMM_PLAN_CRT;
+    return GBMM_PLAN_LIMB_NAIVE;
 }
 
 static bool direct_ok(const Plan &p, int la, int lb, int k) {
+    if (p.split > 0 && std::max(la, lb) >= 2) return false;
     if (p.path == GBMM_PATH_CRT) return crt_feasible(la, lb, k);
     return limb_kernel_fits(la, lb);
 }
@@ -1065,8 +1090,10 @@ size_t dispatch_ws(const Plan &p, int la, int lb, int m, int k, int n, int cn, i
     const int64_t xs = sa ? (int64_t)m * k : (int64_t)k * n;
     const int tn = limbs_needed(sa ? la - hl : la, sa ? lb : lb - hl, k, 0) + 1;
     size_t own = 2 * (align_up((size_t)xs * 4, 256) + 256) + mat_bytes((int64_t)m * n, tn) + 1024;
-    size_t lo = dispatch_ws(p, sa ? hl : la, sa ? lb : hl, m, k, n, cn, accumulate);
-    size_t hi = dispatch_ws(p, sa ? la - hl : la, sa ? lb : lb - hl, m, k, n, tn, 0);
+    Plan q = p;
+    q.split = std::max(0, p.split - 1);
+    size_t lo = dispatch_ws(q, sa ? hl : la, sa ? lb : hl, m, k, n, cn, accumulate);
+    size_t hi = dispatch_ws(q, sa ? la - hl : la, sa ? lb : lb - hl, m, k, n, tn, 0);
     return own + std::max(lo, hi);
 }
 
@@ -1080,8 +1107,13 @@ gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const 
     if (m == 0 || n == 0) return GBMM_OK;
     if (k == 0) return accumulate ? GBMM_OK : launch_mat_zero(c, s);
     if (direct_ok(p, a.nlimbs, b.nlimbs, k)) {
-        if (p.path == GBMM_PATH_CRT)
-            return crt_matmul(h, c, a, b, 32LL * a.nlimbs, 32LL * b.nlimbs, p.nprimes, accumulate, s);
+        if (p.path == GBMM_PATH_CRT) {
+            const int saved = h->crt_tiles;
+            h->crt_tiles = p.tiles;
+            const gbmm_status st = crt_matmul(h, c, a, b, 32LL * a.nlimbs, 32LL * b.nlimbs, p.nprimes, accumulate, s);
+            h->crt_tiles = saved;
+            return st;
+        }
         int levels = p.method == GBMM_METHOD_NAIVE ? 0 : levels_for(std::max(std::max(m, k), n), p.cutoff) + 2;
         int need = limbs_needed(a.nlimbs, b.nlimbs, k, levels);
         if (c.nlimbs < need && p.method != GBMM_METHOD_NAIVE) {
@@ -1116,19 +1148,33 @@ gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const 
     Xhi.nlimbs = X.nlimbs - hl;
     Xhi.limbs = X.limbs + (int64_t)hl * X.ld;
     Xhi.sizes = hi;
-    GBMM_TRY(dispatch(h, c, sa ? Xlo : a, sa ? b : Xlo, p, accumulate, s));
-    GBMM_TRY(dispatch(h, T, sa ? Xhi : a, sa ? b : Xhi, p, 0, s));
+    Plan q = p;
+    q.split = std::max(0, p.split - 1);
+    GBMM_TRY(dispatch(h, c, sa ? Xlo : a, sa ? b : Xlo, q, accumulate, s));
+    GBMM_TRY(dispatch(h, T, sa ? Xhi : a, sa ? b : Xhi, q, 0, s));
     GBMM_TRY(launch_add_shifted(c, c, T, hl, s));
     arena_release(h, mark);
     return GBMM_OK;
 }
 
 gbmm_status resolve_plan(gbmm_handle h, const gbmm_mat &a, const gbmm_mat &b, const gbmm_opts &o, Plan &p) {
+    if (o.plan) {
+        if (o.plan < 1 || o.plan > GBMM_NPLANS) return set_error(GBMM_ERR_INVALID, "unknown plan %d", o.plan - 1);
+        p = plan_of(o.plan - 1);
+        p.nprimes = o.nprimes;
+        return GBMM_OK;
+    }
+    if (o.path == GBMM_PATH_AUTO) {
+        p = plan_of(choose_plan(h, a.rows, a.cols, b.cols, a.nlimbs, b.nlimbs));
+        if (o.cutoff > 0) p.cutoff = o.cutoff;
+        p.nprimes = o.nprimes;
+        return GBMM_OK;
+    }
+    p = Plan();
     p.method = o.method ? o.method : GBMM_METHOD_WINOGRAD;
     p.cutoff = o.cutoff > 0 ? o.cutoff : h->limb_cutoff;
     p.nprimes = o.nprimes;
     p.path = o.path;
-    if (p.path == GBMM_PATH_AUTO) p.path = choose_path(h, a.rows, a.cols, b.cols, a.nlimbs, b.nlimbs, &p.cutoff);
     if (p.path != GBMM_PATH_CRT && p.path != GBMM_PATH_LIMB) return set_error(GBMM_ERR_INVALID, "unknown path %d", o.path);
     return GBMM_OK;
 }

@@ -692,26 +692,43 @@ __global__ void k_max_size(MatArgs A, int64_t count, int32_t *out) {
 // warp-uniform when groups span whole warps).  No carry leaves a column inside
 // the k loop.  After the loop each thread parks its columns in shared memory,
 // the CTA sums the partial columns of every entry (a column gathers the
-// blocks on two neighbouring anti-diagonals), one thread per entry propagates
-// the signed carries, adds the old C for C += A*B, and writes the
-// sign-magnitude result.  A/B limbs for a chunk of KC terms are staged in
-// shared memory with loads coalesced along k (A) and along x (B), read back
-// as 128-bit vectors and reused by every thread of the CTA's TY x TX entries.
+// blocks on two neighbouring anti-diagonals), and the signed carries are
+// propagated (one warp per entry when groups span whole warps, each lane a
+// segment of limbs; else one thread per entry), the old C is added for
+// C += A*B and the sign-magnitude result is written.  A/B limbs for a chunk of
+// KC terms are staged in shared memory by 4-byte cp.async copies coalesced
+// along k (A) and along x (B), double-buffered so the next chunk's copies run
+// during this chunk's MACs, read back as 128-bit vectors and reused by every
+// thread of the CTA's TY x TX entries.  An operand one limb longer than a
+// multiple of R (a Winograd sum of full-length entries) does not get a block
+// row of its own: the threads on the grid's edge fold its top limb in.
 // ======================================================================================
 namespace {
 constexpr int MM_THREADS = 256;       // CTA size when groups of <= 256 threads share a CTA
 constexpr int MM_THREADS_WIDE = 512;  // largest CTA: one group of up to 512 threads
-constexpr int MM_KC = 8;
+constexpr int MM_KC = 16;  // terms per staged chunk (a power of two: staging index math is shifts and masks)
 }
+
+// 4-byte asynchronous global -> shared copy; a copy with valid == false reads
+// nothing and writes a zero (src-size 0).  `gsafe` is any valid global address.
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem, const void *gsafe, bool valid) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(sa), "l"(valid ? gmem : gsafe),
+                 "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 struct MMCfg {
     int R;        // block edge in limbs
     int La, Lb;   // padded limb counts (multiples of R)
     int G, Gp;    // threads per entry (active, padded)
     int NT;       // threads per CTA (entries x Gp, at most MM_THREADS; Gp for one wide group)
-    int thinA, thinB;  // the operand has one limb past a multiple of R: its last block row
-                       // (column) holds that single limb and is multiplied as 1 x R (R x 1)
+    int thinA, thinB;  // the operand has one limb past a multiple of R (and more than R):
+                       // the main grid's edge threads fold that top limb in
     int TY, TX;   // entries per CTA
+    int TXs;      // log2(TX) (TX is a power of two)
     int M;        // inner dimension
     int accumulate;
 };
@@ -727,50 +744,26 @@ struct MMCfg {
         : "+r"(c0), "+r"(c1), "+r"(c2)                                            \
         : "r"(a), "r"(b))
 
-// Block (I, J) of the La x Lb limb square that thread lt of a group owns: the full
-// R x R blocks first, then the thin blocks of a one-limb last block row / column
-// (so thin blocks share warps and their shorter loop does not hold up full ones).
-__device__ __forceinline__ void block_of(int lt, int nbA, int nbB, int thinA, int thinB, int &I, int &J) {
-    const int ma = nbA - thinA, mb = nbB - thinB, nmain = ma * mb;
-    if (lt < nmain) { I = lt / mb; J = lt % mb; return; }
-    int r = lt - nmain;
-    if (thinA) {
-        if (r < mb) { I = nbA - 1; J = r; return; }
-        r -= mb;
-    }
-    if (thinB) {
-        if (r < ma) { I = r; J = nbB - 1; return; }
-    }
-    I = nbA - 1;
-    J = nbB - 1;
-}
+// Top-limb products of a thin operand (one limb past a multiple of R, a
+// Winograd sum of full-length entries): a_top * b_j for every limb j of B
+// (b_top included when B is thin too), then a_i * b_top for every limb i of
+// A's main grid.  Item it goes to thread it % G, which keeps one extra column
+// accumulator per item it holds, so the extra work is spread evenly over the
+// group (one or two MACs a term on top of R * R) instead of loading the grid's
+// edge threads.  At most MM_XMAX items a thread.
+constexpr int MM_XMAX = 3;
 
-// P (+|-)= a-block x b-block; a thin row (column) block has only a[0] (b[0]).
-template <int R, bool NEG>
-__device__ __forceinline__ void block_mac(uint32_t (&P)[2 * R - 1][3], const uint32_t (&a)[R], const uint32_t (&b)[R],
-                                          bool rthin, bool cthin) {
-#define OP_(c, x, y)                                          \
-    do {                                                      \
-        if (NEG) MSC96(P[c][0], P[c][1], P[c][2], x, y);      \
-        else MAC96(P[c][0], P[c][1], P[c][2], x, y);          \
-    } while (0)
-    if (!rthin && !cthin) {
+// P (+|-)= a-block x b-block (R x R, columns 0 .. 2R - 2).
+template <int R, int NC, bool NEG>
+__device__ __forceinline__ void block_mac(uint32_t (&P)[NC][3], const uint32_t (&a)[R], const uint32_t (&b)[R]) {
 #pragma unroll
-        for (int i = 0; i < R; i++)
+    for (int i = 0; i < R; i++)
 #pragma unroll
-            for (int j = 0; j < R; j++) OP_(i + j, a[i], b[j]);
-    } else if (!cthin) {
-#pragma unroll
-        for (int j = 0; j < R; j++) OP_(j, a[0], b[j]);
-    } else if (!rthin) {
-#pragma unroll
-        for (int i = 0; i < R; i++) OP_(i, a[i], b[0]);
-    } else {
-        OP_(0, a[0], b[0]);
-    }
-#undef OP_
+        for (int j = 0; j < R; j++) {
+            if (NEG) MSC96(P[i + j][0], P[i + j][1], P[i + j][2], a[i], b[j]);
+            else MAC96(P[i + j][0], P[i + j][1], P[i + j][2], a[i], b[j]);
+        }
 }
-
 // Signed carry resolution of one entry's column sums by the 32 lanes of a warp
 // (all lanes call it).  col[t] = (s0, s1, s2) for t < Lc is column t's value
 // s0 + s1 2^32 + s2 2^64 (s2 signed); buf has LB = Lc + 2 words.  Lane l takes
@@ -895,15 +888,18 @@ __device__ void store_signed(uint32_t *buf, int L, bool neg, const MatArgs &C, i
 
 // One CTA tile (TY x TX output entries at tile coordinates by, bx) of the
 // per-entry product; shared by the grid kernel and the persistent batched one.
-template <int R>
+// THIN: an operand has one limb past a multiple of R (cfg.thinA / thinB), which
+// the main grid's edge threads fold in.
+template <int R, bool THIN>
 __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, const MatArgs &B, const MMCfg &cfg,
                                           int by, int bx, unsigned char *smem_raw, uint32_t *err) {
     const int La = cfg.La, Lb = cfg.Lb, TY = cfg.TY, TX = cfg.TX;
     const int sa_stride = La + 4, sb_stride = Lb + 4;  // +4 words: fewer bank conflicts, 16B aligned rows
-    uint32_t *sA = reinterpret_cast<uint32_t *>(smem_raw);                 // [TY][KC][La+4]
-    uint32_t *sB = sA + TY * MM_KC * sa_stride;                            // [KC][TX][Lb+4]
-    int32_t *ssA = reinterpret_cast<int32_t *>(sB + MM_KC * TX * sb_stride);  // [TY][KC]
-    int32_t *ssB = ssA + TY * MM_KC;                                       // [KC][TX]
+    // two staging buffers, each [TY][KC][La+4] A limbs, [KC][TX][Lb+4] B limbs,
+    // [TY][KC] A sizes, [KC][TX] B sizes; chunk c + 1 is copied in (cp.async)
+    // while chunk c is multiplied
+    const int stage_words = TY * MM_KC * sa_stride + MM_KC * TX * sb_stride + (TY + TX) * MM_KC;
+    uint32_t *stage_base = reinterpret_cast<uint32_t *>(smem_raw);
 
     const int tid = threadIdx.x, nt = cfg.NT;
     const int g = tid / cfg.Gp, lt = tid % cfg.Gp;
@@ -914,51 +910,97 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
     const int y = y0 + ty, x = x0 + tx;
     const bool valid = has_entry && y < C.rows && x < C.cols;
     const int nbA = La / R, nbB = Lb / R;
+    // the main grid of full R x R blocks: ma x mb (one thread each); a thin operand's
+    // top limb sits in limb ma * R (mb * R) and is folded in by the edge threads
+    const int tA = THIN ? cfg.thinA : 0, tB = THIN ? cfg.thinB : 0;
+    const int ma = nbA - tA, mb = nbB - tB;
     const bool active = valid && lt < cfg.G;
-    int I0 = 0, J0 = 0;
-    if (active) block_of(lt, nbA, nbB, cfg.thinA, cfg.thinB, I0, J0);
-    const bool rthin = cfg.thinA && I0 == nbA - 1, cthin = cfg.thinB && J0 == nbB - 1;
+    const int I0 = active ? lt / mb : 0, J0 = active ? lt % mb : 0;
+    constexpr int NC = 2 * R - 1;
 
-    uint32_t P[2 * R - 1][3];
+    uint32_t P[NC][3];
 #pragma unroll
-    for (int c = 0; c < 2 * R - 1; c++) P[c][0] = P[c][1] = P[c][2] = 0;
+    for (int c = 0; c < NC; c++) P[c][0] = P[c][1] = P[c][2] = 0;
+    // top-limb items of this thread: limb xi[x] of A times limb xj[x] of B
+    constexpr int XM = THIN ? MM_XMAX : 1;
+    const int NA = tA * (mb * R + tB), NX = NA + tB * ma * R;
+    uint32_t X[XM][3];
+    int xi[XM], xj[XM];
+#pragma unroll
+    for (int x = 0; x < XM; x++) {
+        X[x][0] = X[x][1] = X[x][2] = 0;
+        const int it = lt + x * cfg.G;
+        const bool ok = THIN && active && it < NX;
+        xi[x] = !ok ? -1 : it < NA ? ma * R : it - NA;
+        xj[x] = !ok ? -1 : it < NA ? it : mb * R;
+    }
 
-    const int M = cfg.M;
-    for (int k0 = 0; k0 < M; k0 += MM_KC) {
-        const int kc = min(MM_KC, M - k0);
-        __syncthreads();
-        // stage A[y0..y0+TY)[k0..k0+kc) : consecutive threads walk k (contiguous in a plane row)
-        for (int q = tid; q < TY * La * MM_KC; q += nt) {
-            int kk = q % MM_KC, rest = q / MM_KC, i = rest % La, tyy = rest / La;
-            int yy = y0 + tyy;
-            uint32_t v = 0;
-            if (kk < kc && yy < A.rows && i < A.nlimbs) v = A.limbs[(int64_t)i * A.ld + (int64_t)yy * A.rs + k0 + kk];
-            sA[(tyy * MM_KC + kk) * sa_stride + i] = v;
+    const int M = cfg.M, TXs = cfg.TXs;
+    const int nchunks = (M + MM_KC - 1) / MM_KC;
+    auto stage = [&](int c) {
+        uint32_t *sA = stage_base + (c & 1) * stage_words;
+        uint32_t *sB = sA + TY * MM_KC * sa_stride;
+        uint32_t *ssA = sB + MM_KC * TX * sb_stride;
+        uint32_t *ssB = ssA + TY * MM_KC;
+        const int k0 = c * MM_KC, kc = min(MM_KC, M - k0);
+        // A[y0 + tyy][k0 + kk], limb i: consecutive threads walk kk (contiguous in a plane row)
+        for (int tyy = 0; tyy < TY; tyy++) {
+            const int yy = y0 + tyy;
+            const uint32_t *arow = A.limbs + (int64_t)yy * A.rs + k0;
+            for (int q = tid; q < La * MM_KC; q += nt) {
+                const int kk = q & (MM_KC - 1), i = q >> 4;
+                cp_async4(sA + (tyy * MM_KC + kk) * sa_stride + i, arow + (int64_t)i * A.ld + kk, A.limbs,
+                          kk < kc && yy < A.rows && i < A.nlimbs);
+            }
         }
-        // stage B[k0..k0+kc)[x0..x0+TX) : consecutive threads walk x
+        // B[k0 + kk][x0 + txx], limb i: consecutive threads walk txx (contiguous in a plane row)
         for (int q = tid; q < MM_KC * Lb * TX; q += nt) {
-            int txx = q % TX, rest = q / TX, i = rest % Lb, kk = rest / Lb;
-            int xx = x0 + txx;
-            uint32_t v = 0;
-            if (kk < kc && xx < B.cols && i < B.nlimbs) v = B.limbs[(int64_t)i * B.ld + (int64_t)(k0 + kk) * B.rs + xx];
-            sB[(kk * TX + txx) * sb_stride + i] = v;
+            const int txx = q & (TX - 1), r = q >> TXs, kk = r & (MM_KC - 1), i = r >> 4;
+            const int xx = x0 + txx;
+            cp_async4(sB + (kk * TX + txx) * sb_stride + i,
+                      B.limbs + (int64_t)i * B.ld + (int64_t)(k0 + kk) * B.rs + xx, B.limbs,
+                      kk < kc && xx < B.cols && i < B.nlimbs);
         }
         for (int q = tid; q < TY * MM_KC; q += nt) {
-            int kk = q % MM_KC, tyy = q / MM_KC, yy = y0 + tyy;
-            ssA[q] = (kk < kc && yy < A.rows) ? A.sizes[(int64_t)yy * A.rs + k0 + kk] : 0;
+            const int kk = q & (MM_KC - 1), yy = y0 + (q >> 4);
+            cp_async4(ssA + q, A.sizes + (int64_t)yy * A.rs + k0 + kk, A.sizes, kk < kc && yy < A.rows);
         }
         for (int q = tid; q < MM_KC * TX; q += nt) {
-            int txx = q % TX, kk = q / TX, xx = x0 + txx;
-            ssB[q] = (kk < kc && xx < B.cols) ? B.sizes[(int64_t)(k0 + kk) * B.rs + xx] : 0;
+            const int txx = q & (TX - 1), kk = q >> TXs, xx = x0 + txx;
+            cp_async4(ssB + q, B.sizes + (int64_t)(k0 + kk) * B.rs + xx, B.sizes, kk < kc && xx < B.cols);
         }
-        __syncthreads();
+    };
+    stage(0);
+    cp_async_commit();
+    for (int c = 0; c < nchunks; c++) {
+        if (c + 1 < nchunks) stage(c + 1);
+        cp_async_commit();  // an empty group on the last chunk keeps the wait count uniform
+        cp_async_wait1();   // this thread's copies of chunk c have landed
+        __syncthreads();    // ... and every thread's
         if (active) {
+            const uint32_t *sA = stage_base + (c & 1) * stage_words;
+            const uint32_t *sB = sA + TY * MM_KC * sa_stride;
+            const int32_t *ssA = reinterpret_cast<const int32_t *>(sB + MM_KC * TX * sb_stride);
+            const int32_t *ssB = ssA + TY * MM_KC;
+            const int kc = min(MM_KC, M - c * MM_KC);
             for (int kk = 0; kk < kc; kk++) {
                 const int sa = ssA[ty * MM_KC + kk], sb = ssB[kk * TX + tx];
                 if (sa == 0 || sb == 0) continue;
+                const bool pos = (sa ^ sb) >= 0;
+                const uint32_t *ra = sA + (ty * MM_KC + kk) * sa_stride;
+                const uint32_t *rb = sB + (kk * TX + tx) * sb_stride;
+                if (THIN) {
+#pragma unroll
+                    for (int x = 0; x < XM; x++) {
+                        if (xi[x] < 0) continue;
+                        const uint32_t u = ra[xi[x]], v = rb[xj[x]];
+                        if (pos) MAC96(X[x][0], X[x][1], X[x][2], u, v);
+                        else MSC96(X[x][0], X[x][1], X[x][2], u, v);
+                    }
+                }
                 if (I0 * R >= iabs_d(sa) || J0 * R >= iabs_d(sb)) continue;
-                const uint32_t *pa = sA + (ty * MM_KC + kk) * sa_stride + I0 * R;
-                const uint32_t *pb = sB + (kk * TX + tx) * sb_stride + J0 * R;
+                const uint32_t *pa = ra + I0 * R;
+                const uint32_t *pb = rb + J0 * R;
                 uint32_t a[R], b[R];
                 if (R >= 4) {
 #pragma unroll
@@ -972,43 +1014,66 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
 #pragma unroll
                     for (int v = 0; v < R; v++) { a[v] = pa[v]; b[v] = pb[v]; }
                 }
-                if ((sa ^ sb) >= 0) block_mac<R, false>(P, a, b, rthin, cthin);
-                else block_mac<R, true>(P, a, b, rthin, cthin);
+                if (pos) block_mac<R, NC, false>(P, a, b);
+                else block_mac<R, NC, true>(P, a, b);
             }
         }
+        __syncthreads();  // buffer c & 1 is refilled by the copies of chunk c + 2
     }
-    __syncthreads();
 
     // ---- reduction of partial columns ---------------------------------------------------
-    const int Lc = La + Lb;       // product columns
+    const int Lc = La + Lb;       // product columns (padded)
     const int LB = Lc + 2;        // result limbs (two extra for the carry out of the sum over k)
-    const int NC = 2 * R - 1;
     uint32_t *part = reinterpret_cast<uint32_t *>(smem_raw);  // [EPC][G][NC][3]
-    const size_t part_words = (size_t)EPC * cfg.G * NC * 3;
+    uint32_t *xpart = part + (size_t)EPC * cfg.G * NC * 3;     // [EPC][XM][G][3] (thin operands)
+    const size_t part_words = (size_t)EPC * cfg.G * (NC + (THIN ? XM : 0)) * 3;
     unsigned long long *cs = reinterpret_cast<unsigned long long *>(part + ((part_words + 1) & ~(size_t)1));  // [EPC][Lc][3]
     uint32_t *res = reinterpret_cast<uint32_t *>(cs + (size_t)EPC * Lc * 3);                                  // [EPC][LB]
     if (active) {
-        uint32_t *dst = part + ((size_t)g * cfg.G + I0 * nbB + J0) * NC * 3;
+        uint32_t *dst = part + ((size_t)g * cfg.G + I0 * mb + J0) * NC * 3;
 #pragma unroll
         for (int c = 0; c < NC; c++) {
             dst[c * 3 + 0] = P[c][0];
             dst[c * 3 + 1] = P[c][1];
             dst[c * 3 + 2] = P[c][2];
         }
+        if (THIN) {
+#pragma unroll
+            for (int x = 0; x < XM; x++) {
+                uint32_t *xd = xpart + (((size_t)g * XM + x) * cfg.G + lt) * 3;
+                xd[0] = X[x][0];
+                xd[1] = X[x][1];
+                xd[2] = X[x][2];
+            }
+        }
     }
     __syncthreads();
-    // column t of entry gg gathers block diagonal d = t / R at offset t % R and
-    // diagonal d - 1 at offset t % R + R
+    // column t of entry gg gathers the blocks on diagonal d = t / R - h at offset
+    // t % R + h R, for h = 0, 1, and with thin operands the top-limb items that
+    // land in it: a_top * b_(t - ma R) and a_(t - mb R) * b_top
     for (int item = tid; item < EPC * Lc; item += nt) {
         const int gg = item / Lc, t = item % Lc;
         unsigned long long s0 = 0, s1 = 0;
         long long s2 = 0;
-        for (int h = 0; h < 2; h++) {
+#pragma unroll
+        for (int h = 0; h <= (NC - 1) / R; h++) {
             const int d = t / R - h, off = t % R + h * R;
             if (d < 0 || off >= NC) continue;
-            const int i_lo = d - nbB + 1 > 0 ? d - nbB + 1 : 0, i_hi = d < nbA - 1 ? d : nbA - 1;
+            const int i_lo = d - mb + 1 > 0 ? d - mb + 1 : 0, i_hi = d < ma - 1 ? d : ma - 1;
             for (int i = i_lo; i <= i_hi; i++) {
-                const uint32_t *w = part + ((size_t)gg * cfg.G + i * nbB + (d - i)) * NC * 3 + off * 3;
+                const uint32_t *w = part + ((size_t)gg * cfg.G + i * mb + (d - i)) * NC * 3 + off * 3;
+                s0 += w[0];
+                s1 += w[1];
+                s2 += (int32_t)w[2];
+            }
+        }
+        if (THIN) {
+            const int ia = t - ma * R, ib = t - mb * R;
+            const int its[2] = {tA && ia >= 0 && ia < NA ? ia : -1, tB && ib >= 0 && ib < ma * R ? NA + ib : -1};
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                if (its[q] < 0) continue;
+                const uint32_t *w = xpart + (((size_t)gg * XM + its[q] / cfg.G) * cfg.G + its[q] % cfg.G) * 3;
                 s0 += w[0];
                 s1 += w[1];
                 s2 += (int32_t)w[2];
@@ -1059,10 +1124,12 @@ __device__ __forceinline__ void limb_tile(const MatArgs &C, const MatArgs &A, co
     store_signed(buf, LB, carry < 0, C, ic, err);
 }
 
-template <int R, int NT>
-__global__ void __launch_bounds__(NT) k_limb_matmul(MatArgs C, MatArgs A, MatArgs B, MMCfg cfg, uint32_t *err) {
+// 256-thread CTAs are sized for two per SM (at most 128 registers a thread)
+template <int R, int NT, bool THIN>
+__global__ void __launch_bounds__(NT, NT <= MM_THREADS ? 2 : 1)
+    k_limb_matmul(MatArgs C, MatArgs A, MatArgs B, MMCfg cfg, uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    limb_tile<R>(C, A, B, cfg, blockIdx.y, blockIdx.x, smem_raw, err);
+    limb_tile<R, THIN>(C, A, B, cfg, blockIdx.y, blockIdx.x, smem_raw, err);
 }
 
 // Persistent form for batches of uneven products: every CTA takes (job, tile)
@@ -1074,9 +1141,9 @@ struct LimbJob {
     MMCfg cfg;
 };
 
-template <int R, int NT>
-__global__ void __launch_bounds__(NT) k_limb_batched(const LimbJob *jobs, const int *items, int nitems, int *counter,
-                                                     uint32_t *err) {
+template <int R, int NT, bool THIN>
+__global__ void __launch_bounds__(NT, NT <= MM_THREADS ? 2 : 1)
+    k_limb_batched(const LimbJob *jobs, const int *items, int nitems, int *counter, uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int cur;
     for (;;) {
@@ -1087,7 +1154,7 @@ __global__ void __launch_bounds__(NT) k_limb_batched(const LimbJob *jobs, const 
         const LimbJob &j = jobs[items[3 * it]];
         const MatArgs C = j.C, A = j.A, B = j.B;
         const MMCfg cfg = j.cfg;
-        limb_tile<R>(C, A, B, cfg, items[3 * it + 1], items[3 * it + 2], smem_raw, err);
+        limb_tile<R, THIN>(C, A, B, cfg, items[3 * it + 1], items[3 * it + 2], smem_raw, err);
         __syncthreads();
     }
 }
@@ -1199,8 +1266,9 @@ __global__ void k_wino_sums(WinoTree t, int d, int64_t nparents, int h, uint32_t
 }
 
 // All leaf products of the tree: one CTA per (leaf, TY x TX tile of its output).
-template <int R, int NT>
-__global__ void __launch_bounds__(NT) k_wino_leaves(WinoTree t, MMCfg cfg, int ny, int nx, uint32_t *err) {
+template <int R, int NT, bool THIN>
+__global__ void __launch_bounds__(NT, NT <= MM_THREADS ? 2 : 1)
+    k_wino_leaves(WinoTree t, MMCfg cfg, int ny, int nx, uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int64_t tiles = (int64_t)ny * nx;
     const int64_t node = blockIdx.x / tiles;
@@ -1208,7 +1276,7 @@ __global__ void __launch_bounds__(NT) k_wino_leaves(WinoTree t, MMCfg cfg, int n
     const int L = t.levels, h = t.N >> L;
     const MatArgs A = wt_operand(t, 0, L, node), B = wt_operand(t, 1, L, node);
     const MatArgs C = wt_dense(t.p_limbs[L], t.p_sizes[L], node, h, t.capP);
-    limb_tile<R>(C, A, B, cfg, rem / nx, rem % nx, smem_raw, err);
+    limb_tile<R, THIN>(C, A, B, cfg, rem / nx, rem % nx, smem_raw, err);
 }
 
 // Level d's products combined into their parents' outputs (level d - 1): one
@@ -1333,53 +1401,68 @@ gbmm_status launch_mpz_mulops(const gbmm_mat &w, const gbmm_mat &u, const gbmm_m
 
 static int roundup(int x, int m) { return (x + m - 1) / m * m; }
 
-// Picks the block edge R and group size for limb counts la x lb.  Groups of up
-// to 256 threads share 256-thread CTAs; a group of 257..512 threads (entries of
-// up to 181 x 181 limbs, e.g. the one-limb-longer operands a Winograd level
-// forms from 128-limb entries) gets a CTA of its own.
-static bool choose_mm_blocks(int la, int lb, MMCfg &cfg);
+// Launches LAUNCH(R, NT, THIN) for a configuration: the block edge, one group
+// per CTA of up to 512 threads (R = 8) or CTAs of at most 256, and whether an
+// operand is thin (the edge threads fold in a single top limb).
+#define LIMB_DISPATCH(cfg_, LAUNCH)                                              \
+    do {                                                                         \
+        const bool th_ = (cfg_).thinA || (cfg_).thinB;                           \
+        if ((cfg_).NT > MM_THREADS) {                                            \
+            if (th_) LAUNCH(8, MM_THREADS_WIDE, true);                           \
+            else LAUNCH(8, MM_THREADS_WIDE, false);                              \
+        } else if (th_) {                                                        \
+            switch ((cfg_).R) {                                                  \
+                case 2: LAUNCH(2, MM_THREADS, true); break;                      \
+                case 4: LAUNCH(4, MM_THREADS, true); break;                      \
+                default: LAUNCH(8, MM_THREADS, true); break;                     \
+            }                                                                    \
+        } else {                                                                 \
+            switch ((cfg_).R) {                                                  \
+                case 1: LAUNCH(1, MM_THREADS, false); break;                     \
+                case 2: LAUNCH(2, MM_THREADS, false); break;                     \
+                case 4: LAUNCH(4, MM_THREADS, false); break;                     \
+                default: LAUNCH(8, MM_THREADS, false); break;                    \
+            }                                                                    \
+        }                                                                        \
+    } while (0)
+
+// Picks the block edge R and group size for limb counts la x lb.  An operand
+// of one limb past a multiple of R (and longer than R) is "thin": its top limb's
+// products are spread over the main grid's threads as extra items, so the group
+// is the main grid alone (a one-limb-longer Winograd sum of 128-limb entries
+// keeps 16 x 16 threads).  Groups of up to 256 threads share 256-thread CTAs; a group of
+// 257..512 threads (entries of up to about 176 limbs) gets a CTA of its own.
+static bool try_block(int la, int lb, int R, int gmin, int gmax, MMCfg &cfg) {
+    int tA = R > 1 && la > R && la % R == 1, tB = R > 1 && lb > R && lb % R == 1;
+    const int pa = roundup(la, R), pb = roundup(lb, R);
+    int G = (pa / R - tA) * (pb / R - tB);
+    // top-limb items of the thin operands: at most MM_XMAX a thread, else whole blocks
+    const int nx = tA * ((pb / R - tB) * R + tB) + tB * (pa / R - tA) * R;
+    if ((tA || tB) && nx > MM_XMAX * G) {
+        tA = tB = 0;
+        G = (pa / R) * (pb / R);
+    }
+    if (G < gmin || G > gmax) return false;
+    cfg.R = R; cfg.La = pa; cfg.Lb = pb; cfg.G = G; cfg.Gp = roundup(G, 32);
+    cfg.thinA = tA; cfg.thinB = tB;
+    cfg.NT = cfg.Gp > MM_THREADS ? cfg.Gp : MM_THREADS;
+    return true;
+}
 static bool choose_mm(int la, int lb, MMCfg &cfg) {
     la = la < 1 ? 1 : la;
     lb = lb < 1 ? 1 : lb;
-    if (!choose_mm_blocks(la, lb, cfg)) return false;
-    cfg.thinA = cfg.R > 1 && la % cfg.R == 1;
-    cfg.thinB = cfg.R > 1 && lb % cfg.R == 1;
-    return true;
-}
-static bool choose_mm_blocks(int la, int lb, MMCfg &cfg) {
-    cfg.NT = MM_THREADS;
     const int cand[3] = {8, 4, 2};
-    for (int ci = 0; ci < 3; ci++) {
-        int R = cand[ci];
-        int pa = roundup(la, R), pb = roundup(lb, R);
-        int G = (pa / R) * (pb / R);
-        if (G >= 32 && G <= MM_THREADS) {
-            cfg.R = R; cfg.La = pa; cfg.Lb = pb; cfg.G = G; cfg.Gp = roundup(G, 32);
-            return true;
-        }
-    }
-    int mx = la > lb ? la : lb;
+    for (int ci = 0; ci < 3; ci++)
+        if (try_block(la, lb, cand[ci], 32, MM_THREADS, cfg)) return true;
+    const int mx = la > lb ? la : lb;
     if (mx <= 8) {
-        int R = mx <= 1 ? 1 : mx <= 2 ? 2 : mx <= 4 ? 4 : 8;
-        cfg.R = R; cfg.La = R; cfg.Lb = R; cfg.G = 1; cfg.Gp = 1;
+        const int R = mx <= 1 ? 1 : mx <= 2 ? 2 : mx <= 4 ? 4 : 8;
+        cfg.R = R; cfg.La = R; cfg.Lb = R; cfg.G = 1; cfg.Gp = 1; cfg.NT = MM_THREADS;
+        cfg.thinA = cfg.thinB = 0;
         return true;
     }
-    {
-        int R = 2, pa = roundup(la, R), pb = roundup(lb, R), G = (pa / R) * (pb / R);
-        if (G <= MM_THREADS) {
-            cfg.R = R; cfg.La = pa; cfg.Lb = pb; cfg.G = G; cfg.Gp = roundup(G, 32);
-            return true;
-        }
-    }
-    {
-        int R = 8, pa = roundup(la, R), pb = roundup(lb, R), G = (pa / R) * (pb / R);
-        if (G <= MM_THREADS_WIDE) {
-            cfg.R = R; cfg.La = pa; cfg.Lb = pb; cfg.G = G; cfg.Gp = roundup(G, 32);
-            cfg.NT = cfg.Gp;
-            return true;
-        }
-    }
-    return false;
+    if (try_block(la, lb, 2, 1, MM_THREADS, cfg)) return true;
+    return try_block(la, lb, 8, MM_THREADS + 1, MM_THREADS_WIDE, cfg);
 }
 
 // Entries per CTA and their TY x TX arrangement for a chosen group size; the CTA
@@ -1391,6 +1474,8 @@ static void finish_cfg(MMCfg &cfg, int M, int accumulate) {
     while (TY * TY * 4 <= EPC) TY *= 2;
     cfg.TY = TY;
     cfg.TX = EPC / TY;
+    cfg.TXs = 0;
+    while ((1 << cfg.TXs) < cfg.TX) cfg.TXs++;
     cfg.M = M;
     cfg.accumulate = accumulate;
 }
@@ -1401,9 +1486,10 @@ bool limb_kernel_fits(int la, int lb) {
 }
 
 static size_t mm_smem(const MMCfg &c) {
-    size_t stage = (size_t)c.TY * MM_KC * (c.La + 4) * 4 + (size_t)MM_KC * c.TX * (c.Lb + 4) * 4 +
-                   (size_t)(c.TY + c.TX) * MM_KC * 4;
-    const int EPC = c.TY * c.TX, Lc = c.La + c.Lb, NC = 2 * c.R - 1;
+    // two staging buffers (double-buffered chunks), or the reduction's buffers after the loop
+    size_t stage = 2 * ((size_t)c.TY * MM_KC * (c.La + 4) * 4 + (size_t)MM_KC * c.TX * (c.Lb + 4) * 4 +
+                        (size_t)(c.TY + c.TX) * MM_KC * 4);
+    const int EPC = c.TY * c.TX, Lc = c.La + c.Lb, NC = 2 * c.R - 1 + ((c.thinA || c.thinB) ? MM_XMAX : 0);
     size_t red = (size_t)EPC * c.G * NC * 3 * 4 + 8 + (size_t)EPC * Lc * 3 * 8 + (size_t)EPC * (Lc + 2) * 4;
     return stage > red ? stage : red;
 }
@@ -1424,24 +1510,15 @@ gbmm_status launch_limb_matmul(const gbmm_mat &c, const gbmm_mat &a, const gbmm_
     if (smem > 200 * 1024) return set_error(GBMM_ERR_UNSUPPORTED, "limb matmul: shared memory %zu too large", smem);
     dim3 grid((unsigned)((c.cols + cfg.TX - 1) / cfg.TX), (unsigned)((c.rows + cfg.TY - 1) / cfg.TY));
     uint32_t *err = device_error_word();
-#define LAUNCH_R(RR, NTT)                                                                              \
+#define LAUNCH_R(RR, NTT, TH)                                                                          \
     do {                                                                                               \
         if (smem > 48 * 1024)                                                                          \
-            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_limb_matmul<RR, NTT>,                                 \
+            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_limb_matmul<RR, NTT, TH>,                             \
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
         LaunchScope ls_("k_limb_matmul", s);                                                            \
-        k_limb_matmul<RR, NTT><<<grid, cfg.NT, smem, s>>>(margs(c), margs(a), margs(b), cfg, err);    \
+        k_limb_matmul<RR, NTT, TH><<<grid, cfg.NT, smem, s>>>(margs(c), margs(a), margs(b), cfg, err); \
     } while (0)
-    if (cfg.NT > MM_THREADS) {
-        LAUNCH_R(8, MM_THREADS_WIDE);
-    } else {
-        switch (cfg.R) {
-            case 1: LAUNCH_R(1, MM_THREADS); break;
-            case 2: LAUNCH_R(2, MM_THREADS); break;
-            case 4: LAUNCH_R(4, MM_THREADS); break;
-            default: LAUNCH_R(8, MM_THREADS); break;
-        }
-    }
+    LIMB_DISPATCH(cfg, LAUNCH_R);
 #undef LAUNCH_R
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
@@ -1462,25 +1539,28 @@ gbmm_status plan_limb_batch(const std::vector<gbmm_mat> &C, const std::vector<gb
         int job, by, bx;
         double cost;
     };
-    // groups: block edge 1, 2, 4, 8 on 256-thread CTAs, and 8 with one wide group per CTA
-    constexpr int NG = 5;
-    const int Rs[NG] = {1, 2, 4, 8, 8};
+    // groups (one launch each): block edge 1, 2, 4, 8 on 256-thread CTAs and 8 with
+    // one wide group per CTA, each with and without a thin operand
+    constexpr int NG = LimbBatchPlan::MAX_GROUPS;
+    const int Rs[NG] = {1, 1, 2, 2, 4, 4, 8, 8, 8, 8};
     std::vector<LimbJob> jobs[NG];
     std::vector<Item> items[NG];
-    size_t smem[NG] = {0, 0, 0, 0, 0};
-    int nts[NG] = {MM_THREADS, MM_THREADS, MM_THREADS, MM_THREADS, 0};
+    size_t smem[NG] = {};
+    int nts[NG];
+    for (int g = 0; g < NG; g++) nts[g] = g < 8 ? MM_THREADS : 0;
     for (size_t i = 0; i < C.size(); i++) {
         MMCfg cfg;
         if (!choose_mm(A[i].nlimbs, B[i].nlimbs, cfg))
             return set_error(GBMM_ERR_UNSUPPORTED, "batched limb job %zu: entries too long", i);
         finish_cfg(cfg, A[i].cols, 0);
+        const int thin = (cfg.thinA || cfg.thinB) ? 1 : 0;
         int g = 0;
         if (cfg.NT > MM_THREADS) {
             // one launch of the wide group kernel runs with a single CTA size
-            g = NG - 1;
+            g = 8 + thin;
             nts[g] = std::max(nts[g], cfg.NT);
         } else {
-            while (Rs[g] != cfg.R) g++;
+            g = (cfg.R == 1 ? 0 : cfg.R == 2 ? 2 : cfg.R == 4 ? 4 : 6) + thin;
         }
         smem[g] = std::max(smem[g], mm_smem(cfg));
         LimbJob lj;
@@ -1501,6 +1581,7 @@ gbmm_status plan_limb_batch(const std::vector<gbmm_mat> &C, const std::vector<gb
         LimbBatchPlan::Group gr;
         gr.R = Rs[g];
         gr.NT = nts[g];
+        gr.thin = g & 1;
         for (auto &j : jobs[g]) j.cfg.NT = nts[g];
         gr.smem = smem[g];
         gr.nitems = (int)items[g].size();
@@ -1530,26 +1611,22 @@ gbmm_status launch_limb_batch(const LimbBatchPlan &plan, const char *d_blob, int
         const LimbBatchPlan::Group &gr = plan.groups[g];
         const LimbJob *jobs = reinterpret_cast<const LimbJob *>(d_blob + gr.jobs_off);
         const int *items = reinterpret_cast<const int *>(d_blob + gr.items_off);
-#define LAUNCH_B(RR, NTT)                                                                                 \
+#define LAUNCH_B(RR, NTT, TH)                                                                             \
     do {                                                                                                  \
         if (gr.smem > 48 * 1024)                                                                          \
-            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_limb_batched<RR, NTT>,                                   \
+            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_limb_batched<RR, NTT, TH>,                               \
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gr.smem)); \
         const int grid =                                                                                  \
-            std::min(gr.nitems, occupancy_ctas((const void *)k_limb_batched<RR, NTT>, gr.NT, gr.smem));  \
+            std::min(gr.nitems, occupancy_ctas((const void *)k_limb_batched<RR, NTT, TH>, gr.NT, gr.smem)); \
         LaunchScope ls_("k_limb_batched", s);                                                             \
-        k_limb_batched<RR, NTT><<<grid, gr.NT, gr.smem, s>>>(jobs, items, gr.nitems, d_counters + g, err); \
+        k_limb_batched<RR, NTT, TH><<<grid, gr.NT, gr.smem, s>>>(jobs, items, gr.nitems, d_counters + g, err); \
     } while (0)
-        if (gr.NT > MM_THREADS) {
-            LAUNCH_B(8, MM_THREADS_WIDE);
-        } else {
-            switch (gr.R) {
-                case 1: LAUNCH_B(1, MM_THREADS); break;
-                case 2: LAUNCH_B(2, MM_THREADS); break;
-                case 4: LAUNCH_B(4, MM_THREADS); break;
-                default: LAUNCH_B(8, MM_THREADS); break;
-            }
-        }
+        MMCfg gc;
+        gc.R = gr.R;
+        gc.NT = gr.NT;
+        gc.thinA = gr.thin;
+        gc.thinB = 0;
+        LIMB_DISPATCH(gc, LAUNCH_B);
 #undef LAUNCH_B
         GBMM_CUDA_TRY(cudaGetLastError());
     }
@@ -1595,24 +1672,15 @@ gbmm_status launch_wino_leaves(const WinoTree &t, cudaStream_t s) {
     const int64_t blocks = pow7(t.levels) * ny * nx;
     if (blocks > 0x7FFFFFFF) return set_error(GBMM_ERR_UNSUPPORTED, "winograd leaves: %lld tiles", (long long)blocks);
     uint32_t *err = device_error_word();
-#define LAUNCH_W(RR, NTT)                                                                              \
+#define LAUNCH_W(RR, NTT, TH)                                                                          \
     do {                                                                                               \
         if (smem > 48 * 1024)                                                                          \
-            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_wino_leaves<RR, NTT>,                                 \
+            GBMM_CUDA_TRY(cudaFuncSetAttribute(k_wino_leaves<RR, NTT, TH>,                             \
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
         LaunchScope ls_("k_wino_leaves", s);                                                            \
-        k_wino_leaves<RR, NTT><<<(unsigned)blocks, cfg.NT, smem, s>>>(t, cfg, ny, nx, err);           \
+        k_wino_leaves<RR, NTT, TH><<<(unsigned)blocks, cfg.NT, smem, s>>>(t, cfg, ny, nx, err);       \
     } while (0)
-    if (cfg.NT > MM_THREADS) {
-        LAUNCH_W(8, MM_THREADS_WIDE);
-    } else {
-        switch (cfg.R) {
-            case 1: LAUNCH_W(1, MM_THREADS); break;
-            case 2: LAUNCH_W(2, MM_THREADS); break;
-            case 4: LAUNCH_W(4, MM_THREADS); break;
-            default: LAUNCH_W(8, MM_THREADS); break;
-        }
-    }
+    LIMB_DISPATCH(cfg, LAUNCH_W);
 #undef LAUNCH_W
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;

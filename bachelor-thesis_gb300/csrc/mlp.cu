@@ -1,9 +1,9 @@
-// Learned cost model for the dispatcher: an 8 -> 64 -> 64 -> 3 MLP with BF16
-// weights and FP32 accumulation.  Its three heads predict log2(milliseconds)
-// of the three candidate plans for one product (limb path without recursion,
-// limb path with Winograd recursion at cutoff 64, CRT path); GBMM_PATH_AUTO
-// takes the cheapest.  The number of CRT moduli is not a head: it is fixed by
-// the exactness bound.
+// Learned cost model for the dispatcher: an 8 -> 64 -> 64 -> GBMM_NPLANS MLP
+// with BF16 weights and FP32 accumulation.  Its heads predict log2(milliseconds)
+// of each candidate plan for one product (gbmm_plan: the limb kernel alone,
+// Winograd trees of three cutoffs, i.e. recursion depths, CRT with three GEMM
+// tile forms and CRT after a limb-half split, i.e. fewer moduli per product);
+// GBMM_PATH_AUTO runs the cheapest trusted one.
 //
 // Training runs on the GPU with the kernels below (forward, backward with
 // FP32 gradient accumulation, Adam on FP32 master weights that are rounded to
@@ -21,7 +21,7 @@
 namespace gbmm {
 
 namespace {
-constexpr int NF = 8, NH = 64, NO = 3;
+constexpr int NF = 8, NH = 64, NO = GBMM_NPLANS;
 constexpr int NW1 = NF * NH, NW2 = NH * NH, NW3 = NH * NO;
 constexpr int NPARAM = NW1 + NH + NW2 + NH + NW3 + NO;  // weights then biases per layer
 constexpr int OFF_W1 = 0, OFF_B1 = NW1, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NW2, OFF_W3 = OFF_B2 + NH,
@@ -35,7 +35,16 @@ struct Model {
     float *d_master = nullptr, *d_m = nullptr, *d_v = nullptr, *d_grad = nullptr;
     __nv_bfloat16 *d_w16 = nullptr;
     int step = 0;
+    // measured targets each head has trained on (gbmm_model_train); a head with
+    // fewer than MIN_HEAD_SAMPLES is not consulted.  Parameters set from outside
+    // count as trained.
+    int head_samples[NO] = {};
 };
+constexpr int MIN_HEAD_SAMPLES = 8;
+// the model overrides the plain heuristic's plan only when it predicts at least
+// this much gain (log2 of 1.10): switches between plans whose costs differ by
+// less than the model's own error would be noise
+constexpr float OVERRIDE_MARGIN_LOG2 = 0.1375f;
 
 // Features of one product (all scaled to roughly unit range).
 __host__ __device__ inline void job_features(int m, int k, int n, int la, int lb, float *f) {
@@ -242,20 +251,23 @@ static void host_forward(const Model *md, const float *x, float *y) {
     }
 }
 
-int model_choose(gbmm_handle h, int m, int k, int n, int la, int lb, int *cutoff) {
+int model_choose(gbmm_handle h, int m, int k, int n, int la, int lb) {
     const Model *md = model_of(h);
     if (!md) return -1;
     float f[NF], y[NO];
     job_features(m, k, n, la, lb, f);
     host_forward(md, f, y);
-    // candidates the kernels cannot take directly are still legal (dispatch
-    // splits long operands), so the argmin is taken over all three heads
-    int best = 0;
-    for (int o = 1; o < NO; o++)
-        if (y[o] < y[best]) best = o;
-    if (best == 2) return GBMM_PATH_CRT;
-    *cutoff = best == 0 ? (1 << 30) : 64;
-    return GBMM_PATH_LIMB;
+    // only plans the autotuner would have timed for this product, with heads that
+    // trained on enough timings: anything else is an extrapolation, not a prediction
+    int best = -1;
+    for (int o = 0; o < NO; o++) {
+        if (!plan_admissible(o, m, k, n, la, lb) || md->head_samples[o] < MIN_HEAD_SAMPLES) continue;
+        if (best < 0 || y[o] < y[best]) best = o;
+    }
+    const int base = heuristic_plan(m, k, n, la, lb);
+    if (best < 0 || best == base) return base;
+    if (md->head_samples[base] >= MIN_HEAD_SAMPLES && y[best] > y[base] - OVERRIDE_MARGIN_LOG2) return base;
+    return best;
 }
 
 }  // namespace gbmm
@@ -289,6 +301,7 @@ extern "C" gbmm_status gbmm_model_init(gbmm_handle h, uint64_t seed) {
     fill(OFF_W3, NW3, NH);
     for (int i = 0; i < NH; i++) md->master[OFF_B1 + i] = md->master[OFF_B2 + i] = 0.f;
     for (int i = 0; i < NO; i++) md->master[OFF_B3 + i] = 0.f;
+    for (int o = 0; o < NO; o++) md->head_samples[o] = 0;  // untrained heads are not consulted
     return model_upload(md);
 }
 
@@ -297,6 +310,7 @@ extern "C" gbmm_status gbmm_model_set_params(gbmm_handle h, const float *params)
     Model *md = nullptr;
     GBMM_TRY(model_alloc(h, &md));
     memcpy(md->master.data(), params, NPARAM * 4);
+    for (int o = 0; o < NO; o++) md->head_samples[o] = MIN_HEAD_SAMPLES;  // parameters given count as trained
     return model_upload(md);
 }
 
@@ -409,6 +423,8 @@ extern "C" gbmm_status gbmm_model_train(gbmm_handle h, const float *X, const flo
     float *dD1 = dL + 1, *dD2 = dD1 + nH, *dD3 = dD2 + nH;  // error terms per sample
     int count = 0;
     for (size_t i = 0; i < nT; i++) count += !std::isnan(T[i]);
+    for (int o = 0; o < NO; o++)
+        for (int i = 0; i < nsamp; i++) md->head_samples[o] += !std::isnan(T[(size_t)i * NO + o]);
     cudaError_t e = cudaMemcpyAsync(dX, X, nX * 4, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dT, T, nT * 4, cudaMemcpyHostToDevice, s);
     const int grid = (nsamp + MLP_THREADS - 1) / MLP_THREADS;

@@ -23,6 +23,10 @@ LIB_PATH = os.path.join(HERE, "_build", "libgbmm.so")
 OK, ERR_INVALID, ERR_CAPACITY, ERR_CUDA, ERR_PARSE, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(8)
 PATH_AUTO, PATH_LIMB, PATH_CRT = 0, 1, 2
 METHOD_NAIVE, METHOD_STRASSEN, METHOD_WINOGRAD, METHOD_NAIVE_REC = 1, 3, 35, 4
+# gbmm_plan: the candidate plans the autotuner times and the cost model predicts
+(PLAN_LIMB_NAIVE, PLAN_LIMB_W32, PLAN_LIMB_W64, PLAN_LIMB_W128, PLAN_CRT, PLAN_CRT_SINGLE, PLAN_CRT_PAIR,
+ PLAN_CRT_SPLIT) = range(8)
+NPLANS = 8
 
 
 class GbmmError(RuntimeError):
@@ -39,12 +43,13 @@ class Mat(ctypes.Structure):
 
 class Opts(ctypes.Structure):
     _fields_ = [("path", ctypes.c_int32), ("method", ctypes.c_int32), ("cutoff", ctypes.c_int32),
-                ("nprimes", ctypes.c_int32), ("accumulate", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("nprimes", ctypes.c_int32), ("accumulate", ctypes.c_int32), ("plan", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
 
 class Job(ctypes.Structure):
     _fields_ = [("c", Mat), ("a", Mat), ("b", Mat), ("path", ctypes.c_int32), ("cutoff", ctypes.c_int32),
-                ("nprimes", ctypes.c_int32), ("chosen_path", ctypes.c_int32)]
+                ("nprimes", ctypes.c_int32), ("chosen_path", ctypes.c_int32), ("chosen_plan", ctypes.c_int32)]
 
 
 class HostJob(ctypes.Structure):
@@ -338,9 +343,11 @@ class Handle:
     def bind_stream(self):
         check(lib().gbmm_set_stream(self.h, stream_ptr()))
 
-    def matmul(self, C, A, B, path=PATH_AUTO, method=METHOD_WINOGRAD, cutoff=0, nprimes=0, accumulate=False):
+    def matmul(self, C, A, B, path=PATH_AUTO, method=METHOD_WINOGRAD, cutoff=0, nprimes=0, accumulate=False, plan=None):
+        """C = A*B (C += A*B with accumulate); `plan` (a PLAN_* id) runs that plan and
+        overrides path / method / cutoff."""
         self.bind_stream()
-        o = Opts(path, method, cutoff, nprimes, int(bool(accumulate)))
+        o = Opts(path, method, cutoff, nprimes, int(bool(accumulate)), 0 if plan is None else 1 + plan)
         check(lib().gbmm_matmul(self.h, _m(C), _m(A), _m(B), ctypes.byref(o)))
 
     @staticmethod
@@ -352,11 +359,14 @@ class Handle:
             arr[i].path = path
         return arr
 
-    def matmul_batched(self, jobs, path=PATH_AUTO):
-        """Runs a ctypes array of gbmm_job; returns the paths the dispatcher chose."""
+    def matmul_batched(self, jobs, path=PATH_AUTO, plans=False):
+        """Runs a ctypes array of gbmm_job; returns the paths the dispatcher chose
+        (with plans=True: (path, gbmm_plan) pairs)."""
         self.bind_stream()
-        o = Opts(path, METHOD_WINOGRAD, 0, 0, 0)
+        o = Opts(path, METHOD_WINOGRAD, 0, 0, 0, 0)
         check(lib().gbmm_matmul_batched(self.h, jobs, len(jobs), ctypes.byref(o)))
+        if plans:
+            return [(jobs[i].chosen_path, jobs[i].chosen_plan) for i in range(len(jobs))]
         return [jobs[i].chosen_path for i in range(len(jobs))]
 
     @staticmethod
@@ -406,7 +416,7 @@ class Handle:
 
     def model_predict(self, X):
         X = np.ascontiguousarray(X, dtype=np.float32)
-        Y = np.zeros((X.shape[0], 3), dtype=np.float32)
+        Y = np.zeros((X.shape[0], NPLANS), dtype=np.float32)
         self.bind_stream()
         check(lib().gbmm_model_predict(self.h, X.ctypes.data, X.shape[0], Y.ctypes.data))
         return Y
@@ -460,7 +470,7 @@ def model_features(m, k, n, la, lb):
 
 
 def limbs_needed(a_nlimbs, b_nlimbs, inner, path=PATH_LIMB, method=METHOD_WINOGRAD, cutoff=0):
-    o = Opts(path, method, cutoff, 0, 0)
+    o = Opts(path, method, cutoff, 0, 0, 0)
     out = ctypes.c_int32(0)
     check(lib().gbmm_matmul_limbs_needed(a_nlimbs, b_nlimbs, inner, ctypes.byref(o), ctypes.byref(out)))
     return out.value

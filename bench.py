@@ -50,10 +50,12 @@ WORKLOADS = {
                  label="64 uneven products: m,n,k log-uniform [16,512], bits log-uniform [64,16384], 10% zeros"),
     # learned dispatch: jobs drawn as configuration 4 plus rectangular 1024x64x1024
     # products at bit lengths log-uniform in [256, 8192]; the model trains on the
-    # autotuner's timings of one such stream and dispatches another
+    # autotuner's timings of four such batches and dispatches a held-out batch and
+    # a stream of 10^4 jobs
     "cfg5": dict(K=0, M=0, N=0, bits=0, zero=0.1, short=0.0, short_bits=0, cutoff=32, jobs=64, rect=8,
-                 label="learned dispatch: 64 jobs as cfg4 + 8 rectangular 1024x64x1024 at [256,8192] bits; "
-                       "model trained on the autotuner's timings of a separately drawn stream"),
+                 label="learned dispatch: batches of 64 jobs as cfg4 + 8 rectangular 1024x64x1024 at "
+                       "[256,8192] bits; model trained on the autotuner's timings of 4 separately drawn "
+                       "batches; evaluated on a held-out batch and a 10^4-job stream"),
     # the limb form's batched mpn / mpz kernels one by one, on batches larger than L2
     "limbkernels": dict(K=0, M=0, N=0, bits=0, zero=0.0, short=0.0, short_bits=0, cutoff=32,
                         label="limb-form kernels: batched mpn_add_n/sub_n/mul_1/addmul_1/submul_1, "
@@ -551,61 +553,67 @@ def winograd_leaf_macs(N, levels, la, lb):
 
 def measure_limb_path(gbmm, h, dA, dB, dC_crt, K, M, N, nl, args, flush, stream):
     """The plain limb form on the same inputs (the >= 10x comparison of the CRT form is
-    against this): Winograd's breadth-first tree to the cutoff, or the per-entry kernel
-    alone for --limb-method naive.  Its result must equal the CRT result bit for bit.
-    Returns the record for the bench line."""
+    against it): the per-entry kernel alone and Winograd's breadth-first tree down to
+    --limb-cutoff, each timed over --limb-steps steps; the faster is the comparison
+    basis.  Each result must equal the CRT result bit for bit.  Returns the record
+    for the bench line."""
     import torch
-    method = gbmm.METHOD_WINOGRAD if args.limb_method == "winograd" else gbmm.METHOD_NAIVE
-    cutoff = args.limb_cutoff
-    cn = max(gbmm.limbs_needed(nl, nl, M, path=gbmm.PATH_LIMB, method=method, cutoff=cutoff), dC_crt.nlimbs)
-    dL = gbmm.DeviceMatrix(K, N, cn)
-
-    def step():
-        h.matmul(dL, dA, dB, path=gbmm.PATH_LIMB, method=method, cutoff=cutoff)
-
-    step()
-    torch.cuda.synchronize()
-    same = bool(torch.equal(dL.sizes_t, dC_crt.sizes_t)) and bool(
-        torch.equal(dL.limbs_t[:dC_crt.nlimbs * K * N], dC_crt.limbs_t[:dC_crt.nlimbs * K * N])) and not bool(
-        dL.limbs_t[dC_crt.nlimbs * K * N:].any())
-    if not same:
-        raise SystemExit("bench: the limb path and the CRT path differ")
-    times = []
-    l0 = gbmm.kernel_launches()
-    for i in range(args.limb_steps):
-        flush.fill_(i)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        step()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        times.append(e0.elapsed_time(e1))
-    launches = (gbmm.kernel_launches() - l0) // max(1, args.limb_steps)
-    gbmm.profile(True)
-    flush.fill_(7)
-    step()
-    torch.cuda.synchronize()
-    prof = gbmm.profile_read()
-    gbmm.profile(False)
-    levels = 0
-    if method == gbmm.METHOD_WINOGRAD and K == M == N and K > cutoff:
-        # the recursion depth the library uses: floor(log2(N / cutoff)), lowered until 2^levels divides N
-        levels = (K // cutoff).bit_length() - 1
-        while levels > 0 and K % (1 << levels):
-            levels -= 1
-    lk = "k_wino_leaves" if "k_wino_leaves" in prof else "k_limb_matmul"
-    lms = prof.get(lk, (1, 0.0))[1]
-    macs = winograd_leaf_macs(K, levels, nl, nl) if lk == "k_wino_leaves" else K * M * N * nl * nl
     peak = mac_peak(gbmm, stream)
-    ach = macs / (lms * 1e-3)
-    return {"ms_per_step": statistics.median(times), "steps": args.limb_steps, "method": args.limb_method,
+    forms = {}
+    for form, method, cutoff in (("naive", gbmm.METHOD_NAIVE, 0), ("winograd", gbmm.METHOD_WINOGRAD, args.limb_cutoff)):
+        cn = max(gbmm.limbs_needed(nl, nl, M, path=gbmm.PATH_LIMB, method=method, cutoff=cutoff), dC_crt.nlimbs)
+        dL = gbmm.DeviceMatrix(K, N, cn)
+
+        def step():
+            h.matmul(dL, dA, dB, path=gbmm.PATH_LIMB, method=method, cutoff=cutoff)
+
+        step()
+        torch.cuda.synchronize()
+        same = bool(torch.equal(dL.sizes_t, dC_crt.sizes_t)) and bool(
+            torch.equal(dL.limbs_t[:dC_crt.nlimbs * K * N], dC_crt.limbs_t[:dC_crt.nlimbs * K * N])) and not bool(
+            dL.limbs_t[dC_crt.nlimbs * K * N:].any())
+        if not same:
+            raise SystemExit(f"bench: the limb path ({form}) and the CRT path differ")
+        times = []
+        l0 = gbmm.kernel_launches()
+        for i in range(args.limb_steps):
+            flush.fill_(i)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        launches = (gbmm.kernel_launches() - l0) // max(1, args.limb_steps)
+        gbmm.profile(True)
+        flush.fill_(7)
+        step()
+        torch.cuda.synchronize()
+        prof = gbmm.profile_read()
+        gbmm.profile(False)
+        del dL
+        levels = 0
+        if method == gbmm.METHOD_WINOGRAD and K == M == N and K > cutoff:
+            # the recursion depth the library uses: floor(log2(N / cutoff)), lowered until 2^levels divides N
+            levels = (K // cutoff).bit_length() - 1
+            while levels > 0 and K % (1 << levels):
+                levels -= 1
+        lk = "k_wino_leaves" if "k_wino_leaves" in prof else "k_limb_matmul"
+        lms = prof.get(lk, (1, 0.0))[1]
+        macs = winograd_leaf_macs(K, levels, nl, nl) if lk == "k_wino_leaves" else K * M * N * nl * nl
+        ach = macs / (lms * 1e-3)
+        forms[form] = {
+            "ms_per_step": statistics.median(times), "steps": args.limb_steps,
             "cutoff": cutoff if method == gbmm.METHOD_WINOGRAD else None, "levels": levels,
             "launches_per_step": int(launches), "equals_crt_result": same,
             "kernels": {k: {"launches": v[0], "ms_total": round(v[1], 3)} for k, v in sorted(prof.items())},
             "roofline": {"kernel": lk, "bound": "int-mul", "achieved": ach, "peak": peak, "unit": "MAC/s",
                          "frac": ach / peak,
-                         "note": "32x32-bit limb MACs of the leaf products / leaf kernel time; peak: measured "
-                                 "rate of the same 96-bit column MAC step on register operands (k_mac_peak)"}}
+                         "note": "32x32-bit limb MACs of the kernel's products / its time; peak: measured rate "
+                                 "of the same 96-bit column MAC step on register operands (k_mac_peak)"}}
+    best = min(forms, key=lambda f: forms[f]["ms_per_step"])
+    return {"ms_per_step": forms[best]["ms_per_step"], "form": best, "forms": forms,
+            "roofline": forms[best]["roofline"]}
 
 
 def gen_jobs(gbmm, W, seed):
@@ -658,74 +666,174 @@ def time_batched(h, jobs, args, flush, stream):
     return sum(a.elapsed_time(b) for a, b in ev) / args.steps
 
 
+def stream_shapes(rng, njobs, W):
+    """Shapes of configuration 5's job stream: (m, k, n, bits_a, bits_b) drawn as
+    configuration 4 (dims log-uniform in [16, 512], bits in [64, 16384]), with one
+    job in nine a rectangular 1024 x 64 x 1024 product at bits log-uniform in [256, 8192]."""
+    lu = lambda lo, hi: int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
+    out = []
+    for _ in range(njobs):
+        if rng.random() < 1.0 / 9.0:
+            out.append((1024, 64, 1024, lu(256, 8192), lu(256, 8192)))
+        else:
+            out.append((lu(16, 512), lu(16, 512), lu(16, 512), lu(64, 16384), lu(64, 16384)))
+    return out
+
+
+def device_random_matrix(gbmm, torch, rows, cols, bits, zero, gen):
+    """rows x cols signed entries of exactly `bits` bits (top bit set), a fraction
+    `zero` of exact zeros, random signs; generated on the device."""
+    L = (bits + 31) // 32
+    n = rows * cols
+    m = gbmm.DeviceMatrix(rows, cols, L)
+    lv = m.limbs_t.view(L, n)
+    lv.copy_(torch.randint(-2 ** 31, 2 ** 31, (L, n), dtype=torch.int64, device="cuda", generator=gen).to(torch.int32))
+    top = bits - 32 * (L - 1)
+    mask = (1 << top) - 1 if top < 32 else 0xFFFFFFFF
+    hi = 1 << (top - 1)
+    t = lv[L - 1].to(torch.int64) & mask | hi
+    lv[L - 1] = torch.where(t >= 2 ** 31, t - 2 ** 32, t).to(torch.int32)
+    z = torch.rand(n, device="cuda", generator=gen) < zero
+    lv[:, z] = 0
+    sign = torch.where(torch.rand(n, device="cuda", generator=gen) < 0.5, -1, 1).to(torch.int32)
+    m.sizes_t.copy_(torch.where(z, 0, sign * L).to(torch.int32))
+    return m
+
+
+def tune_times(gbmm, h, mats, NP):
+    """The autotuner's timing of every admissible plan of every job:
+    {(m, k, n, la, lb): [ms per plan, NaN where not timed]} and the raw rows."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        log = os.path.join(td, "tune.jsonl")
+        h.autotune(h.jobs([(c, a, b) for c, a, b, _ in mats]), repeats=1, log_path=log)
+        rows = [json.loads(l) for l in open(log)]
+    times = {}
+    for r in rows:
+        times.setdefault((r["m"], r["k"], r["n"], r["la"], r["lb"]), [np.nan] * NP)[r["plan"]] = r["ms"]
+    return times, rows
+
+
 def run_learned(args, W, world, rank, local):
     """Configuration 5: the learned cost model against the plain heuristic.  The
-    autotuner times the candidate plans of one seeded stream; the MLP trains on
-    those timings with its own CUDA kernels; a second, separately drawn stream
-    then runs with the heuristic, with the autotuner's table, and with the model."""
-    import tempfile
+    autotuner times every candidate plan (limb kernel, Winograd at three cutoffs,
+    CRT with three tile forms and with a limb-half split) on four seeded streams;
+    the MLP trains on those timings with its own CUDA kernels.  Then, on inputs
+    drawn separately: (1) a 72-job batch whose every plan is timed too (the summed
+    time of each policy's picks), run as one batched call replayed from its CUDA
+    graph with the heuristic, the autotuner's table and the model; (2) a stream of
+    --stream-jobs jobs (10^4 by default) in batches of 50 with the heuristic and the
+    model, the two policies' products compared bit for bit on the device."""
     import torch
     import gbmm
     torch.cuda.set_device(local)
     stream = torch.cuda.current_stream()
-    train, _ = gen_jobs(gbmm, W, args.seed + 1)
+    NP = gbmm.NPLANS
     ht = gbmm.Handle()
-    tjobs = ht.jobs([(c, a, b) for c, a, b, _ in train])
+    times, rows = {}, []
     t0 = time.perf_counter()
-    with tempfile.TemporaryDirectory() as td:
-        log = os.path.join(td, "tune.jsonl")
-        ht.autotune(tjobs, repeats=1, log_path=log)
-        rows = [json.loads(l) for l in open(log)]
+    for t in range(4):
+        train, _ = gen_jobs(gbmm, W, args.seed + 1 + 1000 * t)
+        tt, rr = tune_times(gbmm, ht, train, NP)
+        times.update(tt)
+        rows += rr
+        del train
+        torch.cuda.empty_cache()
     tune_s = time.perf_counter() - t0
-    head = lambda r: 2 if r["path"] == gbmm.PATH_CRT else (0 if r["method"] == gbmm.METHOD_NAIVE else 1)
-    times = {}
-    for r in rows:
-        times.setdefault((r["m"], r["k"], r["n"], r["la"], r["lb"]), [np.nan] * 3)[head(r)] = r["ms"]
     keys = sorted(times)
     X = np.stack([gbmm.model_features(m, k, n, la, lb) for (m, k, n, la, lb) in keys])
     T = np.log2(np.array([times[k] for k in keys], dtype=np.float64)).astype(np.float32)
     hl = gbmm.Handle()
     hl.model_init(seed=5)
     t0 = time.perf_counter()
-    loss = hl.model_train(X, T, epochs=1500, lr=3e-3)
+    loss = hl.model_train(X, T, epochs=2000, lr=3e-3)
     train_s = time.perf_counter() - t0
     hl.model_use(True)
-    del train, tjobs
-    torch.cuda.empty_cache()
 
+    # (1) held-out batch: every plan timed, then graph replay of each policy
     evals, macs = gen_jobs(gbmm, W, args.seed)
+    he = gbmm.Handle()
+    etimes, _ = tune_times(gbmm, he, evals, NP)
+    he.close()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device="cuda")
     hh = gbmm.Handle()
-    res = {}
-    clocks, launches = None, 0
+    res, picked_ms = {}, {}
+    launches = 0
+    sampler = ClockSampler(local)
+    sampler.start()
+    key = lambda c, a, b: (c.rows, a.cols, c.cols, a.nlimbs, b.nlimbs)
     for name, h in (("heuristic", hh), ("autotuned", ht), ("learned", hl)):
         jobs = h.jobs([(c, a, b) for c, a, b, _ in evals])
-        chosen = h.matmul_batched(jobs)
+        chosen = h.matmul_batched(jobs, plans=True)
         torch.cuda.synchronize()
         check_jobs(evals, name)
+        picked_ms[name] = float(sum(etimes[key(c, a, b)][q] for (c, a, b, _), (_, q) in zip(evals, chosen)))
         if name == "learned":
-            sampler = ClockSampler(local)
-            sampler.start()
             launches0 = gbmm.kernel_launches()
         ms = max_over_ranks(world, time_batched(h, jobs, args, flush, stream))
         if name == "learned":
             launches = gbmm.kernel_launches() - launches0
-            clocks = sampler.stop()
-        res[name] = (ms, {("crt" if p == gbmm.PATH_CRT else "limb"): chosen.count(p) for p in set(chosen)})
+        res[name] = (ms, {str(p): [q for _, q in chosen].count(p) for p in sorted(set(q for _, q in chosen))})
+    picked_ms["best_possible"] = float(sum(np.nanmin(etimes[key(c, a, b)]) for c, a, b, _ in evals))
+    n_eval = len(evals)
+    del evals
+    torch.cuda.empty_cache()
+
+    # (2) the job stream, batches of 50 with inputs made on the device
+    srng = np.random.default_rng(args.seed + 7)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(args.seed)
+    shapes = stream_shapes(srng, args.stream_jobs, W)
+    st_ms = {"heuristic": 0.0, "learned": 0.0}
+    st_macs, compared, plans_used = 0, 0, {}
+    hh.set_graphs(False)
+    hl.set_graphs(False)
+    for c0 in range(0, len(shapes), 50):
+        mats = []
+        for (K, M, N, ba, bb) in shapes[c0:c0 + 50]:
+            dA = device_random_matrix(gbmm, torch, K, M, ba, W["zero"], gen)
+            dB = device_random_matrix(gbmm, torch, M, N, bb, W["zero"], gen)
+            outs = {p: gbmm.DeviceMatrix(K, N, dA.nlimbs + dB.nlimbs + 2) for p in st_ms}
+            mats.append((dA, dB, outs))
+            st_macs += K * M * N * ((ba + 63) // 64) * ((bb + 63) // 64)
+        for name, h in (("heuristic", hh), ("learned", hl)):
+            jobs = h.jobs([(o[name], a, b) for a, b, o in mats])
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            chosen = h.matmul_batched(jobs, plans=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            st_ms[name] += e0.elapsed_time(e1)
+            if name == "learned":
+                for _, q in chosen:
+                    plans_used[str(q)] = plans_used.get(str(q), 0) + 1
+        for a, b, o in mats[::10]:
+            if not (torch.equal(o["heuristic"].sizes_t, o["learned"].sizes_t) and
+                    torch.equal(o["heuristic"].limbs_t, o["learned"].limbs_t)):
+                raise SystemExit("bench: learned and heuristic dispatch gave different products")
+            compared += 1
+        del mats
+    clocks = sampler.stop()
     if rank != 0:
         return 0
-    ms = res["learned"][0]
+    ms = st_ms["learned"]
     line = {
-        "metric": "limb-MAC/s", "value": world * macs / (ms * 1e-3), "unit": "limb-MAC/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "metric": "limb-MAC/s", "value": world * st_macs / (ms * 1e-3), "unit": "limb-MAC/s", "n_gpus": world,
+        "steps": 1, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16+u32", "data": "synthetic",
-        "config": {"workload": W["label"], "seed": args.seed, "limb_macs_per_step": macs,
-                   "ms_per_stream": {k: v[0] for k, v in res.items()},
-                   "paths": {k: v[1] for k, v in res.items()},
-                   "learned_vs_heuristic": res["heuristic"][0] / ms,
-                   "training": {"timings": len(rows), "shapes": len(keys), "autotune_s": tune_s,
-                                "train_s": train_s, "final_loss": loss},
-                   "l2": "flushed between timed steps (512 MiB write)"},
+        "config": workload_config(W, args.seed),
+        "run": {"step": f"one pass over a stream of {len(shapes)} jobs in batches of 50 (learned dispatch)",
+                "stream": {"jobs": len(shapes), "limb_macs": st_macs, "ms": st_ms,
+                           "learned_vs_heuristic": st_ms["heuristic"] / ms, "plans_used": plans_used,
+                           "differential_checks": compared},
+                "held_out_batch": {"jobs": n_eval, "ms_per_call": {k: v[0] for k, v in res.items()},
+                                   "summed_ms_of_picked_plans": picked_ms,
+                                   "plans": {k: v[1] for k, v in res.items()},
+                                   "learned_vs_heuristic": res["heuristic"][0] / res["learned"][0],
+                                   "limb_macs": macs, "graph": "replayed"},
+                "training": {"timings": len(rows), "shapes": len(keys), "autotune_s": tune_s,
+                             "train_s": train_s, "final_loss": loss}},
         "gpu_launches": int(launches), "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
@@ -897,9 +1005,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-limb", action="store_true", help="skip the plain limb form's figure")
-    ap.add_argument("--limb-method", default="winograd", choices=["winograd", "naive"])
     ap.add_argument("--limb-cutoff", type=int, default=64)
     ap.add_argument("--limb-steps", type=int, default=2)
+    ap.add_argument("--stream-jobs", type=int, default=10000, help="configuration 5: jobs in the evaluated stream")
     ap.add_argument("--size", type=int, default=0,
                     help="override K=M=N of a single-product workload (small cases for profiling)")
     ap.add_argument("--bits", type=int, default=0, help="override the entry bit length")

@@ -73,13 +73,31 @@ typedef enum gbmm_method {
     GBMM_METHOD_NAIVE_REC = 4   /* 8-product block recursion */
 } gbmm_method;
 
+/* Candidate plans for one product: the plans gbmm_autotune times and the
+ * learned cost model predicts (one head each), and the unit GBMM_PATH_AUTO
+ * chooses among.  No counterpart in the reference (its method is fixed per run
+ * by -m, mat-gpu/main.cu:358-502). */
+typedef enum gbmm_plan {
+    GBMM_PLAN_LIMB_NAIVE = 0,  /* per-entry kernel over the whole product, no recursion */
+    GBMM_PLAN_LIMB_W32 = 1,    /* Winograd tree down to blocks of 32 (recursion depth from the size) */
+    GBMM_PLAN_LIMB_W64 = 2,    /* ... down to blocks of 64 */
+    GBMM_PLAN_LIMB_W128 = 3,   /* ... down to blocks of 128 */
+    GBMM_PLAN_CRT = 4,         /* CRT, moduli from the bound, GEMM tile form chosen by size */
+    GBMM_PLAN_CRT_SINGLE = 5,  /* CRT with one-CTA tiles of 128 entries in every GEMM */
+    GBMM_PLAN_CRT_PAIR = 6,    /* CRT with CTA-pair tiles of 256 entries in the product and reconstruction */
+    GBMM_PLAN_CRT_SPLIT = 7,   /* CRT after one limb-half split of the longer operand: two products, each
+                                  with fewer moduli (the modulus count per product is the choice) */
+    GBMM_NPLANS = 8
+} gbmm_plan;
+
 typedef struct gbmm_opts {
     int32_t path;        /* gbmm_path */
     int32_t method;      /* gbmm_method (limb path) */
     int32_t cutoff;      /* recursion stops at blocks <= cutoff (0 = library default) */
     int32_t nprimes;     /* CRT: number of moduli (0 = derived from the bit bound) */
     int32_t accumulate;  /* nonzero: C += A*B (mat_addmul) instead of C = A*B */
-    int32_t reserved[3];
+    int32_t plan;        /* 0: path / method / cutoff as above; 1 + gbmm_plan: run that plan */
+    int32_t reserved[2];
 } gbmm_opts;
 
 typedef struct gbmm_handle_s *gbmm_handle;
@@ -192,12 +210,15 @@ typedef struct gbmm_job {
     int32_t cutoff;
     int32_t nprimes;
     int32_t chosen_path; /* out: path the dispatcher used */
+    int32_t chosen_plan; /* out: gbmm_plan the dispatcher ran (-1: the options were given field by field) */
 } gbmm_job;
 
-/* Runs many independent products of uneven shape and bit length: limb-path
- * jobs go through one persistent kernel over a device work queue, CRT jobs
- * through the residue GEMMs; the launch sequence is captured into a CUDA graph
- * and replayed on later calls with the same job signature.
+/* Runs many independent products of uneven shape and bit length: jobs planned
+ * for the limb kernel without recursion go through one persistent kernel over
+ * a device work queue, the others (CRT products, Winograd trees) run side by
+ * side on four streams forked from the handle's stream; the launch sequence is
+ * captured into a CUDA graph and replayed on later calls with the same job
+ * signature.
  * replaces: the unused chunked-stream job DAG (mat-gpu/job.cu:32-338). */
 gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_t njobs, const gbmm_opts *opts);
 /* One product on host buffers: dense limb planes (limb i of entry e at
@@ -240,11 +261,13 @@ gbmm_status gbmm_set_device_budget(gbmm_handle h, uint64_t bytes);
 gbmm_status gbmm_set_graphs(gbmm_handle h, int32_t enable);
 
 /* ---- autotuner / dispatch tables -------------------------------------------
- * gbmm_autotune times candidate plans (limb naive, limb Winograd, CRT) on each
- * job's own buffers (C is overwritten), keeps the fastest per shape class for
- * GBMM_PATH_AUTO, and appends one JSON line per timing to log_path (may be
- * NULL): the timing record the learned cost model trains on.  Limb candidates
- * predicted far slower than any plan needs (m k n la lb > 2e11) are skipped.
+ * gbmm_autotune times every candidate plan (gbmm_plan: the limb kernel alone,
+ * Winograd at three cutoffs, CRT with three tile forms and with a limb-half
+ * split) on each job's own buffers (C is overwritten), keeps the fastest per
+ * shape class for GBMM_PATH_AUTO, and appends one JSON line per timing to
+ * log_path (may be NULL): the timing record the learned cost model trains on.
+ * Limb candidates predicted far slower than any plan needs (m k n la lb > 2e11)
+ * and Winograd cutoffs that give no recursion at this size are skipped.
  * replaces: the fixed BASE_SIZE / TRANSFER_SIZE / GPU_BLK_* tuning constants
  * (mat-gpu/mat-params.h:4-14). */
 gbmm_status gbmm_autotune(gbmm_handle h, const gbmm_job *jobs, int32_t njobs, int32_t repeats,
@@ -253,13 +276,15 @@ gbmm_status gbmm_tune_save(gbmm_handle h, const char *path);
 gbmm_status gbmm_tune_load(gbmm_handle h, const char *path);
 
 /* ---- learned cost model ------------------------------------------------------
- * An 8 -> 64 -> 64 -> 3 MLP (BF16 weights, FP32 accumulation, ReLU) whose three
- * heads predict log2(ms) of the limb path without recursion, the limb path with
- * Winograd recursion (cutoff 64) and the CRT path for one product.  When
- * enabled with gbmm_model_use, GBMM_PATH_AUTO takes the cheapest head; the
+ * An 8 -> 64 -> 64 -> GBMM_NPLANS MLP (BF16 weights, FP32 accumulation, ReLU)
+ * whose heads predict log2(ms) of each gbmm_plan for one product: the path,
+ * the recursion depth (through the Winograd cutoff), the CRT tile form and the
+ * modulus count per product (through the split).  When enabled with
+ * gbmm_model_use, GBMM_PATH_AUTO runs the plan with the cheapest head; the
  * plain heuristic (and the autotuner's table) stay the fallback.  Training
  * runs on the GPU (forward, backward, Adam kernels) on feature rows from
- * gbmm_model_features and targets from the autotuner's timing log.
+ * gbmm_model_features and targets from the autotuner's timing log (one column
+ * per plan, NaN where a plan was not timed).
  * No counterpart in the reference. */
 int32_t gbmm_model_nparams(void);
 gbmm_status gbmm_model_features(int32_t m, int32_t k, int32_t n, int32_t la, int32_t lb, float *out8);
@@ -267,13 +292,16 @@ gbmm_status gbmm_model_init(gbmm_handle h, uint64_t seed);
 gbmm_status gbmm_model_set_params(gbmm_handle h, const float *params);
 gbmm_status gbmm_model_get_params(gbmm_handle h, float *master, uint16_t *bf16_params);
 gbmm_status gbmm_model_use(gbmm_handle h, int32_t enable);
-/* X: nsamp x 8 features, Y: nsamp x 3 predictions (host arrays). */
+/* X: nsamp x 8 features, Y: nsamp x GBMM_NPLANS predictions (host arrays). */
 gbmm_status gbmm_model_predict(gbmm_handle h, const float *X, int32_t nsamp, float *Y);
 /* Mean-squared-error loss and its gradient (gbmm_model_nparams floats) on
  * (X, T); T entries may be NaN for missing heads. */
 gbmm_status gbmm_model_gradient(gbmm_handle h, const float *X, const float *T, int32_t nsamp, float *grad,
                                 float *loss);
-/* Full-batch Adam for `epochs` steps with learning rate lr. */
+/* Full-batch Adam for `epochs` steps with learning rate lr.  The dispatcher
+ * consults a head only once it has trained on at least 8 measured targets, and
+ * runs the model's plan instead of the heuristic's only when the model predicts
+ * it at least 10% faster. */
 gbmm_status gbmm_model_train(gbmm_handle h, const float *X, const float *T, int32_t nsamp, int32_t epochs,
                              float lr, float *final_loss);
 

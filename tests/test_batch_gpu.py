@@ -109,6 +109,7 @@ def test_autotune_table_roundtrip(g, tmp_path):
         if key not in best or r["ms"] < best[key][0]:
             best[key] = (r["ms"], r["path"])
     assert chosen == [best[(64, 64)][1], best[(8, 2)][1]]
+    assert {r["plan"] for r in rows} >= {g.PLAN_LIMB_NAIVE, g.PLAN_CRT, g.PLAN_CRT_SINGLE, g.PLAN_CRT_PAIR}
     for K, M, N, A, B, dA, dB, dC in jobs:
         assert dC.to_ints() == _exact(K, M, N, A, B)
     h.close()

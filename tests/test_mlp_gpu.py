@@ -9,7 +9,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-NF, NH, NO = 8, 64, 3
+NF, NH, NO = 8, 64, 8   # features, hidden width, heads (one per gbmm_plan)
 
 
 def _unpack(w):
@@ -67,7 +67,9 @@ def h(built_lib):
 def _data(n, seed):
     rng = np.random.default_rng(seed)
     X = rng.uniform(0, 1.2, size=(n, NF)).astype(np.float32)
-    T = np.stack([np.sin(3 * X[:, 0]) + X[:, 5], X[:, 1] * X[:, 3] - 0.5, np.cos(2 * X[:, 4]) * X[:, 2]], 1)
+    T = np.stack([np.sin(3 * X[:, 0]) + X[:, 5], X[:, 1] * X[:, 3] - 0.5, np.cos(2 * X[:, 4]) * X[:, 2],
+                  X[:, 6] - X[:, 7], np.sin(X[:, 1] + X[:, 2]), X[:, 0] * X[:, 4], 0.3 * X[:, 3] + 0.1,
+                  np.cos(X[:, 5] * X[:, 6])], 1)
     T = T.astype(np.float32)
     T[rng.random(T.shape) < 0.1] = np.nan
     return X, T
@@ -99,53 +101,78 @@ def test_training_reduces_loss(h):
     assert l1 < 0.2 * l0 and abs(l1 - lf) < 0.05 * l0
 
 
-def test_learned_dispatch_gains_over_heuristic(built_lib, tmp_path):
-    """Times the three candidate plans of a stream of uneven products with the
-    autotuner, trains the model on those timings, and compares the measured
-    cost of the plans each dispatcher picks."""
-    import gbmm
-    rng = random.Random(17)
-    specs = []
-    for _ in range(40):
-        dims = [int(round(np.exp(rng.uniform(np.log(8), np.log(160))))) for _ in range(3)]
-        bits = [int(round(np.exp(rng.uniform(np.log(64), np.log(4096))))) for _ in range(2)]
-        specs.append((*dims, *bits))
+def _stream(gbmm, seed, n):
+    """n products of uneven shape (dims log-uniform in [8, 384]) and bit length
+    (log-uniform in [64, 4096] per matrix), uploaded: [(A, B, C, host planes)]."""
+    rng = np.random.default_rng(seed)
+    lu = lambda lo, hi: int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
+    import bench
     mats = []
-    for K, M, N, ba, bb in specs:
-        la, lb = (ba + 31) // 32, (bb + 31) // 32
-        A = [rng.getrandbits(ba) * rng.choice((-1, 1)) for _ in range(K * M)]
-        B = [rng.getrandbits(bb) * rng.choice((-1, 1)) for _ in range(M * N)]
-        dA = gbmm.DeviceMatrix.from_ints(K, M, A, la)
-        dB = gbmm.DeviceMatrix.from_ints(M, N, B, lb)
-        need = gbmm.limbs_needed(la, lb, M, path=gbmm.PATH_LIMB, cutoff=64)
-        mats.append((dA, dB, gbmm.DeviceMatrix(K, N, need)))
-    hh = gbmm.Handle()
-    jobs = hh.jobs([(c, a, b) for a, b, c in mats])
-    log = str(tmp_path / "t.jsonl")
-    hh.autotune(jobs, repeats=2, log_path=log)
-    rows = [json.loads(l) for l in open(log)]
-    head = lambda r: 2 if r["path"] == gbmm.PATH_CRT else (0 if r["method"] == gbmm.METHOD_NAIVE else 1)
+    for _ in range(n):
+        K, M, N, ba, bb = lu(8, 384), lu(8, 384), lu(8, 384), lu(64, 4096), lu(64, 4096)
+        Al, As = bench.gen_planes(rng, K * M, ba, 0.05, 0.0, 0)
+        Bl, Bs = bench.gen_planes(rng, M * N, bb, 0.05, 0.0, 0)
+        dA, dB = gbmm.DeviceMatrix(K, M, Al.shape[0]), gbmm.DeviceMatrix(M, N, Bl.shape[0])
+        dA.upload(Al, As)
+        dB.upload(Bl, Bs)
+        dC = gbmm.DeviceMatrix(K, N, Al.shape[0] + Bl.shape[0] + 2)
+        mats.append((dA, dB, dC, (Al, As, Bl, Bs)))
+    return mats
+
+
+def _tune(gbmm, h, mats, log):
+    """Times every admissible plan of every product (autotuner); returns
+    {(m, k, n, la, lb): [ms per plan, NaN where not timed]}."""
+    h.autotune(h.jobs([(c, a, b) for a, b, c, _ in mats]), repeats=2, log_path=log)
     times = {}
-    for r in rows:
-        times.setdefault((r["m"], r["k"], r["n"], r["la"], r["lb"]), [np.nan] * 3)[head(r)] = r["ms"]
-    keys = sorted(times)
-    X = np.stack([gbmm.model_features(m, k, n, la, lb) for (m, k, n, la, lb) in keys])
-    T = np.log2(np.array([times[k] for k in keys], dtype=np.float64)).astype(np.float32)
-    hh.model_init(seed=5)
-    hh.model_train(X, T, epochs=1500, lr=3e-3)
-    pred = hh.model_predict(X)
-    tm = np.array([times[k] for k in keys])
-    choose_model = np.nanargmin(np.where(np.isnan(T), np.inf, pred), axis=1)
-    # the heuristic's choice, as the dispatcher makes it without a model or table
-    h0 = gbmm.Handle()
-    chosen = h0.matmul_batched(h0.jobs([(c, a, b) for a, b, c in mats]))
-    by_key = {(a.rows, a.cols, b.cols, a.nlimbs, b.nlimbs): p for (a, b, c), p in zip(mats, chosen)}
-    choose_heur = np.array([2 if by_key[k] == gbmm.PATH_CRT else 1 for k in keys])
-    cost = lambda ch: float(np.nansum([tm[i, ch[i]] if not np.isnan(tm[i, ch[i]]) else np.nanmax(tm[i])
-                                       for i in range(len(keys))]))
-    best = float(np.nansum(np.nanmin(tm, axis=1)))
-    t_model, t_heur = cost(choose_model), cost(choose_heur)
-    print(f"measured ms: heuristic {t_heur:.3f}, learned {t_model:.3f}, best {best:.3f}")
-    assert t_model <= t_heur * 1.02
-    hh.close()
-    h0.close()
+    for r in (json.loads(l) for l in open(log)):
+        times.setdefault((r["m"], r["k"], r["n"], r["la"], r["lb"]), [np.nan] * NO)[r["plan"]] = r["ms"]
+    return times
+
+
+def test_learned_dispatch_gains_over_heuristic_out_of_sample(built_lib, tmp_path):
+    """The model trains on the autotuner's timings of every plan on one seeded
+    stream of 96 uneven products.  On a separately drawn stream of 64 every
+    admissible plan of every product is timed too; the summed measured time of
+    the plans the learned dispatcher picks must be below the summed time of the
+    plain heuristic's picks.  Both dispatchers' batched calls stay exact."""
+    import gbmm
+    import bench
+    train = _stream(gbmm, 17, 96)
+    ht = gbmm.Handle()
+    tt = _tune(gbmm, ht, train, str(tmp_path / "train.jsonl"))
+    keys = sorted(tt)
+    X = np.stack([gbmm.model_features(*k) for k in keys])
+    T = np.log2(np.array([tt[k] for k in keys], dtype=np.float64)).astype(np.float32)
+    hl = gbmm.Handle()
+    hl.model_init(seed=5)
+    hl.model_train(X, T, epochs=2000, lr=3e-3)
+    hl.model_use(True)
+    del train
+    evals = _stream(gbmm, 99, 64)
+    he = gbmm.Handle()
+    et = _tune(gbmm, he, evals, str(tmp_path / "eval.jsonl"))
+    hh = gbmm.Handle()
+    pick_h = hh.matmul_batched(hh.jobs([(c, a, b) for a, b, c, _ in evals]), plans=True)
+    pick_l = hl.matmul_batched(hl.jobs([(c, a, b) for a, b, c, _ in evals]), plans=True)
+    cost_h = cost_l = best = 0.0
+    changed = 0
+    for (dA, dB, dC, _), (_, qh), (_, ql) in zip(evals, pick_h, pick_l):
+        t = et[(dA.rows, dA.cols, dB.cols, dA.nlimbs, dB.nlimbs)]
+        assert not np.isnan(t[qh]) and not np.isnan(t[ql])
+        cost_h += t[qh]
+        cost_l += t[ql]
+        best += np.nanmin(t)
+        changed += qh != ql
+    srng = np.random.default_rng(1)
+    for dA, dB, dC, (Al, As, Bl, Bs) in evals:
+        Cl, Cs = dC.download()
+        y, x = int(srng.integers(dA.rows)), int(srng.integers(dB.cols))
+        exp = sum(bench.entry_int(Al, As, y * dA.cols + k) * bench.entry_int(Bl, Bs, k * dB.cols + x)
+                  for k in range(dA.cols))
+        assert bench.entry_int(Cl, Cs, y * dB.cols + x) == exp
+    print(f"held-out stream, summed measured ms of the picked plans: heuristic {cost_h:.3f}, "
+          f"learned {cost_l:.3f}, best possible {best:.3f}; {changed} of {len(evals)} picks differ")
+    assert cost_l < cost_h
+    for x in (ht, hl, he, hh):
+        x.close()
