@@ -76,6 +76,8 @@ gbmm_status launch_split_sizes(const gbmm_mat &x, int h, int32_t *lo, int32_t *h
 gbmm_status launch_add_shifted(const gbmm_mat &w, const gbmm_mat &u, const gbmm_mat &v, int sh, cudaStream_t s);
 // whether the per-entry product kernel handles la x lb limb entries
 bool limb_kernel_fits(int la, int lb);
+// whether the batched basecase product stages un x vn limb operands on chip
+bool mpn_basecase_on_chip(int un, int vn);
 
 // Breadth-first Winograd recursion: the whole tree of one square product laid out
 // in workspace arrays (see limb.cu).  Level d = 1..levels holds 4 * 7^(d-1) A-side

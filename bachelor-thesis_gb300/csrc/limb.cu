@@ -443,6 +443,265 @@ __global__ void k_mpn_toom22(uint32_t *pp, const uint32_t *ap, int an, const uin
     dev_add_into(p + (int64_t)n * ld, ld, an + bn - n, mid, ld, 2 * n + 1 < an + bn - n ? 2 * n + 1 : an + bn - n);
 }
 
+// ---- on-chip forms of the batched products --------------------------------------------
+// A CTA of NT threads takes NT operands of the batch (one product per thread).
+// Their limbs are staged in shared memory once: 128-bit global loads read limb i
+// of four neighbouring operands (limb planes are contiguous along the batch),
+// a 4 x 4 register transpose turns four such loads into four limbs of each of
+// four operands, and 128-bit shared stores put every operand's limbs
+// contiguous, zero-padded to a multiple of 4.  Per-thread strings sit SS words
+// apart with SS = 4 (mod 8), so the eight threads of a 128-bit access phase hit
+// distinct banks.  Each product is then computed from shared memory in 4 x 4
+// limb blocks: two 128-bit loads feed 16 MACs.
+
+// per-thread stride (words) of a string of n limbs: a multiple of 4, = 4 (mod 8)
+__host__ __device__ __forceinline__ int sm_stride(int n) {
+    const int n4 = (n + 3) & ~3;
+    return (n4 & 7) == 4 ? n4 : n4 + 4;
+}
+
+// Stages limbs [0, n) of operands b0 .. b0 + NT - 1 (limb i of operand b at
+// g[i * ld + b]) into dst[t * SS + i], zero-filling limbs n .. roundup4(n) and
+// operands past nb.  vec: g and ld allow 16-byte loads (g 16-byte aligned, ld % 4 == 0).
+template <int NT>
+__device__ __forceinline__ void sm_stage(uint32_t *dst, int SS, const uint32_t *g, int n, int64_t ld, int64_t b0,
+                                         int64_t nb, bool vec) {
+    const int n4 = (n + 3) >> 2;
+    constexpr int NQ = NT / 4;  // groups of four operands
+    for (int item = threadIdx.x; item < n4 * NQ; item += NT) {
+        const int q = item % NQ, c = item / NQ;  // consecutive threads: neighbouring operand groups
+        const int64_t bq = b0 + 4 * q;
+        uint32_t L[4][4];  // L[k][j]: limb 4c + k of operand bq + j
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int i = 4 * c + k;
+            const uint32_t *row = g + (int64_t)i * ld + bq;
+            if (i < n && vec && bq + 3 < nb) {
+                const uint4 w = *reinterpret_cast<const uint4 *>(row);
+                L[k][0] = w.x; L[k][1] = w.y; L[k][2] = w.z; L[k][3] = w.w;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) L[k][j] = (i < n && bq + j < nb) ? row[j] : 0u;
+            }
+        }
+#pragma unroll
+        for (int jj = 0; jj < 4; jj++) {
+            const int j = (jj + q) & 3;  // rotated: fewer bank conflicts among the stores
+            *reinterpret_cast<uint4 *>(dst + (4 * q + j) * SS + 4 * c) = make_uint4(L[0][j], L[1][j], L[2][j], L[3][j]);
+        }
+    }
+}
+
+// The same staging with a map from destination limb d (the first of a chunk of
+// four) to its source: planes g, first source limb i, limbs below lim valid, vec
+// as above.  Destination limbs d .. d + 3 come from source limbs i .. i + 3.
+template <int NT, class Map>
+__device__ __forceinline__ void sm_stage_map(uint32_t *dst, int SS, int nchunks, int64_t b0, int64_t nb, int64_t ld,
+                                             Map map) {
+    constexpr int NQ = NT / 4;
+    for (int item = threadIdx.x; item < nchunks * NQ; item += NT) {
+        const int q = item % NQ, c = item / NQ;
+        const int64_t bq = b0 + 4 * q;
+        const uint32_t *g;
+        int i0, lim;
+        bool vec;
+        map(4 * c, g, i0, lim, vec);
+        uint32_t L[4][4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int i = i0 + k;
+            const uint32_t *row = g + (int64_t)i * ld + bq;
+            if (i < lim && vec && bq + 3 < nb) {
+                const uint4 w = *reinterpret_cast<const uint4 *>(row);
+                L[k][0] = w.x; L[k][1] = w.y; L[k][2] = w.z; L[k][3] = w.w;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) L[k][j] = (i < lim && bq + j < nb) ? row[j] : 0u;
+            }
+        }
+#pragma unroll
+        for (int jj = 0; jj < 4; jj++) {
+            const int j = (jj + q) & 3;
+            *reinterpret_cast<uint4 *>(dst + (4 * q + j) * SS + 4 * c) = make_uint4(L[0][j], L[1][j], L[2][j], L[3][j]);
+        }
+    }
+}
+
+// r = u * v for strings of nu4 and nv4 chunks of four limbs (16-byte aligned,
+// zero-padded), by block product scanning: column block T gathers the 4 x 4
+// blocks (I, T - I); their 7 columns are summed in 96-bit accumulators, the
+// block's four columns absorb the carry from below and go out in ascending
+// order (out(t, limb) for t < 4 (nu4 + nv4)), the upper three seed the next block.
+template <class Out>
+__device__ __forceinline__ void sm_mul4(const uint32_t *u, int nu4, const uint32_t *v, int nv4, Out out) {
+    uint32_t acc[7][3];
+#pragma unroll
+    for (int c = 0; c < 7; c++) acc[c][0] = acc[c][1] = acc[c][2] = 0;
+    uint32_t k0 = 0, k1 = 0;  // carry into the next column (64 bits)
+    const int nT = nu4 + nv4;
+    for (int T = 0; T < nT; T++) {
+        const int i0 = T - nv4 + 1 > 0 ? T - nv4 + 1 : 0, i1 = T < nu4 - 1 ? T : nu4 - 1;
+        for (int I = i0; I <= i1; I++) {
+            const uint4 a = *reinterpret_cast<const uint4 *>(u + 4 * I);
+            const uint4 b = *reinterpret_cast<const uint4 *>(v + 4 * (T - I));
+            const uint32_t x[4] = {a.x, a.y, a.z, a.w}, y[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) MAC96(acc[i + j][0], acc[i + j][1], acc[i + j][2], x[i], y[j]);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            asm("add.cc.u32 %0, %0, %3;\n\taddc.cc.u32 %1, %1, %4;\n\taddc.u32 %2, %2, 0;"
+                : "+r"(acc[c][0]), "+r"(acc[c][1]), "+r"(acc[c][2])
+                : "r"(k0), "r"(k1));
+            out(4 * T + c, acc[c][0]);
+            k0 = acc[c][1];
+            k1 = acc[c][2];
+        }
+#pragma unroll
+        for (int c = 0; c < 7; c++) {
+#pragma unroll
+            for (int w = 0; w < 3; w++) acc[c][w] = c < 3 ? acc[c + 4][w] : 0u;
+        }
+    }
+}
+
+// Batched basecase product on chip: rp = up * vp (un >= vn), NT operands per CTA.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_mpn_mul_basecase_sm(uint32_t *rp, const uint32_t *up, int un,
+                                                            const uint32_t *vp, int vn, int64_t ld, int64_t nb,
+                                                            int vec_u, int vec_v) {
+    extern __shared__ uint4 sm_raw4[];
+    uint32_t *sm = reinterpret_cast<uint32_t *>(sm_raw4);
+    const int Su = sm_stride(un), Sv = sm_stride(vn);
+    uint32_t *su = sm, *sv = sm + NT * Su;
+    const int64_t b0 = (int64_t)blockIdx.x * NT;
+    sm_stage<NT>(su, Su, up, un, ld, b0, nb, vec_u);
+    sm_stage<NT>(sv, Sv, vp, vn, ld, b0, nb, vec_v);
+    __syncthreads();
+    const int64_t b = b0 + threadIdx.x;
+    if (b >= nb) return;
+    uint32_t *r = rp + b;
+    const int rn = un + vn;
+    sm_mul4(su + threadIdx.x * Su, (un + 3) >> 2, sv + threadIdx.x * Sv, (vn + 3) >> 2, [&](int t, uint32_t x) {
+        if (t < rn) r[(int64_t)t * ld] = x;
+    });
+}
+
+// Shared-memory words per thread of the on-chip Toom-2.2 for an x bn limbs: the
+// halves a1 | a0 | b0 | b1, each zero-padded to n4 = roundup4(ceil(an / 2)).
+__host__ __device__ __forceinline__ int toom22_sm_words(int an, int bn) {
+    (void)bn;
+    const int n = an - (an >> 1);
+    return sm_stride(4 * ((n + 3) & ~3));
+}
+
+// One Karatsuba split (Knuth 4.3.3, as k_mpn_toom22) on chip.  Each thread's
+// shared string holds the operand halves X = [a1 | a0 | b0 | b1] (n4 limbs
+// each, staged straight from the limb planes).  v0 = a0 b0 and vinf = a1 b1 go
+// to the product planes; then |a0 - a1| overwrites a1, |b0 - b1| overwrites b1,
+// and vm1 = |a0 - a1| |b0 - b1| fills the dead a0 | b0 middle, which then turns
+// into the middle term v0 + vinf -/+ vm1 (= a0 b1 + a1 b0) and is added into
+// the product at limb n.  The product planes are read back once for that: the
+// lines were just written by the same CTAs, so the reads hit L2 and HBM sees
+// the operands once and the product once.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_mpn_toom22_sm(uint32_t *pp, const uint32_t *ap, int an, const uint32_t *bp,
+                                                      int bn, int64_t ld, int64_t nb, int vec_a, int vec_b) {
+    extern __shared__ uint4 sm_raw4[];
+    uint32_t *sm = reinterpret_cast<uint32_t *>(sm_raw4);
+    const int s = an >> 1, n = an - s, t = bn - n;
+    const int n4 = (n + 3) & ~3, c4 = n4 >> 2;
+    const int SS = sm_stride(4 * n4);
+    const int64_t b0 = (int64_t)blockIdx.x * NT;
+    // destination chunk c of the four halves -> its source plane (operand, first limb, valid limbs)
+    sm_stage_map<NT>(sm, SS, 4 * c4, b0, nb, ld, [&](int d, const uint32_t *&g, int &i, int &lim, bool &vec) {
+        const int r = d / n4, off = d - r * n4;
+        g = r < 2 ? ap : bp;
+        vec = r < 2 ? vec_a : vec_b;
+        i = (r == 1 || r == 2) ? off : n + off;
+        lim = r == 0 ? n + s : r == 1 ? n : r == 2 ? n : n + t;
+    });
+    __syncthreads();
+    const int64_t bi = b0 + threadIdx.x;
+    if (bi >= nb) return;
+    uint32_t *X = sm + threadIdx.x * SS;
+    uint32_t *A1 = X, *A0 = X + n4, *B0 = X + 2 * n4, *B1 = X + 3 * n4;
+    uint32_t *p = pp + bi;
+    // v0 -> p[0, 2n), vinf -> p[2n, 2n + s + t)
+    sm_mul4(A0, c4, B0, c4, [&](int i, uint32_t x) {
+        if (i < 2 * n) p[(int64_t)i * ld] = x;
+    });
+    sm_mul4(A1, c4, B1, c4, [&](int i, uint32_t x) {
+        if (i < s + t) p[(int64_t)(2 * n + i) * ld] = x;
+    });
+    // |a0 - a1| over a1, |b0 - b1| over b1; neg = the sign of (a0 - a1)(b0 - b1)
+    int ca = 0, cb = 0;
+    for (int i = n - 1; i >= 0 && ca == 0; i--)
+        if (A0[i] != A1[i]) ca = A0[i] < A1[i] ? -1 : 1;
+    for (int i = n - 1; i >= 0 && cb == 0; i--)
+        if (B0[i] != B1[i]) cb = B0[i] < B1[i] ? -1 : 1;
+    {
+        uint32_t bra = 0, brb = 0;
+        for (int i = 0; i < n4; i++) {
+            const uint32_t xa = ca < 0 ? A1[i] : A0[i], ya = ca < 0 ? A0[i] : A1[i];
+            const uint32_t xb = cb < 0 ? B1[i] : B0[i], yb = cb < 0 ? B0[i] : B1[i];
+            const uint64_t da = (uint64_t)xa - ya - bra, db = (uint64_t)xb - yb - brb;
+            A1[i] = (uint32_t)da;
+            B1[i] = (uint32_t)db;
+            bra = (uint32_t)(da >> 63);
+            brb = (uint32_t)(db >> 63);
+        }
+    }
+    const bool neg = (ca < 0) != (cb < 0);
+    // vm1 -> V = X[n4, 3 n4): the a0 | b0 middle, no longer read
+    uint32_t *V = A0;
+    sm_mul4(A1, c4, B1, c4, [&](int i, uint32_t x) { V[i] = x; });
+    // V = v0 + vinf -/+ vm1 over 2n + 1 limbs (V[2n] may lie in the dead |b0 - b1|).
+    // The product planes are read eight limbs at a time, all eight loads issued
+    // before the carry chain uses them (a store in between would order them).
+    {
+        long long c = 0;
+        for (int i0 = 0; i0 < 2 * n + 1; i0 += 8) {
+            uint32_t w0[8], wi[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int i = i0 + k;
+                w0[k] = i < 2 * n ? p[(int64_t)i * ld] : 0u;
+                wi[k] = i < s + t ? p[(int64_t)(2 * n + i) * ld] : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int i = i0 + k;
+                if (i >= 2 * n + 1) break;
+                const long long wm = i < 2 * n ? V[i] : 0;
+                const long long x = (long long)w0[k] + wi[k] + (neg ? wm : -wm) + c;
+                V[i] = (uint32_t)x;
+                c = x >> 32;
+            }
+        }
+    }
+    // p[n, an + bn) += V
+    {
+        uint32_t c = 0;
+        const int pn = an + bn - n;
+        for (int i0 = 0; i0 < pn; i0 += 8) {
+            uint32_t w[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) w[k] = i0 + k < pn ? p[(int64_t)(n + i0 + k) * ld] : 0u;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int i = i0 + k;
+                if (i >= pn) break;
+                const uint64_t x = (uint64_t)w[k] + (i < 2 * n + 1 ? V[i] : 0u) + c;
+                p[(int64_t)(n + i) * ld] = (uint32_t)x;
+                c = (uint32_t)(x >> 32);
+            }
+        }
+    }
+}
+
 // ======================================================================================
 // mpz layer (sign-magnitude with GMP size convention) on matrix views.
 // ======================================================================================
@@ -1334,6 +1593,17 @@ __global__ void __launch_bounds__(256) k_mac_peak(uint32_t *out, int iters, uint
 // ---- host launchers ---------------------------------------------------------------------
 static inline int64_t nentries(const gbmm_mat &m) { return (int64_t)m.rows * m.cols; }
 static inline unsigned grid1(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+// CTA size of the on-chip mpn products for `words` shared-memory words per
+// operand: the largest of 128, 64, 32 whose staging fits, 0 when none does
+constexpr size_t MPN_SM_MAX_BYTES = 200 * 1024;
+static int sm_threads(size_t words) {
+    for (int nt = 128; nt >= 32; nt >>= 1)
+        if ((size_t)nt * words * 4 <= MPN_SM_MAX_BYTES) return nt;
+    return 0;
+}
+bool mpn_basecase_on_chip(int un, int vn) { return sm_threads((size_t)sm_stride(un) + sm_stride(vn)) != 0; }
+// whether limb planes at p with stride ld allow 16-byte loads of four operands
+static int vec16(const void *p, int64_t ld) { return ((uintptr_t)p % 16 == 0 && ld % 4 == 0) ? 1 : 0; }
 
 gbmm_status launch_mat_addsub(const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, int sub, cudaStream_t s) {
     const int64_t n = nentries(c);
@@ -1852,8 +2122,28 @@ extern "C" gbmm_status gbmm_mpn_mul_basecase(uint32_t *rp, const uint32_t *up, i
     if (!vp) return set_error(GBMM_ERR_INVALID, "null pointer");
     if (un < vn || vn < 1) return set_error(GBMM_ERR_INVALID, "mul_basecase needs un >= vn >= 1 (un=%d vn=%d)", un, vn);
     if (nb == 0) return GBMM_OK;
-    LaunchScope ls_("k_mpn_mul_basecase", as_stream(stream));
-    k_mpn_mul_basecase<<<grid1(nb, 128), 128, 0, as_stream(stream)>>>(rp, up, un, vp, vn, ld, nb);
+    const int nt = sm_threads((size_t)sm_stride(un) + sm_stride(vn));
+    if (nt == 0) {
+        // operands too long to stage: the product reads them from global memory
+        LaunchScope ls_("k_mpn_mul_basecase", as_stream(stream));
+        k_mpn_mul_basecase<<<grid1(nb, 128), 128, 0, as_stream(stream)>>>(rp, up, un, vp, vn, ld, nb);
+        GBMM_CUDA_TRY(cudaGetLastError());
+        return GBMM_OK;
+    }
+    const size_t smem = (size_t)nt * (sm_stride(un) + sm_stride(vn)) * 4;
+    const int vu = vec16(up, ld), vv = vec16(vp, ld);
+    LaunchScope ls_("k_mpn_mul_basecase_sm", as_stream(stream));
+#define BASECASE_SM(NT_)                                                                                      \
+    do {                                                                                                      \
+        GBMM_CUDA_TRY(cudaFuncSetAttribute(k_mpn_mul_basecase_sm<NT_>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                           (int)smem));                                                       \
+        k_mpn_mul_basecase_sm<NT_><<<grid1(nb, NT_), NT_, smem, as_stream(stream)>>>(rp, up, un, vp, vn, ld, nb, vu, \
+                                                                                     vv);                      \
+    } while (0)
+    if (nt == 128) BASECASE_SM(128);
+    else if (nt == 64) BASECASE_SM(64);
+    else BASECASE_SM(32);
+#undef BASECASE_SM
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
 }
@@ -1868,6 +2158,33 @@ extern "C" int32_t gbmm_mpn_toom22_mul_itch(int32_t an, int32_t bn) {
     const int64_t itch = toom22_itch64(an);
     return itch > INT32_MAX ? -1 : (int32_t)itch;
 }
+// Toom-2.2 on chip when the per-operand intermediates fit shared memory (the
+// scratch planes are then not touched), else through the scratch planes.
+static gbmm_status launch_toom22(uint32_t *pp, const uint32_t *ap, int an, const uint32_t *bp, int bn,
+                                 uint32_t *scratch, int64_t ld, int64_t nb, cudaStream_t s) {
+    const int nt = sm_threads((size_t)toom22_sm_words(an, bn));
+    if (nt == 0) {
+        LaunchScope ls_("k_mpn_toom22", s);
+        k_mpn_toom22<<<grid1(nb, 128), 128, 0, s>>>(pp, ap, an, bp, bn, scratch, ld, nb);
+        GBMM_CUDA_TRY(cudaGetLastError());
+        return GBMM_OK;
+    }
+    const size_t smem = (size_t)nt * toom22_sm_words(an, bn) * 4;
+    const int va = vec16(ap, ld), vb = vec16(bp, ld);
+    LaunchScope ls_("k_mpn_toom22_sm", s);
+#define TOOM22_SM(NT_)                                                                                          \
+    do {                                                                                                        \
+        GBMM_CUDA_TRY(cudaFuncSetAttribute(k_mpn_toom22_sm<NT_>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                           (int)smem));                                                         \
+        k_mpn_toom22_sm<NT_><<<grid1(nb, NT_), NT_, smem, s>>>(pp, ap, an, bp, bn, ld, nb, va, vb);             \
+    } while (0)
+    if (nt == 128) TOOM22_SM(128);
+    else if (nt == 64) TOOM22_SM(64);
+    else TOOM22_SM(32);
+#undef TOOM22_SM
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
 extern "C" gbmm_status gbmm_mpn_toom22_mul(uint32_t *pp, const uint32_t *ap, int32_t an, const uint32_t *bp, int32_t bn,
                                            uint32_t *scratch, int64_t ld, int64_t nb, void *stream) {
     GBMM_TRY(check_batch(pp, ap, ld, nb, an));
@@ -1877,10 +2194,7 @@ extern "C" gbmm_status gbmm_mpn_toom22_mul(uint32_t *pp, const uint32_t *ap, int
         return set_error(GBMM_ERR_INVALID, "toom22 preconditions violated (an=%d bn=%d)", an, bn);
     if (toom22_itch64(an) > INT32_MAX) return set_error(GBMM_ERR_INVALID, "toom22: an=%d is too long", an);
     if (nb == 0) return GBMM_OK;
-    LaunchScope ls_("k_mpn_toom22", as_stream(stream));
-    k_mpn_toom22<<<grid1(nb, 128), 128, 0, as_stream(stream)>>>(pp, ap, an, bp, bn, scratch, ld, nb);
-    GBMM_CUDA_TRY(cudaGetLastError());
-    return GBMM_OK;
+    return launch_toom22(pp, ap, an, bp, bn, scratch, ld, nb, as_stream(stream));
 }
 
 // ---- Toom-2.2 without any allocation ---------------------------------------------------
@@ -1933,10 +2247,7 @@ extern "C" gbmm_status gbmm_mpn_toom22_mul_noalloc(uint32_t *pp, const uint32_t 
     GBMM_TRY(noalloc_scratch(&scratch));
     // every scratch word the kernel reads it has written first in the same call,
     // so nothing is cleared between calls
-    LaunchScope ls_("k_mpn_toom22", as_stream(stream));
-    k_mpn_toom22<<<grid1(nb, 128), 128, 0, as_stream(stream)>>>(pp, ap, an, bp, bn, scratch, ld, nb);
-    GBMM_CUDA_TRY(cudaGetLastError());
-    return GBMM_OK;
+    return launch_toom22(pp, ap, an, bp, bn, scratch, ld, nb, as_stream(stream));
 }
 
 static gbmm_status check_elementwise(const gbmm_mat &w, const gbmm_mat &u, const gbmm_mat &v) {

@@ -896,19 +896,41 @@ def run_limb_kernels(args, W, world, rank, local):
     rec("mpn_submul_1", "k_mpn_mul1ops", timed(lambda: gbmm.mpn_submul_1(rp, up, n, vl, nb, nb, cy)),
         3 * L4 + 8 * nb, n * nb)
     del rp
-    # products: 2^18 operand pairs of 32 x 32 limbs (basecase) and 64 x 64 limbs (Toom-2.2)
+    # products: 2^18 operand pairs of 32 x 32 limbs (basecase), 64 x 64 limbs (basecase and
+    # Toom-2.2: the Karatsuba split's gain is the ratio of the two times); MAC counts are
+    # schoolbook-equivalent, against the measured rate of the 96-bit column MAC step
+    peak = mac_peak(gbmm, stream)
     pb = 1 << 18
     ua, va = rnd(32, pb), rnd(32, pb)
     ra = torch.zeros(64, pb, dtype=torch.int32, device=dev)
-    rec("mpn_mul_basecase", "k_mpn_mul_basecase", timed(lambda: gbmm.mpn_mul_basecase(ra, ua, 32, va, 32, pb, pb)),
+    rec("mpn_mul_basecase", "k_mpn_mul_basecase_sm", timed(lambda: gbmm.mpn_mul_basecase(ra, ua, 32, va, 32, pb, pb)),
         4 * pb * (32 + 32 + 64), 32 * 32 * pb)
     ub, vb = rnd(64, pb), rnd(64, pb)
     rb = torch.zeros(128, pb, dtype=torch.int32, device=dev)
+    rec("mpn_mul_basecase_64", "k_mpn_mul_basecase_sm",
+        timed(lambda: gbmm.mpn_mul_basecase(rb, ub, 64, vb, 64, pb, pb)), 4 * pb * (64 + 64 + 128), 64 * 64 * pb)
     scratch = torch.zeros(int(gbmm.mpn_toom22_mul_itch(64, 64)), pb, dtype=torch.int32, device=dev)
-    rec("mpn_toom22_mul", "k_mpn_toom22",
+    rec("mpn_toom22_mul", "k_mpn_toom22_sm",
         timed(lambda: gbmm.mpn_toom22_mul(rb, ub, 64, vb, 64, scratch, pb, pb)),
         4 * pb * (64 + 64 + 128), 64 * 64 * pb)
-    del ua, va, ra, ub, vb, rb, scratch, up, vp
+    del ua, va, ra
+    # the Karatsuba split against the basecase at longer operands (2^16 pairs)
+    qb = 1 << 16
+    for L in (128, 192):
+        uq, vq = rnd(L, qb), rnd(L, qb)
+        rq = torch.zeros(2 * L, qb, dtype=torch.int32, device=dev)
+        sq = torch.zeros(int(gbmm.mpn_toom22_mul_itch(L, L)), qb, dtype=torch.int32, device=dev)
+        rec(f"mpn_mul_basecase_{L}", "k_mpn_mul_basecase_sm",
+            timed(lambda: gbmm.mpn_mul_basecase(rq, uq, L, vq, L, qb, qb)), 4 * qb * 4 * L, L * L * qb)
+        rec(f"mpn_toom22_mul_{L}", "k_mpn_toom22_sm",
+            timed(lambda: gbmm.mpn_toom22_mul(rq, uq, L, vq, L, sq, qb, qb)), 4 * qb * 4 * L, L * L * qb)
+        out[f"mpn_toom22_mul_{L}"]["over_basecase"] = out[f"mpn_mul_basecase_{L}"]["ms"] / out[f"mpn_toom22_mul_{L}"]["ms"]
+        del uq, vq, rq, sq
+    for k in out:
+        if k.startswith("mpn_mul_basecase") or k.startswith("mpn_toom22"):
+            out[k]["frac_mac_peak"] = out[k]["MAC/s"] / peak
+    out["mpn_toom22_mul"]["over_basecase"] = out["mpn_mul_basecase_64"]["ms"] / out["mpn_toom22_mul"]["ms"]
+    del ub, vb, rb, scratch, up, vp
     # signed entries of matrices: 1024 x 2048 entries, 32-limb operands (16 for products)
     rng = np.random.default_rng(args.seed)
     R, Cc = 1024, 2048
@@ -933,7 +955,7 @@ def run_limb_kernels(args, W, world, rank, local):
         "metric": "GB/s per limb-form kernel", "value": max(r["GB/s"] for r in out.values()), "unit": "GB/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": W["label"], "hbm_peak_gbs": hbm, "operands": nb, "limbs": n,
+        "config": {"workload": W["label"], "hbm_peak_gbs": hbm, "mac_peak": peak, "operands": nb, "limbs": n,
                    "l2": "every batch is larger than L2"},
         "kernels": out,
     }

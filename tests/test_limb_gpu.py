@@ -183,6 +183,47 @@ def test_mpn_toom22_and_mul(g, oracle, an, bn):
     assert (_host(dp).reshape(an + bn, nb) == exp).all()
 
 
+@pytest.mark.parametrize("kind,an,bn", [("basecase", 33, 7), ("basecase", 130, 129), ("toom22", 41, 40),
+                                          ("toom22", 64, 33), ("toom22", 170, 150)])
+@pytest.mark.parametrize("nb,ld", [(37, 37), (37, 41), (130, 132)])
+def test_mpn_products_on_chip_strides(g, oracle, kind, an, bn, nb, ld):
+    """The shared-memory products with plane strides that rule out 16-byte loads
+    (ld odd: four-operand groups staged limb by limb), a last group of operands
+    cut by nb, planes wider than the batch (columns past nb stay as they were),
+    and operands long enough for 64- and 32-thread CTAs."""
+    import torch
+    rng = np.random.default_rng(an * 31 + bn + nb + ld)
+    a = _rand_planes(rng, an, ld, "ones")
+    b = _rand_planes(rng, bn, ld, "ones")
+    exp = oracle.mpn_mul_basecase(a[:, :nb].copy(), b[:, :nb].copy())
+    dp = torch.full(((an + bn) * ld,), 7, dtype=torch.int32, device="cuda")
+    if kind == "basecase":
+        g.mpn_mul_basecase(dp, _dev(torch, a), an, _dev(torch, b), bn, ld, nb)
+    else:
+        scratch = torch.zeros(g.mpn_toom22_mul_itch(an, bn) * ld, dtype=torch.int32, device="cuda")
+        g.mpn_toom22_mul(dp, _dev(torch, a), an, _dev(torch, b), bn, scratch, ld, nb)
+    torch.cuda.synchronize()
+    got = _host(dp).reshape(an + bn, ld)
+    assert (got[:, :nb] == exp).all()
+    assert (got[:, nb:] == 7).all()
+
+
+@pytest.mark.parametrize("un,vn", [(900, 900), (900, 760), (900, 500)])
+def test_mpn_mul_operands_too_long_to_stage(g, oracle, un, vn):
+    """Operands whose per-thread strings do not fit shared memory: mpn_mul takes
+    Toom-2.2 through caller scratch (balanced) or the global-memory basecase."""
+    import torch
+    rng = np.random.default_rng(un + vn)
+    nb = 48
+    a = _rand_planes(rng, un, nb, "ones")
+    b = _rand_planes(rng, vn, nb, "ones")
+    exp = oracle.mpn_mul_basecase(a, b)
+    dp = torch.zeros((un + vn) * nb, dtype=torch.int32, device="cuda")
+    g.mpn_mul(dp, _dev(torch, a), un, _dev(torch, b), vn, nb, nb)
+    torch.cuda.synchronize()
+    assert (_host(dp).reshape(un + vn, nb) == exp).all()
+
+
 def _signed(rng, n, bits, zero=0.1):
     out = []
     for i in range(n):
