@@ -81,9 +81,10 @@ struct ModConst {
 // Downstream bounds use |red(x)| <= 32772.
 constexpr float RND_MAGIC = 12582912.0f;  // 1.5 * 2^23
 
-// (p, fl(1/p)) of moduli 2i and 2i+1 for the 1024 largest primes below 2^16, in
-// descending order: the moduli of every product are a prefix of this list.  Warps
-// read one modulus at a time (a constant-cache broadcast, no shared-memory traffic).
+// (p, p', fl(1/p), fl(1/p')) of moduli 2i and 2i+1 for the 1024 largest primes
+// below 2^16, in descending order: the moduli of every product are a prefix of
+// this list.  Warps read one pair at a time (a constant-cache broadcast, no
+// shared-memory traffic); each half is a packed operand of the f32x2 arithmetic.
 constexpr int CMOD_PAIRS = 512;
 __constant__ float4 c_modpair[CMOD_PAIRS];
 __device__ __forceinline__ float red(float x, float p, float inv_p) {
@@ -94,6 +95,35 @@ __device__ __forceinline__ float red(float x, float p, float inv_p) {
 __device__ __forceinline__ void bal_split(float r, float &hi, float &lo) {
     hi = __fadd_rn(__fmaf_rn(r, 1.0f / 256.0f, RND_MAGIC), -RND_MAGIC);
     lo = __fmaf_rn(-hi, 256.0f, r);
+}
+
+// ---- the same steps on two values at once (packed f32x2 arithmetic: one FMA-pipe
+// instruction per pair; each lane is rounded exactly as the scalar form) --------
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk2(f32x2 r, float &a, float &b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r)); }
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// red on both lanes: np = (-p, -p'), ip = (1/p, 1/p')
+__device__ __forceinline__ f32x2 red2(f32x2 x, f32x2 np, f32x2 ip) {
+    const f32x2 q = add2(fma2(x, ip, pk2(RND_MAGIC, RND_MAGIC)), pk2(-RND_MAGIC, -RND_MAGIC));
+    return fma2(q, np, x);
+}
+__device__ __forceinline__ void bal_split2(f32x2 r, f32x2 &hi, f32x2 &lo) {
+    hi = add2(fma2(r, pk2(1.0f / 256.0f, 1.0f / 256.0f), pk2(RND_MAGIC, RND_MAGIC)), pk2(-RND_MAGIC, -RND_MAGIC));
+    lo = fma2(hi, pk2(-256.0f, -256.0f), r);
 }
 // bf16 bit patterns of two small integers (|v| <= 256 has at most 9 significant
 // bits, so the low 16 bits of its FP32 encoding are zero and truncation is exact):
@@ -242,7 +272,7 @@ struct ResidueArgs {
     int32_t nk;    // K steps of 64 digits
     int32_t BN, G; // table columns per tile, accumulation groups (G * BN <= 256)
     int32_t P;
-    int32_t ncols;  // 2P table columns
+    int32_t ncols;  // table columns: two per modulus, padded to whole pairs of moduli
     int32_t n_ntiles;
     int32_t ntiles;
     __nv_bfloat16 *R;  // planes [2P][rowsR][kp]
@@ -254,45 +284,70 @@ struct ResidueArgs {
 // shared-memory staging of one epilogue warp's chunk: [32 planes][32 entries] bf16
 constexpr int RES_STG_BYTES = 32 * 32 * 2;
 
-// One chunk of 32 accumulator columns (16 moduli, two table columns each) of
-// group g folded into res: res_j = red(256 red(s1) + red(s0) (+ res_j)).
-// Each term is an integer of magnitude <= 2^24; the sum stays below
-// 257 * 32772 + 32772 < 2^24, so every FP32 step is exact.
-__device__ __forceinline__ void residue_fold(const uint32_t (&v)[32], int mi0, bool first, float (&res)[16]) {
+// One chunk of 32 accumulator columns (16 moduli) of group g folded into res.
+// The table orders each pair of moduli (m, m') as four columns: [lo_m, lo_m',
+// hi_m, hi_m'] (the byte digits of 256^j mod p times 1 and 256), so the lo sums and
+// the hi sums of a pair come as packed operands: res = red(256 red(s1) + red(s0)
+// (+ res)) on both lanes at once.  Each term is an integer of magnitude <= 2^24;
+// the sum stays below 257 * 32772 + 32772 < 2^24, so every FP32 step is exact.
+__device__ __forceinline__ void residue_fold(const uint32_t (&v)[32], int mi0, bool first, f32x2 (&res)[8]) {
 #pragma unroll
-    for (int j = 0; j < 16; j += 2) {
-        const float4 pc = c_modpair[(mi0 + j) >> 1];  // (p, 1/p) of moduli mi0 + j, mi0 + j + 1
-        float t0 = __fmaf_rn(256.f, red(__uint_as_float(v[2 * j + 1]), pc.x, pc.y),
-                             red(__uint_as_float(v[2 * j]), pc.x, pc.y));
-        float t1 = __fmaf_rn(256.f, red(__uint_as_float(v[2 * j + 3]), pc.z, pc.w),
-                             red(__uint_as_float(v[2 * j + 2]), pc.z, pc.w));
-        if (!first) {
-            t0 += res[j];
-            t1 += res[j + 1];
-        }
-        res[j] = red(t0, pc.x, pc.y);
-        res[j + 1] = red(t1, pc.z, pc.w);
+    for (int g = 0; g < 8; g++) {
+        const float4 pc = c_modpair[(mi0 >> 1) + g];  // (p, p', 1/p, 1/p')
+        const f32x2 np = pk2(-pc.x, -pc.y), ip = pk2(pc.z, pc.w);
+        const f32x2 s0 = pk2(__uint_as_float(v[4 * g]), __uint_as_float(v[4 * g + 1]));
+        const f32x2 s1 = pk2(__uint_as_float(v[4 * g + 2]), __uint_as_float(v[4 * g + 3]));
+        f32x2 t = fma2(red2(s1, np, ip), pk2(256.f, 256.f), red2(s0, np, ip));
+        if (!first) t = add2(t, res[g]);
+        res[g] = red2(t, np, ip);
     }
 }
 
 // PAIR: a cluster of two CTAs shares one M = 256 tcgen05.mma.cta_group::2 per K
 // slice (issued by the even CTA); each CTA stages its own 128 entries and half of
 // the tile's table columns, and keeps its own 128 rows of D in its TMEM.
-template <int STAGES, bool PAIR>
+// MC: a cluster of two CTAs with an M = 128 MMA each, on neighbouring 128-entry
+// row blocks and the same table columns: each CTA loads half of the table box and
+// multicasts it to both, so the table is read from L2 once per pair of row blocks,
+// and each CTA's MMA commit frees the stage in both CTAs.
+template <int STAGES, bool PAIR, bool MC = false>
 __global__ void __launch_bounds__(RES_THREADS, 1)
     k_crt_residue(const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmT,
                   const __grid_constant__ CUtensorMap tmR, ResidueArgs a, uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
-    constexpr int NP = PAIR ? 2 : 1;
+    constexpr bool CL = PAIR || MC;     // launched as clusters of two CTAs
+    constexpr int NP = CL ? 2 : 1;      // row blocks per tile (per cluster)
     constexpr int NBUF = PAIR ? 2 : 1;  // staging buffers per epilogue warp
-    const uint32_t A_BYTES = BM * 128, B_BYTES = (uint32_t)(a.BN / NP) * 128, STAGE = A_BYTES + B_BYTES;
+    const uint32_t A_BYTES = BM * 128, B_BYTES = (uint32_t)(PAIR ? a.BN / 2 : a.BN) * 128, STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
     uint8_t *stage_out = reinterpret_cast<uint8_t *>(bars) + SMEM_BARS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t rank = PAIR ? tc::cluster_rank() : 0;
-    const int64_t t0 = PAIR ? (blockIdx.x >> 1) : blockIdx.x, tstep = PAIR ? (gridDim.x >> 1) : gridDim.x;
-    if (PAIR) {
+    const uint32_t rank = CL ? tc::cluster_rank() : 0;
+    const int64_t t0 = CL ? (blockIdx.x >> 1) : blockIdx.x, tstep = CL ? (gridDim.x >> 1) : gridDim.x;
+    if (MC) {
+        // per CTA as below, but every stage is freed by both CTAs' MMA commits
+        if (threadIdx.x == 0) {
+            for (int s = 0; s < STAGES; s++) {
+                tc::mbar_init(&bars->full[s], 1);
+                tc::mbar_init(&bars->empty[s], 2);
+            }
+            for (int b = 0; b < 2; b++) {
+                tc::mbar_init(&bars->tfull[b], 1);
+                tc::mbar_init(&bars->tempty[b], RES_EPI_WARPS);
+            }
+            bars->abort_flag = 0;
+            tc::fence_mbar_init();
+        }
+        if (warp == 1) {
+            tc::tmem_alloc(&bars->tmem_base, 512);
+            tc::tmem_relinquish();
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::cluster_sync_all();  // both CTAs' barriers exist before any multicast lands
+        tc::fence_after_sync();
+    } else if (PAIR) {
         if (threadIdx.x == 0) {
             for (int s = 0; s < STAGES; s++) {
                 tc::mbar_init(&bars->full[s], 1);
@@ -319,7 +374,7 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
     const uint32_t tmem = bars->tmem_base;
     // the last table tile may be narrow: its MMA has only the columns it needs
     // (a multiple of 16, of 32 for a pair so that each CTA stages whole 8-row groups)
-    const int ngran = PAIR ? 32 : 16;
+    const int ngran = CL ? 32 : 16;
 
     if (warp == 0) {
         if (lane == 0) {
@@ -344,6 +399,12 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
                         if (rank == 0) tc::mbar_arrive_expect_tx(&bars->full[st], 2 * STAGE);
                         tc::tma_load_2d_pair(sa, &tmD, full0, s * BK, (int)e0);
                         tc::tma_load_2d_pair(sa + A_BYTES, &tmT, full0, s * BK, n0 + (int)rank * (nn / 2));
+                    } else if (MC) {
+                        // own digit rows; this CTA's half of the table box to both CTAs
+                        tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
+                        tc::tma_load_2d(sa, &tmD, &bars->full[st], s * BK, (int)e0);
+                        tc::tma_load_2d_mc(sa + A_BYTES + rank * (B_BYTES / 2), &tmT, &bars->full[st], s * BK,
+                                           n0 + (int)rank * (a.BN / 2), 0x3);
                     } else {
                         tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
                         tc::tma_load_2d(sa, &tmD, &bars->full[st], s * BK, (int)e0);
@@ -353,14 +414,14 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
             }
         }
     } else if (warp == 1) {
-        if (lane == 0 && rank == 0) {
+        if (lane == 0 && (rank == 0 || MC)) {
             int it = 0, lt = 0;
             bool ok = true;
             for (int t = (int)t0; t < a.ntiles && ok; t += (int)tstep, lt++) {
                 const int b = lt & 1;
                 const int n0 = (t % a.n_ntiles) * a.BN;
                 const int nn = min(a.BN, (a.ncols - n0 + ngran - 1) / ngran * ngran);
-                const uint32_t idesc = tc::idesc_bf16_f32(NP * BM, nn, 0, 0);
+                const uint32_t idesc = tc::idesc_bf16_f32(PAIR ? 2 * BM : BM, nn, 0, 0);
                 if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
                 tc::fence_after_sync();
                 for (int s = 0; s < a.nk; s++, it++) {
@@ -378,6 +439,7 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
                         else tc::mma_bf16(d, adesc, bdesc, idesc, acc);
                     }
                     if (PAIR) tc::mma_commit_pair(&bars->empty[st], 0x3);
+                    else if (MC) tc::mma_commit_mc(&bars->empty[st], 0x3);
                     else tc::mma_commit(&bars->empty[st]);
                 }
                 if (ok) {
@@ -428,8 +490,22 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
                 release();
                 continue;
             }
-            float res[16];
+            f32x2 res[8];  // moduli (mi0 + 2g, mi0 + 2g + 1) of the current chunk
             auto store = [&](int mi0) {
+                // bf16 bits of the two balanced byte digits of each residue
+                uint16_t hb[16], lbits[16];
+#pragma unroll
+                for (int g = 0; g < 8; g++) {
+                    f32x2 h2, l2;
+                    bal_split2(res[g], h2, l2);
+                    float h0, h1, l0, l1;
+                    upk2(h2, h0, h1);
+                    upk2(l2, l0, l1);
+                    hb[2 * g] = (uint16_t)(__float_as_uint(h0) >> 16);
+                    hb[2 * g + 1] = (uint16_t)(__float_as_uint(h1) >> 16);
+                    lbits[2 * g] = (uint16_t)(__float_as_uint(l0) >> 16);
+                    lbits[2 * g + 1] = (uint16_t)(__float_as_uint(l1) >> 16);
+                }
                 if (a.tma_out) {
                     if (ew >= E) return;  // the whole box lies past the last entry
                     if (lane == 0) tc::bulk_wait_read<NBUF - 1>();
@@ -437,10 +513,8 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
                     uint16_t *buf = stg + sbuf * (RES_STG_BYTES / 2);
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
-                        float hi, lo;
-                        bal_split(res[j], hi, lo);
-                        buf[(2 * j) * 32 + lane] = (uint16_t)(__float_as_uint(hi) >> 16);
-                        buf[(2 * j + 1) * 32 + lane] = (uint16_t)(__float_as_uint(lo) >> 16);
+                        buf[(2 * j) * 32 + lane] = hb[j];
+                        buf[(2 * j + 1) * 32 + lane] = lbits[j];
                     }
                     tc::fence_proxy_async_smem();
                     __syncwarp();
@@ -452,24 +526,12 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
                     if (NBUF > 1) sbuf ^= 1;
                 } else if (e < E) {
                     uint16_t *dst = reinterpret_cast<uint16_t *>(a.R + (int64_t)mi0 * pstep + off);
-                    if (mi0 + 16 <= a.P) {
+                    const int nj = a.P - mi0;
 #pragma unroll
-                        for (int j = 0; j < 16; j++) {
-                            float hi, lo;
-                            bal_split(res[j], hi, lo);
-                            dst[j * pstep] = (uint16_t)(__float_as_uint(hi) >> 16);
-                            dst[j * pstep + a.plane] = (uint16_t)(__float_as_uint(lo) >> 16);
-                        }
-                    } else {
-                        const int nj = a.P - mi0;
-#pragma unroll
-                        for (int j = 0; j < 16; j++) {
-                            if (j >= nj) break;
-                            float hi, lo;
-                            bal_split(res[j], hi, lo);
-                            dst[j * pstep] = (uint16_t)(__float_as_uint(hi) >> 16);
-                            dst[j * pstep + a.plane] = (uint16_t)(__float_as_uint(lo) >> 16);
-                        }
+                    for (int j = 0; j < 16; j++) {
+                        if (j >= nj) break;
+                        dst[j * pstep] = hb[j];
+                        dst[j * pstep + a.plane] = lbits[j];
                     }
                 }
             };
@@ -509,6 +571,14 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
         if (warp == 1) {
             tc::fence_after_sync();
             tc::tmem_dealloc_pair(tmem, 512);
+        }
+    } else if (MC) {
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::cluster_sync_all();  // no CTA leaves while its peer may still multicast into it or arrive on it
+        if (warp == 1) {
+            tc::fence_after_sync();
+            tc::tmem_dealloc(tmem, 512);
         }
     } else {
         cta_teardown(bars, 512);
@@ -1614,9 +1684,11 @@ static gbmm_status build_tables(crt_tables *t, int P) {
     {
         // the constant (p, 1/p) list: the same for every table, written with each
         std::vector<float> cm(4 * CMOD_PAIRS);
-        for (int i = 0; i < 2 * CMOD_PAIRS; i++) {
-            cm[2 * i] = (float)pr[i];
-            cm[2 * i + 1] = 1.0f / (float)pr[i];
+        for (int q = 0; q < CMOD_PAIRS; q++) {
+            cm[4 * q] = (float)pr[2 * q];
+            cm[4 * q + 1] = (float)pr[2 * q + 1];
+            cm[4 * q + 2] = 1.0f / (float)pr[2 * q];
+            cm[4 * q + 3] = 1.0f / (float)pr[2 * q + 1];
         }
         GBMM_CUDA_TRY(cudaMemcpyToSymbol(c_modpair, cm.data(), cm.size() * sizeof(float)));
     }
@@ -1632,22 +1704,27 @@ static gbmm_status build_tables(crt_tables *t, int P) {
 // Residue table [2P rows][dxp]: rows 2i / 2i+1 hold the low / high balanced
 // byte of 256^j mod p_i (weighted = 0) or of w_i 256^j mod p_i (weighted = 1, the
 // CRT weight w_i = (Mod/p_i)^-1 mod p_i folded into the B operand).
+// GEMM columns of the residue table for P moduli: two per modulus, padded to whole pairs
+static int residue_cols(int P) { return (2 * P + 3) / 4 * 4; }
 static gbmm_status residue_table(crt_tables *t, int dxp, int weighted, __nv_bfloat16 **out) {
     const int key = 2 * dxp + weighted;
     auto it = t->residue.find(key);
     if (it != t->residue.end()) { *out = it->second; return GBMM_OK; }
     const auto &pr = primes_desc();
-    const int rows = 2 * t->P;
-    std::vector<uint16_t> tab((size_t)rows * dxp);
+    // rows (table columns of the GEMM) in groups of four per pair of moduli (i, i + 1):
+    // [lo_i, lo_i+1, hi_i, hi_i+1]; with P odd the last group's second slot stays zero
+    const int rows = residue_cols(t->P);
+    std::vector<uint16_t> tab((size_t)rows * dxp, 0);
     for (int i = 0; i < t->P; i++) {
         const uint32_t p = pr[i];
+        const size_t r_lo = (size_t)4 * (i >> 1) + (i & 1), r_hi = r_lo + 2;
         uint32_t v = weighted ? t->h_mods[i].w : 1u;  // (w) 256^j mod p
         for (int j = 0; j < dxp; j++) {
             int32_t b = v > p / 2 ? (int32_t)v - (int32_t)p : (int32_t)v;
             int32_t d0 = ((b + 128) & 255) - 128;
             int32_t d1 = (b - d0) / 256;
-            tab[(size_t)(2 * i) * dxp + j] = bf16_bits((float)d0);      // x1
-            tab[(size_t)(2 * i + 1) * dxp + j] = bf16_bits((float)d1);  // x256
+            tab[r_lo * dxp + j] = bf16_bits((float)d0);  // x1
+            tab[r_hi * dxp + j] = bf16_bits((float)d1);  // x256
             v = (uint32_t)(((uint64_t)v * 256) % p);
         }
     }
@@ -1677,9 +1754,10 @@ static constexpr int RES_STAGES_PAIR = 5;  // a pair CTA stages 32 KB per K step
 static constexpr int PROD_STAGES_PAIR = 5;  // a pair CTA stages 40 KB per K step
 static constexpr int PROD_PAIR_MIN_NK = 8;  // K steps (of 64) from which the product runs on CTA pairs
 // residue GEMM form: -1 by the K loop's length, 0 single CTAs, 1 CTA pairs
-static int g_residue_mode = -1;
+static int g_residue_mode = -1;  // -1 by size, 0 one CTA, 1 CTA pairs, 2 multicast clusters
 static constexpr int RES_PAIR_MIN_NK = 1 << 30;  // the pair form of the residue GEMM measured slower at every size
 static bool residue_pair(int nk) { return g_residue_mode < 0 ? nk >= RES_PAIR_MIN_NK : g_residue_mode == 1; }
+static bool residue_mc(int nk) { (void)nk; return g_residue_mode == 2; }
 
 static int num_sms() {
     static int n = 0;
@@ -1752,27 +1830,32 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     int BN = 256;
     while (BN * G > 256) BN /= 2;
     if (BN < 64) return set_error(GBMM_ERR_UNSUPPORTED, "crt: entries longer than 16384 bits");
-    const bool pair = residue_pair(nk);
-    const int NP = pair ? 2 : 1;
+    const bool pair = residue_pair(nk), mc = !pair && residue_mc(nk);
+    const int NP = pair || mc ? 2 : 1;
     CUtensorMap tmD, tmT, tmR;
     GBMM_TRY(make_map(&tmD, D, dxp, E, dxp, BK, BM));
-    GBMM_TRY(make_map(&tmT, T, dxp, 2 * t->P, dxp, BK, BN / NP));
+    GBMM_TRY(make_map(&tmT, T, dxp, residue_cols(t->P), dxp, BK, BN / NP));
     ResidueArgs a;
     if (E > (int64_t)INT32_MAX - 4 * BM)
         return set_error(GBMM_ERR_UNSUPPORTED, "crt: more than 2^31 entries in one operand");
     a.kdim = kdim; a.E = (int32_t)E; a.nk = nk;
     a.BN = BN; a.G = G; a.P = t->P; a.R = R; a.plane = (int64_t)rowsR * kp; a.kp = kp;
-    a.ncols = 2 * t->P;
-    a.n_ntiles = (2 * t->P + BN - 1) / BN;
+    a.ncols = residue_cols(t->P);
+    a.n_ntiles = (a.ncols + BN - 1) / BN;
     a.ntiles = (int32_t)((int64_t)a.n_ntiles * ((E + NP * BM - 1) / (NP * BM)));
     // 32-entry boxes of one plane row: [32 planes][1 row][32 entries]
     a.tma_out = kdim % 32 == 0;
     if (a.tma_out) GBMM_TRY(make_map_planes(&tmR, R, kdim, rowsR, 2 * t->P, kp, a.plane));
     else tmR = tmD;  // unused
     const int stages = pair ? RES_STAGES_PAIR : RES_STAGES;
-    const size_t sm = smem_bytes(stages, BM * 128 + (size_t)(BN / NP) * 128) + (size_t)RES_EPI_WARPS * (pair ? 2 : 1) * RES_STG_BYTES;
+    const size_t sm = smem_bytes(stages, BM * 128 + (size_t)(pair ? BN / 2 : BN) * 128) +
+                      (size_t)RES_EPI_WARPS * (pair ? 2 : 1) * RES_STG_BYTES;
     LaunchScope ls_("k_crt_residue", s);
-    if (pair) {
+    if (mc) {
+        GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false, true>, sm));
+        GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES, false, true>, RES_THREADS, a.ntiles, sm, s, tmD, tmT, tmR, a,
+                              device_error_word()));
+    } else if (pair) {
         GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES_PAIR, true>, sm));
         GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES_PAIR, true>, RES_THREADS, a.ntiles, sm, s, tmD, tmT, tmR, a,
                               device_error_word()));
@@ -2057,6 +2140,6 @@ extern "C" gbmm_status gbmmx_crt_params(int64_t bits_a, int64_t bits_b, int32_t 
 // 1 CTA pairs); returns the previous setting.
 extern "C" int32_t gbmmx_residue_mode(int32_t mode) {
     const int32_t old = g_residue_mode;
-    g_residue_mode = mode < 0 ? -1 : (mode > 0 ? 1 : 0);
+    g_residue_mode = mode < 0 ? -1 : (mode > 2 ? 2 : mode);
     return old;
 }

@@ -886,12 +886,25 @@ __global__ void k_add_shifted(MatArgs W, MatArgs U, MatArgs V, int sh, int64_t c
     if (vn0 == 0 || un == 0 || (su < 0) == (sv < 0)) {
         neg = un ? su < 0 : sv < 0;
         uint32_t c = 0;
-        for (int t = 0; t < mx; t++) {
-            uint64_t x = (uint64_t)ul(t) + vl(t) + c;
-            if (t >= W.nlimbs) { if ((uint32_t)x) { atomicOr(err, DEVERR_CAPACITY); return; } }
-            else wp[(int64_t)t * W.ld] = (uint32_t)x;
-            c = (uint32_t)(x >> 32);
-            if ((uint32_t)x) len = t + 1;
+        // eight limbs at a time: all sixteen loads go out before the chunk's stores (W may
+        // be U itself; a chunk's limbs are read before they are written)
+        for (int t0 = 0; t0 < mx; t0 += 8) {
+            uint32_t xu[8], xv[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                xu[k] = ul(t0 + k);
+                xv[k] = vl(t0 + k);
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int t = t0 + k;
+                if (t >= mx) break;
+                const uint64_t x = (uint64_t)xu[k] + xv[k] + c;
+                if (t >= W.nlimbs) { if ((uint32_t)x) { atomicOr(err, DEVERR_CAPACITY); return; } }
+                else wp[(int64_t)t * W.ld] = (uint32_t)x;
+                c = (uint32_t)(x >> 32);
+                if ((uint32_t)x) len = t + 1;
+            }
         }
         if (c) {
             if (mx >= W.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
@@ -905,13 +918,24 @@ __global__ void k_add_shifted(MatArgs W, MatArgs U, MatArgs V, int sh, int64_t c
             if (ul(t) != vl(t)) cmp = ul(t) < vl(t) ? -1 : 1;
         neg = cmp >= 0 ? su < 0 : sv < 0;
         uint32_t br = 0;
-        for (int t = 0; t < mx; t++) {
-            const uint32_t x = cmp >= 0 ? ul(t) : vl(t), y = cmp >= 0 ? vl(t) : ul(t);
-            uint64_t d = (uint64_t)x - y - br;
-            br = (uint32_t)(d >> 63);
-            if (t >= W.nlimbs) { if ((uint32_t)d) { atomicOr(err, DEVERR_CAPACITY); return; } }
-            else wp[(int64_t)t * W.ld] = (uint32_t)d;
-            if ((uint32_t)d) len = t + 1;
+        for (int t0 = 0; t0 < mx; t0 += 8) {
+            uint32_t xu[8], xv[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                xu[k] = ul(t0 + k);
+                xv[k] = vl(t0 + k);
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int t = t0 + k;
+                if (t >= mx) break;
+                const uint32_t x = cmp >= 0 ? xu[k] : xv[k], y = cmp >= 0 ? xv[k] : xu[k];
+                const uint64_t d = (uint64_t)x - y - br;
+                br = (uint32_t)(d >> 63);
+                if (t >= W.nlimbs) { if ((uint32_t)d) { atomicOr(err, DEVERR_CAPACITY); return; } }
+                else wp[(int64_t)t * W.ld] = (uint32_t)d;
+                if ((uint32_t)d) len = t + 1;
+            }
         }
     }
     for (int t = mx + 1; t < W.nlimbs; t++) wp[(int64_t)t * W.ld] = 0u;

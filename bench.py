@@ -1027,7 +1027,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-limb", action="store_true", help="skip the plain limb form's figure")
-    ap.add_argument("--limb-cutoff", type=int, default=64)
+    ap.add_argument("--limb-cutoff", type=int, default=32)
     ap.add_argument("--limb-steps", type=int, default=2)
     ap.add_argument("--stream-jobs", type=int, default=10000, help="configuration 5: jobs in the evaluated stream")
     ap.add_argument("--size", type=int, default=0,

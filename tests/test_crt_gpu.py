@@ -118,11 +118,13 @@ def test_crt_matmul_vs_oracle(g, oracle, K, M, N, bits):
     assert (limbs == Cl).all()
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 @pytest.mark.parametrize("K,M,N,bits", [(70, 96, 50, 4096), (33, 37, 20, 4096), (20, 64, 24, 8192),
                                         (5, 64, 7, 16000), (10, 32, 9, 1500), (3, 45, 300, 2048)])
 def test_crt_residue_forms(g, mode, K, M, N, bits):
-    """Both forms of the residue GEMM (single CTAs, CTA pairs), with the epilogue's
+    """The three forms of the residue GEMM (single CTAs, CTA pairs, two-CTA
+    clusters sharing the table by multicast, here with odd row-block counts so a
+    cluster's second block can lie past the last entry), with the epilogue's
     TMA-store output (inner dimension a multiple of 32) and its per-entry store
     output (any other), over one to four accumulation groups."""
     rng = random.Random(K + M * 3 + N * 5 + bits + mode)
