@@ -5,7 +5,7 @@
 // recursion are cut into (job, tile) items, sorted largest first, and run by ONE
 // persistent kernel per group (block edge, CTA form, thin operands) that drains a
 // device work queue.  The other jobs (CRT products, Winograd trees) run through
-// dispatch() on four side streams, side by side.  The whole launch
+// dispatch() on eight side streams, side by side.  The whole launch
 // sequence of a batch is captured into a CUDA graph the second time a batch
 // with the same signature (shapes, pointers, paths) is seen, and replayed from
 // then on.  This replaces the reference's chunked multi-stream job DAG
@@ -42,7 +42,7 @@ struct GraphEntry {
     char *d_blob = nullptr;  // work-queue blob owned by this graph
 };
 
-constexpr int NSIDE = 4;  // side streams a batch's dispatched jobs are spread over
+constexpr int NSIDE = 8;  // side streams a batch's dispatched jobs are spread over
 
 struct BatchState {
     std::map<uint64_t, TuneEntry> tune;

@@ -402,7 +402,8 @@ def run_gpu(args, W, world, rank, local):
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
-    roof = kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof)
+    macpk = mac_peak(gbmm, stream) if kname in ("k_limb_matmul", "k_wino_leaves") else None
+    roof = kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof, macpk)
     limb = None
     if path == gbmm.PATH_CRT and not args.no_limb:
         limb = measure_limb_path(gbmm, h, dA, dB, dC, K, M, N, nl, args, flush, stream)
@@ -474,7 +475,7 @@ NCU_DRAM_BYTES_512_4096 = {
 FIXED_POINT_COLUMNS = 14  # reconstruction columns that carry the 2^96 / p_i weights
 
 
-def kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof):
+def kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof, macpk=None):
     """Algorithmic work of the dominant kernel per launch / its mean CUDA-event time.
     Tensor kernels: useful bf16 FLOPs (2 per digit MAC, no tile padding counted).
     Memory kernels: bytes that must move (inputs read once, outputs written once)."""
@@ -504,6 +505,22 @@ def kernel_roofline(kname, klaunch, kms, W, args, K, M, N, nl, cn, peaks, prof):
         return {"kernel": kname, "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
                 "frac": ach / bf16, "traffic": traffic, "peak_source": src + " (bf16 dense, burst)",
                 "ms_per_launch": per_ms, "note": note}
+    if kname in ("k_limb_matmul", "k_wino_leaves") and macpk:
+        # integer-multiply bound: 32x32-bit limb MACs of the kernel's products
+        levels = 0
+        if kname == "k_wino_leaves":
+            cut = args.cutoff or 32
+            levels = (K // cut).bit_length() - 1 if K == M == N and K > cut else 0
+            while levels > 0 and K % (1 << levels):
+                levels -= 1
+            macs = winograd_leaf_macs(K, levels, nl, nl)
+        else:
+            macs = K * M * N * nl * nl
+        ach = macs / (per_ms * 1e-3)
+        return {"kernel": kname, "bound": "int-mul", "achieved": ach, "peak": macpk, "unit": "MAC/s",
+                "frac": ach / macpk, "traffic": None, "peak_source": "measured (k_mac_peak, 96-bit column MAC step)",
+                "ms_per_launch": per_ms, "levels": levels,
+                "note": "32x32-bit limb MACs of the kernel's products per launch / its CUDA-event time"}
     # memory-bound kernels: algorithmic bytes per launch
     if kname == "k_crt_digits":
         bytes_ = ((K * M + M * N) / 2) * (4 * nl + 2 * ((4 * nl + 63) // 64 * 64))

@@ -216,7 +216,7 @@ typedef struct gbmm_job {
 /* Runs many independent products of uneven shape and bit length: jobs planned
  * for the limb kernel without recursion go through one persistent kernel over
  * a device work queue, the others (CRT products, Winograd trees) run side by
- * side on four streams forked from the handle's stream; the launch sequence is
+ * side on eight streams forked from the handle's stream; the launch sequence is
  * captured into a CUDA graph and replayed on later calls with the same job
  * signature.
  * replaces: the unused chunked-stream job DAG (mat-gpu/job.cu:32-338). */
