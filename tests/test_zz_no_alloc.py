@@ -1,8 +1,10 @@
 """gbmm_mpn_toom22_mul_noalloc: the Toom-2.2 product for callers that cannot
-allocate device memory (scratch is the library's fixed device array).  Checked
-through the C ABI against gbmm_mpn_toom22_mul with caller scratch, on two calls
-in a row (the second call reuses the array the first one left dirty).  This
-file is collected last so a failure here leaves every other test already run."""
+allocate device memory.  Operands that fit shared memory run on chip; longer
+ones (above about 800 limbs) use the library's fixed device array as scratch.
+Checked through the C ABI against gbmm_mpn_toom22_mul with caller scratch, on
+calls in a row (a later call reuses the array an earlier one left dirty), and the
+long cases against the exact product.  This file is collected last so a failure
+here leaves every other test already run."""
 import ctypes
 
 import numpy as np
@@ -26,7 +28,8 @@ def _noalloc_fn(gbmm):
 # (an, bn, nb, ld): two calls in a row with ld == nb, one with planes wider than
 # the batch (ld > nb), and one whose scratch is exactly the array's size
 # (itch 512 limbs x ld 8192 x 4 bytes = 16 MiB), which the size check accepts
-CASES = [(64, 60, 3000, 3000), (41, 40, 5000, 5000), (64, 60, 3000, 3500), (170, 150, 8000, 8192)]
+CASES = [(64, 60, 3000, 3000), (41, 40, 5000, 5000), (64, 60, 3000, 3500), (170, 150, 8000, 8192),
+         (850, 800, 64, 64), (851, 700, 40, 41)]
 
 
 def test_toom22_noalloc_matches_scratch_version(built_lib):
@@ -52,6 +55,12 @@ def test_toom22_noalloc_matches_scratch_version(built_lib):
         assert torch.equal(got, ref), f"call {call} differs from the caller-scratch entry point"
         # columns past the batch (ld > nb) are left as they were
         assert bool((got.view(an + bn, ld)[:, nb:] == 5).all())
+        if an >= 800:  # the device-array form: also against the exact product
+            g = got.cpu().numpy().view(np.uint32).reshape(an + bn, ld)
+            for j in (0, nb // 2, nb - 1):
+                x = sum(int(a[i, j]) << (32 * i) for i in range(an))
+                y = sum(int(b[i, j]) << (32 * i) for i in range(bn))
+                assert sum(int(g[i, j]) << (32 * i) for i in range(an + bn)) == x * y, (call, j)
 
 
 def test_toom22_noalloc_rejects_oversized_batches(built_lib):
