@@ -1086,21 +1086,24 @@ size_t dispatch_ws(const Plan &p, int la, int lb, int m, int k, int n, int cn, i
         return (cn < need ? mat_bytes((int64_t)m * n, need) : 0) + rec + 8192;
     }
     const bool sa = la >= lb;
-    const int hl = (sa ? la : lb) / 2;
+    const int hl = (sa ? la : lb) / 2, hn = (sa ? la : lb) - hl;
     const int64_t xs = sa ? (int64_t)m * k : (int64_t)k * n;
-    const int tn = limbs_needed(sa ? la - hl : la, sa ? lb : lb - hl, k, 0) + 1;
-    size_t own = 2 * (align_up((size_t)xs * 4, 256) + 256) + mat_bytes((int64_t)m * n, tn) + 1024;
+    const int tn = limbs_needed(sa ? hn : la, sa ? lb : hn, k, 0) + 1;
+    // half sizes, the stacked halves (2 xs entries of hn limbs) and the stacked product
+    size_t own = 2 * (align_up((size_t)xs * 4, 256) + 256) + mat_bytes(2 * xs, hn) + mat_bytes(2 * (int64_t)m * n, tn) +
+                 1024;
     Plan q = p;
     q.split = std::max(0, p.split - 1);
-    size_t lo = dispatch_ws(q, sa ? hl : la, sa ? lb : hl, m, k, n, cn, accumulate);
-    size_t hi = dispatch_ws(q, sa ? la - hl : la, sa ? lb : lb - hl, m, k, n, tn, 0);
-    return own + std::max(lo, hi);
+    return own + dispatch_ws(q, sa ? hn : la, sa ? lb : hn, sa ? 2 * m : m, k, sa ? n : 2 * n, tn, 0);
 }
 
-// C (+)= A*B with the planned path; operands too long for the chosen kernels
-// are split into low and high limb halves (A = A_hi 2^(32h) + A_lo, the
-// Karatsuba-style split of Knuth 4.3.3 without the middle-product trick):
-// C (+)= A_lo B, T = A_hi B, C += T 2^(32h).
+// C (+)= A*B with the planned path.  An operand too long for the chosen kernels
+// is split into low and high limb halves, X = X_hi 2^(32h) + X_lo (the
+// Karatsuba-style split of Knuth 4.3.3 without the middle-product trick), and
+// the halves are stacked into one operand: A's as rows [A_lo; A_hi], B's as
+// columns [B_lo | B_hi].  One product T against the other operand (whose CRT
+// residues or staged limbs are then formed once) gives both half products, and
+// C (+)= T_0 + T_1 2^(32h).
 gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, const Plan &p,
                      int accumulate, cudaStream_t s) {
     const int m = a.rows, k = a.cols, n = b.cols;
@@ -1134,27 +1137,34 @@ gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const 
     const bool sa = a.nlimbs >= b.nlimbs;
     const gbmm_mat &X = sa ? a : b;
     if (X.nlimbs < 2) return set_error(GBMM_ERR_UNSUPPORTED, "no kernel takes %d x %d limb entries", a.nlimbs, b.nlimbs);
-    const int hl = X.nlimbs / 2;
+    const int hl = X.nlimbs / 2, hn = X.nlimbs - hl;
     size_t mark = arena_mark(h);
     const size_t xs = (size_t)(X.rows - 1) * X.rs + X.cols;
     int32_t *lo = (int32_t *)arena_alloc(h, xs * 4), *hi = (int32_t *)arena_alloc(h, xs * 4);
-    gbmm_mat T;
-    const int tn = limbs_needed(sa ? a.nlimbs - hl : a.nlimbs, sa ? b.nlimbs : b.nlimbs - hl, k, 0) + 1;
-    if (!lo || !hi || !arena_mat(h, m, n, tn, T)) return set_error(GBMM_ERR_NOMEM, "split workspace");
+    // S: the stacked halves (hn limb planes); T: the stacked product
+    gbmm_mat S, T;
+    const int tn = limbs_needed(sa ? hn : a.nlimbs, sa ? b.nlimbs : hn, k, 0) + 1;
+    if (!lo || !hi || !arena_mat(h, sa ? 2 * m : k, sa ? k : 2 * n, hn, S) ||
+        !arena_mat(h, sa ? 2 * m : m, sa ? n : 2 * n, tn, T))
+        return set_error(GBMM_ERR_NOMEM, "split workspace");
     GBMM_TRY(launch_split_sizes(X, hl, lo, hi, s));
     gbmm_mat Xlo = X, Xhi = X;
     Xlo.nlimbs = hl;
     Xlo.sizes = lo;
-    Xhi.nlimbs = X.nlimbs - hl;
+    Xhi.nlimbs = hn;
     Xhi.limbs = X.limbs + (int64_t)hl * X.ld;
     Xhi.sizes = hi;
+    const int xr = X.rows, xc = X.cols;
+    GBMM_TRY(launch_mat_copy(sa ? sub_view(S, 0, 0, xr, xc) : sub_view(S, 0, 0, xr, xc), Xlo, s));
+    GBMM_TRY(launch_mat_copy(sa ? sub_view(S, xr, 0, xr, xc) : sub_view(S, 0, xc, xr, xc), Xhi, s));
     Plan q = p;
     q.split = std::max(0, p.split - 1);
-    GBMM_TRY(dispatch(h, c, sa ? Xlo : a, sa ? b : Xlo, q, accumulate, s));
-    GBMM_TRY(dispatch(h, T, sa ? Xhi : a, sa ? b : Xhi, q, 0, s));
-    GBMM_TRY(launch_add_shifted(c, c, T, hl, s));
+    gbmm_status st = dispatch(h, T, sa ? S : a, sa ? b : S, q, 0, s);
+    const gbmm_mat T0 = sub_view(T, 0, 0, m, n), T1 = sa ? sub_view(T, m, 0, m, n) : sub_view(T, 0, n, m, n);
+    if (st == GBMM_OK && accumulate) st = launch_add_shifted(c, c, T0, 0, s);
+    if (st == GBMM_OK) st = launch_add_shifted(c, accumulate ? c : T0, T1, hl, s);
     arena_release(h, mark);
-    return GBMM_OK;
+    return st;
 }
 
 gbmm_status resolve_plan(gbmm_handle h, const gbmm_mat &a, const gbmm_mat &b, const gbmm_opts &o, Plan &p) {

@@ -950,7 +950,15 @@ __global__ void k_mat_copy(MatArgs D, MatArgs S, int64_t count, uint32_t *err) {
     const int64_t id = ent(D, e), is = ent(S, e);
     const int ss = S.sizes[is], n = iabs_d(ss);
     if (n > D.nlimbs) { atomicOr(err, DEVERR_CAPACITY); return; }
-    for (int i = 0; i < D.nlimbs; i++) D.limbs[(int64_t)i * D.ld + id] = i < n ? S.limbs[(int64_t)i * S.ld + is] : 0u;
+    // eight planes at a time: the loads go out together, ahead of the stores
+    for (int i0 = 0; i0 < D.nlimbs; i0 += 8) {
+        uint32_t v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = i0 + k < n ? S.limbs[(int64_t)(i0 + k) * S.ld + is] : 0u;
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (i0 + k < D.nlimbs) D.limbs[(int64_t)(i0 + k) * D.ld + id] = v[k];
+    }
     D.sizes[id] = ss;
 }
 

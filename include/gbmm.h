@@ -85,8 +85,8 @@ typedef enum gbmm_plan {
     GBMM_PLAN_CRT = 4,         /* CRT, moduli from the bound, GEMM tile form chosen by size */
     GBMM_PLAN_CRT_SINGLE = 5,  /* CRT with one-CTA tiles of 128 entries in every GEMM */
     GBMM_PLAN_CRT_PAIR = 6,    /* CRT with CTA-pair tiles of 256 entries in the product and reconstruction */
-    GBMM_PLAN_CRT_SPLIT = 7,   /* CRT after one limb-half split of the longer operand: two products, each
-                                  with fewer moduli (the modulus count per product is the choice) */
+    GBMM_PLAN_CRT_SPLIT = 7,   /* CRT after one limb-half split of the longer operand, its halves stacked
+                                  into one product with fewer moduli (the modulus count is the choice) */
     GBMM_NPLANS = 8
 } gbmm_plan;
 
