@@ -6,8 +6,9 @@
 // exactly in bf16 and accumulates in FP32; each accumulation is bounded so that
 // every partial sum is an integer of magnitude < 2^24, hence exact.
 //
-//  1. digits    : limb planes -> rows of unsigned byte digits (bf16), one row
-//                 per entry (A in row-major order, B in column-major order).
+//  1. digits    : limb planes -> rows of byte digits (bf16): unsigned bytes, or for
+//                 rows longer than 512 digits balanced digits in [-128, 128]; one
+//                 row per entry (A in row-major order, B in column-major order).
 //  2. residue   : [entries x digits] x [digits x 2P] GEMM with the table
 //                 256^j mod p_i (balanced, split in two signed bytes); the
 //                 epilogue folds the two halves, reduces mod p_i in FP32,
@@ -48,7 +49,11 @@ namespace {
 constexpr int BM = 128;  // tile rows (TMEM lanes)
 constexpr int BK = 64;   // bf16 elements per K step (one 128-byte swizzle row)
 constexpr int UK = 16;   // K of one kind::f16 MMA
-constexpr int GROUP_STEPS = 8;  // K steps per exact accumulation group (512 digits)
+// residue GEMM: K steps per exact accumulation group: 8 (512 unsigned byte digits,
+// 512 * 255 * 128 < 2^24) or, for rows longer than 512 digits, 15 (960 balanced
+// digits, 959 * 128 * 128 + 256 * 128 < 2^24)
+constexpr int RES_GROUP_STEPS_U = 8, RES_GROUP_STEPS_B = 15;
+constexpr int PROD_MAX_K = 512;      // product GEMM: inner dimension of one exact pass
 constexpr int SROWS = 32;       // columns before the first output digit in the reconstruction table
 constexpr int SUSED = 14;       // of which the fixed-point sum uses the first 14 (98 bits)
 constexpr int FIXB = 96;        // fixed-point bits of the 1/p_i weights
@@ -196,15 +201,37 @@ __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: 
 // ======================================================================================
 // 1. digits
 // ======================================================================================
-// bf16 bits of bytes k and k+1 of w, byte k in the low half.  Each byte b
-// becomes the FP32 value 2^23 + b (bits 0x4B000000 | b, built by one byte
-// permute) minus 2^23, which is exact; b has at most 8 significant bits, so the
-// top half of its FP32 encoding is its bf16 encoding.  Integer and FP32-add
-// work only: no int->float conversion instructions.
+// bf16 bits of bytes k and k+1 of w, byte k in the low half (unsigned digits).
+// Each byte b becomes the FP32 value 2^23 + b (bits 0x4B000000 | b, built by one
+// byte permute) minus 2^23, which is exact; b has at most 8 significant bits, so
+// the top half of its FP32 encoding is its bf16 encoding.
 __device__ __forceinline__ uint32_t byte_pair_bf16(uint32_t w, int k) {
     const float lo = __fadd_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + k)), -8388608.0f);
     const float hi = __fadd_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7541u + k)), -8388608.0f);
     return bf16x2_bits(lo, hi);
+}
+
+// Balanced byte digits of limb w: byte b_i becomes d_i = b_i + c_i - 256 m_i with
+// m_i its top bit and c_i the top bit of the byte below (cin for byte 0), so
+// sum d_i 256^i = sum b_i 256^i with every d_i in [-128, 128].  The carry needs no
+// propagation: c_i depends on the byte below only.  The last digit of a row
+// (last, byte 3) keeps its carry and is not reduced: it lies in [0, 256].
+// Computed as e_i = (b_i ^ 128) + c_i = d_i + 128 in [0, 256]: two byte permutes
+// and an integer add build the FP32 bits of 2^23 + e_i, and one exact FADD of
+// -(2^23 + 128) leaves d_i.  With at most 9 significant bits the top half of the
+// FP32 encoding is the bf16 encoding.  No int->float conversion instructions.
+__device__ __forceinline__ void limb_digits_bal(uint32_t w, uint32_t cin, bool last, float (&d)[4]) {
+    const uint32_t x = w ^ 0x80808080u;                          // b_i ^ 128 per byte
+    const uint32_t c = ((w & 0x80808080u) >> 7 << 8) | cin;      // c_i in bit 0 of byte i
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const uint32_t bits = __byte_perm(x, 0x4B000000u, 0x7650u + i) + __byte_perm(c, 0u, 0x4440u + i);
+        d[i] = __fadd_rn(__uint_as_float(bits), -8388736.0f);  // (2^23 + e_i) - (2^23 + 128)
+    }
+    if (last) {
+        // the row's last digit unreduced: b_3 + c_3 (the reduced form subtracted 256 when m_3 = 1)
+        d[3] = (w >> 31) ? __fadd_rn(d[3], 256.0f) : d[3];
+    }
 }
 
 // The digits carry the entry's sign (a negative entry's digits are negated), so
@@ -219,8 +246,12 @@ struct DigitArgs {
     __nv_bfloat16 *out;
 };
 
+// BAL: balanced digits.  s[entry][li - LO] holds limb l0 + li for li >= LO; with
+// balanced digits LO = -1, so slot 0 holds limb l0 - 1 (its top byte carries into the
+// chunk's first digit).  Rows of 65 and 67 words keep the column loads conflict-free.
+template <bool BAL>
 __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
-    __shared__ uint32_t s[128][65];
+    __shared__ uint32_t s[128][BAL ? 67 : 65];
     __shared__ uint32_t sflip[128];  // 0x80008000 for a negative entry: flips both bf16 signs of a word
     const int tr = 4, tcn = 32;
     const int r0 = blockIdx.y * tr, c0 = blockIdx.x * tcn;
@@ -233,13 +264,16 @@ __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
         // one chunk of 64 limbs per block (blockIdx.z): more, shorter blocks keep the
         // last wave of the grid small
         const int l0 = blockIdx.z * 64;
-        // load limbs [l0, l0+64) of the 4 x 32 entries, coalesced along c
-        for (int q = threadIdx.x; q < 64 * 128; q += 256) {
-            int cc = q & 31, rr = (q >> 5) & 3, li = q >> 7;
+        // load limbs [l0 - 1, l0 + 64) of the 4 x 32 entries, coalesced along c: slot
+        // 1 + li holds limb l0 + li, slot 0 limb l0 - 1 (its top byte carries into the
+        // chunk's first digit)
+        constexpr int LO = BAL ? -1 : 0;  // first limb loaded, relative to l0
+        for (int q = threadIdx.x; q < (64 - LO) * 128; q += 256) {
+            int cc = q & 31, rr = (q >> 5) & 3, li = (q >> 7) + LO;
             int r = r0 + rr, c = c0 + cc, l = l0 + li;
             uint32_t v = 0;
-            if (r < a.rows && c < a.cols && l < a.nlimbs) v = a.limbs[(int64_t)l * a.ld + (int64_t)r * a.rs + c];
-            s[rr * 32 + cc][li] = v;
+            if (r < a.rows && c < a.cols && l >= 0 && l < a.nlimbs) v = a.limbs[(int64_t)l * a.ld + (int64_t)r * a.rs + c];
+            s[rr * 32 + cc][li - LO] = v;
         }
         __syncthreads();
         // each warp writes whole digit rows: lane j -> limbs l0+2j, l0+2j+1 (8 digits, 16 bytes)
@@ -250,13 +284,24 @@ __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
             int64_t row = a.transpose ? (int64_t)c * a.rows + r : (int64_t)r * a.cols + c;
             int dg = 4 * (l0 + 2 * lane);
             if (dg >= a.dxp) continue;
-            uint32_t v0 = s[ent][2 * lane], v1 = s[ent][2 * lane + 1];
             const uint32_t flip = sflip[ent];
             uint4 pk;
-            pk.x = byte_pair_bf16(v0, 0) ^ flip;
-            pk.y = byte_pair_bf16(v0, 2) ^ flip;
-            pk.z = byte_pair_bf16(v1, 0) ^ flip;
-            pk.w = byte_pair_bf16(v1, 2) ^ flip;
+            if (BAL) {
+                const uint32_t vp = s[ent][2 * lane], v0 = s[ent][2 * lane + 1], v1 = s[ent][2 * lane + 2];
+                float d0[4], d1[4];
+                limb_digits_bal(v0, vp >> 31, false, d0);
+                limb_digits_bal(v1, v0 >> 31, dg + 8 == a.dxp, d1);
+                pk.x = bf16x2_bits(d0[0], d0[1]) ^ flip;
+                pk.y = bf16x2_bits(d0[2], d0[3]) ^ flip;
+                pk.z = bf16x2_bits(d1[0], d1[1]) ^ flip;
+                pk.w = bf16x2_bits(d1[2], d1[3]) ^ flip;
+            } else {
+                const uint32_t v0 = s[ent][2 * lane], v1 = s[ent][2 * lane + 1];
+                pk.x = byte_pair_bf16(v0, 0) ^ flip;
+                pk.y = byte_pair_bf16(v0, 2) ^ flip;
+                pk.z = byte_pair_bf16(v1, 0) ^ flip;
+                pk.w = byte_pair_bf16(v1, 2) ^ flip;
+            }
             *reinterpret_cast<uint4 *>(a.out + row * a.dxp + dg) = pk;
         }
     }
@@ -310,7 +355,7 @@ __device__ __forceinline__ void residue_fold(const uint32_t (&v)[32], int mi0, b
 // row blocks and the same table columns: each CTA loads half of the table box and
 // multicasts it to both, so the table is read from L2 once per pair of row blocks,
 // and each CTA's MMA commit frees the stage in both CTAs.
-template <int STAGES, bool PAIR, bool MC = false>
+template <int STAGES, bool PAIR, bool MC, int GS>
 __global__ void __launch_bounds__(RES_THREADS, 1)
     k_crt_residue(const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmT,
                   const __grid_constant__ CUtensorMap tmR, ResidueArgs a, uint32_t *err) {
@@ -429,12 +474,14 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
                     if (!tc::mbar_wait(&bars->full[st], (it / STAGES) & 1)) { set_abort(bars, err); ok = false; break; }
                     tc::fence_after_sync();
                     const uint32_t sa = tc::smem_u32(base + st * STAGE);
-                    const uint32_t d = tmem + (uint32_t)(256 * b + (s / GROUP_STEPS) * a.BN);
+                    // accumulation group s / GS (GS K steps each, a compile-time constant: the
+                    // issuing thread is on the critical path)
+                    const uint32_t d = tmem + (uint32_t)(256 * b + (s / GS) * a.BN);
                     const uint64_t ad = tc::sdesc_kmajor(sa), bd = tc::sdesc_kmajor(sa + A_BYTES);
 #pragma unroll
                     for (int kk = 0; kk < BK / UK; kk++) {
                         const uint64_t adesc = tc::sdesc_advance(ad, kk * 32), bdesc = tc::sdesc_advance(bd, kk * 32);
-                        const uint32_t acc = (s % GROUP_STEPS) != 0 || kk != 0;
+                        const uint32_t acc = (s % GS) != 0 || kk != 0;
                         if (PAIR) tc::mma_bf16_pair(d, adesc, bdesc, idesc, acc);
                         else tc::mma_bf16(d, adesc, bdesc, idesc, acc);
                     }
@@ -600,6 +647,7 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
 // ======================================================================================
 struct ProductArgs {
     int32_t m, n, nk, P;
+    int32_t npad;      // entry row pitch of Y: n rounded up to 16 (entry e = y * npad + x)
     int32_t nyt, nxt;
     int64_t ntiles;
     const ModConst *mods;
@@ -607,6 +655,7 @@ struct ProductArgs {
     int64_t yblk;      // elements per 64-entry block (2Pp * 64)
 };
 constexpr int PBX = 64;  // output columns per product tile
+constexpr int YPAD = 16;  // Y's entry rows are padded to a multiple of this (whole 32-byte runs)
 
 // PAIR: a cluster of two CTAs shares one M = 256 tcgen05.mma.cta_group::2 per K
 // slice (issued by the even CTA): each CTA stages its own 128 rows of A1 and A0,
@@ -755,7 +804,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             }
             const ModConst mc = a.mods[mi];
             const float pf = (float)mc.p;
-            const int64_t erow = (int64_t)y * a.n + xh;  // entry index of this warp's first column
+            const int64_t erow = (int64_t)y * a.npad + xh;  // entry index of this warp's first column
             __nv_bfloat16 *yplane = a.Y + (int64_t)(2 * mi) * 64;  // hi plane; lo plane 64 elements on
 #pragma unroll
             for (int c = 0; c < 32; c += 16) {
@@ -777,9 +826,10 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                     plo[j / 2] = bf16x2_bits(l2[0], l2[1]);
                 }
                 if (y >= a.m) continue;
+                // rows of Y are padded to whole groups of 16 entries, so every group but a
+                // row's last partial one is two aligned 32-byte runs inside one 64-entry block
                 const int64_t ec = erow + c;
-                if ((ec & 15) == 0 && xh + c + 16 <= a.n) {
-                    // 16 entries inside one 64-entry block: two 32-byte runs
+                if ((ec & 15) == 0 && xh + c < a.n) {
                     __nv_bfloat16 *dst = yplane + (ec >> 6) * a.yblk + (ec & 63);
                     uint4 *dsth = reinterpret_cast<uint4 *>(dst), *dstl = reinterpret_cast<uint4 *>(dst + 64);
                     dsth[0] = make_uint4(phi[0], phi[1], phi[2], phi[3]);
@@ -829,8 +879,9 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 // ======================================================================================
 struct ReconArgs {
     int64_t mt0;     // first entry tile of this launch (tiles mt0 .. nmt-1)
-    int64_t E;       // entries of C
-    int32_t ncols;   // columns of C (entry e -> row e / ncols, col e % ncols)
+    int64_t E;       // entries of Y: rows of C x padded row length
+    int32_t ncols;   // padded row length of Y's entries (entry e -> row e / ncols, col e % ncols)
+    int32_t ccols;   // columns of C: entries with col >= ccols are padding and not stored
     int32_t nk;      // K steps over 2Pp
     int32_t NT;      // N tiles of 256 table rows
     int32_t Dout;    // output base-128 digit positions
@@ -989,8 +1040,9 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         bool first = true, ok = true;
         for (int64_t t = a.mt0 + t0; t < a.nmt && ok; t += tstep) {
             const int64_t e = t * (NP * BM) + rank * BM + quad * 32 + lane;
-            const bool live = e < a.E;
-            const int64_t coff = live ? (e / a.ncols) * a.crs + (e % a.ncols) : 0;
+            const int64_t er = e / a.ncols, ec = e - er * a.ncols;
+            const bool live = e < a.E && ec < a.ccols;
+            const int64_t coff = live ? er * a.crs + ec : 0;
             // C = sum_u (acc_u - q Mod_u) 128^u; the limbs written are |C| (negated on the
             // fly when the fixed-point sum says C < 0)
             int32_t q = 0, sgn = 1, amb = 0;
@@ -1814,22 +1866,27 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     const int64_t E = (int64_t)X.rows * X.cols;
     __nv_bfloat16 *D = (__nv_bfloat16 *)arena_alloc(h, (size_t)E * dxp * 2 + 1024);
     if (!D) return set_error(GBMM_ERR_NOMEM, "crt: workspace for digits");
+    const int nk = dxp / BK;
+    // unsigned byte digits up to 512 per row; longer rows in balanced digits, whose
+    // groups are nearly twice as long (fewer groups, wider table tiles)
+    const int balanced = nk > RES_GROUP_STEPS_U;
+    const int gsteps = balanced ? RES_GROUP_STEPS_B : RES_GROUP_STEPS_U;
     {
         DigitArgs a;
         a.limbs = X.limbs; a.sizes = X.sizes; a.ld = X.ld; a.rs = X.rs; a.rows = X.rows; a.cols = X.cols;
         a.nlimbs = X.nlimbs; a.transpose = transpose; a.dxp = dxp; a.out = D;
         dim3 grid((unsigned)((X.cols + 31) / 32), (unsigned)((X.rows + 3) / 4), (unsigned)((dxp / 4 + 63) / 64));
         LaunchScope ls_("k_crt_digits", s);
-        k_crt_digits<<<grid, 256, 0, s>>>(a);
+        if (balanced) k_crt_digits<true><<<grid, 256, 0, s>>>(a);
+        else k_crt_digits<false><<<grid, 256, 0, s>>>(a);
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     __nv_bfloat16 *T = nullptr;
     GBMM_TRY(residue_table(t, dxp, weighted, &T));
-    const int nk = dxp / BK;
-    const int G = (nk + GROUP_STEPS - 1) / GROUP_STEPS;
+    const int G = (nk + gsteps - 1) / gsteps;
     int BN = 256;
     while (BN * G > 256) BN /= 2;
-    if (BN < 64) return set_error(GBMM_ERR_UNSUPPORTED, "crt: entries longer than 16384 bits");
+    if (BN < 64) return set_error(GBMM_ERR_UNSUPPORTED, "crt: entries longer than 30720 bits");
     const bool pair = residue_pair(nk), mc = !pair && residue_mc(nk);
     const int NP = pair || mc ? 2 : 1;
     CUtensorMap tmD, tmT, tmR;
@@ -1851,19 +1908,26 @@ static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat
     const size_t sm = smem_bytes(stages, BM * 128 + (size_t)(pair ? BN / 2 : BN) * 128) +
                       (size_t)RES_EPI_WARPS * (pair ? 2 : 1) * RES_STG_BYTES;
     LaunchScope ls_("k_crt_residue", s);
-    if (mc) {
-        GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false, true>, sm));
-        GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES, false, true>, RES_THREADS, a.ntiles, sm, s, tmD, tmT, tmR, a,
-                              device_error_word()));
-    } else if (pair) {
-        GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES_PAIR, true>, sm));
-        GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES_PAIR, true>, RES_THREADS, a.ntiles, sm, s, tmD, tmT, tmR, a,
-                              device_error_word()));
-    } else {
-        GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false>, sm));
-        dim3 grid((unsigned)std::min<int64_t>(a.ntiles, num_sms()));
-        k_crt_residue<RES_STAGES, false><<<grid, RES_THREADS, sm, s>>>(tmD, tmT, tmR, a, device_error_word());
-    }
+#define RESIDUE_LAUNCH(GS_)                                                                                          \
+    do {                                                                                                             \
+        if (mc) {                                                                                                    \
+            GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false, true, GS_>, sm));                       \
+            GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES, false, true, GS_>, RES_THREADS, a.ntiles, sm, s, tmD,   \
+                                  tmT, tmR, a, device_error_word()));                                                \
+        } else if (pair) {                                                                                           \
+            GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES_PAIR, true, false, GS_>, sm));                  \
+            GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES_PAIR, true, false, GS_>, RES_THREADS, a.ntiles, sm, s,  \
+                                  tmD, tmT, tmR, a, device_error_word()));                                           \
+        } else {                                                                                                     \
+            GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false, false, GS_>, sm));                      \
+            dim3 grid((unsigned)std::min<int64_t>(a.ntiles, num_sms()));                                             \
+            k_crt_residue<RES_STAGES, false, false, GS_><<<grid, RES_THREADS, sm, s>>>(tmD, tmT, tmR, a,             \
+                                                                                     device_error_word());         \
+        }                                                                                                            \
+    } while (0)
+    if (gsteps == RES_GROUP_STEPS_B) RESIDUE_LAUNCH(RES_GROUP_STEPS_B);
+    else RESIDUE_LAUNCH(RES_GROUP_STEPS_U);
+#undef RESIDUE_LAUNCH
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
 }
@@ -1882,21 +1946,22 @@ static size_t crt_workspace(const gbmm_mat &a, const gbmm_mat &b, const gbmm_mat
     if (P <= 0) return 0;
     const int Pp = (2 * P + 63) / 64 * 32;
     const int kp = (k + 63) / 64 * 64;
-    const int64_t Ep = ((int64_t)m * n + 63) / 64 * 64;
+    const int64_t Ep = ((int64_t)m * ((n + YPAD - 1) / YPAD * YPAD) + 63) / 64 * 64;
     const int dxa = (4 * std::max(a.nlimbs, 1) + 63) / 64 * 64, dxb = (4 * std::max(b.nlimbs, 1) + 63) / 64 * 64;
     return align256((size_t)2 * P * m * kp * 2) + align256((size_t)2 * P * n * kp * 2) + align256((size_t)2 * Pp * Ep * 2) +
            std::max(align256((size_t)m * k * dxa * 2 + 1024), align256((size_t)k * n * dxb * 2 + 1024)) + 8192;
 }
 
 bool crt_feasible(int la, int lb, int k) {
-    const int P = crt_moduli(32LL * la, 32LL * lb, std::min(k, GROUP_STEPS * BK));
-    return P > 0 && P <= 1023 && 4 * std::max(la, lb) <= 4 * GROUP_STEPS * BK;
+    const int P = crt_moduli(32LL * la, 32LL * lb, std::min(k, PROD_MAX_K));
+    // at most four residue accumulation groups: digit rows of up to 4 * 15 * 64 digits
+    return P > 0 && P <= 1023 && 4 * std::max(la, lb) <= 4 * RES_GROUP_STEPS_B * BK;
 }
 
 size_t crt_workspace_bytes(int la, int lb, int m, int k, int n, int cn) {
     gbmm_mat a, b, c;
     memset(&a, 0, sizeof a); memset(&b, 0, sizeof b); memset(&c, 0, sizeof c);
-    const int kc = std::min(k, GROUP_STEPS * BK);
+    const int kc = std::min(k, PROD_MAX_K);
     a.rows = m; a.cols = kc; a.nlimbs = la;
     b.rows = kc; b.cols = n; b.nlimbs = lb;
     size_t ws = crt_workspace(a, b, c, 32LL * la, 32LL * lb, 0);
@@ -1905,7 +1970,7 @@ size_t crt_workspace_bytes(int la, int lb, int m, int k, int n, int cn) {
     return ws;
 }
 
-bool crt_single_pass(int k) { return k <= GROUP_STEPS * BK; }
+bool crt_single_pass(int k) { return k <= PROD_MAX_K; }
 
 gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, int64_t bits_a,
                        int64_t bits_b, int nprimes, int accumulate, cudaStream_t s) {
@@ -1914,7 +1979,7 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     // waits for B at once and runs the reconstruction whole
     crt_stage_hooks *hk = h->stage;
     h->stage = nullptr;
-    if (hk && (m == 0 || n == 0 || k == 0 || accumulate || k > GROUP_STEPS * BK)) {
+    if (hk && (m == 0 || n == 0 || k == 0 || accumulate || k > PROD_MAX_K)) {
         if (hk->b_ready) GBMM_CUDA_TRY(cudaStreamWaitEvent(s, hk->b_ready, 0));
         hk = nullptr;
     }
@@ -1936,10 +2001,10 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         arena_release(h, mark);
         return st;
     }
-    if (k > GROUP_STEPS * BK) {
+    if (k > PROD_MAX_K) {
         // inner dimension in chunks of 512: C = A_0 B_0, then C += A_j B_j
-        for (int k0 = 0; k0 < k; k0 += GROUP_STEPS * BK) {
-            const int kc = std::min(GROUP_STEPS * BK, k - k0);
+        for (int k0 = 0; k0 < k; k0 += PROD_MAX_K) {
+            const int kc = std::min(PROD_MAX_K, k - k0);
             gbmm_mat ac = sub_view(a, 0, k0, m, kc), bc = sub_view(b, k0, 0, kc, n);
             GBMM_TRY(crt_matmul(h, c, ac, bc, bits_a, bits_b, nprimes, k0 > 0, s));
         }
@@ -1954,7 +2019,10 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     if (!get_encode()) return set_error(GBMM_ERR_CUDA, "crt: no tensor-map encoder");
 
     const int kp = (k + 63) / 64 * 64;  // residue-plane row pitch (TMA needs 16-byte pitches)
-    const int64_t E = (int64_t)m * n;
+    // Y's entries: rows of C times n padded to whole groups of 16 (the product
+    // GEMM's epilogue then stores only whole 32-byte runs)
+    const int npad = (n + YPAD - 1) / YPAD * YPAD;
+    const int64_t E = (int64_t)m * npad;
     const int64_t Ep = (E + 63) / 64 * 64;
     const int dxa = (4 * std::max(a.nlimbs, 1) + 63) / 64 * 64, dxb = (4 * std::max(b.nlimbs, 1) + 63) / 64 * 64;
     (void)dxa; (void)dxb;
@@ -1988,7 +2056,7 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         GBMM_TRY(make_map(&tmA, RA, kp, (uint64_t)2 * P * m, kp, BK, BM));
         GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)2 * P * n, kp, BK, PBX));
         ProductArgs pa;
-        pa.m = m; pa.n = n; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.yblk = (int64_t)2 * t->Pp * 64;
+        pa.m = m; pa.n = n; pa.npad = npad; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.yblk = (int64_t)2 * t->Pp * 64;
         // CTA pairs pay off once the K loop is long enough to hide the pair's per-tile
         // synchronisation (measured: faster at k = 512, slower at k = 256); a plan may
         // fix the form (h->crt_tiles: 1 one-CTA tiles, 2 CTA pairs)
@@ -2020,7 +2088,7 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         const int NP = pair ? 2 : 1, TROWS = 256 / NP;
         GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RTAB, 2 * t->Pp, BK, TROWS));
         ReconArgs ra;
-        ra.E = E; ra.ncols = n; ra.nk = 2 * t->Pp / BK; ra.NT = (SROWS + t->Dout + 255) / 256; ra.Dout = t->Dout;
+        ra.E = E; ra.ncols = npad; ra.ccols = n; ra.nk = 2 * t->Pp / BK; ra.NT = (SROWS + t->Dout + 255) / 256; ra.Dout = t->Dout;
         ra.vtab = t->d_vtab; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
         ra.cnlimbs = c.nlimbs; ra.kpad = 2 * t->Pp;
         const int64_t nmt = (E + NP * BM - 1) / (NP * BM);
@@ -2044,7 +2112,10 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
             GBMM_CUDA_TRY(cudaGetLastError());
             if (hk && parts > 1) {
                 GBMM_CUDA_TRY(cudaEventRecord(hk->part_ev[pi], s));
-                hk->part_end[pi] = std::min<int64_t>(E, ra.nmt * NP * BM);
+                // entries of C (dense, row-major) done after this part: Y's entries below
+                // ra.nmt * NP * BM, mapped back through the padded row length
+                const int64_t ye = std::min<int64_t>(E, ra.nmt * NP * BM);
+                hk->part_end[pi] = std::min<int64_t>((int64_t)m * n, (ye / npad) * n + std::min<int64_t>(ye % npad, n));
             }
         }
         if (hk && parts > 1) hk->parts_done = parts;

@@ -89,6 +89,31 @@ def test_split_for_very_long_entries(g, path):
     assert dC.to_ints() == _exact(K, M, N, A, B)
 
 
+@pytest.mark.parametrize("path", ["limb", "crt"])
+def test_split_accumulate_and_plans(g, path):
+    """C += A*B through the limb-half split, with C of either sign (the combine's
+    subtractions), and the stacked halves along rows (A longer) and columns (B
+    longer); also the CRT_SPLIT plan on operands that would not need it."""
+    rng = random.Random(13)
+    for K, M, N, ba, bb in [(7, 9, 5, 30000, 12000), (6, 10, 9, 9000, 33000), (33, 17, 40, 20000, 20000)]:
+        A, B = _rand(rng, K * M, ba, 0.05), _rand(rng, M * N, bb, 0.05)
+        C0 = _rand(rng, K * N, ba + bb, 0.2)
+        dA = g.DeviceMatrix.from_ints(K, M, A)
+        dB = g.DeviceMatrix.from_ints(M, N, B)
+        dC = g.DeviceMatrix.from_ints(K, N, C0, dA.nlimbs + dB.nlimbs + 3)
+        g.default_handle().matmul(dC, dA, dB, path={"limb": g.PATH_LIMB, "crt": g.PATH_CRT}[path], accumulate=True)
+        exp = _exact(K, M, N, A, B)
+        assert dC.to_ints() == [c + e for c, e in zip(C0, exp)]
+    if path == "crt":
+        K, M, N = 20, 24, 18
+        A, B = _rand(rng, K * M, 3000, 0.1), _rand(rng, M * N, 2500, 0.1)
+        dA = g.DeviceMatrix.from_ints(K, M, A)
+        dB = g.DeviceMatrix.from_ints(M, N, B)
+        dC = g.DeviceMatrix(K, N, dA.nlimbs + dB.nlimbs + 2)
+        g.default_handle().matmul(dC, dA, dB, plan=g.PLAN_CRT_SPLIT)
+        assert dC.to_ints() == _exact(K, M, N, A, B)
+
+
 def test_autotune_table_roundtrip(g, tmp_path):
     rng = random.Random(5)
     jobs = _make_jobs(g, rng, [(64, 64, 64, 2048, 2048), (8, 8, 8, 64, 64)])

@@ -17,6 +17,7 @@ import random
 from fractions import Fraction as F
 
 import numpy as np
+import pytest
 
 MAGIC = F(12582912)  # 1.5 * 2^23
 FIXB = 96
@@ -92,12 +93,60 @@ def test_bal_split_digits():
             assert int(np.array([float(d)], dtype=np.float32).view(np.uint32)[0]) & 0xFFFF == 0
 
 
+def _limb_digits_bal(w, cin, last):
+    """Restatement of limb_digits_bal (csrc/crt.cu) step by step: x = w ^ 0x80808080,
+    the carry bits c = ((w & 0x80808080) >> 7 << 8) | cin, the FP32 bits
+    0x4B000000 + (x_i) + c_i, one FP32 subtraction of 2^23 + 128, and for the row's
+    last digit +256 when its byte's top bit is set."""
+    x = w ^ 0x80808080
+    c = ((((w & 0x80808080) >> 7) << 8) | cin) & 0xFFFFFFFF
+    out = []
+    for i in range(4):
+        bits = 0x4B000000 + ((x >> (8 * i)) & 255) + ((c >> (8 * i)) & 255)
+        v = np.array([bits], dtype=np.uint32).view(np.float32)[0]
+        d = np.float32(v) - np.float32(8388736.0)
+        if last and i == 3 and (w >> 31):
+            d = d + np.float32(256.0)
+        d = float(d)
+        assert d == int(d) and int(np.array([d], dtype=np.float32).view(np.uint32)[0]) & 0xFFFF == 0
+        out.append(int(d))
+    return out
+
+
+@pytest.mark.parametrize("nlimbs,dxp", [(1, 64), (16, 64), (15, 64), (128, 512), (127, 512), (129, 576), (300, 1216)])
+def test_balanced_digit_rows(nlimbs, dxp):
+    """A digit row as k_crt_digits writes it: each limb's digits from its own bytes
+    and the top bit of the limb below; the row's last digit unreduced.  The digits
+    keep the value, lie in [-128, 128] (the last in [0, 256]), and the row's digits
+    past 4 * nlimbs are zero but for one carry digit."""
+    rng = random.Random(nlimbs * 7 + dxp)
+    for kind in ("rand", "ones", "top"):
+        limbs = [rng.getrandbits(32) for _ in range(nlimbs)]
+        if kind == "ones":
+            limbs = [0xFFFFFFFF] * nlimbs
+        elif kind == "top":
+            limbs = [0x80808080 | rng.getrandbits(32) for _ in range(nlimbs)]
+        words = limbs + [0] * (dxp // 4 - nlimbs)
+        digits = []
+        for l, w in enumerate(words):
+            cin = (words[l - 1] >> 31) if l > 0 else 0
+            digits += _limb_digits_bal(w, cin, last=(4 * l + 4 == dxp))
+        assert len(digits) == dxp
+        x = sum(w << (32 * l) for l, w in enumerate(limbs))
+        assert sum(d << (8 * i) for i, d in enumerate(digits)) == x
+        assert all(-128 <= d <= 128 for d in digits[:-1]) and 0 <= digits[-1] <= 256
+        assert all(d == 0 for d in digits[4 * nlimbs + 1:])
+
+
 def test_epilogue_sums_stay_exact():
     # residue: 256 red(s1) + red(s0) + res; product: 256 red(D_hi) + red(D_lo)
     assert 256 * 32772 + 32772 + 32772 < 1 << 24
-    # residue groups: 512 digits x 255 x 128; product: 2k = 1024 terms of 128^2;
+    # residue groups: 512 unsigned byte digits, or 960 balanced digits (|d| <= 128, the row's last digit <= 256)
+    # against table digits |t| <= 128; product: 2k = 1024 terms of 128^2;
     # reconstruction: 2P = 2046 terms of 128 x 64
     assert 512 * 255 * 128 <= 1 << 24
+    assert 959 * 128 * 128 + 256 * 128 < 1 << 24
+    assert 960 == 15 * 64
     assert 1024 * 128 * 128 <= 1 << 24
     assert 2046 * 128 * 64 <= 1 << 24
 
