@@ -4,8 +4,10 @@
 // gbmm_matmul_batched splits the jobs by plan.  Limb jobs planned without
 // recursion are cut into (job, tile) items, sorted largest first, and run by ONE
 // persistent kernel per group (block edge, CTA form, thin operands) that drains a
-// device work queue.  The other jobs (CRT products, Winograd trees) run through
-// dispatch() on eight side streams, side by side.  The whole launch
+// device work queue.  CRT jobs with one pass over k (directly or after one
+// limb-half split) run in grouped launches: one persistent launch per CRT stage
+// and kernel form over the tiles of all of them.  The other jobs (Winograd
+// trees, longer CRT products) run through dispatch() on side streams.  The whole launch
 // sequence of a batch is captured into a CUDA graph the second time a batch
 // with the same signature (shapes, pointers, paths) is seen, and replayed from
 // then on.  This replaces the reference's chunked multi-stream job DAG
@@ -17,6 +19,7 @@
 
 #include <algorithm>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -39,7 +42,7 @@ struct TuneEntry {
 
 struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
-    char *d_blob = nullptr;  // work-queue blob owned by this graph
+    char *d_blob = nullptr;  // work-queue and grouped-CRT blob owned by this graph
 };
 
 constexpr int NSIDE = 8;  // side streams a batch's dispatched jobs are spread over
@@ -49,6 +52,7 @@ struct BatchState {
     // side streams and the events that fork them from and join them to the handle's stream
     cudaStream_t side[NSIDE] = {};
     cudaEvent_t fork_ev = nullptr, join_ev[NSIDE] = {};
+    cudaEvent_t post_ev = nullptr;  // grouped CRT: its post steps' stream waits for it
     // graph cache
     std::map<std::string, GraphEntry> graphs;
     std::map<std::string, int> seen;
@@ -78,6 +82,7 @@ void batch_state_destroy(gbmm_handle h) {
         if (b->join_ev[i]) cudaEventDestroy(b->join_ev[i]);
     }
     if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    if (b->post_ev) cudaEventDestroy(b->post_ev);
     if (b->h_stage) cudaFreeHost(b->h_stage);
     if (b->d_counter) cudaFree(b->d_counter);
     delete b;
@@ -150,6 +155,7 @@ static gbmm_status side_streams(BatchState &bs) {
         GBMM_CUDA_TRY(cudaStreamCreateWithFlags(&bs.side[i], cudaStreamNonBlocking));
         GBMM_CUDA_TRY(cudaEventCreateWithFlags(&bs.join_ev[i], cudaEventDisableTiming));
     }
+    GBMM_CUDA_TRY(cudaEventCreateWithFlags(&bs.post_ev, cudaEventDisableTiming));
     GBMM_CUDA_TRY(cudaEventCreateWithFlags(&bs.fork_ev, cudaEventDisableTiming));
     return GBMM_OK;
 }
@@ -166,35 +172,41 @@ static int nside_for(size_t njobs) { return (int)std::min<size_t>(NSIDE, njobs);
 // current top) and the handle's stream waits for all of them at the end.
 static gbmm_status enqueue_batch(gbmm_handle h, const gbmm_job *jobs, const std::vector<Plan> &plans,
                                  const LimbBatchPlan &lp, const char *d_blob, const std::vector<int> &other,
-                                 size_t slice) {
+                                 size_t slice, size_t base, crt_group *grp, const char *d_crt) {
     BatchState &bs = bstate(h);
-    const int ns = nside_for(other.size());
+    // the grouped CRT launches take side stream 0 (and 1 for their post steps),
+    // the dispatched jobs the others
+    const int gs = grp && !crt_group_empty(grp) ? 2 : 0;
+    const int ns = std::min(NSIDE, gs + nside_for(other.size()));
     if (ns > 0) {
         GBMM_TRY(side_streams(bs));
         GBMM_CUDA_TRY(cudaEventRecord(bs.fork_ev, h->stream));
         for (int i = 0; i < ns; i++) GBMM_CUDA_TRY(cudaStreamWaitEvent(bs.side[i], bs.fork_ev, 0));
     }
     if (!lp.groups.empty()) GBMM_TRY(launch_limb_batch(lp, d_blob, bs.d_counter, h->stream));
+    gbmm_status st = GBMM_OK;
+    if (gs) st = crt_group_launch(grp, d_crt, bs.side[0], bs.side[1], bs.post_ev);
     std::vector<int> order(other);
     auto work = [&](int j) {
         const gbmm_job &q = jobs[j];
         return (double)q.a.rows * q.a.cols * q.b.cols * std::max(q.a.nlimbs, 1) * std::max(q.b.nlimbs, 1);
     };
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work(x) > work(y); });
-    std::vector<double> load(ns, 0.0);
-    // slices start above 0, so a reservation inside dispatch() that did not fit its
-    // slice fails ("grow while in use") instead of reallocating the arena under
-    // work still queued on the other side streams
-    const size_t base = ((arena_mark(h) + 255) & ~(size_t)255) + 256;
-    gbmm_status st = GBMM_OK;
+    // slice i of the arena (from `base`) serves side stream gs + i.  Slices start
+    // above 0, so a reservation inside dispatch() that did not fit its slice fails
+    // ("grow while in use") instead of reallocating the arena under work still
+    // queued on the other side streams
+    const int nd = ns - gs;
+    std::vector<double> load(std::max(nd, 1), 0.0);
     for (int j : order) {
+        if (st != GBMM_OK) break;
         int i = 0;
-        for (int t = 1; t < ns; t++)
+        for (int t = 1; t < nd; t++)
             if (load[t] < load[i]) i = t;
         load[i] += work(j);
         const size_t mark = arena_mark(h);
         h->ws.top = base + (size_t)i * slice;
-        st = dispatch(h, jobs[j].c, jobs[j].a, jobs[j].b, plans[j], 0, bs.side[i]);
+        st = dispatch(h, jobs[j].c, jobs[j].a, jobs[j].b, plans[j], 0, bs.side[gs + i]);
         arena_release(h, mark);
         if (st != GBMM_OK) break;
     }
@@ -230,11 +242,29 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
         GBMM_TRY(resolve_plan(h, q.a, q.b, oj, plans[j]));
         jobs[j].chosen_path = plans[j].path;
         jobs[j].chosen_plan = plans[j].id;
-        ws = std::max(ws, dispatch_ws(plans[j], q.a.nlimbs, q.b.nlimbs, q.a.rows, q.a.cols, q.b.cols, q.c.nlimbs, 0));
     }
     if (njobs == 0) return GBMM_OK;
-    std::vector<int> queue_jobs, other;
+    std::vector<int> queue_jobs, other, grouped;
     split_batch(jobs, njobs, plans, queue_jobs, other);
+    {
+        // CRT jobs with one pass over k go to the grouped launches
+        std::vector<int> rest;
+        for (int j : other) {
+            const gbmm_job &q = jobs[j];
+            if (crt_groupable(plans[j], q.a.nlimbs, q.b.nlimbs, q.a.rows, q.a.cols, q.b.cols)) grouped.push_back(j);
+            else rest.push_back(j);
+        }
+        other.swap(rest);
+    }
+    size_t gws = 0;  // the grouped products' workspace, all carved at once
+    for (int j : grouped) {
+        const gbmm_job &q = jobs[j];
+        gws += crt_group_job_ws(plans[j], q.a.nlimbs, q.b.nlimbs, q.a.rows, q.a.cols, q.b.cols) + 4096;
+    }
+    for (int j : other) {
+        const gbmm_job &q = jobs[j];
+        ws = std::max(ws, dispatch_ws(plans[j], q.a.nlimbs, q.b.nlimbs, q.a.rows, q.a.cols, q.b.cols, q.c.nlimbs, 0));
+    }
     LimbBatchPlan lp;
     {
         std::vector<gbmm_mat> C, A, B;
@@ -248,10 +278,13 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
     BatchState &bs = bstate(h);
     if (!bs.d_counter) GBMM_CUDA_TRY(cudaMalloc(&bs.d_counter, LimbBatchPlan::MAX_GROUPS * sizeof(int)));
     if (!bs.staged) GBMM_CUDA_TRY(cudaEventCreateWithFlags(&bs.staged, cudaEventDisableTiming));
-    // one arena slice per side stream, each large enough for any dispatched job
+    // one arena slice per side stream of the dispatched jobs, each large enough for
+    // any of them, then the grouped products' region and the blob; the grouped
+    // records take at most 4 KB per product
     const size_t slice = (ws + 65536 + 255) & ~(size_t)255;
     const int ns = nside_for(other.size());
-    GBMM_TRY(arena_reserve(h, (size_t)std::max(ns, 1) * slice + lp.blob.size() + 65536 + 1024));
+    const size_t crt_blob_max = 4096 * grouped.size() + 4096;
+    GBMM_TRY(arena_reserve(h, (size_t)std::max(ns, 1) * slice + gws + lp.blob.size() + crt_blob_max + 65536 + 1024));
 
     const std::string sig = bs.use_graphs ? job_signature(jobs, njobs, plans) : std::string();
     if (bs.use_graphs) {
@@ -263,38 +296,69 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
         }
     }
     const bool capture = bs.use_graphs && h->stream != nullptr && bs.seen[sig]++ > 0;
+    // Arena layout from the current mark: the dispatched jobs' slices, then the
+    // grouped products' workspace (carved now, before any launch or capture: tables
+    // and tensor maps are built here), then (eager calls) the blob.  The blob is
+    // the work queue followed, 256-byte aligned, by the grouped CRT records.
+    const size_t mark = arena_mark(h);
+    const size_t base = ((mark + 255) & ~(size_t)255) + 256;
+    std::unique_ptr<crt_group, void (*)(crt_group *)> grp(crt_group_create(), crt_group_destroy);
+    h->ws.top = base + (size_t)std::max(ns, 1) * slice;
+    for (int j : grouped) {
+        gbmm_status st = crt_collect(h, grp.get(), jobs[j].c, jobs[j].a, jobs[j].b, plans[j]);
+        if (st != GBMM_OK) {
+            arena_release(h, mark);
+            return st;
+        }
+    }
+    std::vector<char> blob(lp.blob);
+    size_t crt_off = 0;
+    if (!crt_group_empty(grp.get())) {
+        const std::vector<char> &cb = crt_group_blob(grp.get());
+        crt_off = (blob.size() + 255) & ~(size_t)255;
+        blob.resize(crt_off);
+        blob.insert(blob.end(), cb.begin(), cb.end());
+    }
     if (!capture) {
-        // eager: the work-queue blob goes through pinned staging into the arena
-        size_t mark = arena_mark(h);
+        // eager: the blob goes through pinned staging into the arena
         char *d_blob = nullptr;
-        if (!lp.blob.empty()) {
+        if (!blob.empty()) {
             GBMM_CUDA_TRY(cudaEventSynchronize(bs.staged));  // the previous copy out of the staging is done
-            if (bs.h_cap < lp.blob.size()) {
+            if (bs.h_cap < blob.size()) {
                 if (bs.h_stage) GBMM_CUDA_TRY(cudaFreeHost(bs.h_stage));
                 bs.h_stage = nullptr;
                 bs.h_cap = 0;
-                GBMM_CUDA_TRY(cudaHostAlloc((void **)&bs.h_stage, lp.blob.size(), cudaHostAllocDefault));
-                bs.h_cap = lp.blob.size();
+                GBMM_CUDA_TRY(cudaHostAlloc((void **)&bs.h_stage, blob.size(), cudaHostAllocDefault));
+                bs.h_cap = blob.size();
             }
-            memcpy(bs.h_stage, lp.blob.data(), lp.blob.size());
-            d_blob = (char *)arena_alloc(h, lp.blob.size());
-            if (!d_blob) return set_error(GBMM_ERR_NOMEM, "batch work queue");
-            GBMM_CUDA_TRY(cudaMemcpyAsync(d_blob, bs.h_stage, lp.blob.size(), cudaMemcpyHostToDevice, h->stream));
+            memcpy(bs.h_stage, blob.data(), blob.size());
+            d_blob = (char *)arena_alloc(h, blob.size());
+            if (!d_blob) {
+                arena_release(h, mark);
+                return set_error(GBMM_ERR_NOMEM, "batch work queue");
+            }
+            GBMM_CUDA_TRY(cudaMemcpyAsync(d_blob, bs.h_stage, blob.size(), cudaMemcpyHostToDevice, h->stream));
             GBMM_CUDA_TRY(cudaEventRecord(bs.staged, h->stream));
         }
-        gbmm_status st = enqueue_batch(h, jobs, plans, lp, d_blob, other, slice);
+        gbmm_status st = enqueue_batch(h, jobs, plans, lp, d_blob, other, slice, base, grp.get(), d_blob + crt_off);
         arena_release(h, mark);
         return st;
     }
     // capture: the blob gets its own device buffer, filled before capture begins
     GraphEntry ge;
-    if (!lp.blob.empty()) {
-        GBMM_CUDA_TRY(cudaMalloc(&ge.d_blob, lp.blob.size()));
-        GBMM_CUDA_TRY(cudaMemcpy(ge.d_blob, lp.blob.data(), lp.blob.size(), cudaMemcpyHostToDevice));
+    if (!blob.empty()) {
+        cudaError_t e = cudaMalloc(&ge.d_blob, blob.size());
+        if (e == cudaSuccess) e = cudaMemcpy(ge.d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(ge.d_blob);
+            arena_release(h, mark);
+            return cuda_error(e, "batch blob");
+        }
     }
     cudaGraph_t graph = nullptr;
     GBMM_CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    gbmm_status st = enqueue_batch(h, jobs, plans, lp, ge.d_blob, other, slice);
+    gbmm_status st = enqueue_batch(h, jobs, plans, lp, ge.d_blob, other, slice, base, grp.get(), ge.d_blob + crt_off);
+    arena_release(h, mark);
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     if (st == GBMM_OK && e != cudaSuccess) st = cuda_error(e, "cudaStreamEndCapture");
     if (st == GBMM_OK) {

@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <utility>
 #include <cmath>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -61,6 +62,7 @@ constexpr int CTA_THREADS = 192;   // warp 0 TMA, warp 1 MMA, warps 2..5 epilogu
 constexpr int CTA_THREADS8 = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue (two per lane quadrant)
 constexpr int RES_EPI_WARPS = 16;   // residue GEMM: four epilogue warps per lane quadrant
 constexpr int RES_THREADS = 32 * (2 + RES_EPI_WARPS);
+constexpr int PROD_THREADS = 32 * (2 + 16);  // product GEMM: two groups of 8 epilogue warps, one per TMEM buffer
 constexpr int RTAB = 256;          // reconstruction table rows are padded to a multiple of this
 }  // namespace
 
@@ -198,6 +200,26 @@ __device__ __forceinline__ int epi_row() { return ((threadIdx.x >> 5) & 3) * 32 
 __device__ __forceinline__ uint32_t lane_base(uint32_t tmem) { return tmem + (((threadIdx.x >> 5) & 3) * 32u << 16); }
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
 
+// A grouped launch runs the tiles of several products in one persistent kernel.
+// Job j owns the global tiles [tile0[j], tile0[j + 1]); every role of a CTA walks
+// the same tile sequence and looks each tile's job up by binary search.  The job
+// records (arguments and 64-byte aligned tensor maps) sit in global memory.
+template <typename J>
+struct Group {
+    const J *jobs;
+    const int64_t *tile0;  // njobs + 1 entries, tile0[njobs] = all tiles
+    int32_t njobs;
+};
+__device__ __forceinline__ int group_job(const int64_t *tile0, int n, int64_t T) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(tile0 + mid) <= T) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // ======================================================================================
 // 1. digits
 // ======================================================================================
@@ -249,12 +271,35 @@ struct DigitArgs {
 // BAL: balanced digits.  s[entry][li - LO] holds limb l0 + li for li >= LO; with
 // balanced digits LO = -1, so slot 0 holds limb l0 - 1 (its top byte carries into the
 // chunk's first digit).  Rows of 65 and 67 words keep the column loads conflict-free.
-template <bool BAL>
-__global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
+// One operand of a grouped digits launch: its blocks are (bx, by, bz) in x-fastest
+// order, nbx x nby x (chunks of 64 limbs).
+struct DigitJob {
+    DigitArgs a;
+    int32_t nbx, nby;
+};
+
+template <bool BAL, bool GRP>
+__global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a0, Group<DigitJob> grp) {
     __shared__ uint32_t s[128][BAL ? 67 : 65];
     __shared__ uint32_t sflip[128];  // 0x80008000 for a negative entry: flips both bf16 signs of a word
+    DigitArgs a;
+    int bx, by, bz;
+    if (GRP) {
+        const int j = group_job(grp.tile0, grp.njobs, blockIdx.x);
+        const DigitJob &J = grp.jobs[j];
+        a = J.a;
+        const int b = (int)(blockIdx.x - __ldg(grp.tile0 + j));
+        bx = b % J.nbx;
+        by = (b / J.nbx) % J.nby;
+        bz = b / J.nbx / J.nby;
+    } else {
+        a = a0;
+        bx = blockIdx.x;
+        by = blockIdx.y;
+        bz = blockIdx.z;
+    }
     const int tr = 4, tcn = 32;
-    const int r0 = blockIdx.y * tr, c0 = blockIdx.x * tcn;
+    const int r0 = by * tr, c0 = bx * tcn;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x < 128) {
         const int r = r0 + (threadIdx.x >> 5), c = c0 + (threadIdx.x & 31);
@@ -263,7 +308,7 @@ __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a) {
     {
         // one chunk of 64 limbs per block (blockIdx.z): more, shorter blocks keep the
         // last wave of the grid small
-        const int l0 = blockIdx.z * 64;
+        const int l0 = bz * 64;
         // load limbs [l0 - 1, l0 + 64) of the 4 x 32 entries, coalesced along c: slot
         // 1 + li holds limb l0 + li, slot 0 limb l0 - 1 (its top byte carries into the
         // chunk's first digit)
@@ -325,6 +370,11 @@ struct ResidueArgs {
     int32_t kp;
     int32_t tma_out;  // kdim % 32 == 0: each warp's 32 entries share a plane row; TMA stores
 };
+// One operand of a grouped residue launch.
+struct ResidueJob {
+    CUtensorMap tmD, tmT, tmR;
+    ResidueArgs a;
+};
 
 // shared-memory staging of one epilogue warp's chunk: [32 planes][32 entries] bf16
 constexpr int RES_STG_BYTES = 32 * 32 * 2;
@@ -355,16 +405,19 @@ __device__ __forceinline__ void residue_fold(const uint32_t (&v)[32], int mi0, b
 // row blocks and the same table columns: each CTA loads half of the table box and
 // multicasts it to both, so the table is read from L2 once per pair of row blocks,
 // and each CTA's MMA commit frees the stage in both CTAs.
-template <int STAGES, bool PAIR, bool MC, int GS>
+// GRP: a grouped launch (single CTAs only); every stage is sized for 256 table columns.
+template <int STAGES, bool PAIR, bool MC, int GS, bool GRP>
 __global__ void __launch_bounds__(RES_THREADS, 1)
     k_crt_residue(const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmT,
-                  const __grid_constant__ CUtensorMap tmR, ResidueArgs a, uint32_t *err) {
+                  const __grid_constant__ CUtensorMap tmR, ResidueArgs a0, Group<ResidueJob> grp, uint32_t *err) {
+    static_assert(!GRP || (!PAIR && !MC), "grouped residue launches use single CTAs");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
     constexpr bool CL = PAIR || MC;     // launched as clusters of two CTAs
     constexpr int NP = CL ? 2 : 1;      // row blocks per tile (per cluster)
     constexpr int NBUF = PAIR ? 2 : 1;  // staging buffers per epilogue warp
-    const uint32_t A_BYTES = BM * 128, B_BYTES = (uint32_t)(PAIR ? a.BN / 2 : a.BN) * 128, STAGE = A_BYTES + B_BYTES;
+    const uint32_t A_BYTES = BM * 128, B_BYTES = GRP ? 256u * 128 : (uint32_t)(PAIR ? a0.BN / 2 : a0.BN) * 128,
+                   STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
     uint8_t *stage_out = reinterpret_cast<uint8_t *>(bars) + SMEM_BARS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -420,13 +473,38 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
     // the last table tile may be narrow: its MMA has only the columns it needs
     // (a multiple of 16, of 32 for a pair so that each CTA stages whole 8-row groups)
     const int ngran = CL ? 32 : 16;
+    const int64_t total = GRP ? grp.tile0[grp.njobs] : (int64_t)a0.ntiles;
+    // global tile T -> its operand's arguments and maps, and the tile within it
+    auto tile_job = [&](int64_t T, ResidueArgs &a, const CUtensorMap *&mD, const CUtensorMap *&mT,
+                        const CUtensorMap *&mR) -> int {
+        if (GRP) {
+            const int j = group_job(grp.tile0, grp.njobs, T);
+            const ResidueJob *J = grp.jobs + j;
+            a = J->a;
+            mD = &J->tmD;
+            mT = &J->tmT;
+            mR = &J->tmR;
+            return (int)(T - __ldg(grp.tile0 + j));
+        }
+        a = a0;
+        mD = &tmD;
+        mT = &tmT;
+        mR = &tmR;
+        return (int)T;
+    };
 
     if (warp == 0) {
         if (lane == 0) {
-            tc::prefetch_tmap(&tmD);
-            tc::prefetch_tmap(&tmT);
+            if (!GRP) {
+                tc::prefetch_tmap(&tmD);
+                tc::prefetch_tmap(&tmT);
+            }
             int it = 0;
-            for (int t = (int)t0; t < a.ntiles && !aborted(bars); t += (int)tstep) {
+            for (int64_t T = t0; T < total && !aborted(bars); T += tstep) {
+                ResidueArgs a;
+                const CUtensorMap *mD, *mT, *mR;
+                const int t = tile_job(T, a, mD, mT, mR);
+                (void)mR;
                 const int rb = t / a.n_ntiles;
                 const int e0 = rb * (NP * BM) + (int)rank * BM;
                 const int n0 = (t - rb * a.n_ntiles) * a.BN;
@@ -442,18 +520,19 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
                         // this CTA's half of the tile's columns: n0 + rank * nn / 2 onwards
                         const uint32_t full0 = tc::mapa(tc::smem_u32(&bars->full[st]), 0);
                         if (rank == 0) tc::mbar_arrive_expect_tx(&bars->full[st], 2 * STAGE);
-                        tc::tma_load_2d_pair(sa, &tmD, full0, s * BK, (int)e0);
-                        tc::tma_load_2d_pair(sa + A_BYTES, &tmT, full0, s * BK, n0 + (int)rank * (nn / 2));
+                        tc::tma_load_2d_pair(sa, mD, full0, s * BK, (int)e0);
+                        tc::tma_load_2d_pair(sa + A_BYTES, mT, full0, s * BK, n0 + (int)rank * (nn / 2));
                     } else if (MC) {
                         // own digit rows; this CTA's half of the table box to both CTAs
                         tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                        tc::tma_load_2d(sa, &tmD, &bars->full[st], s * BK, (int)e0);
-                        tc::tma_load_2d_mc(sa + A_BYTES + rank * (B_BYTES / 2), &tmT, &bars->full[st], s * BK,
+                        tc::tma_load_2d(sa, mD, &bars->full[st], s * BK, (int)e0);
+                        tc::tma_load_2d_mc(sa + A_BYTES + rank * (B_BYTES / 2), mT, &bars->full[st], s * BK,
                                            n0 + (int)rank * (a.BN / 2), 0x3);
                     } else {
-                        tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                        tc::tma_load_2d(sa, &tmD, &bars->full[st], s * BK, (int)e0);
-                        tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, n0);
+                        // a grouped stage holds this operand's BN table rows of its 256
+                        tc::mbar_arrive_expect_tx(&bars->full[st], GRP ? A_BYTES + (uint32_t)a.BN * 128 : STAGE);
+                        tc::tma_load_2d(sa, mD, &bars->full[st], s * BK, (int)e0);
+                        tc::tma_load_2d(sa + A_BYTES, mT, &bars->full[st], s * BK, n0);
                     }
                 }
             }
@@ -462,7 +541,11 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
         if (lane == 0 && (rank == 0 || MC)) {
             int it = 0, lt = 0;
             bool ok = true;
-            for (int t = (int)t0; t < a.ntiles && ok; t += (int)tstep, lt++) {
+            for (int64_t T = t0; T < total && ok; T += tstep, lt++) {
+                ResidueArgs a;
+                const CUtensorMap *mD, *mT, *mR;
+                const int t = tile_job(T, a, mD, mT, mR);
+                (void)mD, (void)mT, (void)mR;
                 const int b = lt & 1;
                 const int n0 = (t % a.n_ntiles) * a.BN;
                 const int nn = min(a.BN, (a.ncols - n0 + ngran - 1) / ngran * ngran);
@@ -501,16 +584,20 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
         // times G groups ("units", one 32-column TMEM load each), chunk-major.  Four
         // warps per scheduler hide the loads' latency.
         const int quad = warp & 3, slot = (warp - 2) >> 2;
-        const int cpw = max(1, a.BN / 128);                          // chunks per warp
-        const int hcols = slot * cpw * 32;                           // the warp's first column in a tile
-        const int nch = max(0, min(cpw, (a.BN - hcols) / 32)), G = a.G;
         const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
         const uint32_t tempty0 = PAIR ? tc::mapa(tc::smem_u32(&bars->tempty[0]), 0) : 0;
         uint16_t *stg = reinterpret_cast<uint16_t *>(stage_out + (warp - 2) * NBUF * RES_STG_BYTES);
-        const int64_t pstep = 2 * a.plane;  // planes of one modulus
-        const uint32_t kdim = (uint32_t)a.kdim, E = (uint32_t)a.E;
         int lt = 0, sbuf = 0;
-        for (int t = (int)t0; t < a.ntiles; t += (int)tstep, lt++) {
+        for (int64_t T = t0; T < total; T += tstep, lt++) {
+            ResidueArgs a;
+            const CUtensorMap *mD, *mT, *mR;
+            const int t = tile_job(T, a, mD, mT, mR);
+            (void)mD, (void)mT;
+            const int cpw = max(1, a.BN / 128);                          // chunks per warp
+            const int hcols = slot * cpw * 32;                           // the warp's first column in a tile
+            const int nch = max(0, min(cpw, (a.BN - hcols) / 32)), G = a.G;
+            const int64_t pstep = 2 * a.plane;  // planes of one modulus
+            const uint32_t kdim = (uint32_t)a.kdim, E = (uint32_t)a.E;
             const int b = lt & 1;
             const int rb = t / a.n_ntiles;
             const int n0 = (t - rb * a.n_ntiles) * a.BN;
@@ -567,7 +654,7 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
                     __syncwarp();
                     if (lane == 0) {
                         // planes past 2P and rows past the last entry are clipped by the map
-                        tc::tma_store_3d(&tmR, buf, (int)cw, (int)rw, 2 * mi0);
+                        tc::tma_store_3d(mR, buf, (int)cw, (int)rw, 2 * mi0);
                         tc::bulk_commit_group();
                     }
                     if (NBUF > 1) sbuf ^= 1;
@@ -654,6 +741,11 @@ struct ProductArgs {
     __nv_bfloat16 *Y;  // blocked [Ep/64][2Pp][64]: 64 entries per row, 2Pp rows per block
     int64_t yblk;      // elements per 64-entry block (2Pp * 64)
 };
+// One product of a grouped product launch.
+struct ProductJob {
+    CUtensorMap tmA, tmB;
+    ProductArgs a;
+};
 constexpr int PBX = 64;  // output columns per product tile
 constexpr int YPAD = 16;  // Y's entry rows are padded to a multiple of this (whole 32-byte runs)
 
@@ -661,10 +753,10 @@ constexpr int YPAD = 16;  // Y's entry rows are padded to a multiple of this (wh
 // slice (issued by the even CTA): each CTA stages its own 128 rows of A1 and A0,
 // the even CTA U1's 64 rows and the odd CTA U0's, so per SM a K step moves 40 KB
 // instead of 48 KB and the MMAs read 12 KB of shared memory instead of 16 KB.
-template <int STAGES, bool PAIR>
-__global__ void __launch_bounds__(CTA_THREADS8, 1)
-    k_crt_product(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, ProductArgs a,
-                  uint32_t *err) {
+template <int STAGES, bool PAIR, bool GRP>
+__global__ void __launch_bounds__(PROD_THREADS, 1)
+    k_crt_product(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, ProductArgs a0,
+                  Group<ProductJob> grp, uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
     constexpr int NP = PAIR ? 2 : 1;
@@ -683,7 +775,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             }
             for (int b = 0; b < 2; b++) {
                 tc::mbar_init(&bars->tfull[b], 1);
-                tc::mbar_init(&bars->tempty[b], 16);  // the even CTA's: 8 epilogue warps of each CTA
+                tc::mbar_init(&bars->tempty[b], 16);  // the even CTA's: the buffer's 8 epilogue warps in each CTA
             }
             bars->abort_flag = 0;
             tc::fence_mbar_init();
@@ -700,14 +792,35 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         cta_setup(bars, STAGES, 512, 1, 8);
     }
     const uint32_t tmem = bars->tmem_base;
-    const int64_t per_mod = (int64_t)a.nyt * a.nxt;
+    const int64_t total = GRP ? grp.tile0[grp.njobs] : a0.ntiles;
+    // global tile T -> its product's arguments and maps, and the tile within it
+    auto tile_job = [&](int64_t T, ProductArgs &a, const CUtensorMap *&mA, const CUtensorMap *&mB) -> int64_t {
+        if (GRP) {
+            const int j = group_job(grp.tile0, grp.njobs, T);
+            const ProductJob *J = grp.jobs + j;
+            a = J->a;
+            mA = &J->tmA;
+            mB = &J->tmB;
+            return T - __ldg(grp.tile0 + j);
+        }
+        a = a0;
+        mA = &tmA;
+        mB = &tmB;
+        return T;
+    };
 
     if (warp == 0) {
         if (lane == 0) {
-            tc::prefetch_tmap(&tmA);
-            tc::prefetch_tmap(&tmB);
+            if (!GRP) {
+                tc::prefetch_tmap(&tmA);
+                tc::prefetch_tmap(&tmB);
+            }
             int it = 0;
-            for (int64_t t = t0; t < a.ntiles && !aborted(bars); t += tstep) {
+            for (int64_t T = t0; T < total && !aborted(bars); T += tstep) {
+                ProductArgs a;
+                const CUtensorMap *mA, *mB;
+                const int64_t t = tile_job(T, a, mA, mB);
+                const int64_t per_mod = (int64_t)a.nyt * a.nxt;
                 const int mi = (int)(t / per_mod), r = (int)(t % per_mod);
                 const int y0 = (r / a.nxt) * (NP * BM) + (int)rank * BM, x0 = (r % a.nxt) * PBX;
                 for (int s = 0; s < a.nk; s++, it++) {
@@ -720,15 +833,15 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                     if (PAIR) {
                         const uint32_t full0 = tc::mapa(tc::smem_u32(&bars->full[st]), 0);
                         if (rank == 0) tc::mbar_arrive_expect_tx(&bars->full[st], 2 * STAGE);
-                        tc::tma_load_2d_pair(sa, &tmA, full0, s * BK, (2 * mi) * a.m + y0);
-                        tc::tma_load_2d_pair(sa + A_BYTES, &tmA, full0, s * BK, (2 * mi + 1) * a.m + y0);
-                        tc::tma_load_2d_pair(sa + 2 * A_BYTES, &tmB, full0, s * BK, (2 * mi + (int)rank) * a.n + x0);
+                        tc::tma_load_2d_pair(sa, mA, full0, s * BK, (2 * mi) * a.m + y0);
+                        tc::tma_load_2d_pair(sa + A_BYTES, mA, full0, s * BK, (2 * mi + 1) * a.m + y0);
+                        tc::tma_load_2d_pair(sa + 2 * A_BYTES, mB, full0, s * BK, (2 * mi + (int)rank) * a.n + x0);
                     } else {
                         tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                        tc::tma_load_2d(sa, &tmA, &bars->full[st], s * BK, (2 * mi) * a.m + y0);
-                        tc::tma_load_2d(sa + A_BYTES, &tmA, &bars->full[st], s * BK, (2 * mi + 1) * a.m + y0);
-                        tc::tma_load_2d(sa + 2 * A_BYTES, &tmB, &bars->full[st], s * BK, (2 * mi) * a.n + x0);
-                        tc::tma_load_2d(sa + 2 * A_BYTES + B_BYTES, &tmB, &bars->full[st], s * BK,
+                        tc::tma_load_2d(sa, mA, &bars->full[st], s * BK, (2 * mi) * a.m + y0);
+                        tc::tma_load_2d(sa + A_BYTES, mA, &bars->full[st], s * BK, (2 * mi + 1) * a.m + y0);
+                        tc::tma_load_2d(sa + 2 * A_BYTES, mB, &bars->full[st], s * BK, (2 * mi) * a.n + x0);
+                        tc::tma_load_2d(sa + 2 * A_BYTES + B_BYTES, mB, &bars->full[st], s * BK,
                                         (2 * mi + 1) * a.n + x0);
                     }
                 }
@@ -739,7 +852,11 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             const uint32_t idesc = tc::idesc_bf16_f32(NP * BM, 2 * PBX, 0, 0);
             int it = 0, lt = 0;
             bool ok = true;
-            for (int64_t t = t0; t < a.ntiles && ok; t += tstep, lt++) {
+            for (int64_t T = t0; T < total && ok; T += tstep, lt++) {
+                ProductArgs a;
+                const CUtensorMap *mA, *mB;
+                tile_job(T, a, mA, mB);
+                (void)mA, (void)mB;
                 const int b = lt & 1;
                 if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) { set_abort(bars, err); break; }
                 tc::fence_after_sync();
@@ -775,40 +892,48 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             }
         }
     } else {
-        // warp (2..9) -> lane quadrant warp % 4, output columns 32 * ((warp - 2) / 4) + [0, 32).
-        // All four accumulators' 32 columns are read first, so the buffer goes back to the
-        // MMA before the arithmetic.
-        const int quad = warp & 3, half = (warp - 2) >> 2;
+        // Two groups of 8 warps; group gb (warps 2..9, 10..17) owns TMEM buffer gb and so
+        // takes every other tile: the epilogues of two tiles run at once.  Within a
+        // group, warp -> lane quadrant warp % 4 and output columns 32 * half + [0, 32),
+        // read and reduced 16 columns at a time (the buffer goes back to the MMA after
+        // the second read).
+        const int quad = warp & 3, gb = (warp - 2) >> 3, half = ((warp - 2) >> 2) & 1;
         const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
         const uint32_t tempty0 = PAIR ? tc::mapa(tc::smem_u32(&bars->tempty[0]), 0) : 0;
-        int lt = 0;
-        for (int64_t t = t0; t < a.ntiles; t += tstep, lt++) {
+        int lt = gb;
+        for (int64_t T = t0 + gb * tstep; T < total; T += 2 * tstep, lt += 2) {
+            ProductArgs a;
+            const CUtensorMap *mA, *mB;
+            const int64_t t = tile_job(T, a, mA, mB);
+            (void)mA, (void)mB;
+            const int64_t per_mod = (int64_t)a.nyt * a.nxt;
             const int b = lt & 1;
             const int mi = (int)(t / per_mod), r = (int)(t % per_mod);
             const int y = (r / a.nxt) * (NP * BM) + (int)rank * BM + quad * 32 + lane;
             const int xh = (r % a.nxt) * PBX + half * 32;  // this warp's 32 output columns
             if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); break; }
             tc::fence_after_sync();
-            uint32_t D11[32], D10[32], D01[32], D00[32];
-            const uint32_t col = 256u * b + half * 32;
-            tc::tmem_ld32(lb + col, D11);
-            tc::tmem_ld32(lb + col + PBX, D10);
-            tc::tmem_ld32(lb + col + 2 * PBX, D01);
-            tc::tmem_ld32(lb + col + 3 * PBX, D00);
-            tc::tmem_ld_wait();
-            tc::fence_before_sync();
-            __syncwarp();
-            if (lane == 0) {
-                if (PAIR) tc::mbar_arrive_cluster(tempty0 + 8u * b);
-                else tc::mbar_arrive(&bars->tempty[b]);
-            }
             const ModConst mc = a.mods[mi];
             const float pf = (float)mc.p;
             const int64_t erow = (int64_t)y * a.npad + xh;  // entry index of this warp's first column
             __nv_bfloat16 *yplane = a.Y + (int64_t)(2 * mi) * 64;  // hi plane; lo plane 64 elements on
 #pragma unroll
             for (int c = 0; c < 32; c += 16) {
-                const uint32_t *d11 = D11 + c, *d10 = D10 + c, *d01 = D01 + c, *d00 = D00 + c;
+                uint32_t d11[16], d10[16], d01[16], d00[16];
+                const uint32_t col = 256u * b + half * 32 + c;
+                tc::tmem_ld16(lb + col, d11);
+                tc::tmem_ld16(lb + col + PBX, d10);
+                tc::tmem_ld16(lb + col + 2 * PBX, d01);
+                tc::tmem_ld16(lb + col + 3 * PBX, d00);
+                tc::tmem_ld_wait();
+                if (c == 16) {
+                    tc::fence_before_sync();
+                    __syncwarp();
+                    if (lane == 0) {
+                        if (PAIR) tc::mbar_arrive_cluster(tempty0 + 8u * b);
+                        else tc::mbar_arrive(&bars->tempty[b]);
+                    }
+                }
                 uint32_t phi[8], plo[8];
 #pragma unroll
                 for (int j = 0; j < 16; j += 2) {
@@ -893,6 +1018,11 @@ struct ReconArgs {
     int64_t cld, crs;
     int32_t cnlimbs;
 };
+// One product of a grouped reconstruction launch (its tiles start at entry tile 0).
+struct ReconJob {
+    CUtensorMap tmY, tmT;
+    ReconArgs a;
+};
 // Hand-off between the two epilogue warps of a TMEM lane quadrant (per entry slots).
 struct ReconXfer {
     uint64_t to1[4], to0[4], qready[4];  // mbarriers per quadrant: half 0 -> 1, half 1 -> 0, q ready
@@ -903,10 +1033,15 @@ struct ReconXfer {
     uint32_t drop0[128];                 // half 0's dropped-limb flags (bit 0 nonzero, bit 1 all ones)
 };
 
-template <int STAGES, bool PAIR>
+// Y's map is 3-D, [Ep/64 blocks][2P rows][64 entries]: the rows 2P .. 2Pp-1 of a
+// block's last K step lie outside it and read as zeros.  GRP: a grouped launch;
+// Mod's chunk values are then read from global memory (each product has its own),
+// and the epilogue's hand-offs take the form that holds for any sequence of N-tile
+// counts (see the half-0 wait at an entry tile's first N tile).
+template <int STAGES, bool PAIR, bool GRP>
 __global__ void __launch_bounds__(CTA_THREADS8, 1)
-    k_crt_recon(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmT, ReconArgs a,
-                uint32_t *err) {
+    k_crt_recon(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmT, ReconArgs a0,
+                Group<ReconJob> grp, uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = align1024(smem_raw);
     constexpr int NP = PAIR ? 2 : 1;
@@ -919,8 +1054,26 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t rank = PAIR ? tc::cluster_rank() : 0;
     const int64_t t0 = PAIR ? (blockIdx.x >> 1) : blockIdx.x, tstep = PAIR ? (gridDim.x >> 1) : gridDim.x;
-    for (int i = threadIdx.x; i < (a.Dout + 31) / 32 * 8; i += blockDim.x) svtab[i] = a.vtab[i];
-    ReconXfer *xf = reinterpret_cast<ReconXfer *>(reinterpret_cast<uint8_t *>(svtab) + (a.Dout + 31) / 32 * 32);
+    const int vwords = GRP ? 0 : (a0.Dout + 31) / 32 * 8;
+    for (int i = threadIdx.x; i < vwords; i += blockDim.x) svtab[i] = a0.vtab[i];
+    ReconXfer *xf = reinterpret_cast<ReconXfer *>(svtab + vwords);
+    // entry tiles [tbeg, total) in global numbering; tile_job maps one to its
+    // product's arguments and maps and to the entry tile within that product
+    const int64_t tbeg = GRP ? 0 : a0.mt0, total = GRP ? grp.tile0[grp.njobs] : a0.nmt;
+    auto tile_job = [&](int64_t T, ReconArgs &a, const CUtensorMap *&mY, const CUtensorMap *&mT) -> int64_t {
+        if (GRP) {
+            const int j = group_job(grp.tile0, grp.njobs, T);
+            const ReconJob *J = grp.jobs + j;
+            a = J->a;
+            mY = &J->tmY;
+            mT = &J->tmT;
+            return T - __ldg(grp.tile0 + j);
+        }
+        a = a0;
+        mY = &tmY;
+        mT = &tmT;
+        return T;
+    };
     if (threadIdx.x == 0)
         for (int qd = 0; qd < 4; qd++) {
             tc::mbar_init(&xf->to1[qd], 1);
@@ -955,10 +1108,15 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            tc::prefetch_tmap(&tmY);
-            tc::prefetch_tmap(&tmT);
+            if (!GRP) {
+                tc::prefetch_tmap(&tmY);
+                tc::prefetch_tmap(&tmT);
+            }
             int it = 0;
-            for (int64_t t = a.mt0 + t0; t < a.nmt && !aborted(bars); t += tstep) {
+            for (int64_t T = tbeg + t0; T < total && !aborted(bars); T += tstep) {
+                ReconArgs a;
+                const CUtensorMap *mY, *mT;
+                const int64_t t = tile_job(T, a, mY, mT);
                 const int blk0 = (int)(t * (2 * NP) + 2 * rank);  // this CTA's two 64-entry blocks
                 for (int j = 0; j < a.NT && !aborted(bars); j++) {
                     for (int s = 0; s < a.nk; s++, it++) {
@@ -973,14 +1131,14 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                         if (PAIR) {
                             const uint32_t full0 = tc::mapa(tc::smem_u32(&bars->full[st]), 0);
                             if (rank == 0) tc::mbar_arrive_expect_tx(&bars->full[st], 2 * STAGE);
-                            tc::tma_load_2d_pair(sa, &tmY, full0, 0, blk0 * a.kpad + s * BK);
-                            tc::tma_load_2d_pair(sa + BOX, &tmY, full0, 0, (blk0 + 1) * a.kpad + s * BK);
-                            tc::tma_load_2d_pair(sa + A_BYTES, &tmT, full0, s * BK, j * RBN + (int)rank * TROWS);
+                            tc::tma_load_3d_pair(sa, mY, full0, 0, s * BK, blk0);
+                            tc::tma_load_3d_pair(sa + BOX, mY, full0, 0, s * BK, blk0 + 1);
+                            tc::tma_load_2d_pair(sa + A_BYTES, mT, full0, s * BK, j * RBN + (int)rank * TROWS);
                         } else {
                             tc::mbar_arrive_expect_tx(&bars->full[st], STAGE);
-                            tc::tma_load_2d(sa, &tmY, &bars->full[st], 0, blk0 * a.kpad + s * BK);
-                            tc::tma_load_2d(sa + BOX, &tmY, &bars->full[st], 0, (blk0 + 1) * a.kpad + s * BK);
-                            tc::tma_load_2d(sa + A_BYTES, &tmT, &bars->full[st], s * BK, j * RBN);
+                            tc::tma_load_3d(sa, mY, &bars->full[st], 0, s * BK, blk0);
+                            tc::tma_load_3d(sa + BOX, mY, &bars->full[st], 0, s * BK, blk0 + 1);
+                            tc::tma_load_2d(sa + A_BYTES, mT, &bars->full[st], s * BK, j * RBN);
                         }
                     }
                 }
@@ -991,7 +1149,11 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             const uint32_t idesc = tc::idesc_bf16_f32(NP * BM, RBN, 1, 0);
             int it = 0, lt = 0;
             bool ok = true;
-            for (int64_t t = a.mt0 + t0; t < a.nmt && ok; t += tstep) {
+            for (int64_t T = tbeg + t0; T < total && ok; T += tstep) {
+                ReconArgs a;
+                const CUtensorMap *mY, *mT;
+                tile_job(T, a, mY, mT);
+                (void)mY, (void)mT;
                 for (int j = 0; j < a.NT && ok; j++, lt++) {
                     const int b = lt & 1;
                     if (lt >= 2 && !tc::mbar_wait(&bars->tempty[b], ((lt >> 1) & 1) ^ 1)) {
@@ -1038,7 +1200,16 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
         const uint32_t tempty0 = PAIR ? tc::mapa(tc::smem_u32(&bars->tempty[0]), 0) : 0;
         int lt = 0, ph1 = 0, ph0 = 0, phq = 0;  // tiles seen; hand-off phases consumed
         bool first = true, ok = true;
-        for (int64_t t = a.mt0 + t0; t < a.nmt && ok; t += tstep) {
+        for (int64_t T = tbeg + t0; T < total && ok; T += tstep) {
+            ReconArgs a;
+            const CUtensorMap *mY, *mT;
+            const int64_t t = tile_job(T, a, mY, mT);
+            (void)mY, (void)mT;
+            // UNI: half 1 hands on at the end of an entry tile only after its finalize,
+            // and half 0 takes that hand-off before it writes the next tile's slots (the
+            // only order that is safe when N-tile counts vary from tile to tile); else
+            // the one-N-tile case alone waits for the finalize
+            const bool UNI = GRP || a.NT == 1;
             const int64_t e = t * (NP * BM) + rank * BM + quad * 32 + lane;
             const int64_t er = e / a.ncols, ec = e - er * a.ncols;
             const bool live = e < a.E && ec < a.ccols;
@@ -1050,7 +1221,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             bool drop_nz = false, drop_ones = true;
             long long carry_final = 0;
             uint32_t nc_final = 1;
-            const bool last_t = t + tstep >= a.nmt;
+            const bool last_t = T + tstep >= total;
             for (int j = 0; j < a.NT; j++, lt++) {
                 const int b = lt & 1;
                 if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); ok = false; break; }
@@ -1063,12 +1234,12 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                 bool took0 = false;  // half 0: the hand-off from half 1 is already taken
                 if (j == 0) {
                     if (hf == 0) {
-                        // with one N tile per entry tile, the q, top0 and drop0 slots are free
-                        // only once half 1 is done with the previous entry tile (its finalize
-                        // included): take that hand-off before writing them, so that the slots
-                        // and qready never run a tile ahead.  With more N tiles, the hand-off
-                        // at j = 1 already orders them.
-                        if (!first && a.NT == 1) {
+                        // the q, top0 and drop0 slots are free only once half 1 is done with
+                        // the previous entry tile (its finalize included).  UNI: take that
+                        // hand-off before writing them, so that the slots and qready never run
+                        // a tile ahead.  Otherwise (the same N tiles, more than one, for every
+                        // entry tile) the hand-off at j = 1 already orders them.
+                        if (!first && UNI) {
                             if (!tc::mbar_wait(&xf->to0[quad], ph0 & 1)) { set_abort(bars, err); ok = false; break; }
                             ph0++;
                             took0 = true;
@@ -1123,7 +1294,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                     }
                     const int pos = pos0 + 32 * k;
                     if (k < k0 || !live || pos >= a.Dout) continue;
-                    const uint32_t *W = svtab + (pos >> 5) * 8;
+                    const uint32_t *W = (GRP ? a.vtab : svtab) + (pos >> 5) * 8;
                     long long A[7];
                     A[0] = c;
 #pragma unroll
@@ -1209,9 +1380,9 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                         xf->carry0[idx] = c;
                         xf->ripple0[idx] = nin;
                     }
-                    // after an entry's last N tile the hand-off waits for the finalize when the
-                    // entry tile has only that one (see half 0's early take at j = 0)
-                    if (j < a.NT - 1 || (a.NT > 1 && !last_t)) {
+                    // after an entry's last N tile the hand-off waits for the finalize under
+                    // UNI (see half 0's early take at j = 0)
+                    if (j < a.NT - 1 || (!UNI && !last_t)) {
                         __syncwarp();
                         if (lane == 0) tc::mbar_arrive(&xf->to0[quad]);
                     }
@@ -1257,7 +1428,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                 for (int li = written; li < a.cnlimbs; li++) a.climbs[(int64_t)li * a.cld + coff] = 0u;
                 a.csizes[coff] = top == 0 ? 0 : (neg ? -top : top);
             }
-            if (hf == 1 && !last_t && a.NT == 1) {
+            if (hf == 1 && !last_t && UNI) {
                 // the finalize is done with half 0's slots: hand on to half 0's next entry tile
                 __syncwarp();
                 if (lane == 0) tc::mbar_arrive(&xf->to0[quad]);
@@ -1857,78 +2028,194 @@ static gbmm_status launch_pairs(void (*kern)(KArgs...), int threads, int64_t wor
     return GBMM_OK;
 }
 
-// digits + residues of one operand into planes [2P][rowsR][kp] (A: a1, a0 per
-// modulus); B's table is weighted, so B's planes hold u = w b (u1, u0)
-static gbmm_status operand_residues(gbmm_handle h, crt_tables *t, const gbmm_mat &X, int transpose, int rowsR, int kdim,
-                                    int kp, int weighted, __nv_bfloat16 *R, cudaStream_t s) {
-    const int L = std::max(X.nlimbs, 1);
-    const int dxp = (4 * L + 63) / 64 * 64;
+// ---- launch plans of the four stages (one product, or one record of a grouped launch) ----------
+
+// digit-row length of an operand's entries: 4 digits per limb, padded to 64
+static int operand_dxp(const gbmm_mat &X) { return (4 * std::max(X.nlimbs, 1) + 63) / 64 * 64; }
+static size_t digits_bytes(const gbmm_mat &X) { return (size_t)X.rows * X.cols * operand_dxp(X) * 2 + 1024; }
+
+// Digits + residues of one operand into planes [2P][rowsR][kp] (A: a1, a0 per
+// modulus); B's table is weighted, so B's planes hold u = w b (u1, u0).  Only
+// the first kdim columns of each plane row are written.
+struct OperandPlan {
+    DigitArgs da;
+    dim3 dgrid;
+    int balanced = 0, gsteps = 0;
+    bool pair = false, mc = false;
+    CUtensorMap tmD, tmT, tmR;
+    ResidueArgs ra;
+    size_t smem = 0;
+};
+static gbmm_status plan_operand(crt_tables *t, const gbmm_mat &X, int transpose, int rowsR, int kdim, int kp, int weighted,
+                                __nv_bfloat16 *R, __nv_bfloat16 *D, bool grouped, OperandPlan &op) {
+    const int dxp = operand_dxp(X);
     const int64_t E = (int64_t)X.rows * X.cols;
-    __nv_bfloat16 *D = (__nv_bfloat16 *)arena_alloc(h, (size_t)E * dxp * 2 + 1024);
-    if (!D) return set_error(GBMM_ERR_NOMEM, "crt: workspace for digits");
+    if (E > (int64_t)INT32_MAX - 4 * BM) return set_error(GBMM_ERR_UNSUPPORTED, "crt: more than 2^31 entries in one operand");
     const int nk = dxp / BK;
     // unsigned byte digits up to 512 per row; longer rows in balanced digits, whose
     // groups are nearly twice as long (fewer groups, wider table tiles)
-    const int balanced = nk > RES_GROUP_STEPS_U;
-    const int gsteps = balanced ? RES_GROUP_STEPS_B : RES_GROUP_STEPS_U;
-    {
-        DigitArgs a;
-        a.limbs = X.limbs; a.sizes = X.sizes; a.ld = X.ld; a.rs = X.rs; a.rows = X.rows; a.cols = X.cols;
-        a.nlimbs = X.nlimbs; a.transpose = transpose; a.dxp = dxp; a.out = D;
-        dim3 grid((unsigned)((X.cols + 31) / 32), (unsigned)((X.rows + 3) / 4), (unsigned)((dxp / 4 + 63) / 64));
-        LaunchScope ls_("k_crt_digits", s);
-        if (balanced) k_crt_digits<true><<<grid, 256, 0, s>>>(a);
-        else k_crt_digits<false><<<grid, 256, 0, s>>>(a);
-        GBMM_CUDA_TRY(cudaGetLastError());
-    }
+    op.balanced = nk > RES_GROUP_STEPS_U;
+    op.gsteps = op.balanced ? RES_GROUP_STEPS_B : RES_GROUP_STEPS_U;
+    DigitArgs &a = op.da;
+    memset(&a, 0, sizeof a);
+    a.limbs = X.limbs; a.sizes = X.sizes; a.ld = X.ld; a.rs = X.rs; a.rows = X.rows; a.cols = X.cols;
+    a.nlimbs = X.nlimbs; a.transpose = transpose; a.dxp = dxp; a.out = D;
+    op.dgrid = dim3((unsigned)((X.cols + 31) / 32), (unsigned)((X.rows + 3) / 4), (unsigned)((dxp / 4 + 63) / 64));
     __nv_bfloat16 *T = nullptr;
     GBMM_TRY(residue_table(t, dxp, weighted, &T));
-    const int G = (nk + gsteps - 1) / gsteps;
+    const int G = (nk + op.gsteps - 1) / op.gsteps;
     int BN = 256;
     while (BN * G > 256) BN /= 2;
     if (BN < 64) return set_error(GBMM_ERR_UNSUPPORTED, "crt: entries longer than 30720 bits");
-    const bool pair = residue_pair(nk), mc = !pair && residue_mc(nk);
-    const int NP = pair || mc ? 2 : 1;
-    CUtensorMap tmD, tmT, tmR;
-    GBMM_TRY(make_map(&tmD, D, dxp, E, dxp, BK, BM));
-    GBMM_TRY(make_map(&tmT, T, dxp, residue_cols(t->P), dxp, BK, BN / NP));
-    ResidueArgs a;
-    if (E > (int64_t)INT32_MAX - 4 * BM)
-        return set_error(GBMM_ERR_UNSUPPORTED, "crt: more than 2^31 entries in one operand");
-    a.kdim = kdim; a.E = (int32_t)E; a.nk = nk;
-    a.BN = BN; a.G = G; a.P = t->P; a.R = R; a.plane = (int64_t)rowsR * kp; a.kp = kp;
-    a.ncols = residue_cols(t->P);
-    a.n_ntiles = (a.ncols + BN - 1) / BN;
-    a.ntiles = (int32_t)((int64_t)a.n_ntiles * ((E + NP * BM - 1) / (NP * BM)));
+    op.pair = !grouped && residue_pair(nk);
+    op.mc = !grouped && !op.pair && residue_mc(nk);
+    const int NP = op.pair || op.mc ? 2 : 1;
+    GBMM_TRY(make_map(&op.tmD, D, dxp, E, dxp, BK, BM));
+    GBMM_TRY(make_map(&op.tmT, T, dxp, residue_cols(t->P), dxp, BK, BN / NP));
+    ResidueArgs &r = op.ra;
+    memset(&r, 0, sizeof r);
+    r.kdim = kdim; r.E = (int32_t)E; r.nk = nk;
+    r.BN = BN; r.G = G; r.P = t->P; r.R = R; r.plane = (int64_t)rowsR * kp; r.kp = kp;
+    r.ncols = residue_cols(t->P);
+    r.n_ntiles = (r.ncols + BN - 1) / BN;
+    r.ntiles = (int32_t)((int64_t)r.n_ntiles * ((E + NP * BM - 1) / (NP * BM)));
     // 32-entry boxes of one plane row: [32 planes][1 row][32 entries]
-    a.tma_out = kdim % 32 == 0;
-    if (a.tma_out) GBMM_TRY(make_map_planes(&tmR, R, kdim, rowsR, 2 * t->P, kp, a.plane));
-    else tmR = tmD;  // unused
-    const int stages = pair ? RES_STAGES_PAIR : RES_STAGES;
-    const size_t sm = smem_bytes(stages, BM * 128 + (size_t)(pair ? BN / 2 : BN) * 128) +
-                      (size_t)RES_EPI_WARPS * (pair ? 2 : 1) * RES_STG_BYTES;
+    r.tma_out = kdim % 32 == 0;
+    if (r.tma_out) GBMM_TRY(make_map_planes(&op.tmR, R, kdim, rowsR, 2 * t->P, kp, r.plane));
+    else op.tmR = op.tmD;  // unused
+    // a grouped launch sizes every stage for 256 table columns
+    const int bcols = grouped ? 256 : (op.pair ? BN / 2 : BN);
+    op.smem = smem_bytes(op.pair ? RES_STAGES_PAIR : RES_STAGES, BM * 128 + (size_t)bcols * 128) +
+              (size_t)RES_EPI_WARPS * (op.pair ? 2 : 1) * RES_STG_BYTES;
+    return GBMM_OK;
+}
+
+static gbmm_status launch_operand(const OperandPlan &op, cudaStream_t s) {
+    {
+        LaunchScope ls_("k_crt_digits", s);
+        const Group<DigitJob> none{nullptr, nullptr, 0};
+        if (op.balanced) k_crt_digits<true, false><<<op.dgrid, 256, 0, s>>>(op.da, none);
+        else k_crt_digits<false, false><<<op.dgrid, 256, 0, s>>>(op.da, none);
+        GBMM_CUDA_TRY(cudaGetLastError());
+    }
+    const Group<ResidueJob> none{nullptr, nullptr, 0};
+    const size_t sm = op.smem;
     LaunchScope ls_("k_crt_residue", s);
 #define RESIDUE_LAUNCH(GS_)                                                                                          \
     do {                                                                                                             \
-        if (mc) {                                                                                                    \
-            GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false, true, GS_>, sm));                       \
-            GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES, false, true, GS_>, RES_THREADS, a.ntiles, sm, s, tmD,   \
-                                  tmT, tmR, a, device_error_word()));                                                \
-        } else if (pair) {                                                                                           \
-            GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES_PAIR, true, false, GS_>, sm));                  \
-            GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES_PAIR, true, false, GS_>, RES_THREADS, a.ntiles, sm, s,  \
-                                  tmD, tmT, tmR, a, device_error_word()));                                           \
+        if (op.mc) {                                                                                                 \
+            GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false, true, GS_, false>, sm));                \
+            GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES, false, true, GS_, false>, RES_THREADS, op.ra.ntiles, sm, \
+                                  s, op.tmD, op.tmT, op.tmR, op.ra, none, device_error_word()));                     \
+        } else if (op.pair) {                                                                                        \
+            GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES_PAIR, true, false, GS_, false>, sm));           \
+            GBMM_TRY(launch_pairs(k_crt_residue<RES_STAGES_PAIR, true, false, GS_, false>, RES_THREADS,            \
+                                  op.ra.ntiles, sm, s, op.tmD, op.tmT, op.tmR, op.ra, none, device_error_word()));   \
         } else {                                                                                                     \
-            GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false, false, GS_>, sm));                      \
-            dim3 grid((unsigned)std::min<int64_t>(a.ntiles, num_sms()));                                             \
-            k_crt_residue<RES_STAGES, false, false, GS_><<<grid, RES_THREADS, sm, s>>>(tmD, tmT, tmR, a,             \
-                                                                                     device_error_word());         \
+            GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false, false, GS_, false>, sm));               \
+            dim3 grid((unsigned)std::min<int64_t>(op.ra.ntiles, num_sms()));                                         \
+            k_crt_residue<RES_STAGES, false, false, GS_, false><<<grid, RES_THREADS, sm, s>>>(                       \
+                op.tmD, op.tmT, op.tmR, op.ra, none, device_error_word());                                           \
         }                                                                                                            \
     } while (0)
-    if (gsteps == RES_GROUP_STEPS_B) RESIDUE_LAUNCH(RES_GROUP_STEPS_B);
+    if (op.gsteps == RES_GROUP_STEPS_B) RESIDUE_LAUNCH(RES_GROUP_STEPS_B);
     else RESIDUE_LAUNCH(RES_GROUP_STEPS_U);
 #undef RESIDUE_LAUNCH
     GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+// Product GEMM over residue planes RA [2P][m][kp] and RB [2P][n][kp].  The maps'
+// inner extent is k, not kp: the columns k .. kp-1 of the last K step lie outside
+// and read as zeros, so the planes need no cleared padding.
+struct ProductPlan {
+    CUtensorMap tmA, tmB;
+    ProductArgs pa;
+    bool pair = false;
+    size_t smem = 0;
+};
+static gbmm_status plan_product(crt_tables *t, __nv_bfloat16 *RA, __nv_bfloat16 *RB, __nv_bfloat16 *Y, int m, int k, int n,
+                                int kp, int npad, int tiles, bool grouped, ProductPlan &pp) {
+    const int P = t->P;
+    GBMM_TRY(make_map(&pp.tmA, RA, k, (uint64_t)2 * P * m, kp, BK, BM));
+    GBMM_TRY(make_map(&pp.tmB, RB, k, (uint64_t)2 * P * n, kp, BK, PBX));
+    ProductArgs &pa = pp.pa;
+    memset(&pa, 0, sizeof pa);
+    pa.m = m; pa.n = n; pa.npad = npad; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y;
+    pa.yblk = (int64_t)2 * t->Pp * 64;
+    // CTA pairs pay off once the K loop is long enough to hide the pair's per-tile
+    // synchronisation (measured: faster at k = 512, slower at k = 256); a plan may
+    // fix the form (tiles: 1 one-CTA tiles, 2 CTA pairs); grouped launches use one-CTA tiles
+    pp.pair = !grouped && (tiles == 0 ? pa.nk >= PROD_PAIR_MIN_NK : tiles == 2);
+    const int NP = pp.pair ? 2 : 1;
+    pa.nyt = (m + NP * BM - 1) / (NP * BM);
+    pa.nxt = (n + PBX - 1) / PBX;
+    pa.ntiles = (int64_t)P * pa.nyt * pa.nxt;
+    pp.smem = pp.pair ? smem_bytes(PROD_STAGES_PAIR, 2 * BM * 128 + PBX * 128)
+                      : smem_bytes(PROD_STAGES, 2 * BM * 128 + 2 * PBX * 128);
+    return GBMM_OK;
+}
+
+static gbmm_status launch_product(const ProductPlan &pp, cudaStream_t s) {
+    const Group<ProductJob> none{nullptr, nullptr, 0};
+    uint32_t *err = device_error_word();
+    LaunchScope ls_("k_crt_product", s);
+    if (pp.pair) {
+        GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES_PAIR, true, false>, pp.smem));
+        GBMM_TRY(launch_pairs(k_crt_product<PROD_STAGES_PAIR, true, false>, PROD_THREADS, pp.pa.ntiles, pp.smem, s,
+                              pp.tmA, pp.tmB, pp.pa, none, err));
+    } else {
+        GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES, false, false>, pp.smem));
+        dim3 grid((unsigned)std::min<int64_t>(pp.pa.ntiles, num_sms()));
+        k_crt_product<PROD_STAGES, false, false><<<grid, PROD_THREADS, pp.smem, s>>>(pp.tmA, pp.tmB, pp.pa, none, err);
+    }
+    GBMM_CUDA_TRY(cudaGetLastError());
+    return GBMM_OK;
+}
+
+// Y as a 3-D map [Ep/64 blocks][2P rows][64 entries] with a block pitch of 2Pp
+// rows: boxes of 64 entries x 64 rows; rows 2P .. 2Pp-1 read as zeros.
+static gbmm_status make_map_yblocks(CUtensorMap *m, const void *ptr, uint64_t rows, uint64_t rows_pitch, uint64_t blocks) {
+    PFN_encodeTiled enc = get_encode();
+    if (!enc) return set_error(GBMM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    if (reinterpret_cast<uintptr_t>(ptr) & 15) return set_error(GBMM_ERR_INVALID, "tensor map base not 16-byte aligned");
+    cuuint64_t dims[3] = {64, rows, blocks};
+    cuuint64_t strides[2] = {64 * 2, rows_pitch * 64 * 2};
+    cuuint32_t box[3] = {64, (cuuint32_t)BK, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(ptr), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(GBMM_ERR_CUDA, "cuTensorMapEncodeTiled (Y blocks) failed (%d)", (int)r);
+    return GBMM_OK;
+}
+
+// Reconstruction of C (m x n, Y's entries in rows of npad) from Y.
+struct ReconPlan {
+    CUtensorMap tmY, tmT;
+    ReconArgs ra;
+    bool pair = false;
+    size_t smem = 0;
+};
+static gbmm_status plan_recon(crt_tables *t, __nv_bfloat16 *Y, int m, int n, int npad, const gbmm_mat &c, int tiles,
+                              bool grouped, ReconPlan &rp) {
+    const int64_t E = (int64_t)m * npad, Ep = (E + 63) / 64 * 64;
+    GBMM_TRY(make_map_yblocks(&rp.tmY, Y, (uint64_t)2 * t->P, (uint64_t)2 * t->Pp, (uint64_t)(Ep / 64)));
+    // CTA pairs once the K loop over the 2Pp moduli digits is long enough (see the
+    // product), unless the plan fixes the form; grouped launches use CTA pairs
+    rp.pair = grouped || (tiles == 0 ? 2 * t->Pp / BK >= PROD_PAIR_MIN_NK : tiles == 2);
+    const int NP = rp.pair ? 2 : 1, TROWS = 256 / NP;
+    GBMM_TRY(make_map(&rp.tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RTAB, 2 * t->Pp, BK, TROWS));
+    ReconArgs &ra = rp.ra;
+    memset(&ra, 0, sizeof ra);
+    ra.E = E; ra.ncols = npad; ra.ccols = n; ra.nk = 2 * t->Pp / BK; ra.NT = (SROWS + t->Dout + 255) / 256;
+    ra.Dout = t->Dout; ra.vtab = t->d_vtab; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
+    ra.cnlimbs = c.nlimbs; ra.kpad = 2 * t->Pp;
+    ra.mt0 = 0;
+    ra.nmt = (E + NP * BM - 1) / (NP * BM);
+    // a grouped launch reads Mod's chunk values from global memory
+    const size_t extra = (grouped ? 0 : (size_t)(t->Dout + 31) / 32 * 32) + sizeof(ReconXfer) + 64;
+    rp.smem = smem_bytes(rp.pair ? REC_STAGES_PAIR : REC_STAGES, BM * 128 + TROWS * 128) + extra;
     return GBMM_OK;
 }
 
@@ -1938,18 +2225,19 @@ int crt_moduli(int64_t bits_a, int64_t bits_b, int k) {
     return moduli_for_bits(bits_a + bits_b + lg + 2 + 16);
 }
 
-// device workspace (bytes) one crt_matmul call carves from the arena
-static size_t crt_workspace(const gbmm_mat &a, const gbmm_mat &b, const gbmm_mat &, int64_t bits_a, int64_t bits_b,
-                            int nprimes) {
+// device workspace (bytes) of one single-pass product: residue planes, Y, and
+// digits (one operand's at a time, or both when `both_digits`)
+static size_t crt_workspace(const gbmm_mat &a, const gbmm_mat &b, int64_t bits_a, int64_t bits_b, int nprimes,
+                            bool both_digits) {
     const int m = a.rows, k = a.cols, n = b.cols;
     int P = nprimes > 0 ? nprimes : crt_moduli(bits_a, bits_b, k);
     if (P <= 0) return 0;
     const int Pp = (2 * P + 63) / 64 * 32;
     const int kp = (k + 63) / 64 * 64;
     const int64_t Ep = ((int64_t)m * ((n + YPAD - 1) / YPAD * YPAD) + 63) / 64 * 64;
-    const int dxa = (4 * std::max(a.nlimbs, 1) + 63) / 64 * 64, dxb = (4 * std::max(b.nlimbs, 1) + 63) / 64 * 64;
+    const size_t da = align256(digits_bytes(a)), db = align256(digits_bytes(b));
     return align256((size_t)2 * P * m * kp * 2) + align256((size_t)2 * P * n * kp * 2) + align256((size_t)2 * Pp * Ep * 2) +
-           std::max(align256((size_t)m * k * dxa * 2 + 1024), align256((size_t)k * n * dxb * 2 + 1024)) + 8192;
+           (both_digits ? da + db : std::max(da, db)) + 8192;
 }
 
 bool crt_feasible(int la, int lb, int k) {
@@ -1958,13 +2246,16 @@ bool crt_feasible(int la, int lb, int k) {
     return P > 0 && P <= 1023 && 4 * std::max(la, lb) <= 4 * RES_GROUP_STEPS_B * BK;
 }
 
+static gbmm_mat shape_only(int rows, int cols, int nlimbs) {
+    gbmm_mat x;
+    memset(&x, 0, sizeof x);
+    x.rows = rows; x.cols = cols; x.nlimbs = nlimbs;
+    return x;
+}
+
 size_t crt_workspace_bytes(int la, int lb, int m, int k, int n, int cn) {
-    gbmm_mat a, b, c;
-    memset(&a, 0, sizeof a); memset(&b, 0, sizeof b); memset(&c, 0, sizeof c);
     const int kc = std::min(k, PROD_MAX_K);
-    a.rows = m; a.cols = kc; a.nlimbs = la;
-    b.rows = kc; b.cols = n; b.nlimbs = lb;
-    size_t ws = crt_workspace(a, b, c, 32LL * la, 32LL * lb, 0);
+    size_t ws = crt_workspace(shape_only(m, kc, la), shape_only(kc, n, lb), 32LL * la, 32LL * lb, 0, false);
     // an accumulating chunk adds a product-sized temporary
     if (k > kc) ws += align256((size_t)m * n * (std::max(cn, la + lb + 4) + 1) * 4) + 8192;
     return ws;
@@ -1990,7 +2281,7 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         size_t mark = arena_mark(h);
         const int cn = std::max(c.nlimbs, (int)((bits_a + bits_b + 64) / 32) + 2);
         size_t need = align256((size_t)m * n * cn * 4) + align256((size_t)m * n * 4) + 4096;
-        GBMM_TRY(arena_reserve(h, need + crt_workspace(a, b, c, bits_a, bits_b, nprimes)));
+        GBMM_TRY(arena_reserve(h, need + crt_workspace(a, b, bits_a, bits_b, nprimes, false)));
         gbmm_mat T;
         T.rows = m; T.cols = n; T.nlimbs = cn; T.pad_ = 0; T.rs = n; T.ld = (int64_t)m * n;
         T.limbs = (uint32_t *)arena_alloc(h, (size_t)m * n * cn * 4);
@@ -2024,90 +2315,57 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
     const int npad = (n + YPAD - 1) / YPAD * YPAD;
     const int64_t E = (int64_t)m * npad;
     const int64_t Ep = (E + 63) / 64 * 64;
-    const int dxa = (4 * std::max(a.nlimbs, 1) + 63) / 64 * 64, dxb = (4 * std::max(b.nlimbs, 1) + 63) / 64 * 64;
-    (void)dxa; (void)dxb;
-    GBMM_TRY(arena_reserve(h, crt_workspace(a, b, c, bits_a, bits_b, P)));
+    GBMM_TRY(arena_reserve(h, crt_workspace(a, b, bits_a, bits_b, P, false)));
     size_t mark = arena_mark(h);
     __nv_bfloat16 *RA = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * P * m * kp * 2);
     __nv_bfloat16 *RB = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * P * n * kp * 2);
     __nv_bfloat16 *Y = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * t->Pp * Ep * 2);
     if (!RA || !RB || !Y) return set_error(GBMM_ERR_NOMEM, "crt: workspace");
-    if (kp != k) {
-        GBMM_CUDA_TRY(cudaMemsetAsync(RA, 0, (size_t)2 * P * m * kp * 2, s));
-        GBMM_CUDA_TRY(cudaMemsetAsync(RB, 0, (size_t)2 * P * n * kp * 2, s));
-    }
-    // Y is blocked [Ep/64][2Pp][64]; the padding rows 2P..2Pp-1 of every block meet
-    // zero table columns but must not hold NaN patterns, so they are cleared.  Padding
-    // entries E..Ep-1 only reach accumulator rows that are never stored.
-    if (t->Pp != P)
-        GBMM_CUDA_TRY(cudaMemset2DAsync(Y + (size_t)2 * P * 64, (size_t)2 * t->Pp * 64 * 2, 0,
-                                        (size_t)(2 * t->Pp - 2 * P) * 64 * 2, (size_t)(Ep / 64), s));
+    // Nothing is cleared: the product reads RA / RB through maps k columns wide and
+    // Y through a map 2P rows deep per 64-entry block, and the padding entries
+    // E .. Ep-1 of Y only reach accumulator rows that are never stored.
     {
         size_t mk = arena_mark(h);
-        GBMM_TRY(operand_residues(h, t, a, 0, m, k, kp, 0, RA, s));
+        OperandPlan op;
+        __nv_bfloat16 *D = (__nv_bfloat16 *)arena_alloc(h, digits_bytes(a));
+        if (!D) return set_error(GBMM_ERR_NOMEM, "crt: workspace for digits");
+        GBMM_TRY(plan_operand(t, a, 0, m, k, kp, 0, RA, D, false, op));
+        GBMM_TRY(launch_operand(op, s));
         arena_release(h, mk);
         if (hk && hk->b_ready) GBMM_CUDA_TRY(cudaStreamWaitEvent(s, hk->b_ready, 0));
-        GBMM_TRY(operand_residues(h, t, b, 1, n, k, kp, 1, RB, s));
+        D = (__nv_bfloat16 *)arena_alloc(h, digits_bytes(b));
+        if (!D) return set_error(GBMM_ERR_NOMEM, "crt: workspace for digits");
+        GBMM_TRY(plan_operand(t, b, 1, n, k, kp, 1, RB, D, false, op));
+        GBMM_TRY(launch_operand(op, s));
         arena_release(h, mk);
     }
-    uint32_t *err = device_error_word();
     {
-        CUtensorMap tmA, tmB;
-        GBMM_TRY(make_map(&tmA, RA, kp, (uint64_t)2 * P * m, kp, BK, BM));
-        GBMM_TRY(make_map(&tmB, RB, kp, (uint64_t)2 * P * n, kp, BK, PBX));
-        ProductArgs pa;
-        pa.m = m; pa.n = n; pa.npad = npad; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y; pa.yblk = (int64_t)2 * t->Pp * 64;
-        // CTA pairs pay off once the K loop is long enough to hide the pair's per-tile
-        // synchronisation (measured: faster at k = 512, slower at k = 256); a plan may
-        // fix the form (h->crt_tiles: 1 one-CTA tiles, 2 CTA pairs)
-        const bool pair = h->crt_tiles == 0 ? pa.nk >= PROD_PAIR_MIN_NK : h->crt_tiles == 2;
-        const int NP = pair ? 2 : 1;
-        pa.nyt = (m + NP * BM - 1) / (NP * BM);
-        pa.nxt = (n + PBX - 1) / PBX;
-        pa.ntiles = (int64_t)P * pa.nyt * pa.nxt;
-        LaunchScope ls_("k_crt_product", s);
-        if (pair) {
-            const size_t sm = smem_bytes(PROD_STAGES_PAIR, 2 * BM * 128 + PBX * 128);
-            GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES_PAIR, true>, sm));
-            GBMM_TRY(launch_pairs(k_crt_product<PROD_STAGES_PAIR, true>, CTA_THREADS8, pa.ntiles, sm, s, tmA, tmB, pa,
-                                  err));
-        } else {
-            const size_t sm = smem_bytes(PROD_STAGES, 2 * BM * 128 + 2 * PBX * 128);
-            GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES, false>, sm));
-            dim3 grid((unsigned)std::min<int64_t>(pa.ntiles, num_sms()));
-            k_crt_product<PROD_STAGES, false><<<grid, CTA_THREADS8, sm, s>>>(tmA, tmB, pa, err);
-        }
-        GBMM_CUDA_TRY(cudaGetLastError());
+        ProductPlan pp;
+        GBMM_TRY(plan_product(t, RA, RB, Y, m, k, n, kp, npad, h->crt_tiles, false, pp));
+        GBMM_TRY(launch_product(pp, s));
     }
     {
-        CUtensorMap tmY, tmT;
-        GBMM_TRY(make_map(&tmY, Y, 64, (uint64_t)(Ep / 64) * 2 * t->Pp, 64, 64, BK));
-        // CTA pairs once the K loop over the 2Pp moduli digits is long enough (see the
-        // product), unless the plan fixes the form
-        const bool pair = h->crt_tiles == 0 ? 2 * t->Pp / BK >= PROD_PAIR_MIN_NK : h->crt_tiles == 2;
-        const int NP = pair ? 2 : 1, TROWS = 256 / NP;
-        GBMM_TRY(make_map(&tmT, t->d_recon, 2 * t->Pp, (uint64_t)t->NT * RTAB, 2 * t->Pp, BK, TROWS));
-        ReconArgs ra;
-        ra.E = E; ra.ncols = npad; ra.ccols = n; ra.nk = 2 * t->Pp / BK; ra.NT = (SROWS + t->Dout + 255) / 256; ra.Dout = t->Dout;
-        ra.vtab = t->d_vtab; ra.climbs = c.limbs; ra.csizes = c.sizes; ra.cld = c.ld; ra.crs = c.rs;
-        ra.cnlimbs = c.nlimbs; ra.kpad = 2 * t->Pp;
-        const int64_t nmt = (E + NP * BM - 1) / (NP * BM);
-        const size_t extra = (size_t)(t->Dout + 31) / 32 * 32 + sizeof(ReconXfer) + 64;
-        const size_t sm = smem_bytes(pair ? REC_STAGES_PAIR : REC_STAGES, BM * 128 + TROWS * 128) + extra;
-        if (pair) GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES_PAIR, true>, sm));
-        else GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES, false>, sm));
+        ReconPlan rp;
+        GBMM_TRY(plan_recon(t, Y, m, n, npad, c, h->crt_tiles, false, rp));
+        ReconArgs ra = rp.ra;
+        const int64_t nmt = ra.nmt;
+        const Group<ReconJob> none{nullptr, nullptr, 0};
+        uint32_t *err = device_error_word();
+        if (rp.pair) GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES_PAIR, true, false>, rp.smem));
+        else GBMM_TRY(set_smem((const void *)k_crt_recon<REC_STAGES, false, false>, rp.smem));
+        const int NP = rp.pair ? 2 : 1;
         // one launch, or (stage hooks) entry ranges each followed by an event
         const int parts = hk ? (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)hk->parts, (int64_t)CRT_MAX_PARTS, nmt})) : 1;
         for (int pi = 0; pi < parts; pi++) {
             ra.mt0 = nmt * pi / parts;
             ra.nmt = nmt * (pi + 1) / parts;
             LaunchScope ls_("k_crt_recon", s);
-            if (pair) {
-                GBMM_TRY(launch_pairs(k_crt_recon<REC_STAGES_PAIR, true>, CTA_THREADS8, ra.nmt - ra.mt0, sm, s, tmY, tmT,
-                                      ra, err));
+            if (rp.pair) {
+                GBMM_TRY(launch_pairs(k_crt_recon<REC_STAGES_PAIR, true, false>, CTA_THREADS8, ra.nmt - ra.mt0, rp.smem, s,
+                                      rp.tmY, rp.tmT, ra, none, err));
             } else {
                 dim3 grid((unsigned)std::min<int64_t>(ra.nmt - ra.mt0, num_sms()));
-                k_crt_recon<REC_STAGES, false><<<grid, CTA_THREADS8, sm, s>>>(tmY, tmT, ra, err);
+                k_crt_recon<REC_STAGES, false, false><<<grid, CTA_THREADS8, rp.smem, s>>>(rp.tmY, rp.tmT, ra, none, err);
             }
             GBMM_CUDA_TRY(cudaGetLastError());
             if (hk && parts > 1) {
@@ -2121,6 +2379,231 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
         if (hk && parts > 1) hk->parts_done = parts;
     }
     arena_release(h, mark);
+    return GBMM_OK;
+}
+
+// ---- grouped launches -------------------------------------------------------------------------
+// The CRT products of a batch, collected without launching: every product's
+// workspace is carved at once, its stage records go into per-stage lists, and
+// each stage then runs as ONE persistent launch per kernel form over the tiles of
+// all products (digits and residues by digit form, products on one-CTA tiles,
+// reconstructions on CTA pairs).  Records are ordered by the cost of one tile,
+// largest first, so that the long tiles start in the first wave.
+struct crt_group {
+    struct Rec {
+        std::vector<char> bytes;  // one record
+        int64_t tiles = 0;
+        double cost = 0;  // per tile
+    };
+    // dig / res by digit form (unsigned, balanced); rec[1]: products with a post step
+    std::vector<Rec> dig[2], res[2], prod, rec[2];
+    std::vector<std::function<gbmm_status(cudaStream_t)>> post;
+    struct Sect {
+        size_t jobs_off = 0, tile0_off = 0;
+        int n = 0;
+        int64_t total = 0;
+    };
+    Sect sdig[2], sres[2], sprod, srec[2];
+    size_t smem_res = 0, smem_prod = 0, smem_rec = 0;
+    std::vector<char> blob;
+};
+
+crt_group *crt_group_create() { return new crt_group(); }
+void crt_group_destroy(crt_group *g) { delete g; }
+bool crt_group_empty(const crt_group *g) { return g->prod.empty() && g->post.empty(); }
+void crt_group_post(crt_group *g, std::function<gbmm_status(cudaStream_t)> f) { g->post.push_back(std::move(f)); }
+
+size_t crt_group_ws(int la, int lb, int m, int k, int n) {
+    return crt_workspace(shape_only(m, k, la), shape_only(k, n, lb), 32LL * la, 32LL * lb, 0, true) + 2048;
+}
+
+template <typename J>
+static crt_group::Rec make_rec(const J &j, int64_t tiles, double cost) {
+    crt_group::Rec r;
+    r.bytes.resize(sizeof(J));
+    memcpy(r.bytes.data(), &j, sizeof(J));
+    r.tiles = tiles;
+    r.cost = cost;
+    return r;
+}
+
+gbmm_status crt_group_add(gbmm_handle h, crt_group *g, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b,
+                          int64_t bits_a, int64_t bits_b, int nprimes, const crt_halves *halves) {
+    const int m = a.rows, k = a.cols, n = b.cols;
+    if (m == 0 || n == 0 || k == 0 || k > PROD_MAX_K)
+        return set_error(GBMM_ERR_UNSUPPORTED, "crt group: needs a nonempty single-pass product");
+    const int P = nprimes > 0 ? nprimes : crt_moduli(bits_a, bits_b, k);
+    if (P <= 0 || P > 1023)
+        return set_error(GBMM_ERR_UNSUPPORTED, "crt: product bound needs %d moduli (at most 1023)", P);
+    crt_tables *t = nullptr;
+    GBMM_TRY(get_tables(h->crt, P, &t));
+    if (!get_encode()) return set_error(GBMM_ERR_CUDA, "crt: no tensor-map encoder");
+    const int kp = (k + 63) / 64 * 64;
+    const int npad = (n + YPAD - 1) / YPAD * YPAD;
+    const int64_t Ep = ((int64_t)m * npad + 63) / 64 * 64;
+    __nv_bfloat16 *RA = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * P * m * kp * 2);
+    __nv_bfloat16 *RB = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * P * n * kp * 2);
+    __nv_bfloat16 *Y = (__nv_bfloat16 *)arena_alloc(h, (size_t)2 * t->Pp * Ep * 2);
+    __nv_bfloat16 *DA = (__nv_bfloat16 *)arena_alloc(h, digits_bytes(a));
+    __nv_bfloat16 *DB = (__nv_bfloat16 *)arena_alloc(h, digits_bytes(b));
+    if (!RA || !RB || !Y || !DA || !DB) return set_error(GBMM_ERR_NOMEM, "crt group: workspace");
+    for (int side = 0; side < 2; side++) {
+        OperandPlan op;
+        if (side == 0) GBMM_TRY(plan_operand(t, a, 0, m, k, kp, 0, RA, DA, true, op));
+        else GBMM_TRY(plan_operand(t, b, 1, n, k, kp, 1, RB, DB, true, op));
+        if (halves && halves->side == side) {
+            // the stacked operand's digit rows straight from x's two limb halves: the
+            // high half's rows follow the low half's (A: rows m.., B: columns n..); both
+            // halves carry x's sign, and digits past a half's limbs read as zeros
+            const gbmm_mat &x = halves->x;
+            const int64_t xe = (int64_t)x.rows * x.cols;
+            for (int hf = 0; hf < 2; hf++) {
+                DigitJob dj;
+                memset(&dj, 0, sizeof dj);
+                dj.a = op.da;
+                dj.a.limbs = x.limbs + (hf ? (int64_t)halves->hl * x.ld : 0);
+                dj.a.sizes = x.sizes;
+                dj.a.ld = x.ld;
+                dj.a.rs = x.rs;
+                dj.a.rows = x.rows;
+                dj.a.cols = x.cols;
+                dj.a.nlimbs = hf ? x.nlimbs - halves->hl : halves->hl;
+                dj.a.out = op.da.out + (hf ? xe * op.da.dxp : 0);
+                dj.nbx = (x.cols + 31) / 32;
+                dj.nby = (x.rows + 3) / 4;
+                g->dig[op.balanced].push_back(make_rec(dj, (int64_t)dj.nbx * dj.nby * op.dgrid.z, 1.0));
+            }
+        } else {
+            DigitJob dj;
+            memset(&dj, 0, sizeof dj);
+            dj.a = op.da;
+            dj.nbx = (int32_t)op.dgrid.x;
+            dj.nby = (int32_t)op.dgrid.y;
+            g->dig[op.balanced].push_back(make_rec(dj, (int64_t)op.dgrid.x * op.dgrid.y * op.dgrid.z, 1.0));
+        }
+        ResidueJob rj;
+        memset(&rj, 0, sizeof rj);
+        rj.tmD = op.tmD; rj.tmT = op.tmT; rj.tmR = op.tmR; rj.a = op.ra;
+        g->res[op.gsteps == RES_GROUP_STEPS_B].push_back(make_rec(rj, op.ra.ntiles, (double)op.ra.nk * op.ra.BN));
+        g->smem_res = std::max(g->smem_res, op.smem);
+    }
+    ProductPlan pp;
+    GBMM_TRY(plan_product(t, RA, RB, Y, m, k, n, kp, npad, 0, true, pp));
+    ProductJob pj;
+    memset(&pj, 0, sizeof pj);
+    pj.tmA = pp.tmA; pj.tmB = pp.tmB; pj.a = pp.pa;
+    g->prod.push_back(make_rec(pj, pp.pa.ntiles, (double)pp.pa.nk));
+    g->smem_prod = std::max(g->smem_prod, pp.smem);
+    ReconPlan rp;
+    GBMM_TRY(plan_recon(t, Y, m, n, npad, c, 0, true, rp));
+    ReconJob rj;
+    memset(&rj, 0, sizeof rj);
+    rj.tmY = rp.tmY; rj.tmT = rp.tmT; rj.a = rp.ra;
+    g->rec[halves ? 1 : 0].push_back(make_rec(rj, rp.ra.nmt, (double)rp.ra.NT * rp.ra.nk));
+    g->smem_rec = std::max(g->smem_rec, rp.smem);
+    return GBMM_OK;
+}
+
+// One stage's records, largest tile cost first, then their tile offsets.
+static void pack_section(std::vector<char> &blob, std::vector<crt_group::Rec> &recs, crt_group::Sect &sec) {
+    std::stable_sort(recs.begin(), recs.end(),
+                     [](const crt_group::Rec &x, const crt_group::Rec &y) { return x.cost > y.cost; });
+    sec.n = (int)recs.size();
+    sec.total = 0;
+    if (recs.empty()) return;
+    blob.resize((blob.size() + 127) & ~(size_t)127);
+    sec.jobs_off = blob.size();
+    for (const auto &r : recs) blob.insert(blob.end(), r.bytes.begin(), r.bytes.end());
+    blob.resize((blob.size() + 127) & ~(size_t)127);
+    sec.tile0_off = blob.size();
+    std::vector<int64_t> t0(recs.size() + 1, 0);
+    for (size_t i = 0; i < recs.size(); i++) t0[i + 1] = t0[i] + recs[i].tiles;
+    sec.total = t0.back();
+    const char *p = reinterpret_cast<const char *>(t0.data());
+    blob.insert(blob.end(), p, p + t0.size() * sizeof(int64_t));
+}
+
+const std::vector<char> &crt_group_blob(crt_group *g) {
+    g->blob.clear();
+    for (int f = 0; f < 2; f++) pack_section(g->blob, g->dig[f], g->sdig[f]);
+    for (int f = 0; f < 2; f++) pack_section(g->blob, g->res[f], g->sres[f]);
+    pack_section(g->blob, g->prod, g->sprod);
+    for (int f = 0; f < 2; f++) pack_section(g->blob, g->rec[f], g->srec[f]);
+    return g->blob;
+}
+
+template <typename J>
+static Group<J> group_at(const char *d_blob, const crt_group::Sect &sec) {
+    return Group<J>{reinterpret_cast<const J *>(d_blob + sec.jobs_off),
+                    reinterpret_cast<const int64_t *>(d_blob + sec.tile0_off), sec.n};
+}
+
+gbmm_status crt_group_launch(crt_group *g, const char *d_blob, cudaStream_t s, cudaStream_t s2, cudaEvent_t ev) {
+    if (reinterpret_cast<uintptr_t>(d_blob) & 127) return set_error(GBMM_ERR_INVALID, "crt group: blob not 128-byte aligned");
+    uint32_t *err = device_error_word();
+    static const CUtensorMap zmap = {};
+    for (int f = 0; f < 2; f++) {
+        const crt_group::Sect &sec = g->sdig[f];
+        if (!sec.n) continue;
+        if (sec.total > INT32_MAX) return set_error(GBMM_ERR_UNSUPPORTED, "crt group: too many digit blocks");
+        DigitArgs none;
+        memset(&none, 0, sizeof none);
+        LaunchScope ls_("k_crt_digits", s);
+        if (f) k_crt_digits<true, true><<<(unsigned)sec.total, 256, 0, s>>>(none, group_at<DigitJob>(d_blob, sec));
+        else k_crt_digits<false, true><<<(unsigned)sec.total, 256, 0, s>>>(none, group_at<DigitJob>(d_blob, sec));
+        GBMM_CUDA_TRY(cudaGetLastError());
+    }
+    for (int f = 0; f < 2; f++) {
+        const crt_group::Sect &sec = g->sres[f];
+        if (!sec.n) continue;
+        ResidueArgs none;
+        memset(&none, 0, sizeof none);
+        const dim3 grid((unsigned)std::min<int64_t>(sec.total, num_sms()));
+        LaunchScope ls_("k_crt_residue", s);
+        if (f) {
+            auto kern = k_crt_residue<RES_STAGES, false, false, RES_GROUP_STEPS_B, true>;
+            GBMM_TRY(set_smem((const void *)kern, g->smem_res));
+            kern<<<grid, RES_THREADS, g->smem_res, s>>>(zmap, zmap, zmap, none, group_at<ResidueJob>(d_blob, sec), err);
+        } else {
+            auto kern = k_crt_residue<RES_STAGES, false, false, RES_GROUP_STEPS_U, true>;
+            GBMM_TRY(set_smem((const void *)kern, g->smem_res));
+            kern<<<grid, RES_THREADS, g->smem_res, s>>>(zmap, zmap, zmap, none, group_at<ResidueJob>(d_blob, sec), err);
+        }
+        GBMM_CUDA_TRY(cudaGetLastError());
+    }
+    if (g->sprod.n) {
+        ProductArgs none;
+        memset(&none, 0, sizeof none);
+        auto kern = k_crt_product<PROD_STAGES, false, true>;
+        GBMM_TRY(set_smem((const void *)kern, g->smem_prod));
+        const dim3 grid((unsigned)std::min<int64_t>(g->sprod.total, num_sms()));
+        LaunchScope ls_("k_crt_product", s);
+        kern<<<grid, PROD_THREADS, g->smem_prod, s>>>(zmap, zmap, none, group_at<ProductJob>(d_blob, g->sprod), err);
+        GBMM_CUDA_TRY(cudaGetLastError());
+    }
+    // the products with post steps first: their shifted adds then run on s2 while
+    // the other reconstructions do
+    for (int f = 1; f >= 0; f--) {
+        const crt_group::Sect &sec = g->srec[f];
+        if (sec.n) {
+            ReconArgs none;
+            memset(&none, 0, sizeof none);
+            auto kern = k_crt_recon<REC_STAGES_PAIR, true, true>;
+            GBMM_TRY(set_smem((const void *)kern, g->smem_rec));
+            LaunchScope ls_("k_crt_recon", s);
+            GBMM_TRY(launch_pairs(kern, CTA_THREADS8, sec.total, g->smem_rec, s, zmap, zmap, none,
+                                  group_at<ReconJob>(d_blob, sec), err));
+        }
+        if (f == 1 && !g->post.empty()) {
+            cudaStream_t sp = s;
+            if (s2 && ev) {
+                GBMM_CUDA_TRY(cudaEventRecord(ev, s));
+                GBMM_CUDA_TRY(cudaStreamWaitEvent(s2, ev, 0));
+                sp = s2;
+            }
+            for (auto &fn : g->post) GBMM_TRY(fn(sp));
+        }
+    }
     return GBMM_OK;
 }
 

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -111,6 +112,36 @@ bool crt_feasible(int la, int lb, int k);
 size_t crt_workspace_bytes(int la, int lb, int m, int k, int n, int cn);
 // whether crt_matmul covers inner dimension k in one pass (no chunks of k)
 bool crt_single_pass(int k);
+// Grouped CRT launches (a batch's CRT products): products are collected without
+// launching, each with its whole workspace carved from the arena at once, and
+// then run stage by stage, one persistent launch per stage and kernel form over
+// the tiles of all of them.  crt_group_add takes single-pass products only (k <=
+// 512, no accumulation).
+struct crt_group;
+crt_group *crt_group_create();
+void crt_group_destroy(crt_group *g);
+bool crt_group_empty(const crt_group *g);
+// An operand of a grouped product given as the two limb halves of x (a limb-half
+// split), read in place: side 0, A = [x_lo; x_hi] stacked by rows; side 1, B =
+// [x_lo | x_hi] stacked by columns; x_lo holds x's low hl limbs, x_hi the rest.
+// The stacked operand passed to crt_group_add then only gives the shape.
+struct crt_halves {
+    int side;
+    gbmm_mat x;
+    int hl;
+};
+gbmm_status crt_group_add(gbmm_handle h, crt_group *g, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b,
+                          int64_t bits_a, int64_t bits_b, int nprimes, const crt_halves *halves = nullptr);
+// a step run after the reconstructions of the products added with halves (their
+// shifted adds): on a second stream while the other reconstructions run
+void crt_group_post(crt_group *g, std::function<gbmm_status(cudaStream_t)> f);
+// arena bytes crt_group_add takes for one product of these shapes
+size_t crt_group_ws(int la, int lb, int m, int k, int n);
+// the stage records as one blob (built once every product is added); it goes to
+// device memory 128-byte aligned, and crt_group_launch reads it there.  The post
+// steps run on s2 (after `ev`, recorded on s) when s2 is given, else on s.
+const std::vector<char> &crt_group_blob(crt_group *g);
+gbmm_status crt_group_launch(crt_group *g, const char *d_blob, cudaStream_t s, cudaStream_t s2, cudaEvent_t ev);
 // Stage hooks the host-buffer pipeline hands to one single-pass CRT product
 // (gbmm_handle::stage, consumed and cleared by crt_matmul): B's digits and
 // residues wait for b_ready, so A's run while B is still uploading; the
@@ -168,6 +199,13 @@ int choose_plan(gbmm_handle h, int m, int k, int n, int la, int lb);
 size_t dispatch_ws(const Plan &p, int la, int lb, int m, int k, int n, int cn, int accumulate);
 gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, const Plan &p,
                      int accumulate, cudaStream_t s);
+// whether a batch runs this job in the grouped CRT launches (a CRT plan, one pass
+// over k, directly or after one limb-half split), the arena bytes it then takes,
+// and its collection into the group (workspace carved, nothing launched)
+bool crt_groupable(const Plan &p, int la, int lb, int m, int k, int n);
+size_t crt_group_job_ws(const Plan &p, int la, int lb, int m, int k, int n);
+gbmm_status crt_collect(gbmm_handle h, crt_group *g, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b,
+                        const Plan &p);
 gbmm_status resolve_plan(gbmm_handle h, const gbmm_mat &a, const gbmm_mat &b, const gbmm_opts &o, Plan &p);
 void invalidate_graphs(gbmm_handle h);
 void batch_state_destroy(gbmm_handle h);

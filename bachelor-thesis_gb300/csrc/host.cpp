@@ -1167,6 +1167,69 @@ gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const 
     return st;
 }
 
+// The split above for a batch's grouped CRT launches: the direct form, or one
+// limb-half split whose halves go through one single-pass CRT product.
+static bool split_halves(const Plan &p, int la, int lb, int k, int &hl, int &hn, Plan &q) {
+    const bool sa = la >= lb;
+    const int xl = sa ? la : lb;
+    if (xl < 2) return false;
+    hl = xl / 2;
+    hn = xl - hl;
+    q = p;
+    q.split = std::max(0, p.split - 1);
+    return direct_ok(q, sa ? hn : la, sa ? lb : hn, k);
+}
+
+bool crt_groupable(const Plan &p, int la, int lb, int m, int k, int n) {
+    if (p.path != GBMM_PATH_CRT || m == 0 || n == 0 || k == 0 || !crt_single_pass(k)) return false;
+    if (direct_ok(p, la, lb, k)) return true;
+    int hl, hn;
+    Plan q;
+    return split_halves(p, la, lb, k, hl, hn, q);
+}
+
+size_t crt_group_job_ws(const Plan &p, int la, int lb, int m, int k, int n) {
+    if (direct_ok(p, la, lb, k)) return crt_group_ws(la, lb, m, k, n);
+    int hl, hn;
+    Plan q;
+    if (!split_halves(p, la, lb, k, hl, hn, q)) return 0;
+    const bool sa = la >= lb;
+    const int tn = limbs_needed(sa ? hn : la, sa ? lb : hn, k, 0) + 1;
+    return mat_bytes(2 * (int64_t)m * n, tn) + 1024 + crt_group_ws(sa ? hn : la, sa ? lb : hn, sa ? 2 * m : m, k, sa ? n : 2 * n);
+}
+
+gbmm_status crt_collect(gbmm_handle h, crt_group *g, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b,
+                        const Plan &p) {
+    const int m = a.rows, k = a.cols, n = b.cols;
+    if (direct_ok(p, a.nlimbs, b.nlimbs, k))
+        return crt_group_add(h, g, c, a, b, 32LL * a.nlimbs, 32LL * b.nlimbs, p.nprimes);
+    int hl, hn;
+    Plan q;
+    if (!split_halves(p, a.nlimbs, b.nlimbs, k, hl, hn, q))
+        return set_error(GBMM_ERR_UNSUPPORTED, "crt group: no single-pass form for %d x %d limb entries", a.nlimbs,
+                         b.nlimbs);
+    // as dispatch(): one product T against the halves stacked (read in place by the
+    // digits stage), then C = T_0 + T_1 2^(32 hl); T stays carved until the group has run
+    const bool sa = a.nlimbs >= b.nlimbs;
+    const gbmm_mat &X = sa ? a : b;
+    gbmm_mat S, T;
+    memset(&S, 0, sizeof S);
+    S.rows = sa ? 2 * m : k;
+    S.cols = sa ? k : 2 * n;
+    S.nlimbs = hn;
+    const int tn = limbs_needed(sa ? hn : a.nlimbs, sa ? b.nlimbs : hn, k, 0) + 1;
+    if (!arena_mat(h, sa ? 2 * m : m, sa ? n : 2 * n, tn, T)) return set_error(GBMM_ERR_NOMEM, "crt group: split workspace");
+    crt_halves hv;
+    hv.side = sa ? 0 : 1;
+    hv.x = X;
+    hv.hl = hl;
+    GBMM_TRY(crt_group_add(h, g, T, sa ? S : a, sa ? b : S, 32LL * (sa ? hn : a.nlimbs), 32LL * (sa ? b.nlimbs : hn),
+                           q.nprimes, &hv));
+    const gbmm_mat T0 = sub_view(T, 0, 0, m, n), T1 = sa ? sub_view(T, m, 0, m, n) : sub_view(T, 0, n, m, n);
+    crt_group_post(g, [=](cudaStream_t s) { return launch_add_shifted(c, T0, T1, hl, s); });
+    return GBMM_OK;
+}
+
 gbmm_status resolve_plan(gbmm_handle h, const gbmm_mat &a, const gbmm_mat &b, const gbmm_opts &o, Plan &p) {
     if (o.plan) {
         if (o.plan < 1 || o.plan > GBMM_NPLANS) return set_error(GBMM_ERR_INVALID, "unknown plan %d", o.plan - 1);

@@ -73,6 +73,13 @@ __device__ __forceinline__ void tma_load_2d_mc(void *smem_dst, const CUtensorMap
         "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y), "h"(mask)
         : "memory");
 }
+__device__ __forceinline__ void tma_load_3d(void *smem_dst, const CUtensorMap *map, uint64_t *bar, int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(
+            smem_u32(smem_dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+        : "memory");
+}
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
 }
@@ -229,6 +236,14 @@ __device__ __forceinline__ void tma_load_2d_pair(void *smem_dst, const CUtensorM
         "cp.async.bulk.tensor.2d.shared::cta.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%3, "
         "%4}], [%2];" ::"r"(smem_u32(smem_dst)),
         "l"(map), "r"(bar_cluster), "r"(x), "r"(y)
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_3d_pair(void *smem_dst, const CUtensorMap *map, uint32_t bar_cluster, int x,
+                                                 int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cta.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%3, "
+        "%4, %5}], [%2];" ::"r"(smem_u32(smem_dst)),
+        "l"(map), "r"(bar_cluster), "r"(x), "r"(y), "r"(z)
         : "memory");
 }
 __device__ __forceinline__ void mma_bf16_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,

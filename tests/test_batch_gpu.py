@@ -2,6 +2,7 @@
 graph replay), the limb-half split for entries longer than any kernel takes,
 and the autotuner's dispatch table.  Bit-exact against Python integers."""
 import json
+import math
 import os
 import random
 
@@ -74,6 +75,35 @@ def test_batched_graph_replay_sees_new_inputs(g):
         h.matmul_batched(arr)
         for K, M, N, A, B, dA, dB, dC in jobs:
             assert dC.to_ints() == _exact(K, M, N, A, B), rnd
+    h.close()
+
+
+def test_grouped_crt_launches_mixed_products(g):
+    """The batch's CRT products run in grouped launches: one launch per stage over
+    the tiles of all of them.  Thirty products of log-uniform shapes (1 to 48) and
+    bit lengths (64 to 16384, each operand its own) put, in the same launches,
+    moduli counts from about 10 to over 1023 (limb-half split), unsigned and
+    balanced digit rows, and reconstructions of 1 to 9 N tiles, so that one CTA
+    walks entry tiles of different N-tile counts.  Eager call, capturing call and
+    replay each give the exact product of the current inputs."""
+    rng = random.Random(21)
+    lu = lambda lo, hi: int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+    specs = [(lu(1, 48), lu(1, 48), lu(1, 48), lu(64, 16384), lu(64, 16384)) for _ in range(30)]
+    specs += [(3, 7, 2, 16384, 16000), (40, 3, 1, 9000, 64)]
+    jobs = _make_jobs(g, rng, specs)
+    h = g.Handle()
+    arr = h.jobs([(j[7], j[5], j[6]) for j in jobs], path=g.PATH_CRT)
+    for rnd in range(3):
+        if rnd:
+            for idx, (K, M, N, A, B, dA, dB, dC) in enumerate(jobs):
+                A = _rand(rng, K * M, specs[idx][3])
+                B = _rand(rng, M * N, specs[idx][4])
+                dA.upload(*g.ints_to_planes(A, dA.nlimbs))
+                dB.upload(*g.ints_to_planes(B, dB.nlimbs))
+                jobs[idx] = (K, M, N, A, B, dA, dB, dC)
+        h.matmul_batched(arr, path=g.PATH_CRT)
+        for K, M, N, A, B, dA, dB, dC in jobs:
+            assert dC.to_ints() == _exact(K, M, N, A, B), (rnd, K, M, N)
     h.close()
 
 

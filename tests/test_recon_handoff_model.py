@@ -15,19 +15,26 @@ consumed `ph` phases tests parity ph & 1, so a barrier two phases ahead looks
 incomplete (aliasing).  A read must see the value written for its own tile and N
 tile.  The protocol the kernel uses is checked to be free of overwrites, aliasing
 and deadlock; the order it replaced is shown to break for one N tile per entry tile.
+The grouped form (entry tiles of several products, so N-tile counts that vary
+from tile to tile) is checked on random tile sequences.
 """
 import random
 
 import pytest
 
 
-def half0_ops(T, NT, fixed):
+def half0_ops(nts, mode):
+    """nts: the N-tile count of each entry tile of the CTA.  mode: "old" (the
+    order the kernel replaced), "fixed" (the kernel's single-product form: the
+    early take when an entry tile has one N tile) or "uni" (the grouped form: the
+    early take at every entry tile but the first)."""
     ops, first = [], True
-    for t in range(T):
+    for t, NT in enumerate(nts):
+        uni = mode == "uni" or (mode == "fixed" and NT == 1)
         for j in range(NT):
             took0 = False
             if j == 0:
-                if fixed and not first and NT == 1:
+                if not first and uni:
                     ops.append(("wait", "to0"))
                     took0 = True
                 ops.append(("write", "q", t))
@@ -44,10 +51,11 @@ def half0_ops(T, NT, fixed):
     return ops
 
 
-def half1_ops(T, NT, fixed):
+def half1_ops(nts, mode):
     ops = []
-    for t in range(T):
-        last_t = t == T - 1
+    for t, NT in enumerate(nts):
+        uni = mode == "uni" or (mode == "fixed" and NT == 1)
+        last_t = t == len(nts) - 1
         for j in range(NT):
             if j == 0:
                 ops.append(("wait", "qready"))
@@ -56,20 +64,20 @@ def half1_ops(T, NT, fixed):
             ops.append(("read", "carry1", (t, j)))
             if j < NT - 1:
                 ops.append(("write", "carry0", (t, j)))
-            if fixed:
-                if j < NT - 1 or (NT > 1 and not last_t):
+            if mode != "old":
+                if j < NT - 1 or (not uni and not last_t):
                     ops.append(("arrive", "to0"))
             elif not (last_t and j == NT - 1):
                 ops.append(("arrive", "to0"))
         ops.append(("read", "top0", t))  # the finalize
-        if fixed and NT == 1 and not last_t:
+        if mode != "old" and uni and not last_t:
             ops.append(("arrive", "to0"))
     return ops
 
 
-def run(T, NT, fixed, rng):
+def run(nts, mode, rng):
     """One random interleaving; returns None, or the first violation."""
-    progs = [half0_ops(T, NT, fixed), half1_ops(T, NT, fixed)]
+    progs = [half0_ops(nts, mode), half1_ops(nts, mode)]
     pc = [0, 0]
     done = {"qready": 0, "to1": 0, "to0": 0}   # completed phases
     used = [dict(done), dict(done)]            # phases each half has waited for
@@ -113,14 +121,34 @@ def run(T, NT, fixed, rng):
 def test_protocol_is_safe(T, NT):
     rng = random.Random(1000 * T + NT)
     for _ in range(3000):
-        err = run(T, NT, True, rng)
+        err = run([NT] * T, "fixed", rng)
         assert err is None, (T, NT, err)
 
 
 def test_replaced_order_breaks_for_one_table_tile():
     rng = random.Random(7)
-    errors = {run(3, 1, False, rng) for _ in range(3000)} - {None}
+    errors = {run([1] * 3, "old", rng) for _ in range(3000)} - {None}
     assert errors, "the model should expose the old order's race"
     # with more than one N tile the old order was already safe
     for NT in (2, 3):
-        assert all(run(3, NT, False, rng) is None for _ in range(3000))
+        assert all(run([NT] * 3, "old", rng) is None for _ in range(3000))
+
+
+def test_grouped_protocol_is_safe_for_any_tile_sequence():
+    """A grouped launch hands one CTA entry tiles of different products, so the
+    N-tile count changes from tile to tile; the grouped form stays safe."""
+    rng = random.Random(11)
+    for _ in range(400):
+        nts = [rng.choice([1, 1, 2, 3, 5]) for _ in range(rng.randint(1, 6))]
+        for _ in range(40):
+            err = run(nts, "uni", rng)
+            assert err is None, (nts, err)
+
+
+def test_single_product_form_breaks_when_tile_counts_vary():
+    """The single-product form relies on one N-tile count for every entry tile:
+    a tile of several N tiles followed by one of a single N tile lets half 0
+    overwrite the quotient slot before half 1 has read it."""
+    rng = random.Random(5)
+    errors = {run([2, 1, 1], "fixed", rng) for _ in range(3000)} - {None}
+    assert errors
