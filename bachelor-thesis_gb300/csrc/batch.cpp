@@ -43,6 +43,7 @@ struct TuneEntry {
 struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
     char *d_blob = nullptr;  // work-queue and grouped-CRT blob owned by this graph
+    uint64_t nkern = 0;      // library kernels in the graph (counted as launches per replay)
 };
 
 constexpr int NSIDE = 8;  // side streams a batch's dispatched jobs are spread over
@@ -290,7 +291,7 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
     if (bs.use_graphs) {
         auto g = bs.graphs.find(sig);
         if (g != bs.graphs.end()) {
-            count_launch(1);
+            count_launch(g->second.nkern);
             GBMM_CUDA_TRY(cudaGraphLaunch(g->second.exec, h->stream));
             return GBMM_OK;
         }
@@ -357,7 +358,10 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
     }
     cudaGraph_t graph = nullptr;
     GBMM_CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    // the kernels captured are counted once here (the graph runs right after)
+    const uint64_t k0 = gbmm_kernel_launches();
     gbmm_status st = enqueue_batch(h, jobs, plans, lp, ge.d_blob, other, slice, base, grp.get(), ge.d_blob + crt_off);
+    ge.nkern = gbmm_kernel_launches() - k0;
     arena_release(h, mark);
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     if (st == GBMM_OK && e != cudaSuccess) st = cuda_error(e, "cudaStreamEndCapture");
@@ -371,7 +375,6 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
         return st;
     }
     bs.graphs[sig] = ge;
-    count_launch(1);
     GBMM_CUDA_TRY(cudaGraphLaunch(ge.exec, h->stream));
     return GBMM_OK;
 }

@@ -1057,11 +1057,17 @@ bool plan_admissible(int id, int m, int k, int n, int la, int lb) {
 
 // Plain dispatch rule: the CRT form for products with enough limb work (it pays
 // off once the residue and reconstruction passes are amortised), the per-entry
-// limb kernel otherwise.  Entries too long for one CRT product (more than 1023
-// moduli) still take the CRT path: dispatch() splits them into limb halves that fit.
+// limb kernel otherwise.  Entries of fewer than 16 limbs together take the CRT
+// form from 2^25 schoolbook MACs on (in a batch their CRT stages join the grouped
+// launches; measured on the 64 uneven products of configuration 4: 2^25 gave the
+// shortest batch among thresholds 2^24 .. 2^30).  Entries too long for one CRT
+// product (more than 1023 moduli) still take the CRT path: dispatch() splits them
+// into limb halves that fit.
+static int64_t g_crt_short_work = (int64_t)1 << 25;  // 0: never for short entries
 int heuristic_plan(int m, int k, int n, int la, int lb) {
     const int64_t work = (int64_t)m * k * n * la * lb;
     if (la + lb >= 16 && work >= ((int64_t)1 << 22)) return GBMM_PLAN_CRT;
+    if (g_crt_short_work > 0 && work >= g_crt_short_work) return GBMM_PLAN_CRT;
     return GBMM_PLAN_LIMB_NAIVE;
 }
 
@@ -1180,8 +1186,16 @@ static bool split_halves(const Plan &p, int la, int lb, int k, int &hl, int &hn,
     return direct_ok(q, sa ? hn : la, sa ? lb : hn, k);
 }
 
+// Products of C with at least this many entries fill the GPU alone (their
+// reconstruction alone has 128 or more CTA-pair tiles) and keep their own
+// tile forms on a side stream; measured on configuration 4's batch and a
+// configuration-5 batch against grouping every product (8.10 / 26.1 ms against
+// 8.54 / 28.5 ms) and grouping none (8.31 / 26.4 ms), with 2^17 in between.
+constexpr int64_t GROUP_MAX_ENTRIES = (int64_t)1 << 15;
+
 bool crt_groupable(const Plan &p, int la, int lb, int m, int k, int n) {
     if (p.path != GBMM_PATH_CRT || m == 0 || n == 0 || k == 0 || !crt_single_pass(k)) return false;
+    if ((int64_t)m * n >= GROUP_MAX_ENTRIES) return false;
     if (direct_ok(p, la, lb, k)) return true;
     int hl, hn;
     Plan q;
@@ -1253,6 +1267,14 @@ gbmm_status resolve_plan(gbmm_handle h, const gbmm_mat &a, const gbmm_mat &b, co
 }
 
 }  // namespace gbmm
+
+// Internal hook: schoolbook work (m k n la lb) from which the heuristic takes the CRT
+// form for entries of fewer than 16 limbs together (0: never); returns the old value.
+extern "C" int64_t gbmmx_crt_short_work(int64_t work) {
+    const int64_t old = g_crt_short_work;
+    g_crt_short_work = work < 0 ? 0 : work;
+    return old;
+}
 
 extern "C" gbmm_status gbmm_matmul(gbmm_handle h, gbmm_mat c, gbmm_mat a, gbmm_mat b, const gbmm_opts *opts) {
     if (!h) return set_error(GBMM_ERR_INVALID, "null handle");

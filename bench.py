@@ -1064,10 +1064,16 @@ def main():
         if args.workload in ("cfg4", "cfg5", "limbkernels"):
             return run_reference(args, WORKLOADS["cfg3"], world, rank)
         return run_reference(args, W, world, rank)
-    if args.workload == "cfg4":
-        return run_batched(args, W, world, rank, local)
-    if args.workload == "cfg5":
-        return run_learned(args, W, world, rank, local)
+    if args.workload in ("cfg4", "cfg5"):
+        # batched calls run on a stream of their own: a handle bound to the legacy
+        # default stream runs every batch eagerly, one on a real stream captures its
+        # launch sequence into a CUDA graph on the second call and replays it after
+        import torch
+        torch.cuda.set_device(local)
+        with torch.cuda.stream(torch.cuda.Stream()):
+            if args.workload == "cfg4":
+                return run_batched(args, W, world, rank, local)
+            return run_learned(args, W, world, rank, local)
     if args.workload == "limbkernels":
         return run_limb_kernels(args, W, world, rank, local)
     return run_gpu(args, W, world, rank, local)

@@ -215,10 +215,15 @@ typedef struct gbmm_job {
 
 /* Runs many independent products of uneven shape and bit length: jobs planned
  * for the limb kernel without recursion go through one persistent kernel over
- * a device work queue, the others (CRT products, Winograd trees) run side by
- * side on eight streams forked from the handle's stream; the launch sequence is
- * captured into a CUDA graph and replayed on later calls with the same job
- * signature.
+ * a device work queue; CRT products with inner dimension up to 512 and fewer
+ * than 2^15 entries in C (directly or after one limb-half split) run in grouped
+ * launches, one persistent launch per CRT stage over the tiles of all of them;
+ * the others (Winograd trees, larger CRT products) run side by side on streams
+ * forked from the handle's stream.
+ * The launch sequence is captured into a CUDA graph and replayed on later calls
+ * with the same job signature.  The CRT_SINGLE / CRT_PAIR plans fix the tile
+ * form of a product run alone; in the grouped launches every product uses the
+ * grouped forms (one-CTA product tiles, CTA-pair reconstruction tiles).
  * replaces: the unused chunked-stream job DAG (mat-gpu/job.cu:32-338). */
 gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_t njobs, const gbmm_opts *opts);
 /* One product on host buffers: dense limb planes (limb i of entry e at

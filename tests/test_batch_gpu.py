@@ -26,6 +26,26 @@ def _exact(K, M, N, A, B):
     return [sum(A[y * M + k] * B[k * N + x] for k in range(M)) for y in range(K) for x in range(N)]
 
 
+class _own_stream:
+    """Runs the block on a torch stream of its own, so that a handle binds a real
+    stream and batched calls capture and replay CUDA graphs (a handle on the
+    legacy default stream runs every batch eagerly)."""
+
+    def __enter__(self):
+        import torch
+        self.s = torch.cuda.Stream()
+        self.s.wait_stream(torch.cuda.current_stream())
+        self.ctx = torch.cuda.stream(self.s)
+        self.ctx.__enter__()
+        return self.s
+
+    def __exit__(self, *exc):
+        import torch
+        self.ctx.__exit__(*exc)
+        torch.cuda.current_stream().wait_stream(self.s)
+        return False
+
+
 def _make_jobs(g, rng, specs):
     out = []
     for K, M, N, ba, bb in specs:
@@ -62,20 +82,21 @@ def test_batched_graph_replay_sees_new_inputs(g):
     rng = random.Random(3)
     specs = [(33, 40, 21, 300, 500), (64, 64, 64, 2048, 2048), (8, 9, 10, 64, 5000)]
     jobs = _make_jobs(g, rng, specs)
-    h = g.Handle()
-    arr = h.jobs([(j[7], j[5], j[6]) for j in jobs])
-    for rnd in range(4):
-        if rnd:
-            for idx, (K, M, N, A, B, dA, dB, dC) in enumerate(jobs):
-                A = _rand(rng, K * M, specs[idx][3])
-                B = _rand(rng, M * N, specs[idx][4])
-                dA.upload(*g.ints_to_planes(A, dA.nlimbs))
-                dB.upload(*g.ints_to_planes(B, dB.nlimbs))
-                jobs[idx] = (K, M, N, A, B, dA, dB, dC)
-        h.matmul_batched(arr)
-        for K, M, N, A, B, dA, dB, dC in jobs:
-            assert dC.to_ints() == _exact(K, M, N, A, B), rnd
-    h.close()
+    with _own_stream():
+        h = g.Handle()
+        arr = h.jobs([(j[7], j[5], j[6]) for j in jobs])
+        for rnd in range(4):
+            if rnd:
+                for idx, (K, M, N, A, B, dA, dB, dC) in enumerate(jobs):
+                    A = _rand(rng, K * M, specs[idx][3])
+                    B = _rand(rng, M * N, specs[idx][4])
+                    dA.upload(*g.ints_to_planes(A, dA.nlimbs))
+                    dB.upload(*g.ints_to_planes(B, dB.nlimbs))
+                    jobs[idx] = (K, M, N, A, B, dA, dB, dC)
+            h.matmul_batched(arr)
+            for K, M, N, A, B, dA, dB, dC in jobs:
+                assert dC.to_ints() == _exact(K, M, N, A, B), rnd
+        h.close()
 
 
 def test_grouped_crt_launches_mixed_products(g):
@@ -91,20 +112,55 @@ def test_grouped_crt_launches_mixed_products(g):
     specs = [(lu(1, 48), lu(1, 48), lu(1, 48), lu(64, 16384), lu(64, 16384)) for _ in range(30)]
     specs += [(3, 7, 2, 16384, 16000), (40, 3, 1, 9000, 64)]
     jobs = _make_jobs(g, rng, specs)
-    h = g.Handle()
-    arr = h.jobs([(j[7], j[5], j[6]) for j in jobs], path=g.PATH_CRT)
-    for rnd in range(3):
-        if rnd:
-            for idx, (K, M, N, A, B, dA, dB, dC) in enumerate(jobs):
-                A = _rand(rng, K * M, specs[idx][3])
-                B = _rand(rng, M * N, specs[idx][4])
-                dA.upload(*g.ints_to_planes(A, dA.nlimbs))
-                dB.upload(*g.ints_to_planes(B, dB.nlimbs))
-                jobs[idx] = (K, M, N, A, B, dA, dB, dC)
-        h.matmul_batched(arr, path=g.PATH_CRT)
-        for K, M, N, A, B, dA, dB, dC in jobs:
-            assert dC.to_ints() == _exact(K, M, N, A, B), (rnd, K, M, N)
-    h.close()
+    with _own_stream():
+        h = g.Handle()
+        arr = h.jobs([(j[7], j[5], j[6]) for j in jobs], path=g.PATH_CRT)
+        for rnd in range(3):
+            if rnd:
+                for idx, (K, M, N, A, B, dA, dB, dC) in enumerate(jobs):
+                    A = _rand(rng, K * M, specs[idx][3])
+                    B = _rand(rng, M * N, specs[idx][4])
+                    dA.upload(*g.ints_to_planes(A, dA.nlimbs))
+                    dB.upload(*g.ints_to_planes(B, dB.nlimbs))
+                    jobs[idx] = (K, M, N, A, B, dA, dB, dC)
+            h.matmul_batched(arr, path=g.PATH_CRT)
+            for K, M, N, A, B, dA, dB, dC in jobs:
+                assert dC.to_ints() == _exact(K, M, N, A, B), (rnd, K, M, N)
+        h.close()
+
+
+def test_batched_graph_capture_on_own_stream(g):
+    """A handle bound to a stream of its own (not the legacy default stream) runs
+    the first call eagerly, captures the launch sequence into a CUDA graph on the
+    second and replays it from the third: per-entry limb jobs (work queue), grouped
+    CRT jobs (one of them split), and a CRT job with k > 512 (side stream).  Each
+    call computes the exact product of the current inputs; a replay launches no
+    more kernels than the capture recorded."""
+    rng = random.Random(31)
+    specs = [(40, 30, 20, 200, 96), (33, 40, 21, 3000, 2500), (6, 9, 5, 16000, 4000), (9, 700, 8, 400, 300),
+             (64, 64, 64, 2048, 1024), (3, 4, 5, 64, 64)]
+    jobs = _make_jobs(g, rng, specs)
+    with _own_stream() as s:
+        h = g.Handle()
+        arr = h.jobs([(j[7], j[5], j[6]) for j in jobs])
+        counts = []
+        for rnd in range(5):
+            if rnd:
+                for idx, (K, M, N, A, B, dA, dB, dC) in enumerate(jobs):
+                    A = _rand(rng, K * M, specs[idx][3])
+                    B = _rand(rng, M * N, specs[idx][4])
+                    dA.upload(*g.ints_to_planes(A, dA.nlimbs))
+                    dB.upload(*g.ints_to_planes(B, dB.nlimbs))
+                    jobs[idx] = (K, M, N, A, B, dA, dB, dC)
+            n0 = g.kernel_launches()
+            h.matmul_batched(arr)
+            counts.append(g.kernel_launches() - n0)
+            s.synchronize()
+            for K, M, N, A, B, dA, dB, dC in jobs:
+                assert dC.to_ints() == _exact(K, M, N, A, B), rnd
+        h.close()
+    # eager, capture (its kernels counted as they are recorded), then replays
+    assert counts[2] == counts[3] == counts[4] == counts[1] > 0, counts
 
 
 @pytest.mark.parametrize("path", ["limb", "crt"])
