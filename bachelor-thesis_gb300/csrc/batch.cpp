@@ -349,11 +349,11 @@ extern "C" gbmm_status gbmm_matmul_batched(gbmm_handle h, gbmm_job *jobs, int32_
     GraphEntry ge;
     if (!blob.empty()) {
         cudaError_t e = cudaMalloc(&ge.d_blob, blob.size());
-        if (e == cudaSuccess) e = cudaMemcpy(ge.d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) {
+        gbmm_status su = e == cudaSuccess ? upload_now(ge.d_blob, blob.data(), blob.size()) : cuda_error(e, "batch blob");
+        if (su != GBMM_OK) {
             cudaFree(ge.d_blob);
             arena_release(h, mark);
-            return cuda_error(e, "batch blob");
+            return su;
         }
     }
     cudaGraph_t graph = nullptr;

@@ -34,11 +34,13 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <utility>
 #include <cmath>
 #include <functional>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "gbmm_internal.h"
@@ -1744,21 +1746,24 @@ static uint32_t big_mod_small(const big &x, uint32_t d) {
     for (size_t i = x.size(); i-- > 0;) r = ((r << 32) | x[i]) % d;
     return (uint32_t)r;
 }
-// balanced base-128 digits (each in [-64, 63]) of a nonnegative integer
-static std::vector<int> balanced128(const big &x, int ndig) {
-    std::vector<int> out(ndig, 0);
-    const int nbits = (int)(32 * x.size());
+// balanced base-128 digits (each in [-64, 63]) of a nonnegative integer: digit t
+// takes bits [7t, 7t + 7) plus the carry of the digit below
+static void balanced128(const big &x, int ndig, int *out) {
+    const size_t nw = x.size();
     int carry = 0;
     for (int t = 0; t < ndig; t++) {
-        int v = carry;
-        for (int b = 0; b < 7; b++) {
-            const int bit = 7 * t + b;
-            if (bit < nbits && ((x[bit / 32] >> (bit % 32)) & 1u)) v += 1 << b;
-        }
+        const int bit = 7 * t;
+        const size_t w = (size_t)(bit >> 5);
+        const uint64_t lo = w < nw ? x[w] : 0, hi = w + 1 < nw ? x[w + 1] : 0;
+        const int v = carry + (int)((((hi << 32) | lo) >> (bit & 31)) & 127u);
         const int d = v >= 64 ? v - 128 : v;
         carry = (v - d) / 128;
         out[t] = d;
     }
+}
+static std::vector<int> balanced128(const big &x, int ndig) {
+    std::vector<int> out(ndig, 0);
+    balanced128(x, ndig, out.data());
     return out;
 }
 static uint32_t inv_mod(uint32_t a, uint32_t p) {
@@ -1791,6 +1796,15 @@ static uint16_t bf16_bits(float f) {
     uint16_t b;
     memcpy(&b, &h, 2);
     return b;
+}
+// bf16 bits of the integers -256 .. 256 (every table digit lies in this range)
+static uint16_t bf16_small(int v) {
+    static const std::vector<uint16_t> lut = [] {
+        std::vector<uint16_t> l(513);
+        for (int i = -256; i <= 256; i++) l[i + 256] = bf16_bits((float)i);
+        return l;
+    }();
+    return lut[v + 256];
 }
 
 struct crt_tables {
@@ -1830,19 +1844,32 @@ static int moduli_for_bits(int64_t bits) {
     return acc >= (double)bits ? n : -1;
 }
 
-static gbmm_status build_tables(crt_tables *t, int P) {
+// Host side of a table set: moduli constants, the reconstruction table, Mod's
+// chunk values and the constant (p, 1/p) list.
+struct crt_tables_host {
+    int P = 0, Pp = 0, Dout = 0, NT = 0;
+    std::vector<ModConst> mods;
+    std::vector<uint16_t> recon;  // [NT * RTAB][2Pp] bf16 bits
+    std::vector<uint32_t> vtab;   // [ceil(Dout / 32)][8]
+    std::vector<float> cmod;      // 4 * CMOD_PAIRS
+};
+
+static void build_tables_host(int P, crt_tables_host &o) {
     const auto &pr = primes_desc();
-    t->P = P;
-    t->Pp = (2 * P + 63) / 64 * 32;
+    o.P = P;
+    o.Pp = (2 * P + 63) / 64 * 32;
     big Mod{1};
     for (int i = 0; i < P; i++) big_mul_small(Mod, pr[i]);
     int modbits = (int)(32 * Mod.size());
-    t->Dout = (modbits + 6) / 7 + 2;  // base-128 output digits
-    t->NT = (SROWS + t->Dout + RTAB - 1) / RTAB;  // in units of RTAB rows
-    const int rows = t->NT * RTAB, cols = 2 * t->Pp;
-    std::vector<uint16_t> tab((size_t)rows * cols, bf16_bits(0.f));
-    t->h_mods.resize(P);
-    for (int i = 0; i < P; i++) {
+    o.Dout = (modbits + 6) / 7 + 2;  // base-128 output digits
+    o.NT = (SROWS + o.Dout + RTAB - 1) / RTAB;  // in units of RTAB rows
+    const int rows = o.NT * RTAB, cols = 2 * o.Pp;
+    o.recon.assign((size_t)rows * cols, bf16_bits(0.f));
+    std::vector<uint16_t> &tab = o.recon;
+    o.mods.resize(P);
+    // the moduli are independent: contiguous ranges of them on up to 16 host threads
+    // (each writes its own table columns)
+    auto one = [&](int i, std::vector<int> &dh, std::vector<int> &dl) {
         const uint32_t p = pr[i];
         uint32_t rem = 0;
         big Mi = big_div_small(Mod, p, &rem);
@@ -1856,39 +1883,53 @@ static gbmm_status build_tables(crt_tables *t, int P) {
         mc.mu = (uint32_t)(((uint64_t)1 << 32) / p);
         mc.h16 = (uint32_t)((1u << 16) % p);
         mc.w = w;
-        t->h_mods[i] = mc;
+        o.mods[i] = mc;
         // column 2i multiplies the high digit (x256), column 2i+1 the low digit
-        std::vector<int> dh = balanced128(Mi256, t->Dout), dl = balanced128(Mi, t->Dout);
-        for (int r = 0; r < t->Dout; r++) {
-            tab[(size_t)(SROWS + r) * cols + 2 * i] = bf16_bits((float)dh[r]);
-            tab[(size_t)(SROWS + r) * cols + 2 * i + 1] = bf16_bits((float)dl[r]);
+        balanced128(Mi256, o.Dout, dh.data());
+        balanced128(Mi, o.Dout, dl.data());
+        for (int r = 0; r < o.Dout; r++) {
+            tab[(size_t)(SROWS + r) * cols + 2 * i] = bf16_small(dh[r]);
+            tab[(size_t)(SROWS + r) * cols + 2 * i + 1] = bf16_small(dl[r]);
         }
         // fixed-point weights: round(2^(FIXB+8) / p) for the high digit, round(2^FIXB / p) for the low digit
         const unsigned __int128 one = 1;
         const unsigned __int128 gh = ((one << (FIXB + 8)) + p / 2) / p;
         const unsigned __int128 gl = ((one << FIXB) + p / 2) / p;
         big bh, bl;
-        for (int w = 0; w < 4; w++) {
-            bh.push_back((uint32_t)(gh >> (32 * w)));
-            bl.push_back((uint32_t)(gl >> (32 * w)));
+        for (int w2 = 0; w2 < 4; w2++) {
+            bh.push_back((uint32_t)(gh >> (32 * w2)));
+            bl.push_back((uint32_t)(gl >> (32 * w2)));
         }
         std::vector<int> sh = balanced128(bh, SUSED), sl = balanced128(bl, SUSED);
         for (int r = 0; r < SUSED; r++) {
-            tab[(size_t)r * cols + 2 * i] = bf16_bits((float)sh[r]);
-            tab[(size_t)r * cols + 2 * i + 1] = bf16_bits((float)sl[r]);
+            tab[(size_t)r * cols + 2 * i] = bf16_small(sh[r]);
+            tab[(size_t)r * cols + 2 * i + 1] = bf16_small(sl[r]);
         }
+    };
+    const int nthr = std::max(1, std::min<int>({16, (int)std::thread::hardware_concurrency(), (P + 31) / 32}));
+    auto range = [&](int th) {
+        std::vector<int> dh(o.Dout), dl(o.Dout);
+        for (int i = (int)((int64_t)P * th / nthr); i < (int)((int64_t)P * (th + 1) / nthr); i++) one(i, dh, dl);
+    };
+    if (nthr == 1) {
+        range(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (int th = 1; th < nthr; th++) pool.emplace_back(range, th);
+        range(0);
+        for (auto &th : pool) th.join();
     }
     // Mod's balanced base-128 digits, summed per 32-digit chunk n into the 224-bit
     // value V_n = sum_u Mod_(32n+u) 128^u, kept as 8 words of a 256-bit two's
     // complement number (|V_n| < 2^223, so word 7 is the sign extension)
-    std::vector<int> md = balanced128(Mod, t->Dout);
-    const int nch = (t->Dout + 31) / 32;
-    std::vector<uint32_t> vt((size_t)nch * 8, 0u);
+    std::vector<int> md = balanced128(Mod, o.Dout);
+    const int nch = (o.Dout + 31) / 32;
+    o.vtab.assign((size_t)nch * 8, 0u);
     for (int n = 0; n < nch; n++) {
-        uint32_t *w = &vt[(size_t)n * 8];
+        uint32_t *w = &o.vtab[(size_t)n * 8];
         for (int u = 0; u < 32; u++) {
             const int r = 32 * n + u;
-            if (r >= t->Dout || md[r] == 0) continue;
+            if (r >= o.Dout || md[r] == 0) continue;
             const int bit = 7 * u, k = bit / 32;
             const uint64_t v = (uint64_t)((int64_t)md[r] * ((int64_t)1 << (bit % 32)));  // two's complement
             uint32_t add[8];
@@ -1904,23 +1945,39 @@ static gbmm_status build_tables(crt_tables *t, int P) {
             }
         }
     }
+    // the constant (p, 1/p) list: the same for every table, written with each
+    o.cmod.resize(4 * CMOD_PAIRS);
+    for (int q = 0; q < CMOD_PAIRS; q++) {
+        o.cmod[4 * q] = (float)pr[2 * q];
+        o.cmod[4 * q + 1] = (float)pr[2 * q + 1];
+        o.cmod[4 * q + 2] = 1.0f / (float)pr[2 * q];
+        o.cmod[4 * q + 3] = 1.0f / (float)pr[2 * q + 1];
+    }
+}
+
+static gbmm_status build_tables(crt_tables *t, int P) {
+    crt_tables_host o;
+    build_tables_host(P, o);
+    t->P = o.P;
+    t->Pp = o.Pp;
+    t->Dout = o.Dout;
+    t->NT = o.NT;
+    t->h_mods = o.mods;
+    // every upload has landed before the tables are used (kernels that use them may
+    // run on any stream)
     {
-        // the constant (p, 1/p) list: the same for every table, written with each
-        std::vector<float> cm(4 * CMOD_PAIRS);
-        for (int q = 0; q < CMOD_PAIRS; q++) {
-            cm[4 * q] = (float)pr[2 * q];
-            cm[4 * q + 1] = (float)pr[2 * q + 1];
-            cm[4 * q + 2] = 1.0f / (float)pr[2 * q];
-            cm[4 * q + 3] = 1.0f / (float)pr[2 * q + 1];
-        }
-        GBMM_CUDA_TRY(cudaMemcpyToSymbol(c_modpair, cm.data(), cm.size() * sizeof(float)));
+        cudaStream_t cs = copy_stream();
+        if (!cs) return set_error(GBMM_ERR_CUDA, "no copy stream");
+        GBMM_CUDA_TRY(cudaMemcpyToSymbolAsync(c_modpair, o.cmod.data(), o.cmod.size() * sizeof(float), 0,
+                                              cudaMemcpyHostToDevice, cs));
+        GBMM_CUDA_TRY(cudaStreamSynchronize(cs));
     }
     GBMM_CUDA_TRY(cudaMalloc(&t->d_mods, sizeof(ModConst) * P));
-    GBMM_CUDA_TRY(cudaMemcpy(t->d_mods, t->h_mods.data(), sizeof(ModConst) * P, cudaMemcpyHostToDevice));
-    GBMM_CUDA_TRY(cudaMalloc(&t->d_recon, tab.size() * 2));
-    GBMM_CUDA_TRY(cudaMemcpy(t->d_recon, tab.data(), tab.size() * 2, cudaMemcpyHostToDevice));
-    GBMM_CUDA_TRY(cudaMalloc(&t->d_vtab, vt.size() * 4));
-    GBMM_CUDA_TRY(cudaMemcpy(t->d_vtab, vt.data(), vt.size() * 4, cudaMemcpyHostToDevice));
+    GBMM_TRY(upload_now(t->d_mods, o.mods.data(), sizeof(ModConst) * P));
+    GBMM_CUDA_TRY(cudaMalloc(&t->d_recon, o.recon.size() * 2));
+    GBMM_TRY(upload_now(t->d_recon, o.recon.data(), o.recon.size() * 2));
+    GBMM_CUDA_TRY(cudaMalloc(&t->d_vtab, o.vtab.size() * 4));
+    GBMM_TRY(upload_now(t->d_vtab, o.vtab.data(), o.vtab.size() * 4));
     return GBMM_OK;
 }
 
@@ -1938,22 +1995,35 @@ static gbmm_status residue_table(crt_tables *t, int dxp, int weighted, __nv_bflo
     // [lo_i, lo_i+1, hi_i, hi_i+1]; with P odd the last group's second slot stays zero
     const int rows = residue_cols(t->P);
     std::vector<uint16_t> tab((size_t)rows * dxp, 0);
-    for (int i = 0; i < t->P; i++) {
-        const uint32_t p = pr[i];
-        const size_t r_lo = (size_t)4 * (i >> 1) + (i & 1), r_hi = r_lo + 2;
-        uint32_t v = weighted ? t->h_mods[i].w : 1u;  // (w) 256^j mod p
-        for (int j = 0; j < dxp; j++) {
-            int32_t b = v > p / 2 ? (int32_t)v - (int32_t)p : (int32_t)v;
-            int32_t d0 = ((b + 128) & 255) - 128;
-            int32_t d1 = (b - d0) / 256;
-            tab[r_lo * dxp + j] = bf16_bits((float)d0);  // x1
-            tab[r_hi * dxp + j] = bf16_bits((float)d1);  // x256
-            v = (uint32_t)(((uint64_t)v * 256) % p);
+    auto range = [&](int i0, int i1) {
+        for (int i = i0; i < i1; i++) {
+            const uint32_t p = pr[i];
+            const size_t r_lo = (size_t)4 * (i >> 1) + (i & 1), r_hi = r_lo + 2;
+            uint32_t v = weighted ? t->h_mods[i].w : 1u;  // (w) 256^j mod p
+            for (int j = 0; j < dxp; j++) {
+                int32_t b = v > p / 2 ? (int32_t)v - (int32_t)p : (int32_t)v;
+                int32_t d0 = ((b + 128) & 255) - 128;
+                int32_t d1 = (b - d0) / 256;
+                tab[r_lo * dxp + j] = bf16_small(d0);  // x1
+                tab[r_hi * dxp + j] = bf16_small(d1);  // x256
+                v = (uint32_t)(((uint64_t)v * 256) % p);
+            }
         }
+    };
+    // the moduli's rows are independent: contiguous ranges on up to 16 host threads
+    const int P = t->P;
+    const int nthr = std::max(1, std::min<int>({16, (int)std::thread::hardware_concurrency(), (P * dxp) >> 16}));
+    if (nthr == 1) {
+        range(0, P);
+    } else {
+        std::vector<std::thread> pool;
+        for (int th = 1; th < nthr; th++) pool.emplace_back(range, (int)((int64_t)P * th / nthr), (int)((int64_t)P * (th + 1) / nthr));
+        range(0, P / nthr);
+        for (auto &th : pool) th.join();
     }
     __nv_bfloat16 *d = nullptr;
     GBMM_CUDA_TRY(cudaMalloc(&d, tab.size() * 2));
-    GBMM_CUDA_TRY(cudaMemcpy(d, tab.data(), tab.size() * 2, cudaMemcpyHostToDevice));
+    GBMM_TRY(upload_now(d, tab.data(), tab.size() * 2));
     t->residue[key] = d;
     *out = d;
     return GBMM_OK;
@@ -2688,6 +2758,26 @@ extern "C" gbmm_status gbmmx_crt_params(int64_t bits_a, int64_t bits_b, int32_t 
     if (!nmoduli) return set_error(GBMM_ERR_INVALID, "null pointer");
     *nmoduli = crt_moduli(bits_a, bits_b, k);
     return GBMM_OK;
+}
+
+// Internal hook: builds the host side of the table set for P moduli (no device
+// work) and returns an FNV-1a checksum of its contents; *ms gets the build time.
+extern "C" uint64_t gbmmx_table_build(int32_t P, double *ms) {
+    if (P < 1 || P > 2 * CMOD_PAIRS) return 0;
+    const auto t0 = std::chrono::steady_clock::now();
+    crt_tables_host o;
+    build_tables_host(P, o);
+    const auto t1 = std::chrono::steady_clock::now();
+    if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void *p, size_t n) {
+        const unsigned char *c = (const unsigned char *)p;
+        for (size_t i = 0; i < n; i++) h = (h ^ c[i]) * 1099511628211ull;
+    };
+    mix(o.recon.data(), o.recon.size() * 2);
+    mix(o.vtab.data(), o.vtab.size() * 4);
+    mix(o.mods.data(), o.mods.size() * sizeof(ModConst));
+    return h;
 }
 
 // Test hook: the residue GEMM's form (-1 by the K loop's length, 0 single CTAs,

@@ -39,6 +39,15 @@ enum device_error_bits : uint32_t {
 uint32_t *device_error_word();  // device pointer, allocated once per device
 gbmm_status check_device_error(cudaStream_t s);
 
+// ---- uploads that have landed when they return ---------------------------------
+// A plain cudaMemcpy from pageable host memory may return before its DMA has
+// completed, ordered only against the legacy default stream: a kernel launched
+// right after on a non-blocking stream could read the old contents.  These copy
+// (or fill) on a private per-device stream and wait for that stream.
+gbmm_status upload_now(void *dst, const void *src, size_t bytes);
+gbmm_status fill_now(void *dst, int value, size_t bytes);
+cudaStream_t copy_stream();  // the private stream of the current device
+
 // ---- launch accounting -------------------------------------------------------------
 // Every kernel launch made by the library bumps this counter (reported through
 // gbmm_kernel_launches so a benchmark can state how many of its kernels ran).

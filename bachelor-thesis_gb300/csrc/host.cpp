@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -84,6 +85,36 @@ uint32_t *device_error_word() {
         g_err_words[dev] = p;
     }
     return g_err_words[dev];
+}
+
+cudaStream_t copy_stream() {
+    static std::mutex mu;
+    static std::map<int, cudaStream_t> streams;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = streams.find(dev);
+    if (it != streams.end()) return it->second;
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    streams[dev] = s;
+    return s;
+}
+
+gbmm_status upload_now(void *dst, const void *src, size_t bytes) {
+    cudaStream_t s = copy_stream();
+    if (!s) return set_error(GBMM_ERR_CUDA, "no copy stream");
+    GBMM_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    GBMM_CUDA_TRY(cudaStreamSynchronize(s));
+    return GBMM_OK;
+}
+
+gbmm_status fill_now(void *dst, int value, size_t bytes) {
+    cudaStream_t s = copy_stream();
+    if (!s) return set_error(GBMM_ERR_CUDA, "no copy stream");
+    GBMM_CUDA_TRY(cudaMemsetAsync(dst, value, bytes, s));
+    GBMM_CUDA_TRY(cudaStreamSynchronize(s));
+    return GBMM_OK;
 }
 
 gbmm_status check_device_error(cudaStream_t s) {

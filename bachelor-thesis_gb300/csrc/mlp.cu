@@ -220,10 +220,10 @@ static gbmm_status model_alloc(gbmm_handle h, Model **out) {
 
 static gbmm_status model_upload(Model *md) {
     for (int i = 0; i < NPARAM; i++) md->w16[i] = __float2bfloat16_rn(md->master[i]);
-    GBMM_CUDA_TRY(cudaMemcpy(md->d_master, md->master.data(), NPARAM * 4, cudaMemcpyHostToDevice));
-    GBMM_CUDA_TRY(cudaMemcpy(md->d_w16, md->w16.data(), NPARAM * 2, cudaMemcpyHostToDevice));
-    GBMM_CUDA_TRY(cudaMemset(md->d_m, 0, NPARAM * 4));
-    GBMM_CUDA_TRY(cudaMemset(md->d_v, 0, NPARAM * 4));
+    GBMM_TRY(upload_now(md->d_master, md->master.data(), NPARAM * 4));
+    GBMM_TRY(upload_now(md->d_w16, md->w16.data(), NPARAM * 2));
+    GBMM_TRY(fill_now(md->d_m, 0, NPARAM * 4));
+    GBMM_TRY(fill_now(md->d_v, 0, NPARAM * 4));
     md->step = 0;
     return GBMM_OK;
 }

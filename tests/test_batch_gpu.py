@@ -163,6 +163,28 @@ def test_batched_graph_capture_on_own_stream(g):
     assert counts[2] == counts[3] == counts[4] == counts[1] > 0, counts
 
 
+def test_batched_tables_built_mid_batch(g):
+    """Products too large for the grouped launches run on side streams, and a
+    product whose moduli count the handle has not met yet builds its CRT tables
+    just before its launches.  The tables must have landed in device memory by
+    then, whatever stream the handle is bound to: fresh handles on a stream of
+    their own, eight such products of distinct moduli counts per batch, every
+    product checked against Python integers on sampled entries."""
+    rng = random.Random(41)
+    for rnd in range(3):
+        specs = [(200, 24, 180, 300 + 397 * i + 61 * rnd, 500 + 211 * i) for i in range(8)]
+        jobs = _make_jobs(g, rng, specs)
+        with _own_stream():
+            h = g.Handle()
+            h.matmul_batched(h.jobs([(j[7], j[5], j[6]) for j in jobs]))
+            for K, M, N, A, B, dA, dB, dC in jobs:
+                C = dC.to_ints()
+                for _ in range(6):
+                    y, x = rng.randrange(K), rng.randrange(N)
+                    assert C[y * N + x] == sum(A[y * M + k] * B[k * N + x] for k in range(M)), (rnd, K, M, N)
+            h.close()
+
+
 @pytest.mark.parametrize("path", ["limb", "crt"])
 def test_split_for_very_long_entries(g, path):
     rng = random.Random(11)

@@ -159,3 +159,40 @@ def test_parallel_text_and_gmp_conversions_match_serial(built_lib):
         assert outcomes[0] == outcomes[1] and all(r is not None for r in outcomes[0])
     finally:
         _threads(gbmm, old)
+
+
+# FNV-1a checksums of the host-built CRT tables (reconstruction table, Mod's chunk
+# values, moduli constants), recorded from the first, one-thread bit-by-bit
+# builder; the threaded word-level builder must reproduce them bit for bit.
+TABLE_SUMS = {16: 0xf5de9e1fbafc5d3d, 100: 0x29cee628a1c924d9, 516: 0x89360cf85f8369fa,
+              1023: 0x583a7024eea96029}
+
+
+@pytest.mark.parametrize("P", sorted(TABLE_SUMS))
+def test_crt_table_build_is_unchanged(built_lib, P):
+    f = built_lib.gbmmx_table_build
+    f.restype = ctypes.c_uint64
+    f.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
+    ms = ctypes.c_double()
+    assert f(P, ctypes.byref(ms)) == TABLE_SUMS[P]
+
+
+def test_no_plain_host_to_device_copies():
+    """A plain cudaMemcpy from pageable host memory may return before its DMA has
+    landed, ordered only against the legacy default stream, so a kernel launched
+    next on a non-blocking stream can read stale data (a batch's side-stream
+    products read fresh CRT tables this way).  Host-to-device copies and fills
+    that are not stream-ordered go through upload_now / fill_now instead."""
+    csrc = os.path.join(ROOT, "bachelor-thesis_gb300", "csrc")
+    bad = []
+    for name in sorted(os.listdir(csrc)):
+        if not name.endswith((".cu", ".cpp", ".cuh", ".h")):
+            continue
+        for no, line in enumerate(open(os.path.join(csrc, name)), 1):
+            code = line.split("//")[0]
+            if re.search(r"\bcudaMemcpy\([^;]*cudaMemcpyHostToDevice", code) or \
+                    re.search(r"\bcudaMemcpyToSymbol\(", code) or re.search(r"\bcudaMemset\(", code):
+                bad.append(f"{name}:{no}: {line.strip()}")
+    # the device error word is cleared once with a device-wide synchronisation after it
+    bad = [b for b in bad if "cudaMemset(p, 0, sizeof(uint32_t))" not in b]
+    assert not bad, bad
