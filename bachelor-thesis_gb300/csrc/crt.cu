@@ -64,7 +64,6 @@ constexpr int CTA_THREADS = 192;   // warp 0 TMA, warp 1 MMA, warps 2..5 epilogu
 constexpr int CTA_THREADS8 = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue (two per lane quadrant)
 constexpr int RES_EPI_WARPS = 16;   // residue GEMM: four epilogue warps per lane quadrant
 constexpr int RES_THREADS = 32 * (2 + RES_EPI_WARPS);
-constexpr int PROD_THREADS = 32 * (2 + 16);  // product GEMM: two groups of 8 epilogue warps, one per TMEM buffer
 constexpr int RTAB = 256;          // reconstruction table rows are padded to a multiple of this
 }  // namespace
 
@@ -756,7 +755,7 @@ constexpr int YPAD = 16;  // Y's entry rows are padded to a multiple of this (wh
 // the even CTA U1's 64 rows and the odd CTA U0's, so per SM a K step moves 40 KB
 // instead of 48 KB and the MMAs read 12 KB of shared memory instead of 16 KB.
 template <int STAGES, bool PAIR, bool GRP>
-__global__ void __launch_bounds__(PROD_THREADS, 1)
+__global__ void __launch_bounds__(CTA_THREADS8, 1)
     k_crt_product(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, ProductArgs a0,
                   Group<ProductJob> grp, uint32_t *err) {
     extern __shared__ uint8_t smem_raw[];
@@ -777,7 +776,7 @@ __global__ void __launch_bounds__(PROD_THREADS, 1)
             }
             for (int b = 0; b < 2; b++) {
                 tc::mbar_init(&bars->tfull[b], 1);
-                tc::mbar_init(&bars->tempty[b], 16);  // the even CTA's: the buffer's 8 epilogue warps in each CTA
+                tc::mbar_init(&bars->tempty[b], 16);  // the even CTA's: 8 epilogue warps of each CTA
             }
             bars->abort_flag = 0;
             tc::fence_mbar_init();
@@ -894,16 +893,14 @@ __global__ void __launch_bounds__(PROD_THREADS, 1)
             }
         }
     } else {
-        // Two groups of 8 warps; group gb (warps 2..9, 10..17) owns TMEM buffer gb and so
-        // takes every other tile: the epilogues of two tiles run at once.  Within a
-        // group, warp -> lane quadrant warp % 4 and output columns 32 * half + [0, 32),
-        // read and reduced 16 columns at a time (the buffer goes back to the MMA after
-        // the second read).
-        const int quad = warp & 3, gb = (warp - 2) >> 3, half = ((warp - 2) >> 2) & 1;
+        // warp (2..9) -> lane quadrant warp % 4, output columns 32 * ((warp - 2) / 4) + [0, 32).
+        // All four accumulators' 32 columns are read first, so the buffer goes back to the
+        // MMA before the arithmetic.
+        const int quad = warp & 3, half = (warp - 2) >> 2;
         const uint32_t lb = tmem + ((uint32_t)(quad * 32) << 16);
         const uint32_t tempty0 = PAIR ? tc::mapa(tc::smem_u32(&bars->tempty[0]), 0) : 0;
-        int lt = gb;
-        for (int64_t T = t0 + gb * tstep; T < total; T += 2 * tstep, lt += 2) {
+        int lt = 0;
+        for (int64_t T = t0; T < total; T += tstep, lt++) {
             ProductArgs a;
             const CUtensorMap *mA, *mB;
             const int64_t t = tile_job(T, a, mA, mB);
@@ -915,27 +912,26 @@ __global__ void __launch_bounds__(PROD_THREADS, 1)
             const int xh = (r % a.nxt) * PBX + half * 32;  // this warp's 32 output columns
             if (!tc::mbar_wait(&bars->tfull[b], (lt >> 1) & 1)) { set_abort(bars, err); break; }
             tc::fence_after_sync();
+            uint32_t D11[32], D10[32], D01[32], D00[32];
+            const uint32_t col = 256u * b + half * 32;
+            tc::tmem_ld32(lb + col, D11);
+            tc::tmem_ld32(lb + col + PBX, D10);
+            tc::tmem_ld32(lb + col + 2 * PBX, D01);
+            tc::tmem_ld32(lb + col + 3 * PBX, D00);
+            tc::tmem_ld_wait();
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) {
+                if (PAIR) tc::mbar_arrive_cluster(tempty0 + 8u * b);
+                else tc::mbar_arrive(&bars->tempty[b]);
+            }
             const ModConst mc = a.mods[mi];
             const float pf = (float)mc.p;
             const int64_t erow = (int64_t)y * a.npad + xh;  // entry index of this warp's first column
             __nv_bfloat16 *yplane = a.Y + (int64_t)(2 * mi) * 64;  // hi plane; lo plane 64 elements on
 #pragma unroll
             for (int c = 0; c < 32; c += 16) {
-                uint32_t d11[16], d10[16], d01[16], d00[16];
-                const uint32_t col = 256u * b + half * 32 + c;
-                tc::tmem_ld16(lb + col, d11);
-                tc::tmem_ld16(lb + col + PBX, d10);
-                tc::tmem_ld16(lb + col + 2 * PBX, d01);
-                tc::tmem_ld16(lb + col + 3 * PBX, d00);
-                tc::tmem_ld_wait();
-                if (c == 16) {
-                    tc::fence_before_sync();
-                    __syncwarp();
-                    if (lane == 0) {
-                        if (PAIR) tc::mbar_arrive_cluster(tempty0 + 8u * b);
-                        else tc::mbar_arrive(&bars->tempty[b]);
-                    }
-                }
+                const uint32_t *d11 = D11 + c, *d10 = D10 + c, *d01 = D01 + c, *d00 = D00 + c;
                 uint32_t phi[8], plo[8];
 #pragma unroll
                 for (int j = 0; j < 16; j += 2) {
@@ -2232,12 +2228,12 @@ static gbmm_status launch_product(const ProductPlan &pp, cudaStream_t s) {
     LaunchScope ls_("k_crt_product", s);
     if (pp.pair) {
         GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES_PAIR, true, false>, pp.smem));
-        GBMM_TRY(launch_pairs(k_crt_product<PROD_STAGES_PAIR, true, false>, PROD_THREADS, pp.pa.ntiles, pp.smem, s,
+        GBMM_TRY(launch_pairs(k_crt_product<PROD_STAGES_PAIR, true, false>, CTA_THREADS8, pp.pa.ntiles, pp.smem, s,
                               pp.tmA, pp.tmB, pp.pa, none, err));
     } else {
         GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES, false, false>, pp.smem));
         dim3 grid((unsigned)std::min<int64_t>(pp.pa.ntiles, num_sms()));
-        k_crt_product<PROD_STAGES, false, false><<<grid, PROD_THREADS, pp.smem, s>>>(pp.tmA, pp.tmB, pp.pa, none, err);
+        k_crt_product<PROD_STAGES, false, false><<<grid, CTA_THREADS8, pp.smem, s>>>(pp.tmA, pp.tmB, pp.pa, none, err);
     }
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
@@ -2648,7 +2644,7 @@ gbmm_status crt_group_launch(crt_group *g, const char *d_blob, cudaStream_t s, c
         GBMM_TRY(set_smem((const void *)kern, g->smem_prod));
         const dim3 grid((unsigned)std::min<int64_t>(g->sprod.total, num_sms()));
         LaunchScope ls_("k_crt_product", s);
-        kern<<<grid, PROD_THREADS, g->smem_prod, s>>>(zmap, zmap, none, group_at<ProductJob>(d_blob, g->sprod), err);
+        kern<<<grid, CTA_THREADS8, g->smem_prod, s>>>(zmap, zmap, none, group_at<ProductJob>(d_blob, g->sprod), err);
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     // the products with post steps first: their shifted adds then run on s2 while
