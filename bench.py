@@ -377,7 +377,9 @@ def run_gpu(args, W, world, rank, local):
     hA, hAs, hB, hBs = pin(Al), pin(As), pin(Bl), pin(Bs)
     hC = pin(np.zeros((cn, K * N), dtype=np.uint32))
     hCs = pin(np.zeros(K * N, dtype=np.int32))
-    ne = max(4, args.steps)
+    # 40 products (or --steps, if more): the pipeline's fill (the first product's
+    # upload) and drain (the last one's download) spread over the whole stream
+    ne = max(40, args.steps)
     hjobs = h.host_jobs([(K, M, N, (hA, hAs), (hB, hBs), (hC, hCs))] * ne, path=path, method=method, cutoff=cutoff)
     h.matmul_host(h.host_jobs([(K, M, N, (hA, hAs), (hB, hBs), (hC, hCs))] * 2, path=path, method=method,
                               cutoff=cutoff))
