@@ -221,7 +221,8 @@ typedef struct gbmm_job {
  * the others (Winograd trees, larger CRT products) run side by side on streams
  * forked from the handle's stream.
  * The launch sequence is captured into a CUDA graph and replayed on later calls
- * with the same job signature.  The CRT_SINGLE / CRT_PAIR plans fix the tile
+ * with the same job signature; capture needs the handle bound to a created stream
+ * (gbmm_set_stream): on the legacy default stream every call runs eagerly.  The CRT_SINGLE / CRT_PAIR plans fix the tile
  * form of a product run alone; in the grouped launches every product uses the
  * grouped forms (one-CTA product tiles, CTA-pair reconstruction tiles).
  * replaces: the unused chunked-stream job DAG (mat-gpu/job.cu:32-338). */
