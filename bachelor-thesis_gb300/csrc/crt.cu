@@ -220,6 +220,20 @@ __device__ __forceinline__ int group_job(const int64_t *tile0, int n, int64_t T)
     }
     return lo;
 }
+// A role's walk through the tiles only moves forward: the current job and its tile
+// range are kept until the walk leaves that range, so most tiles need no lookup
+// (the binary search is a chain of dependent loads).
+struct GroupCursor {
+    int j = -1;
+    int64_t beg = 0, end = 0;
+    template <typename J>
+    __device__ __forceinline__ void seek(const Group<J> &g, int64_t T) {
+        if (j >= 0 && T < end) return;
+        j = group_job(g.tile0, g.njobs, T);
+        beg = __ldg(g.tile0 + j);
+        end = __ldg(g.tile0 + j + 1);
+    }
+};
 
 // ======================================================================================
 // 1. digits
@@ -476,16 +490,17 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
     const int ngran = CL ? 32 : 16;
     const int64_t total = GRP ? grp.tile0[grp.njobs] : (int64_t)a0.ntiles;
     // global tile T -> its operand's arguments and maps, and the tile within it
+    GroupCursor cur;
     auto tile_job = [&](int64_t T, ResidueArgs &a, const CUtensorMap *&mD, const CUtensorMap *&mT,
                         const CUtensorMap *&mR) -> int {
         if (GRP) {
-            const int j = group_job(grp.tile0, grp.njobs, T);
-            const ResidueJob *J = grp.jobs + j;
+            cur.seek(grp, T);
+            const ResidueJob *J = grp.jobs + cur.j;
             a = J->a;
             mD = &J->tmD;
             mT = &J->tmT;
             mR = &J->tmR;
-            return (int)(T - __ldg(grp.tile0 + j));
+            return (int)(T - cur.beg);
         }
         a = a0;
         mD = &tmD;
@@ -795,14 +810,15 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
     const uint32_t tmem = bars->tmem_base;
     const int64_t total = GRP ? grp.tile0[grp.njobs] : a0.ntiles;
     // global tile T -> its product's arguments and maps, and the tile within it
+    GroupCursor cur;
     auto tile_job = [&](int64_t T, ProductArgs &a, const CUtensorMap *&mA, const CUtensorMap *&mB) -> int64_t {
         if (GRP) {
-            const int j = group_job(grp.tile0, grp.njobs, T);
-            const ProductJob *J = grp.jobs + j;
+            cur.seek(grp, T);
+            const ProductJob *J = grp.jobs + cur.j;
             a = J->a;
             mA = &J->tmA;
             mB = &J->tmB;
-            return T - __ldg(grp.tile0 + j);
+            return T - cur.beg;
         }
         a = a0;
         mA = &tmA;
@@ -925,8 +941,10 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
                 if (PAIR) tc::mbar_arrive_cluster(tempty0 + 8u * b);
                 else tc::mbar_arrive(&bars->tempty[b]);
             }
-            const ModConst mc = a.mods[mi];
-            const float pf = (float)mc.p;
+            // p and fl(1/p) of modulus mi from the constant list (a broadcast: the warp's
+            // lanes share mi); the same values as the moduli table's
+            const float4 cmp = c_modpair[mi >> 1];
+            const float pf = (mi & 1) ? cmp.y : cmp.x, ipf = (mi & 1) ? cmp.w : cmp.z;
             const int64_t erow = (int64_t)y * a.npad + xh;  // entry index of this warp's first column
             __nv_bfloat16 *yplane = a.Y + (int64_t)(2 * mi) * 64;  // hi plane; lo plane 64 elements on
 #pragma unroll
@@ -939,11 +957,11 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
 #pragma unroll
                     for (int u = 0; u < 2; u++) {
                         // |a1 u0 + a0 u1| <= 2^24; each step below stays under 257 * 32772 < 2^24
-                        const float r2 = red(__uint_as_float(d11[j + u]), pf, mc.inv_p);
-                        const float r1 = red(__uint_as_float(d10[j + u]) + __uint_as_float(d01[j + u]), pf, mc.inv_p);
-                        const float r0 = red(__uint_as_float(d00[j + u]), pf, mc.inv_p);
-                        const float tt = red(__fmaf_rn(256.f, r2, r1), pf, mc.inv_p);
-                        bal_split(red(__fmaf_rn(256.f, tt, r0), pf, mc.inv_p), h2[u], l2[u]);
+                        const float r2 = red(__uint_as_float(d11[j + u]), pf, ipf);
+                        const float r1 = red(__uint_as_float(d10[j + u]) + __uint_as_float(d01[j + u]), pf, ipf);
+                        const float r0 = red(__uint_as_float(d00[j + u]), pf, ipf);
+                        const float tt = red(__fmaf_rn(256.f, r2, r1), pf, ipf);
+                        bal_split(red(__fmaf_rn(256.f, tt, r0), pf, ipf), h2[u], l2[u]);
                     }
                     phi[j / 2] = bf16x2_bits(h2[0], h2[1]);
                     plo[j / 2] = bf16x2_bits(l2[0], l2[1]);
@@ -1058,14 +1076,15 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
     // entry tiles [tbeg, total) in global numbering; tile_job maps one to its
     // product's arguments and maps and to the entry tile within that product
     const int64_t tbeg = GRP ? 0 : a0.mt0, total = GRP ? grp.tile0[grp.njobs] : a0.nmt;
+    GroupCursor cur;
     auto tile_job = [&](int64_t T, ReconArgs &a, const CUtensorMap *&mY, const CUtensorMap *&mT) -> int64_t {
         if (GRP) {
-            const int j = group_job(grp.tile0, grp.njobs, T);
-            const ReconJob *J = grp.jobs + j;
+            cur.seek(grp, T);
+            const ReconJob *J = grp.jobs + cur.j;
             a = J->a;
             mY = &J->tmY;
             mT = &J->tmT;
-            return T - __ldg(grp.tile0 + j);
+            return T - cur.beg;
         }
         a = a0;
         mY = &tmY;

@@ -1049,12 +1049,17 @@ def main():
     ap.add_argument("--limb-cutoff", type=int, default=32)
     ap.add_argument("--limb-steps", type=int, default=2)
     ap.add_argument("--stream-jobs", type=int, default=10000, help="configuration 5: jobs in the evaluated stream")
+    ap.add_argument("--jobs", type=int, default=0,
+                    help="configuration 4: draw only the first N of its products (small cases for profiling)")
     ap.add_argument("--size", type=int, default=0,
                     help="override K=M=N of a single-product workload (small cases for profiling)")
     ap.add_argument("--bits", type=int, default=0, help="override the entry bit length")
     ap.add_argument("--shape", default="", help="override K,M,N (C is KxN, inner dimension M)")
     args = ap.parse_args()
     W = WORKLOADS[args.workload]
+    if args.jobs and args.workload == "cfg4":
+        W = dict(W, jobs=min(args.jobs, W["jobs"]),
+                 label=f"the first {min(args.jobs, W['jobs'])} of " + W["label"] + " (profiling subset)")
     if (args.size or args.bits or args.shape) and args.workload not in ("cfg4", "cfg5"):
         K = M = N = args.size or W["K"]
         if args.shape:
