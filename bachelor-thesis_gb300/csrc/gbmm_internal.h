@@ -212,6 +212,12 @@ gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const 
 // over k, directly or after one limb-half split), the arena bytes it then takes,
 // and its collection into the group (workspace carved, nothing launched)
 bool crt_groupable(const Plan &p, int la, int lb, int m, int k, int n);
+// Winograd's breadth-first tree with CRT leaf products (GBMM_METHOD_WINOGRAD_CRT):
+// whether it takes this product, its workspace, and the product itself
+bool wino_crt_ok(int la, int lb, int m, int k, int n, int cutoff);
+size_t wino_crt_ws(int la, int lb, int N, int cn, int cutoff);
+gbmm_status wino_crt(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, int cutoff,
+                     cudaStream_t s);
 size_t crt_group_job_ws(const Plan &p, int la, int lb, int m, int k, int n);
 gbmm_status crt_collect(gbmm_handle h, crt_group *g, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b,
                         const Plan &p);

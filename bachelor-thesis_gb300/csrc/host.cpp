@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <atomic>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -1057,6 +1058,151 @@ gbmm_status matmul_limb(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, con
     if (accumulate) return rec_square(ctx, method, c, a, b, a.rows, levels_for(a.rows, cutoff), 1);
     return squarify(ctx, method, c, a, b);
 }
+
+// ---- Winograd's tree with CRT leaf products ------------------------------------------------
+// Host twins of the tree's view arithmetic (wt_quad / wt_dense / wt_operand in limb.cu):
+// the operand of node `node` at level d is a quadrant of an ancestor's operand or
+// one of the dense sums of its parent.
+static gbmm_mat wt_quad_h(gbmm_mat m, int qr, int qc, int h) {
+    const int64_t off = (int64_t)qr * h * m.rs + (int64_t)qc * h;
+    m.limbs += off;
+    m.sizes += off;
+    m.rows = h;
+    m.cols = h;
+    return m;
+}
+static gbmm_mat wt_dense_h(uint32_t *limbs, int32_t *sizes, int64_t q, int h, int cap) {
+    gbmm_mat m;
+    memset(&m, 0, sizeof m);
+    const int64_t e = (int64_t)h * h;
+    m.limbs = limbs + q * e * cap;
+    m.sizes = sizes + q * e;
+    m.rs = h;
+    m.ld = e;
+    m.rows = h;
+    m.cols = h;
+    m.nlimbs = cap;
+    return m;
+}
+static gbmm_mat wt_operand_h(const WinoTree &t, int which, int d, int64_t node) {
+    gbmm_mat v = which ? t.B : t.A;
+    int h = t.N;
+    int64_t pw = 1;
+    for (int l = 1; l < d; l++) pw *= 7;
+    for (int l = 1; l <= d; l++) {
+        const int64_t self = node / pw;  // this node's ancestor at level l
+        const int j = (int)(self % 7);
+        const int64_t parent = self / 7;
+        h >>= 1;
+        int sidx = -1;
+        if (which == 0) {
+            if (j == 0) v = wt_quad_h(v, 0, 0, h);
+            else if (j == 1) v = wt_quad_h(v, 0, 1, h);
+            else if (j == 3) v = wt_quad_h(v, 1, 1, h);
+            else sidx = j == 2 ? 3 : j - 4;
+        } else {
+            if (j == 0) v = wt_quad_h(v, 0, 0, h);
+            else if (j == 1) v = wt_quad_h(v, 1, 0, h);
+            else if (j == 2) v = wt_quad_h(v, 1, 1, h);
+            else sidx = j == 3 ? 3 : j - 4;
+        }
+        if (sidx >= 0)
+            v = which ? wt_dense_h(t.sb_limbs[l], t.sb_sizes[l], 4 * parent + sidx, h, t.capSB)
+                      : wt_dense_h(t.sa_limbs[l], t.sa_sizes[l], 4 * parent + sidx, h, t.capSA);
+        pw /= 7;
+    }
+    return v;
+}
+
+static int64_t pow7_h(int l) {
+    int64_t r = 1;
+    while (l-- > 0) r *= 7;
+    return r;
+}
+static constexpr int WINO_CRT_MAX_LEVELS = 4;  // 2401 leaf products at most
+
+// Whether a product takes Winograd's tree with CRT leaves: square, at least one
+// level above the cutoff, and leaves that one CRT pass takes (k <= 512, at most
+// 1023 moduli for the one-limb-longer sums).
+bool wino_crt_ok(int la, int lb, int m, int k, int n, int cutoff) {
+    if (m != k || k != n || cutoff < 1) return false;
+    const int L = levels_for(m, cutoff);
+    if (L < 1 || L > WINO_CRT_MAX_LEVELS) return false;
+    const int hL = m >> L;
+    return crt_single_pass(hL) && crt_feasible(la + 1, lb + 1, hL);
+}
+
+// Workspace of wino_crt: the tree, a result with headroom when C has too few
+// planes, every leaf's CRT workspace and the records' blob.
+size_t wino_crt_ws(int la, int lb, int N, int cn, int cutoff) {
+    const int L = levels_for(N, cutoff), hL = N >> L;
+    const int capSA = la + 1, capSB = lb + 1, need = limbs_needed(la, lb, N, L + 2);
+    const int capP = std::max(cn, need);
+    const int64_t leaves = pow7_h(L);
+    return wino_bf_ws(N, L, capSA, capSB, capP) + (cn < need ? mat_bytes((int64_t)N * N, capP) : 0) +
+           (size_t)leaves * (crt_group_ws(capSA, capSB, hL, hL, hL) + 1024) + 4096 * (size_t)leaves + 16384;
+}
+
+// C = A B through Winograd's breadth-first tree down to the cutoff: the sums of
+// every level and the combinations as limb kernels (k_wino_sums / k_wino_combine),
+// the 7^L leaf products as CRT products in the grouped launches, one persistent
+// launch per CRT stage over all leaves.  The same tree and operation order as the
+// limb form, so the same exact result.  The caller checked wino_crt_ok.
+gbmm_status wino_crt(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const gbmm_mat &b, int cutoff,
+                     cudaStream_t s) {
+    const int N = a.rows, L = levels_for(N, cutoff), hL = N >> L;
+    const int need = limbs_needed(a.nlimbs, b.nlimbs, N, L + 2);
+    WinoTree t;
+    t.A = a;
+    t.B = b;
+    t.N = N;
+    t.levels = L;
+    t.capSA = a.nlimbs + 1;
+    t.capSB = b.nlimbs + 1;
+    t.capP = std::max(c.nlimbs, need);
+    const size_t mark = arena_mark(h);
+    gbmm_status st = GBMM_OK;
+    auto fail = [&](gbmm_status e) {
+        arena_release(h, mark);
+        return e;
+    };
+    t.C = c;
+    if (c.nlimbs < need && !arena_mat(h, N, N, t.capP, t.C)) return fail(set_error(GBMM_ERR_NOMEM, "winograd crt: result"));
+    int64_t np = 1;
+    for (int d = 1; d <= L; d++) {
+        const int64_t hd = N >> d, e = hd * hd;
+        t.sa_limbs[d] = (uint32_t *)arena_alloc(h, (size_t)(4 * np * e) * t.capSA * 4);
+        t.sa_sizes[d] = (int32_t *)arena_alloc(h, (size_t)(4 * np * e) * 4);
+        t.sb_limbs[d] = (uint32_t *)arena_alloc(h, (size_t)(4 * np * e) * t.capSB * 4);
+        t.sb_sizes[d] = (int32_t *)arena_alloc(h, (size_t)(4 * np * e) * 4);
+        t.p_limbs[d] = (uint32_t *)arena_alloc(h, (size_t)(7 * np * e) * t.capP * 4);
+        t.p_sizes[d] = (int32_t *)arena_alloc(h, (size_t)(7 * np * e) * 4);
+        if (!t.sa_limbs[d] || !t.sa_sizes[d] || !t.sb_limbs[d] || !t.sb_sizes[d] || !t.p_limbs[d] || !t.p_sizes[d])
+            return fail(set_error(GBMM_ERR_NOMEM, "winograd crt: tree exceeds the reserved workspace"));
+        np *= 7;
+    }
+    // every leaf product joins one group: its workspace is carved now, nothing launched
+    std::unique_ptr<crt_group, void (*)(crt_group *)> g(crt_group_create(), crt_group_destroy);
+    for (int64_t leaf = 0; leaf < np; leaf++) {
+        const gbmm_mat la = wt_operand_h(t, 0, L, leaf), lb = wt_operand_h(t, 1, L, leaf);
+        const gbmm_mat lp = wt_dense_h(t.p_limbs[L], t.p_sizes[L], leaf, hL, t.capP);
+        st = crt_group_add(h, g.get(), lp, la, lb, 32LL * la.nlimbs, 32LL * lb.nlimbs, 0);
+        if (st != GBMM_OK) return fail(st);
+    }
+    const std::vector<char> &blob = crt_group_blob(g.get());
+    char *d_blob = (char *)arena_alloc(h, blob.size());
+    if (!d_blob) return fail(set_error(GBMM_ERR_NOMEM, "winograd crt: records"));
+    // stream-ordered: the region may still serve earlier work on s (pageable source:
+    // staged before the call returns)
+    cudaError_t ce = cudaMemcpyAsync(d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice, s);
+    if (ce != cudaSuccess) return fail(cuda_error(ce, "winograd crt: records"));
+    for (int d = 1; d <= L && st == GBMM_OK; d++) st = launch_wino_sums(t, d, s);
+    if (st == GBMM_OK) st = crt_group_launch(g.get(), d_blob, s, nullptr, nullptr);
+    for (int d = L; d >= 1 && st == GBMM_OK; d--) st = launch_wino_combine(t, d, s);
+    if (st == GBMM_OK && t.C.limbs != c.limbs) st = launch_mat_copy(c, t.C, s);
+    arena_release(h, mark);
+    return st;
+}
 }  // namespace gbmm
 
 namespace gbmm {
@@ -1111,6 +1257,9 @@ static bool direct_ok(const Plan &p, int la, int lb, int k) {
 // Upper bound of the device workspace dispatch() carves from the arena.
 size_t dispatch_ws(const Plan &p, int la, int lb, int m, int k, int n, int cn, int accumulate) {
     if (m == 0 || n == 0 || k == 0) return 0;
+    if (p.path == GBMM_PATH_CRT && p.method == GBMM_METHOD_WINOGRAD_CRT && !accumulate &&
+        wino_crt_ok(la, lb, m, k, n, p.cutoff))
+        return wino_crt_ws(la, lb, m, cn, p.cutoff);
     if (direct_ok(p, la, lb, k)) {
         if (p.path == GBMM_PATH_CRT) return crt_workspace_bytes(la, lb, m, k, n, cn);
         if (p.method == GBMM_METHOD_NAIVE) return 0;
@@ -1146,6 +1295,9 @@ gbmm_status dispatch(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, const 
     const int m = a.rows, k = a.cols, n = b.cols;
     if (m == 0 || n == 0) return GBMM_OK;
     if (k == 0) return accumulate ? GBMM_OK : launch_mat_zero(c, s);
+    if (p.path == GBMM_PATH_CRT && p.method == GBMM_METHOD_WINOGRAD_CRT && !accumulate &&
+        wino_crt_ok(a.nlimbs, b.nlimbs, m, k, n, p.cutoff))
+        return wino_crt(h, c, a, b, p.cutoff, s);
     if (direct_ok(p, a.nlimbs, b.nlimbs, k)) {
         if (p.path == GBMM_PATH_CRT) {
             const int saved = h->crt_tiles;
@@ -1292,7 +1444,8 @@ gbmm_status resolve_plan(gbmm_handle h, const gbmm_mat &a, const gbmm_mat &b, co
     p.method = o.method ? o.method : GBMM_METHOD_WINOGRAD;
     p.cutoff = o.cutoff > 0 ? o.cutoff : h->limb_cutoff;
     p.nprimes = o.nprimes;
-    p.path = o.path;
+    // the tree with CRT leaves is a CRT form whatever path was asked for
+    p.path = p.method == GBMM_METHOD_WINOGRAD_CRT ? GBMM_PATH_CRT : o.path;
     if (p.path != GBMM_PATH_CRT && p.path != GBMM_PATH_LIMB) return set_error(GBMM_ERR_INVALID, "unknown path %d", o.path);
     return GBMM_OK;
 }

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libgbmm.so")
 
 OK, ERR_INVALID, ERR_CAPACITY, ERR_CUDA, ERR_PARSE, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(8)
 PATH_AUTO, PATH_LIMB, PATH_CRT = 0, 1, 2
-METHOD_NAIVE, METHOD_STRASSEN, METHOD_WINOGRAD, METHOD_NAIVE_REC = 1, 3, 35, 4
+METHOD_NAIVE, METHOD_STRASSEN, METHOD_WINOGRAD, METHOD_NAIVE_REC, METHOD_WINOGRAD_CRT = 1, 3, 35, 4, 350
 # gbmm_plan: the candidate plans the autotuner times and the cost model predicts
 (PLAN_LIMB_NAIVE, PLAN_LIMB_W32, PLAN_LIMB_W64, PLAN_LIMB_W128, PLAN_CRT, PLAN_CRT_SINGLE, PLAN_CRT_PAIR,
  PLAN_CRT_SPLIT) = range(8)

@@ -70,7 +70,12 @@ typedef enum gbmm_method {
     GBMM_METHOD_NAIVE = 1,      /* one per-entry kernel over the whole product */
     GBMM_METHOD_STRASSEN = 3,   /* Strassen 7-product recursion, 3 temporaries */
     GBMM_METHOD_WINOGRAD = 35,  /* Winograd 7-product recursion, 3 temporaries */
-    GBMM_METHOD_NAIVE_REC = 4   /* 8-product block recursion */
+    GBMM_METHOD_NAIVE_REC = 4,  /* 8-product block recursion */
+    /* Winograd's tree down to the cutoff with CRT leaf products (no mat-gpu
+     * counterpart): the tree's sums and combinations run as limb kernels, its 7^L
+     * leaf products together in the grouped CRT launches.  Square products of
+     * single-pass leaves (k <= 512); others take the plain CRT form. */
+    GBMM_METHOD_WINOGRAD_CRT = 350
 } gbmm_method;
 
 /* Candidate plans for one product: the plans gbmm_autotune times and the

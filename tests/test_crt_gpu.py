@@ -145,6 +145,30 @@ def test_crt_residue_forms(g, mode, K, M, N, bits):
     assert dC.to_ints() == exp
 
 
+@pytest.mark.parametrize("K,M,N,bits,cutoff", [(64, 64, 64, 1024, 32), (128, 128, 128, 2048, 32),
+                                               (96, 96, 96, 700, 24), (128, 128, 128, 4096, 64),
+                                               (64, 32, 64, 512, 16)])
+def test_winograd_tree_with_crt_leaves(g, K, M, N, bits, cutoff):
+    """GBMM_METHOD_WINOGRAD_CRT: Winograd's breadth-first tree (limb-kernel sums
+    and combinations) whose 7^L leaf products run as CRT products in the grouped
+    launches, one or two levels, leaves of 24 to 64.  The result equals the plain
+    CRT form's bit for bit, and sampled entries equal Python integers; a
+    rectangular product takes the plain CRT form."""
+    rng = random.Random(K * 3 + bits + cutoff)
+    A = _signed(rng, K * M, bits)
+    B = _signed(rng, M * N, bits)
+    dA = g.DeviceMatrix.from_ints(K, M, A)
+    dB = g.DeviceMatrix.from_ints(M, N, B)
+    ref = _crt(g, K, M, N, dA, dB)
+    dC = g.DeviceMatrix(K, N, ref.nlimbs)
+    g.default_handle().matmul(dC, dA, dB, path=g.PATH_CRT, method=g.METHOD_WINOGRAD_CRT, cutoff=cutoff)
+    got = dC.to_ints()
+    assert got == ref.to_ints()
+    for _ in range(8):
+        y, x = rng.randrange(K), rng.randrange(N)
+        assert got[y * N + x] == sum(A[y * M + k] * B[k * N + x] for k in range(M))
+
+
 def test_crt_cancellation_and_tiny_results(g):
     # rows of A whose products cancel exactly (C entries 0 or tiny): the sign is
     # then decided on the two's-complement path of the reconstruction
