@@ -420,8 +420,9 @@ __device__ __forceinline__ void residue_fold(const uint32_t (&v)[32], int mi0, b
 // row blocks and the same table columns: each CTA loads half of the table box and
 // multicasts it to both, so the table is read from L2 once per pair of row blocks,
 // and each CTA's MMA commit frees the stage in both CTAs.
-// GRP: a grouped launch (single CTAs only); every stage is sized for 256 table columns.
-template <int STAGES, bool PAIR, bool MC, int GS, bool GRP>
+// GRP: a grouped launch (single CTAs only); every stage is sized for GBN table
+// columns (the launch's operands have table tiles of at most GBN columns).
+template <int STAGES, bool PAIR, bool MC, int GS, bool GRP, int GBN = 256>
 __global__ void __launch_bounds__(RES_THREADS, 1)
     k_crt_residue(const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmT,
                   const __grid_constant__ CUtensorMap tmR, ResidueArgs a0, Group<ResidueJob> grp, uint32_t *err) {
@@ -431,7 +432,7 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
     constexpr bool CL = PAIR || MC;     // launched as clusters of two CTAs
     constexpr int NP = CL ? 2 : 1;      // row blocks per tile (per cluster)
     constexpr int NBUF = PAIR ? 2 : 1;  // staging buffers per epilogue warp
-    const uint32_t A_BYTES = BM * 128, B_BYTES = GRP ? 256u * 128 : (uint32_t)(PAIR ? a0.BN / 2 : a0.BN) * 128,
+    const uint32_t A_BYTES = BM * 128, B_BYTES = GRP ? (uint32_t)GBN * 128 : (uint32_t)(PAIR ? a0.BN / 2 : a0.BN) * 128,
                    STAGE = A_BYTES + B_BYTES;
     Barriers *bars = reinterpret_cast<Barriers *>(base + STAGES * STAGE);
     uint8_t *stage_out = reinterpret_cast<uint8_t *>(bars) + SMEM_BARS;
@@ -2480,16 +2481,19 @@ struct crt_group {
         int64_t tiles = 0;
         double cost = 0;  // per tile
     };
-    // dig / res by digit form (unsigned, balanced); rec[1]: products with a post step
-    std::vector<Rec> dig[2], res[2], prod, rec[2];
+    // dig by digit form (unsigned, balanced); res by accumulation groups: unsigned
+    // digits (one group), balanced with one group (256-column table tiles), balanced
+    // with several (table tiles of 128 or 64 columns, a deeper ring of smaller
+    // stages); rec[1]: products with a post step
+    std::vector<Rec> dig[2], res[3], prod, rec[2];
     std::vector<std::function<gbmm_status(cudaStream_t)>> post;
     struct Sect {
         size_t jobs_off = 0, tile0_off = 0;
         int n = 0;
         int64_t total = 0;
     };
-    Sect sdig[2], sres[2], sprod, srec[2];
-    size_t smem_res = 0, smem_prod = 0, smem_rec = 0;
+    Sect sdig[2], sres[3], sprod, srec[2];
+    size_t smem_prod = 0, smem_rec = 0;
     std::vector<char> blob;
 };
 
@@ -2569,8 +2573,8 @@ gbmm_status crt_group_add(gbmm_handle h, crt_group *g, const gbmm_mat &c, const 
         ResidueJob rj;
         memset(&rj, 0, sizeof rj);
         rj.tmD = op.tmD; rj.tmT = op.tmT; rj.tmR = op.tmR; rj.a = op.ra;
-        g->res[op.gsteps == RES_GROUP_STEPS_B].push_back(make_rec(rj, op.ra.ntiles, (double)op.ra.nk * op.ra.BN));
-        g->smem_res = std::max(g->smem_res, op.smem);
+        const int rf = op.gsteps == RES_GROUP_STEPS_U ? 0 : (op.ra.BN > 128 ? 1 : 2);
+        g->res[rf].push_back(make_rec(rj, op.ra.ntiles, (double)op.ra.nk * op.ra.BN));
     }
     ProductPlan pp;
     GBMM_TRY(plan_product(t, RA, RB, Y, m, k, n, kp, npad, 0, true, pp));
@@ -2611,7 +2615,7 @@ static void pack_section(std::vector<char> &blob, std::vector<crt_group::Rec> &r
 const std::vector<char> &crt_group_blob(crt_group *g) {
     g->blob.clear();
     for (int f = 0; f < 2; f++) pack_section(g->blob, g->dig[f], g->sdig[f]);
-    for (int f = 0; f < 2; f++) pack_section(g->blob, g->res[f], g->sres[f]);
+    for (int f = 0; f < 3; f++) pack_section(g->blob, g->res[f], g->sres[f]);
     pack_section(g->blob, g->prod, g->sprod);
     for (int f = 0; f < 2; f++) pack_section(g->blob, g->rec[f], g->srec[f]);
     return g->blob;
@@ -2638,21 +2642,32 @@ gbmm_status crt_group_launch(crt_group *g, const char *d_blob, cudaStream_t s, c
         else k_crt_digits<false, true><<<(unsigned)sec.total, 256, 0, s>>>(none, group_at<DigitJob>(d_blob, sec));
         GBMM_CUDA_TRY(cudaGetLastError());
     }
-    for (int f = 0; f < 2; f++) {
+    // residue GEMMs: 4 stages of 48 KB for 256-column table tiles, 6 of 32 KB for
+    // operands whose several accumulation groups narrow the tiles to 128 columns
+    static constexpr int RES_STAGES_NARROW = 6;
+    for (int f = 0; f < 3; f++) {
         const crt_group::Sect &sec = g->sres[f];
         if (!sec.n) continue;
         ResidueArgs none;
         memset(&none, 0, sizeof none);
         const dim3 grid((unsigned)std::min<int64_t>(sec.total, num_sms()));
+        const size_t stg = (size_t)RES_EPI_WARPS * RES_STG_BYTES;
         LaunchScope ls_("k_crt_residue", s);
-        if (f) {
-            auto kern = k_crt_residue<RES_STAGES, false, false, RES_GROUP_STEPS_B, true>;
-            GBMM_TRY(set_smem((const void *)kern, g->smem_res));
-            kern<<<grid, RES_THREADS, g->smem_res, s>>>(zmap, zmap, zmap, none, group_at<ResidueJob>(d_blob, sec), err);
+        if (f == 0) {
+            auto kern = k_crt_residue<RES_STAGES, false, false, RES_GROUP_STEPS_U, true, 256>;
+            const size_t sm = smem_bytes(RES_STAGES, BM * 128 + 256 * 128) + stg;
+            GBMM_TRY(set_smem((const void *)kern, sm));
+            kern<<<grid, RES_THREADS, sm, s>>>(zmap, zmap, zmap, none, group_at<ResidueJob>(d_blob, sec), err);
+        } else if (f == 1) {
+            auto kern = k_crt_residue<RES_STAGES, false, false, RES_GROUP_STEPS_B, true, 256>;
+            const size_t sm = smem_bytes(RES_STAGES, BM * 128 + 256 * 128) + stg;
+            GBMM_TRY(set_smem((const void *)kern, sm));
+            kern<<<grid, RES_THREADS, sm, s>>>(zmap, zmap, zmap, none, group_at<ResidueJob>(d_blob, sec), err);
         } else {
-            auto kern = k_crt_residue<RES_STAGES, false, false, RES_GROUP_STEPS_U, true>;
-            GBMM_TRY(set_smem((const void *)kern, g->smem_res));
-            kern<<<grid, RES_THREADS, g->smem_res, s>>>(zmap, zmap, zmap, none, group_at<ResidueJob>(d_blob, sec), err);
+            auto kern = k_crt_residue<RES_STAGES_NARROW, false, false, RES_GROUP_STEPS_B, true, 128>;
+            const size_t sm = smem_bytes(RES_STAGES_NARROW, BM * 128 + 128 * 128) + stg;
+            GBMM_TRY(set_smem((const void *)kern, sm));
+            kern<<<grid, RES_THREADS, sm, s>>>(zmap, zmap, zmap, none, group_at<ResidueJob>(d_blob, sec), err);
         }
         GBMM_CUDA_TRY(cudaGetLastError());
     }
