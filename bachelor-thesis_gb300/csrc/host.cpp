@@ -1236,8 +1236,9 @@ bool plan_admissible(int id, int m, int k, int n, int la, int lb) {
 // off once the residue and reconstruction passes are amortised), the per-entry
 // limb kernel otherwise.  Entries of fewer than 16 limbs together take the CRT
 // form from 2^25 schoolbook MACs on (in a batch their CRT stages join the grouped
-// launches; measured on the 64 uneven products of configuration 4: 2^25 gave the
-// shortest batch among thresholds 2^24 .. 2^30).  Entries too long for one CRT
+// launches; measured on a batch of 64 products with m, k, n log-uniform in [16, 512]
+// and bit lengths log-uniform in [64, 16384]: 2^25 gave the shortest batch among
+// thresholds 2^24 .. 2^30).  Entries too long for one CRT
 // product (more than 1023 moduli) still take the CRT path: dispatch() splits them
 // into limb halves that fit.
 static int64_t g_crt_short_work = (int64_t)1 << 25;  // 0: never for short entries
@@ -1371,9 +1372,10 @@ static bool split_halves(const Plan &p, int la, int lb, int k, int &hl, int &hn,
 
 // Products of C with at least this many entries fill the GPU alone (their
 // reconstruction alone has 128 or more CTA-pair tiles) and keep their own
-// tile forms on a side stream; measured on configuration 4's batch and a
-// configuration-5 batch against grouping every product (8.10 / 26.1 ms against
-// 8.54 / 28.5 ms) and grouping none (8.31 / 26.4 ms), with 2^17 in between.
+// tile forms on a side stream.  Measured on a batch of 64 products with m, k, n
+// log-uniform in [16, 512] and bit lengths log-uniform in [64, 16384], and on one
+// of 72 that adds eight 1024 x 64 x 1024 products: 8.10 / 26.1 ms, against 8.54 /
+// 28.5 ms grouping every product and 8.31 / 26.4 ms grouping none (2^17 in between).
 constexpr int64_t GROUP_MAX_ENTRIES = (int64_t)1 << 15;
 
 bool crt_groupable(const Plan &p, int la, int lb, int m, int k, int n) {
