@@ -1763,18 +1763,25 @@ static uint32_t big_mod_small(const big &x, uint32_t d) {
     return (uint32_t)r;
 }
 // balanced base-128 digits (each in [-64, 63]) of a nonnegative integer: digit t
-// takes bits [7t, 7t + 7) plus the carry of the digit below
+// takes bits [7t, 7t + 7) plus the carry of the digit below.  32 digits span
+// exactly 7 words, so each chunk of 32 reads its words once and extracts the
+// digits with fixed shifts; the carry is one compare per digit.
 static void balanced128(const big &x, int ndig, int *out) {
     const size_t nw = x.size();
-    int carry = 0;
-    for (int t = 0; t < ndig; t++) {
-        const int bit = 7 * t;
-        const size_t w = (size_t)(bit >> 5);
-        const uint64_t lo = w < nw ? x[w] : 0, hi = w + 1 < nw ? x[w + 1] : 0;
-        const int v = carry + (int)((((hi << 32) | lo) >> (bit & 31)) & 127u);
-        const int d = v >= 64 ? v - 128 : v;
-        carry = (v - d) / 128;
-        out[t] = d;
+    int c = 0;
+    for (int t0 = 0; t0 < ndig; t0 += 32) {
+        const size_t w0 = (size_t)(t0 / 32) * 7;
+        uint64_t w[8];
+        for (int k = 0; k < 8; k++) w[k] = w0 + k < nw ? x[w0 + k] : 0;
+        const int lim = std::min(32, ndig - t0);
+        for (int u = 0; u < 32; u++) {
+            if (u >= lim) break;
+            const int bit = 7 * u;
+            const int b = (int)(((w[bit >> 5] | (w[(bit >> 5) + 1] << 32)) >> (bit & 31)) & 127u);
+            const int v = b + c;
+            c = v >= 64;
+            out[t0 + u] = v - (c << 7);
+        }
     }
 }
 static std::vector<int> balanced128(const big &x, int ndig) {
@@ -1885,47 +1892,61 @@ static void build_tables_host(int P, crt_tables_host &o) {
     o.mods.resize(P);
     // the moduli are independent: contiguous ranges of them on up to 16 host threads
     // (each writes its own table columns)
-    auto one = [&](int i, std::vector<int> &dh, std::vector<int> &dl) {
-        const uint32_t p = pr[i];
-        uint32_t rem = 0;
-        big Mi = big_div_small(Mod, p, &rem);
-        big Mi256 = Mi;
-        big_mul_small(Mi256, 256);
-        const uint32_t w = inv_mod(big_mod_small(Mi, p), p);
-        ModConst mc;
-        memset(&mc, 0, sizeof mc);
-        mc.p = (int32_t)p;
-        mc.inv_p = 1.0f / (float)p;
-        mc.mu = (uint32_t)(((uint64_t)1 << 32) / p);
-        mc.h16 = (uint32_t)((1u << 16) % p);
-        mc.w = w;
-        o.mods[i] = mc;
-        // column 2i multiplies the high digit (x256), column 2i+1 the low digit
-        balanced128(Mi256, o.Dout, dh.data());
-        balanced128(Mi, o.Dout, dl.data());
+    // The moduli are independent: blocks of MB on up to 16 host threads.  A block's
+    // digits go to a small row-major buffer first and then into the table row by
+    // row, 2 MB adjacent columns at a time (writing one column at a time would
+    // touch a new cache line with every 2-byte store).
+    constexpr int MB = 32;
+    auto block = [&](int i0, int i1, std::vector<int8_t> &dig, std::vector<int> &tmp) {
+        const int nb = i1 - i0;
+        for (int q = 0; q < nb; q++) {
+            const int i = i0 + q;
+            const uint32_t p = pr[i];
+            uint32_t rem = 0;
+            big Mi = big_div_small(Mod, p, &rem);
+            big Mi256 = Mi;
+            big_mul_small(Mi256, 256);
+            const uint32_t w = inv_mod(big_mod_small(Mi, p), p);
+            ModConst mc;
+            memset(&mc, 0, sizeof mc);
+            mc.p = (int32_t)p;
+            mc.inv_p = 1.0f / (float)p;
+            mc.mu = (uint32_t)(((uint64_t)1 << 32) / p);
+            mc.h16 = (uint32_t)((1u << 16) % p);
+            mc.w = w;
+            o.mods[i] = mc;
+            // column 2i multiplies the high digit (x256), column 2i+1 the low digit
+            balanced128(Mi256, o.Dout, tmp.data());
+            for (int r = 0; r < o.Dout; r++) dig[(size_t)r * (2 * MB) + 2 * q] = (int8_t)tmp[r];
+            balanced128(Mi, o.Dout, tmp.data());
+            for (int r = 0; r < o.Dout; r++) dig[(size_t)r * (2 * MB) + 2 * q + 1] = (int8_t)tmp[r];
+            // fixed-point weights: round(2^(FIXB+8) / p) for the high digit, round(2^FIXB / p) for the low digit
+            const unsigned __int128 one = 1;
+            const unsigned __int128 gh = ((one << (FIXB + 8)) + p / 2) / p;
+            const unsigned __int128 gl = ((one << FIXB) + p / 2) / p;
+            big bh, bl;
+            for (int w2 = 0; w2 < 4; w2++) {
+                bh.push_back((uint32_t)(gh >> (32 * w2)));
+                bl.push_back((uint32_t)(gl >> (32 * w2)));
+            }
+            std::vector<int> sh = balanced128(bh, SUSED), sl = balanced128(bl, SUSED);
+            for (int r = 0; r < SUSED; r++) {
+                tab[(size_t)r * cols + 2 * i] = bf16_small(sh[r]);
+                tab[(size_t)r * cols + 2 * i + 1] = bf16_small(sl[r]);
+            }
+        }
         for (int r = 0; r < o.Dout; r++) {
-            tab[(size_t)(SROWS + r) * cols + 2 * i] = bf16_small(dh[r]);
-            tab[(size_t)(SROWS + r) * cols + 2 * i + 1] = bf16_small(dl[r]);
-        }
-        // fixed-point weights: round(2^(FIXB+8) / p) for the high digit, round(2^FIXB / p) for the low digit
-        const unsigned __int128 one = 1;
-        const unsigned __int128 gh = ((one << (FIXB + 8)) + p / 2) / p;
-        const unsigned __int128 gl = ((one << FIXB) + p / 2) / p;
-        big bh, bl;
-        for (int w2 = 0; w2 < 4; w2++) {
-            bh.push_back((uint32_t)(gh >> (32 * w2)));
-            bl.push_back((uint32_t)(gl >> (32 * w2)));
-        }
-        std::vector<int> sh = balanced128(bh, SUSED), sl = balanced128(bl, SUSED);
-        for (int r = 0; r < SUSED; r++) {
-            tab[(size_t)r * cols + 2 * i] = bf16_small(sh[r]);
-            tab[(size_t)r * cols + 2 * i + 1] = bf16_small(sl[r]);
+            uint16_t *row = &tab[(size_t)(SROWS + r) * cols + 2 * i0];
+            const int8_t *src = &dig[(size_t)r * (2 * MB)];
+            for (int c = 0; c < 2 * nb; c++) row[c] = bf16_small(src[c]);
         }
     };
-    const int nthr = std::max(1, std::min<int>({16, (int)std::thread::hardware_concurrency(), (P + 31) / 32}));
+    const int nblocks = (P + MB - 1) / MB;
+    const int nthr = std::max(1, std::min<int>({16, (int)std::thread::hardware_concurrency(), nblocks}));
     auto range = [&](int th) {
-        std::vector<int> dh(o.Dout), dl(o.Dout);
-        for (int i = (int)((int64_t)P * th / nthr); i < (int)((int64_t)P * (th + 1) / nthr); i++) one(i, dh, dl);
+        std::vector<int8_t> dig((size_t)o.Dout * 2 * MB);
+        std::vector<int> tmp(o.Dout);
+        for (int bk = th; bk < nblocks; bk += nthr) block(bk * MB, std::min(P, (bk + 1) * MB), dig, tmp);
     };
     if (nthr == 1) {
         range(0);
