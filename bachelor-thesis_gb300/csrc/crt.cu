@@ -1830,7 +1830,9 @@ static uint16_t bf16_small(int v) {
     return lut[v + 256];
 }
 
+struct crt_cache;
 struct crt_tables {
+    crt_cache *cache = nullptr;  // the cache that holds these tables (and the shared residue table)
     int P = 0, Pp = 0;   // moduli, padded 2P/2 (2Pp multiple of 64)
     int Dout = 0, NT = 0;
     ModConst *d_mods = nullptr;
@@ -1843,7 +1845,12 @@ struct crt_tables {
 struct crt_cache {
     std::mutex mu;
     std::map<int, crt_tables *> by_p;
+    // the unweighted residue table of every modulus (256^j mod p_i for all 1024
+    // moduli and every digit position an operand can have): each product's
+    // unweighted table is a view of it (its first moduli, its first dxp columns)
+    __nv_bfloat16 *d_res_all = nullptr;
     ~crt_cache() {
+        cudaFree(d_res_all);
         for (auto &kv : by_p) {
             crt_tables *t = kv.second;
             cudaFree(t->d_mods);
@@ -2023,15 +2030,49 @@ static gbmm_status build_tables(crt_tables *t, int P) {
 // CRT weight w_i = (Mod/p_i)^-1 mod p_i folded into the B operand).
 // GEMM columns of the residue table for P moduli: two per modulus, padded to whole pairs
 static int residue_cols(int P) { return (2 * P + 3) / 4 * 4; }
-static gbmm_status residue_table(crt_tables *t, int dxp, int weighted, __nv_bfloat16 **out) {
+// Digit positions an operand's rows can have: four groups of 15 K steps of 64.
+constexpr int RES_DXMAX = 4 * RES_GROUP_STEPS_B * BK;
+// Fills rows [2P padded][dxp] of a residue table (pitch `pitch`) for moduli 0..P-1.
+static void residue_rows(const crt_tables *t, int P, int dxp, int pitch, int weighted, uint16_t *tab);
+// The table of this product and operand: the unweighted one is a view of the
+// cache's shared table (pitch RES_DXMAX), the weighted one is built per (P, dxp).
+static gbmm_status residue_table(crt_tables *t, int dxp, int weighted, __nv_bfloat16 **out, int *pitch) {
+    if (!weighted) {
+        crt_cache *c = t->cache;
+        if (!c->d_res_all) {
+            const int rows = residue_cols(2 * CMOD_PAIRS);
+            std::vector<uint16_t> tab((size_t)rows * RES_DXMAX, 0);
+            residue_rows(t, 2 * CMOD_PAIRS, RES_DXMAX, RES_DXMAX, 0, tab.data());
+            __nv_bfloat16 *d = nullptr;
+            GBMM_CUDA_TRY(cudaMalloc(&d, tab.size() * 2));
+            GBMM_TRY(upload_now(d, tab.data(), tab.size() * 2));
+            c->d_res_all = d;
+        }
+        *out = c->d_res_all;
+        *pitch = RES_DXMAX;
+        return GBMM_OK;
+    }
+    *pitch = dxp;
     const int key = 2 * dxp + weighted;
     auto it = t->residue.find(key);
     if (it != t->residue.end()) { *out = it->second; return GBMM_OK; }
+    std::vector<uint16_t> tab((size_t)residue_cols(t->P) * dxp, 0);
+    residue_rows(t, t->P, dxp, dxp, 1, tab.data());
+    __nv_bfloat16 *d = nullptr;
+    GBMM_CUDA_TRY(cudaMalloc(&d, tab.size() * 2));
+    GBMM_TRY(upload_now(d, tab.data(), tab.size() * 2));
+    t->residue[key] = d;
+    *out = d;
+    return GBMM_OK;
+}
+
+// Rows (table columns of the GEMM) in groups of four per pair of moduli (i, i + 1):
+// [lo_i, lo_i+1, hi_i, hi_i+1]; with P odd the last group's second slot stays zero.
+// In the shared table every slot holds its modulus; a product with P odd then
+// computes one residue past its moduli in the padding column of its last pair,
+// bounded like the others and never stored.
+static void residue_rows(const crt_tables *t, int P, int dxp, int pitch, int weighted, uint16_t *tab) {
     const auto &pr = primes_desc();
-    // rows (table columns of the GEMM) in groups of four per pair of moduli (i, i + 1):
-    // [lo_i, lo_i+1, hi_i, hi_i+1]; with P odd the last group's second slot stays zero
-    const int rows = residue_cols(t->P);
-    std::vector<uint16_t> tab((size_t)rows * dxp, 0);
     auto range = [&](int i0, int i1) {
         for (int i = i0; i < i1; i++) {
             const uint32_t p = pr[i];
@@ -2041,14 +2082,13 @@ static gbmm_status residue_table(crt_tables *t, int dxp, int weighted, __nv_bflo
                 int32_t b = v > p / 2 ? (int32_t)v - (int32_t)p : (int32_t)v;
                 int32_t d0 = ((b + 128) & 255) - 128;
                 int32_t d1 = (b - d0) / 256;
-                tab[r_lo * dxp + j] = bf16_small(d0);  // x1
-                tab[r_hi * dxp + j] = bf16_small(d1);  // x256
+                tab[r_lo * pitch + j] = bf16_small(d0);  // x1
+                tab[r_hi * pitch + j] = bf16_small(d1);  // x256
                 v = (uint32_t)(((uint64_t)v * 256) % p);
             }
         }
     };
     // the moduli's rows are independent: contiguous ranges on up to 16 host threads
-    const int P = t->P;
     const int nthr = std::max(1, std::min<int>({16, (int)std::thread::hardware_concurrency(), (P * dxp) >> 16}));
     if (nthr == 1) {
         range(0, P);
@@ -2058,12 +2098,6 @@ static gbmm_status residue_table(crt_tables *t, int dxp, int weighted, __nv_bflo
         range(0, P / nthr);
         for (auto &th : pool) th.join();
     }
-    __nv_bfloat16 *d = nullptr;
-    GBMM_CUDA_TRY(cudaMalloc(&d, tab.size() * 2));
-    GBMM_TRY(upload_now(d, tab.data(), tab.size() * 2));
-    t->residue[key] = d;
-    *out = d;
-    return GBMM_OK;
 }
 
 static gbmm_status get_tables(crt_cache *c, int P, crt_tables **out) {
@@ -2071,6 +2105,7 @@ static gbmm_status get_tables(crt_cache *c, int P, crt_tables **out) {
     auto it = c->by_p.find(P);
     if (it != c->by_p.end()) { *out = it->second; return GBMM_OK; }
     crt_tables *t = new crt_tables();
+    t->cache = c;
     gbmm_status st = build_tables(t, P);
     if (st != GBMM_OK) { delete t; return st; }
     c->by_p[P] = t;
@@ -2169,7 +2204,8 @@ static gbmm_status plan_operand(crt_tables *t, const gbmm_mat &X, int transpose,
     a.nlimbs = X.nlimbs; a.transpose = transpose; a.dxp = dxp; a.out = D;
     op.dgrid = dim3((unsigned)((X.cols + 31) / 32), (unsigned)((X.rows + 3) / 4), (unsigned)((dxp / 4 + 63) / 64));
     __nv_bfloat16 *T = nullptr;
-    GBMM_TRY(residue_table(t, dxp, weighted, &T));
+    int tpitch = dxp;
+    GBMM_TRY(residue_table(t, dxp, weighted, &T, &tpitch));
     const int G = (nk + op.gsteps - 1) / op.gsteps;
     int BN = 256;
     while (BN * G > 256) BN /= 2;
@@ -2178,7 +2214,7 @@ static gbmm_status plan_operand(crt_tables *t, const gbmm_mat &X, int transpose,
     op.mc = !grouped && !op.pair && residue_mc(nk);
     const int NP = op.pair || op.mc ? 2 : 1;
     GBMM_TRY(make_map(&op.tmD, D, dxp, E, dxp, BK, BM));
-    GBMM_TRY(make_map(&op.tmT, T, dxp, residue_cols(t->P), dxp, BK, BN / NP));
+    GBMM_TRY(make_map(&op.tmT, T, dxp, residue_cols(t->P), tpitch, BK, BN / NP));
     ResidueArgs &r = op.ra;
     memset(&r, 0, sizeof r);
     r.kdim = kdim; r.E = (int32_t)E; r.nk = nk;
