@@ -754,7 +754,6 @@ struct ProductArgs {
     int32_t npad;      // entry row pitch of Y: n rounded up to 16 (entry e = y * npad + x)
     int32_t nyt, nxt;
     int64_t ntiles;
-    const ModConst *mods;
     __nv_bfloat16 *Y;  // blocked [Ep/64][2Pp][64]: 64 entries per row, 2Pp rows per block
     int64_t yblk;      // elements per 64-entry block (2Pp * 64)
 };
@@ -1835,7 +1834,6 @@ struct crt_tables {
     crt_cache *cache = nullptr;  // the cache that holds these tables (and the shared residue table)
     int P = 0, Pp = 0;   // moduli, padded 2P/2 (2Pp multiple of 64)
     int Dout = 0, NT = 0;
-    ModConst *d_mods = nullptr;
     __nv_bfloat16 *d_recon = nullptr;  // [NT * RTAB][2Pp]
     uint32_t *d_vtab = nullptr;        // [ceil(Dout / 32)][8]: Mod's digits per 32-digit chunk
     std::map<int, __nv_bfloat16 *> residue;  // 2 * dxp + weighted -> [2P rows][dxp]
@@ -1853,7 +1851,6 @@ struct crt_cache {
         cudaFree(d_res_all);
         for (auto &kv : by_p) {
             crt_tables *t = kv.second;
-            cudaFree(t->d_mods);
             cudaFree(t->d_recon);
             cudaFree(t->d_vtab);
             for (auto &r : t->residue) cudaFree(r.second);
@@ -2016,8 +2013,6 @@ static gbmm_status build_tables(crt_tables *t, int P) {
                                               cudaMemcpyHostToDevice, cs));
         GBMM_CUDA_TRY(cudaStreamSynchronize(cs));
     }
-    GBMM_CUDA_TRY(cudaMalloc(&t->d_mods, sizeof(ModConst) * P));
-    GBMM_TRY(upload_now(t->d_mods, o.mods.data(), sizeof(ModConst) * P));
     GBMM_CUDA_TRY(cudaMalloc(&t->d_recon, o.recon.size() * 2));
     GBMM_TRY(upload_now(t->d_recon, o.recon.data(), o.recon.size() * 2));
     GBMM_CUDA_TRY(cudaMalloc(&t->d_vtab, o.vtab.size() * 4));
@@ -2284,7 +2279,7 @@ static gbmm_status plan_product(crt_tables *t, __nv_bfloat16 *RA, __nv_bfloat16 
     GBMM_TRY(make_map(&pp.tmB, RB, k, (uint64_t)2 * P * n, kp, BK, PBX));
     ProductArgs &pa = pp.pa;
     memset(&pa, 0, sizeof pa);
-    pa.m = m; pa.n = n; pa.npad = npad; pa.nk = kp / BK; pa.P = P; pa.mods = t->d_mods; pa.Y = Y;
+    pa.m = m; pa.n = n; pa.npad = npad; pa.nk = kp / BK; pa.P = P; pa.Y = Y;
     pa.yblk = (int64_t)2 * t->Pp * 64;
     // CTA pairs pay off once the K loop is long enough to hide the pair's per-tile
     // synchronisation (measured: faster at k = 512, slower at k = 256); a plan may
