@@ -128,16 +128,22 @@ def test_cfg4_batched_draw_full_output(g, orc):
     W = bench.WORKLOADS["cfg4"]
     mats, _ = bench.gen_jobs(g, W, 2024)
     exps = [_expect(orc, K, M, N, (Al, As), (Bl, Bs), dC.nlimbs) for dC, _, _, (Al, As, Bl, Bs, K, M, N) in mats]
-    h = g.Handle()
-    jobs = h.jobs([(c, a, b) for c, a, b, _ in mats])
-    for call in range(3):
-        for dC, _, _, _ in mats:
-            dC.limbs_t.fill_(-1)   # stale output must not survive a call
-            dC.sizes_t.fill_(7)
-        chosen = h.matmul_batched(jobs)
-        for i, ((dC, _, _, (_, _, _, _, K, M, N)), exp) in enumerate(zip(mats, exps)):
-            try:
-                _same(dC.download(), exp)
-            except AssertionError as e:
-                raise AssertionError(f"call {call}, job {i} ({K}x{M}x{N}, path {chosen[i]}): {e}") from None
-    h.close()
+    import torch
+    # a stream of its own: on the legacy default stream a batch never captures a graph
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        h = g.Handle()
+        jobs = h.jobs([(c, a, b) for c, a, b, _ in mats])
+        for call in range(3):
+            for dC, _, _, _ in mats:
+                dC.limbs_t.fill_(-1)   # stale output must not survive a call
+                dC.sizes_t.fill_(7)
+            chosen = h.matmul_batched(jobs)
+            for i, ((dC, _, _, (_, _, _, _, K, M, N)), exp) in enumerate(zip(mats, exps)):
+                try:
+                    _same(dC.download(), exp)
+                except AssertionError as e:
+                    raise AssertionError(f"call {call}, job {i} ({K}x{M}x{N}, path {chosen[i]}): {e}") from None
+        h.close()
+    torch.cuda.current_stream().wait_stream(s)
