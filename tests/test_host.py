@@ -196,3 +196,42 @@ def test_no_plain_host_to_device_copies():
     # the device error word is cleared once with a device-wide synchronisation after it
     bad = [b for b in bad if "cudaMemset(p, 0, sizeof(uint32_t))" not in b]
     assert not bad, bad
+
+
+def _primes_desc_below_2_16():
+    sieve = bytearray([1]) * 65536
+    sieve[0] = sieve[1] = 0
+    for i in range(2, 256):
+        if sieve[i]:
+            sieve[i * i::i] = bytearray(len(range(i * i, 65536, i)))
+    return [p for p in range(65535, 2, -1) if sieve[p]]
+
+
+def test_modulus_count_covers_the_product_bound(built_lib):
+    """The CRT form takes the largest odd primes below 2^16 in descending order,
+    as few as make Mod >= 2^(bits_a + bits_b + ceil(log2 k) + 18).  An entry of C
+    is a sum of k products below 2^(bits_a + bits_b) in magnitude, so Mod exceeds
+    twice its magnitude, with 16 bits to spare for the reconstruction's
+    fixed-point sign decision.  Checked with exact integers against the host rule
+    (floating-point log2 sums) on the benchmark shapes and random ones."""
+    f = built_lib.gbmmx_crt_params
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+    assert f(64, 64, 16, None) == 1  # GBMM_ERR_INVALID
+    primes = _primes_desc_below_2_16()
+    prefix = [1]
+    rng = random.Random(11)
+    cases = [(4096, 4096, 512), (2048, 2048, 256), (16384, 16384, 512), (16384, 64, 16),
+             (64, 64, 16), (1, 1, 1), (32, 32, 2), (8192, 8192, 1024)]
+    cases += [(rng.randint(1, 16384), rng.randint(1, 16384), rng.randint(1, 4096)) for _ in range(200)]
+    for ba, bb, k in cases:
+        out = ctypes.c_int32()
+        assert f(ba, bb, k, ctypes.byref(out)) == 0
+        P = out.value
+        assert 1 <= P <= len(primes)
+        while len(prefix) <= P:
+            prefix.append(prefix[-1] * primes[len(prefix) - 1])
+        need = ba + bb + (k - 1).bit_length() + 18
+        assert prefix[P] >= 1 << need, (ba, bb, k, P)
+        assert prefix[P - 1] < 1 << need, (ba, bb, k, P)
+        assert prefix[P] > 2 * k * (1 << (ba + bb)) << 16
