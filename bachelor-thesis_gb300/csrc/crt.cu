@@ -299,6 +299,8 @@ __global__ void __launch_bounds__(256) k_crt_digits(DigitArgs a0, Group<DigitJob
     __shared__ uint32_t sflip[128];  // 0x80008000 for a negative entry: flips both bf16 signs of a word
     DigitArgs a;
     int bx, by, bz;
+    tc::grid_dep_wait();    // the operand this launch reads is complete
+    tc::grid_dep_launch();  // the residue GEMM's CTAs may set up while the last blocks run
     if (GRP) {
         const int j = group_job(grp.tile0, grp.njobs, blockIdx.x);
         const DigitJob &J = grp.jobs[j];
@@ -485,6 +487,7 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
     } else {
         cta_setup(bars, STAGES, 512, 1, RES_EPI_WARPS);
     }
+    tc::grid_dep_wait();  // the digits this launch reads are complete
     const uint32_t tmem = bars->tmem_base;
     // the last table tile may be narrow: its MMA has only the columns it needs
     // (a multiple of 16, of 32 for a pair so that each CTA stages whole 8-row groups)
@@ -715,6 +718,7 @@ __global__ void __launch_bounds__(RES_THREADS, 1)
         if (lane == 0) tc::bulk_wait_all();  // staging buffers stay live until the stores finish
         __syncwarp();
     }
+    tc::grid_dep_launch();
     if (PAIR) {
         tc::fence_before_sync();
         __syncthreads();
@@ -807,6 +811,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
     } else {
         cta_setup(bars, STAGES, 512, 1, 8);
     }
+    tc::grid_dep_wait();  // the planes this launch reads are complete
     const uint32_t tmem = bars->tmem_base;
     const int64_t total = GRP ? grp.tile0[grp.njobs] : a0.ntiles;
     // global tile T -> its product's arguments and maps, and the tile within it
@@ -990,6 +995,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             }
         }
     }
+    tc::grid_dep_launch();
     if (PAIR) {
         tc::fence_before_sync();
         __syncthreads();
@@ -1121,6 +1127,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
     } else {
         cta_setup(bars, STAGES, 512, 1, 8);
     }
+    tc::grid_dep_wait();  // the planes this launch reads are complete
     const uint32_t tmem = bars->tmem_base;
 
     if (warp == 0) {
@@ -1452,6 +1459,7 @@ __global__ void __launch_bounds__(CTA_THREADS8, 1)
             }
         }
     }
+    tc::grid_dep_launch();
     if (PAIR) {
         tc::fence_before_sync();
         __syncthreads();
@@ -2138,6 +2146,37 @@ static gbmm_status set_smem(const void *fn, size_t bytes) {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Programmatic dependent launch: every kernel of the four CRT stages is launched
+// with programmatic stream serialization, so its CTAs may be scheduled, set up
+// their barriers and allocate TMEM while the kernel before it in the stream
+// finishes its last tiles.  Each of them calls tc::grid_dep_wait() before its
+// first global-memory access and tc::grid_dep_launch() when its work is issued.
+// A kernel's dependences on other streams (events) stay full dependences.
+static bool g_pdl = true;
+
+static void set_pdl(cudaLaunchAttribute &at) {
+    at.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at.val.programmaticStreamSerializationAllowed = 1;
+}
+
+// Launch of one of the four stages' kernels on plain CTAs.
+template <typename... KArgs, typename... Args>
+static gbmm_status launch_one(void (*kern)(KArgs...), dim3 grid, int threads, size_t smem, cudaStream_t s,
+                              Args &&...args) {
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cudaLaunchAttribute attr[1];
+    set_pdl(attr[0]);
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = g_pdl ? 1 : 0;
+    GBMM_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
+    return GBMM_OK;
+}
+
 // Launch of a persistent kernel in clusters of two CTAs (one CTA per SM): the
 // grid is as many pairs as can be resident at once (GPCs with an odd number of
 // free SMs leave one SM without a partner), capped by the work.
@@ -2146,7 +2185,7 @@ static gbmm_status launch_pairs(void (*kern)(KArgs...), int threads, int64_t wor
                                 Args &&...args) {
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof cfg);
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = 2;
     attr[0].val.clusterDim.y = 1;
@@ -2161,6 +2200,8 @@ static gbmm_status launch_pairs(void (*kern)(KArgs...), int threads, int64_t wor
     GBMM_CUDA_TRY(cudaOccupancyMaxActiveClusters(&resident, (const void *)kern, &cfg));
     if (resident < 1) return set_error(GBMM_ERR_UNSUPPORTED, "no CTA pair of this kernel fits on the device");
     cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(work_pairs, resident)));
+    set_pdl(attr[1]);
+    cfg.numAttrs = g_pdl ? 2 : 1;
     GBMM_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
     return GBMM_OK;
 }
@@ -2232,8 +2273,8 @@ static gbmm_status launch_operand(const OperandPlan &op, cudaStream_t s) {
     {
         LaunchScope ls_("k_crt_digits", s);
         const Group<DigitJob> none{nullptr, nullptr, 0};
-        if (op.balanced) k_crt_digits<true, false><<<op.dgrid, 256, 0, s>>>(op.da, none);
-        else k_crt_digits<false, false><<<op.dgrid, 256, 0, s>>>(op.da, none);
+        if (op.balanced) GBMM_TRY(launch_one(k_crt_digits<true, false>, op.dgrid, 256, 0, s, op.da, none));
+        else GBMM_TRY(launch_one(k_crt_digits<false, false>, op.dgrid, 256, 0, s, op.da, none));
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     const Group<ResidueJob> none{nullptr, nullptr, 0};
@@ -2252,8 +2293,8 @@ static gbmm_status launch_operand(const OperandPlan &op, cudaStream_t s) {
         } else {                                                                                                     \
             GBMM_TRY(set_smem((const void *)k_crt_residue<RES_STAGES, false, false, GS_, false>, sm));               \
             dim3 grid((unsigned)std::min<int64_t>(op.ra.ntiles, num_sms()));                                         \
-            k_crt_residue<RES_STAGES, false, false, GS_, false><<<grid, RES_THREADS, sm, s>>>(                       \
-                op.tmD, op.tmT, op.tmR, op.ra, none, device_error_word());                                           \
+            GBMM_TRY(launch_one(k_crt_residue<RES_STAGES, false, false, GS_, false>, grid, RES_THREADS, sm, s,      \
+                                op.tmD, op.tmT, op.tmR, op.ra, none, device_error_word()));                          \
         }                                                                                                            \
     } while (0)
     if (op.gsteps == RES_GROUP_STEPS_B) RESIDUE_LAUNCH(RES_GROUP_STEPS_B);
@@ -2305,7 +2346,8 @@ static gbmm_status launch_product(const ProductPlan &pp, cudaStream_t s) {
     } else {
         GBMM_TRY(set_smem((const void *)k_crt_product<PROD_STAGES, false, false>, pp.smem));
         dim3 grid((unsigned)std::min<int64_t>(pp.pa.ntiles, num_sms()));
-        k_crt_product<PROD_STAGES, false, false><<<grid, CTA_THREADS8, pp.smem, s>>>(pp.tmA, pp.tmB, pp.pa, none, err);
+        GBMM_TRY(launch_one(k_crt_product<PROD_STAGES, false, false>, grid, CTA_THREADS8, pp.smem, s, pp.tmA, pp.tmB,
+                            pp.pa, none, err));
     }
     GBMM_CUDA_TRY(cudaGetLastError());
     return GBMM_OK;
@@ -2503,7 +2545,8 @@ gbmm_status crt_matmul(gbmm_handle h, const gbmm_mat &c, const gbmm_mat &a, cons
                                       rp.tmY, rp.tmT, ra, none, err));
             } else {
                 dim3 grid((unsigned)std::min<int64_t>(ra.nmt - ra.mt0, num_sms()));
-                k_crt_recon<REC_STAGES, false, false><<<grid, CTA_THREADS8, rp.smem, s>>>(rp.tmY, rp.tmT, ra, none, err);
+                GBMM_TRY(launch_one(k_crt_recon<REC_STAGES, false, false>, grid, CTA_THREADS8, rp.smem, s, rp.tmY,
+                                    rp.tmT, ra, none, err));
             }
             GBMM_CUDA_TRY(cudaGetLastError());
             if (hk && parts > 1) {
@@ -2690,8 +2733,9 @@ gbmm_status crt_group_launch(crt_group *g, const char *d_blob, cudaStream_t s, c
         DigitArgs none;
         memset(&none, 0, sizeof none);
         LaunchScope ls_("k_crt_digits", s);
-        if (f) k_crt_digits<true, true><<<(unsigned)sec.total, 256, 0, s>>>(none, group_at<DigitJob>(d_blob, sec));
-        else k_crt_digits<false, true><<<(unsigned)sec.total, 256, 0, s>>>(none, group_at<DigitJob>(d_blob, sec));
+        const dim3 grid((unsigned)sec.total);
+        if (f) GBMM_TRY(launch_one(k_crt_digits<true, true>, grid, 256, 0, s, none, group_at<DigitJob>(d_blob, sec)));
+        else GBMM_TRY(launch_one(k_crt_digits<false, true>, grid, 256, 0, s, none, group_at<DigitJob>(d_blob, sec)));
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     // residue GEMMs: 4 stages of 48 KB for 256-column table tiles, 6 of 32 KB for
@@ -2709,17 +2753,20 @@ gbmm_status crt_group_launch(crt_group *g, const char *d_blob, cudaStream_t s, c
             auto kern = k_crt_residue<RES_STAGES, false, false, RES_GROUP_STEPS_U, true, 256>;
             const size_t sm = smem_bytes(RES_STAGES, BM * 128 + 256 * 128) + stg;
             GBMM_TRY(set_smem((const void *)kern, sm));
-            kern<<<grid, RES_THREADS, sm, s>>>(zmap, zmap, zmap, none, group_at<ResidueJob>(d_blob, sec), err);
+            GBMM_TRY(launch_one(kern, grid, RES_THREADS, sm, s, zmap, zmap, zmap, none,
+                                group_at<ResidueJob>(d_blob, sec), err));
         } else if (f == 1) {
             auto kern = k_crt_residue<RES_STAGES, false, false, RES_GROUP_STEPS_B, true, 256>;
             const size_t sm = smem_bytes(RES_STAGES, BM * 128 + 256 * 128) + stg;
             GBMM_TRY(set_smem((const void *)kern, sm));
-            kern<<<grid, RES_THREADS, sm, s>>>(zmap, zmap, zmap, none, group_at<ResidueJob>(d_blob, sec), err);
+            GBMM_TRY(launch_one(kern, grid, RES_THREADS, sm, s, zmap, zmap, zmap, none,
+                                group_at<ResidueJob>(d_blob, sec), err));
         } else {
             auto kern = k_crt_residue<RES_STAGES_NARROW, false, false, RES_GROUP_STEPS_B, true, 128>;
             const size_t sm = smem_bytes(RES_STAGES_NARROW, BM * 128 + 128 * 128) + stg;
             GBMM_TRY(set_smem((const void *)kern, sm));
-            kern<<<grid, RES_THREADS, sm, s>>>(zmap, zmap, zmap, none, group_at<ResidueJob>(d_blob, sec), err);
+            GBMM_TRY(launch_one(kern, grid, RES_THREADS, sm, s, zmap, zmap, zmap, none,
+                                group_at<ResidueJob>(d_blob, sec), err));
         }
         GBMM_CUDA_TRY(cudaGetLastError());
     }
@@ -2730,7 +2777,8 @@ gbmm_status crt_group_launch(crt_group *g, const char *d_blob, cudaStream_t s, c
         GBMM_TRY(set_smem((const void *)kern, g->smem_prod));
         const dim3 grid((unsigned)std::min<int64_t>(g->sprod.total, num_sms()));
         LaunchScope ls_("k_crt_product", s);
-        kern<<<grid, CTA_THREADS8, g->smem_prod, s>>>(zmap, zmap, none, group_at<ProductJob>(d_blob, g->sprod), err);
+        GBMM_TRY(launch_one(kern, grid, CTA_THREADS8, g->smem_prod, s, zmap, zmap, none,
+                            group_at<ProductJob>(d_blob, g->sprod), err));
         GBMM_CUDA_TRY(cudaGetLastError());
     }
     // the products with post steps first: their shifted adds then run on s2 while
@@ -2860,6 +2908,15 @@ extern "C" uint64_t gbmmx_table_build(int32_t P, double *ms) {
     mix(o.vtab.data(), o.vtab.size() * 4);
     mix(o.mods.data(), o.mods.size() * sizeof(ModConst));
     return h;
+}
+
+// Test hook: launch the four stages' kernels with programmatic stream
+// serialization (1, the default) or as plain stream-ordered launches (0); returns
+// the previous setting.
+extern "C" int32_t gbmmx_launch_pdl(int32_t enable) {
+    const int32_t old = g_pdl ? 1 : 0;
+    g_pdl = enable != 0;
+    return old;
 }
 
 // Test hook: the residue GEMM's form (-1 by the K loop's length, 0 single CTAs,

@@ -229,6 +229,16 @@ __device__ __forceinline__ uint32_t mapa(uint32_t saddr, uint32_t rank) {
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+
+// ---- programmatic dependent launch -----------------------------------------------------------
+// A kernel launched with programmatic stream serialization may start while the
+// kernel before it in the stream is still running.  grid_dep_wait() returns once
+// that kernel has completed and its memory operations are visible; a kernel calls
+// it before its first global-memory access.  grid_dep_launch() lets the next kernel
+// be scheduled once every CTA of this grid has called it or exited.  Both are
+// no-ops in a kernel launched without the attribute.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 // TMA load into this CTA's shared memory, completing on an mbarrier that may sit in the peer CTA
 __device__ __forceinline__ void tma_load_2d_pair(void *smem_dst, const CUtensorMap *map, uint32_t bar_cluster, int x,
                                                  int y) {
