@@ -273,12 +273,19 @@ extern "C" gbmm_status gbmm_set_stream(gbmm_handle h, void *stream) {
 // ======================================================================================
 // text <-> limb planes
 // ======================================================================================
-static inline int hexval(unsigned char c) {
-    if (c >= '0' && c <= '9') return c - '0';
-    if (c >= 'a' && c <= 'f') return c - 'a' + 10;
-    if (c >= 'A' && c <= 'F') return c - 'A' + 10;
-    return -1;
-}
+// value of a hexadecimal digit, -1 for any other byte
+struct HexTable {
+    int8_t v[256];
+    constexpr HexTable() : v() {
+        for (int c = 0; c < 256; c++)
+            v[c] = (int8_t)(c >= '0' && c <= '9' ? c - '0'
+                            : c >= 'a' && c <= 'f' ? c - 'a' + 10
+                            : c >= 'A' && c <= 'F' ? c - 'A' + 10
+                                                   : -1);
+    }
+};
+static constexpr HexTable HEXV{};
+static inline int hexval(unsigned char c) { return HEXV.v[c]; }
 static inline bool is_ws(unsigned char c) { return c == ' ' || c == '\n' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
 
 // ---- host-side parallelism for the text and GMP conversions -----------------------------
@@ -325,15 +332,17 @@ static gbmm_status parse_one(const char *text, size_t len, size_t &p, int64_t e,
         snprintf(msg, msgcap, "entry %lld needs %d limbs, capacity %d", (long long)e, need, nlimbs);
         return GBMM_ERR_CAPACITY;
     }
-    for (int i = 0; i < nlimbs; i++) limbs[(int64_t)i * ld + e] = 0u;
-    for (size_t i = 0; i < nd; i++) {
-        size_t pos = nd - 1 - i;  // digit index from the least significant end
-        if (pos / 8 < (size_t)nlimbs)
-            limbs[(int64_t)(pos / 8) * ld + e] |= (uint32_t)hexval((unsigned char)text[s + i]) << (4 * (pos % 8));
+    // limb i holds digits [nd - 8(i+1), nd - 8i) of the token, built in a register
+    // and stored once; the top limb has the first (nonzero) digit, so it is nonzero
+    const unsigned char *d = reinterpret_cast<const unsigned char *>(text + s);
+    for (int i = 0; i < need; i++) {
+        const size_t hi = nd - 8 * (size_t)i, lo = hi >= 8 ? hi - 8 : 0;
+        uint32_t v = 0;
+        for (size_t q = lo; q < hi; q++) v = (v << 4) | (uint32_t)HEXV.v[d[q]];
+        limbs[(int64_t)i * ld + e] = v;
     }
-    int n = need;
-    while (n > 0 && limbs[(int64_t)(n - 1) * ld + e] == 0) n--;
-    sizes[e] = neg ? -n : n;
+    for (int i = need; i < nlimbs; i++) limbs[(int64_t)i * ld + e] = 0u;
+    sizes[e] = neg ? -need : need;
     return GBMM_OK;
 }
 
