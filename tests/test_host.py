@@ -235,3 +235,37 @@ def test_modulus_count_covers_the_product_bound(built_lib):
         assert prefix[P] >= 1 << need, (ba, bb, k, P)
         assert prefix[P - 1] < 1 << need, (ba, bb, k, P)
         assert prefix[P] > 2 * k * (1 << (ba + bb)) << 16
+
+
+def test_parse_limb_boundaries(built_lib):
+    """Tokens of 8j - 1, 8j and 8j + 1 digits (a limb's digits end exactly at a
+    limb boundary or one past it), tokens that fill the planes exactly, and tokens
+    longer than the planes only through leading zeros; the planes past a token's
+    limbs are cleared even when they held data."""
+    import gbmm
+    nl = 4
+    vals = []
+    for j in range(1, nl + 1):
+        for nd in (8 * j - 1, 8 * j, 8 * j + 1):
+            if nd <= 8 * nl:
+                vals.append(int("f" + "0" * (nd - 2) + "1", 16) if nd > 1 else 1)
+                vals.append(-int("8" + "7" * (nd - 1), 16))
+    text = " ".join(format(v, "x") if v >= 0 else "-" + format(-v, "x") for v in vals)
+    text += " " + "0" * 40 + "abc" + " -" + "0" * 33 + "f" * 32
+    vals += [0xabc, -int("f" * 32, 16)]
+    n = len(vals)
+    limbs = np.full((nl, n), 0xDEADBEEF, dtype=np.uint32)
+    sizes = np.full(n, 77, dtype=np.int32)
+    used = ctypes.c_size_t(0)
+    b = text.encode()
+    gbmm.check(gbmm.lib().gbmm_parse_hex(b, len(b), n, limbs.ctypes.data, sizes.ctypes.data, nl, n,
+                                         ctypes.byref(used)))
+    assert used.value == len(b)
+    assert gbmm.planes_to_ints(limbs, sizes) == vals
+    for e, v in enumerate(vals):
+        need = (abs(v).bit_length() + 31) // 32
+        assert abs(int(sizes[e])) == need
+        assert (limbs[need:, e] == 0).all()
+    with pytest.raises(gbmm.GbmmError) as err:
+        gbmm.parse_hex("1" + "0" * (8 * nl), 1, nl)
+    assert err.value.status == gbmm.ERR_CAPACITY
